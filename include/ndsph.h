@@ -1,0 +1,242 @@
+/*
+ * ndsph.h -- C-ABI of the GB300-native NDSPMHD hot path (libndsph_gpu.so).
+ *
+ * The reference (danieljprice/ndspmhd, serial Fortran 90) runs its per-step
+ * SPH hot path through argument-less subroutines that talk through Fortran
+ * module globals.  This header is the drop-in boundary: a Fortran shim
+ * (ndspmhd_gb300/fortran/gpu_sph.f90) keeps the subroutine names and forwards
+ * c_loc() of the module arrays to the entry points below.
+ *
+ * Conventions (identical to the Fortran side):
+ *   - real     == double, integer == int32_t
+ *   - x(ndim,n) is AoS per particle: x[i*ndim + d]
+ *   - vel, Bevol, Bfield, force, dBevoldt, daldt, curlB, graddivv, alpha are
+ *     (3,n) arrays: v[i*3 + d]   (ndimV = ndimB = 3 in every dimension)
+ *   - particle indices passed across the boundary (ireal) are 1-based
+ *   - every entry point returns 0 on success or an NDSPH_E* code; the shim
+ *     maps a non-zero code to the reference's `call quit`.
+ *   - one host thread calls the library; each handle owns one CUDA stream.
+ */
+#ifndef NDSPH_H
+#define NDSPH_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define NDSPH_API __attribute__((visibility("default")))
+#else
+#define NDSPH_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (mirror the reference's quit/stop sites) ---------------- */
+#define NDSPH_OK               0
+#define NDSPH_E_ARG            1   /* bad argument / option out of scope         */
+#define NDSPH_E_CUDA           2   /* CUDA runtime error                         */
+#define NDSPH_E_H_NONPOS       3   /* h <= 0       iterate_density.f90:99-102    */
+#define NDSPH_E_RHO_NONPOS     4   /* rho <= 0     iterate_density.f90:168-170   */
+#define NDSPH_E_NOT_CONVERGED  5   /* NR budget    iterate_density.f90:349-351   */
+#define NDSPH_E_VSIG_DET       6   /* MHD det < 0  ratesND_mhd.f90:1422-1429     */
+#define NDSPH_E_NAN            7   /* non-finite result                          */
+#define NDSPH_E_CELLS          8   /* cell grid invalid (box < 3 cells, h > box) */
+#define NDSPH_E_CLUMP          9   /* dx = 0 pair  ratesND_mhd.f90:419-424       */
+#define NDSPH_E_CAPACITY      10   /* size above a fixed maximum                 */
+
+/* ---- particle types (variablesND.f90:165-171) ------------------------------ */
+#define NDSPH_ITYPE_GAS      0
+#define NDSPH_ITYPE_BND      1
+#define NDSPH_ITYPE_DUST     2
+#define NDSPH_ITYPE_BNDDUST 12
+
+/* ---- pair-sum precision forms ---------------------------------------------- */
+#define NDSPH_PREC_FP64  0   /* plain FP64, table-exact kernel (parity form)      */
+#define NDSPH_PREC_FP32  1   /* FP32 pair terms, FP64 separations/accumulation    */
+
+/*
+ * Runtime options: the subset of the reference's `options`, `artvi`, `eos`,
+ * `bound`, `setup_params` and `timestep` modules that the hot path reads
+ * (defaults.f90:29-120).  Options outside the supported subset (ikernel != 0,
+ * ikernav != 3, icty != 0, igravity != 0, iresist != 0, idivbzero != 0, ...)
+ * have no field here: the library implements the reference's defaults for them.
+ */
+typedef struct ndsph_opts {
+    int32_t ndim;            /* 1, 2 or 3 (dimen?D.f90)                           */
+    int32_t ibound[3];       /* 0 none, 1 fixed particles, 3 periodic             */
+    double  xmin[3];         /* bound module                                      */
+    double  xmax[3];
+    double  hfact;           /* 1.2                                               */
+    double  tolh;            /* 1e-3                                              */
+    double  psep;            /* setup particle spacing (h bump when numneigh<=1)  */
+    int32_t maxdensits;      /* 250                                               */
+    int32_t imhd;            /* 0, 1 (evolve B/rho) or 11 (evolve B)              */
+    int32_t imagforce;       /* 2 (tensor form, stressmax correction)             */
+    int32_t iener;           /* 2 (thermal energy) or 0 (polytropic/isothermal)   */
+    int32_t iav;             /* 2                                                 */
+    int32_t iavlim[3];       /* (2,1,0)                                           */
+    double  alphamin;        /* 0.1                                               */
+    double  alphaumin;       /* 0.0                                               */
+    double  alphaBmin;       /* 1.0                                               */
+    double  beta;            /* 2.0                                               */
+    double  avdecayconst;    /* 0.1                                               */
+    double  gamma;           /* 5/3                                               */
+    double  polyk;           /* 1.0 (iener=0)                                     */
+    int32_t idust;           /* 0 or 2 (two-fluid)                                */
+    int32_t idrag_nature;    /* 1 (constant K)                                    */
+    double  Kdrag;
+    double  C_cour;          /* 0.3                                               */
+    double  C_force;         /* 0.25                                              */
+    int32_t precision;       /* NDSPH_PREC_*                                      */
+    int32_t learned_h;       /* 1: MLP h predictor in front of NR (device forms)  */
+} ndsph_opts;
+
+/* Fill `o` with the reference defaults (defaults.f90:29-120) for `ndim`. */
+NDSPH_API void ndsph_default_opts(ndsph_opts* o, int32_t ndim);
+
+/*
+ * Host particle arrays, Fortran module layout.  `n` below is the number of
+ * real particles (npart); arrays must hold at least n entries (times the
+ * per-particle stride).  Inputs are read, outputs are written; a caller may
+ * pass the same pointers on every call.
+ */
+typedef struct ndsph_particles {
+    /* part module: state (inputs) */
+    double*  x;          /* (ndim,n)                                            */
+    double*  vel;        /* (3,n)                                               */
+    double*  Bevol;      /* (3,n)  B/rho (imhd 1..9) or B (imhd 11..)            */
+    double*  en;         /* (n)    thermal energy (iener=2)                      */
+    double*  hh;         /* (n)    smoothing length: in, updated by NR (inout)   */
+    double*  pmass;      /* (n)                                                 */
+    double*  alpha;      /* (3,n)  AV / conductivity / resistivity parameters   */
+    int32_t* itype;      /* (n)                                                 */
+    int32_t* ireal;      /* (n)    1-based source of fixed particles, 0 = none  */
+    /* density / hterms outputs */
+    double*  rho;        /* (n)                                                 */
+    double*  rhoalt;     /* (n)    number-density sum (densn)                   */
+    double*  drhodt;     /* (n)                                                 */
+    double*  dhdt;       /* (n)                                                 */
+    double*  gradh;      /* (n)    1/omega                                      */
+    double*  gradhn;     /* (n)                                                 */
+    double*  gradgradh;  /* (n)    zeta term                                    */
+    int32_t* numneigh;   /* (n)                                                 */
+    /* conservative2primitive outputs */
+    double*  dens;       /* (n)                                                 */
+    double*  uu;         /* (n)                                                 */
+    double*  pr;         /* (n)                                                 */
+    double*  spsound;    /* (n)                                                 */
+    double*  Bfield;     /* (3,n)                                               */
+    /* rates module outputs */
+    double*  force;      /* (3,n)                                               */
+    double*  dBevoldt;   /* (3,n)                                               */
+    double*  dudt;       /* (n)                                                 */
+    double*  dendt;      /* (n)                                                 */
+    double*  daldt;      /* (3,n)                                               */
+    double*  divB;       /* (n)                                                 */
+    double*  curlB;      /* (3,n)                                               */
+    double*  del2u;      /* (n)    conductivity-switch source                   */
+    double*  graddivv;   /* (3,n)  curl-v estimate (iavlim(1) /= 3)             */
+} ndsph_particles;
+
+/* Timestep scalars of the `timestep` module plus diagnostics. */
+typedef struct ndsph_dt {
+    double  dtcourant;   /* ratesND_mhd.f90:1481                                */
+    double  dtforce;     /* ratesND_mhd.f90:938-943                             */
+    double  dtav;
+    double  dtdrag;      /* ratesND_mhd.f90:545 (min t_s)                       */
+    double  dtvisc;
+    double  vsigmax;
+    double  stressmax;   /* ratesND_mhd.f90:232-245                             */
+    double  hhmax;       /* bound module                                        */
+    double  dt;          /* next leapfrog dt (stepND_leapfrog_mhd.f90:252)      */
+    double  time;
+    int32_t its;         /* NR passes of the last iterate_density (itsdensity)  */
+    int32_t ncalctotal;  /* particles summed over all passes                    */
+    int32_t nsteps;
+    int32_t nrelink;     /* cell-grid rebuilds inside the NR loop               */
+} ndsph_dt;
+
+typedef struct ndsph_ctx ndsph_ctx;   /* opaque: device mirrors, stream, tables */
+
+/* ---- life cycle -------------------------------------------------------------
+ * ndsph_init mirrors setkernels(ikernel=0,...) + setkerndrag(41) + init_drag
+ * (initialiseND_mhd.f90:188-223, kernelND.f90:102-117): it builds the 4001-point
+ * cubic-spline and double-hump tables in FP64 on the host, uploads them, and
+ * reserves device capacity for `nmax` particles (grown on demand).            */
+NDSPH_API int ndsph_init(ndsph_ctx** ctx, const ndsph_opts* opts, int32_t nmax);
+NDSPH_API int ndsph_finalize(ndsph_ctx* ctx);
+NDSPH_API const char* ndsph_last_error(ndsph_ctx* ctx);
+
+/* ---- drop-in entry points (host arrays, one H2D/D2H per call) ---------------
+ * ndsph_set_linklist  replaces set_linklist        linkND.f90:45-161
+ *                     (+ periodic wrap boundaryND.f90:30-90; ghosts are not
+ *                     built: periodic images are taken inside the sweeps the
+ *                     way ghostND_mhd.f90:224-225 places them)
+ * ndsph_iterate_density replaces iterate_density   iterate_density.f90:43-360
+ *                     with density   density_sums.f90:38-379 (first pass) and
+ *                     density_partial density_sums.f90:396-658 (later passes)
+ * ndsph_conservative2primitive replaces the in-scope part of
+ *                     conservative2primitive.f90:42-470 and eos.f90:40-106
+ * ndsph_get_rates     replaces get_rates           ratesND_mhd.f90:29-979
+ *                     (rates_core :1175-1690, artificial_dissipation
+ *                     :1700-1894, mhd_terms :2377-2720, drag_forces
+ *                     :1074-1169, get_tstop dust.f90:77-101)
+ * ndsph_derivs        replaces derivs              derivs.f90:27-287
+ *                     (boundary, link, iterate_density, cons2prim, get_rates)
+ *                     in one H2D + one D2H.
+ * ndsph_step          replaces step               stepND_leapfrog_mhd.f90:31-275
+ *                     (predictor, derivs, corrector, boundary, dt) with the
+ *                     leapfrog on the device; state in host arrays.            */
+NDSPH_API int ndsph_set_linklist(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts);
+NDSPH_API int ndsph_iterate_density(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts);
+NDSPH_API int ndsph_conservative2primitive(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart);
+NDSPH_API int ndsph_get_rates(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts);
+NDSPH_API int ndsph_derivs(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts);
+NDSPH_API int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts);
+
+/* primitive2conservative (conservative2primitive.f90:478-799): initial h from
+ * hfact*(m/rho)^(1/ndim) with rho = dens on input, density iteration,
+ * Bevol and en from Bfield and uu, then one derivs.  Inputs: x, vel, pmass,
+ * itype, ireal, dens (as initial rho), uu, Bfield, alpha.                     */
+NDSPH_API int ndsph_primitive2conservative(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts);
+
+/* ---- device-resident form ----------------------------------------------------
+ * State lives in HBM between steps (sorted by cell); upload/download convert
+ * to and from the host layout.  ndsph_dev_step runs one full leapfrog step on
+ * the device with no host synchronisation except the NR pass count.           */
+NDSPH_API int ndsph_dev_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart);
+NDSPH_API int ndsph_dev_download(ndsph_ctx* ctx, ndsph_particles* p, ndsph_dt* dts);
+NDSPH_API int ndsph_dev_step(ndsph_ctx* ctx, int32_t nsteps, ndsph_dt* dts);
+NDSPH_API int ndsph_dev_derivs(ndsph_ctx* ctx, ndsph_dt* dts);
+/* set the leapfrog clock of the device-resident state (evolve.f90:50-56 starts
+ * with dt = 0; later steps use the dt returned by the previous step)          */
+NDSPH_API int ndsph_dev_set_time(ndsph_ctx* ctx, double dt, double time, int32_t nsteps);
+
+/* ---- parity / debug helpers (never on a timed path) -------------------------
+ * ndsph_neighbour_csr: after ndsph_set_linklist, the 1-based neighbour set of
+ * every real particle under the criterion `mode` (0: q_i<2 gather as
+ * density_partial, 1: q_i<2 or q_j<2 as density/get_rates), as CSR.  The
+ * replacement of check_neighbourlist.f90:27-182.  `offsets` has npart+1
+ * entries; `neigh` capacity `cap`; returns NDSPH_E_CAPACITY if too small.     */
+NDSPH_API int ndsph_neighbour_csr(ndsph_ctx* ctx, int32_t mode, int64_t* offsets, int32_t* neigh, int64_t cap);
+
+/* kernel tables as built on the host (for the table parity test): 5*4001
+ * doubles: wij, grwij, grgrwij, wijdrag, grwijdrag.                            */
+NDSPH_API int ndsph_kernel_tables(int32_t ndim, double* out);
+
+/* per-kernel device timings of the last call (ms), for the bench's roofline. */
+typedef struct ndsph_timing {
+    float link_ms, density_ms, density_pass1_ms, eos_ms, rates_ms, post_ms, step_ms, total_ms;
+    int32_t density_passes;
+    int32_t launches;
+    int64_t pairs_density;   /* accepted (i,j) pairs summed in pass 1          */
+    int64_t pairs_rates;     /* accepted (i,j) pairs in the rates sweep        */
+} ndsph_timing;
+NDSPH_API int ndsph_get_timing(ndsph_ctx* ctx, ndsph_timing* t);
+NDSPH_API int ndsph_set_profiling(ndsph_ctx* ctx, int32_t on);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NDSPH_H */

@@ -1,0 +1,1084 @@
+// ndsph_api.cu -- the C-ABI of include/ndsph.h: context, device memory,
+// kernel tables and the host orchestration of link -> iterate_density ->
+// conservative2primitive -> get_rates (-> leapfrog).
+//
+// One context = one CUDA stream on the current device.  All device memory is
+// owned here (cudaMalloc at init / on growth, freed in ndsph_finalize); the
+// caller's host arrays are only read and written inside the entry points.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include "ndsph_launch.h"
+
+namespace ndsph {
+void launch_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, cudaStream_t st);
+void launch_density_init2(FieldPtrs F, Side S, int n, Reduce* red, cudaStream_t st);
+}
+
+using namespace ndsph;
+
+struct ndsph_ctx {
+    ndsph_opts opts;
+    DevOpts o;
+    cudaStream_t st = nullptr;
+    int device = 0;
+    int cap = 0;          // particle capacity
+    int n = 0;            // particles currently on the device
+    // slab double buffers
+    double* slab[2] = {nullptr, nullptr};
+    int cur = 0;
+    FieldPtrs F;          // pointer table of the current slab (HH/HNEXT may be swapped)
+    // side arrays (two sets of the permuted ints)
+    Side S;
+    int* itype2 = nullptr;
+    int* id2 = nullptr;
+    int* ireal2 = nullptr;
+    SortScratch srt;
+    int* d_fields = nullptr;     // field index list for the gather
+    // tables
+    double2* tab64 = nullptr;
+    float2* tab32 = nullptr;
+    Tables t;
+    // grid
+    Grid g;
+    double cell_hmax = 0.0;      // hmax the grid was built for
+    bool linked = false;
+    // reductions
+    Reduce* red = nullptr;
+    Reduce* h_red = nullptr;     // pinned mirror
+    double* d_dtout = nullptr;
+    double* h_dtout = nullptr;
+    int* d_ncalc = nullptr;
+    // host staging
+    double* d_stage = nullptr;   // n*3 doubles
+    int* d_istage = nullptr;
+    // timing
+    bool profiling = false;
+    cudaEvent_t ev[16];
+    ndsph_timing timing;
+    ndsph_dt last_dt;
+    std::string err;
+    double time = 0.0, dt = 0.0;
+    int nsteps = 0;
+};
+
+static thread_local std::string g_err;
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            if (ctx) ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);        \
+            return NDSPH_E_CUDA;                                                          \
+        }                                                                                 \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// kernel tables, kernelND.f90:127-157 (structure), cubic spline :4143-4192 and
+// normalisation :4279-4289 (truncated pi, 1D constant 0.66666666666), drag
+// kernel 41 :1659-1697; slope(i) = (t(i+1)-t(i))*ddq2table with the last
+// entry's slope 0 (index1 clamped to ikern, kernelND.f90:4383-4384)
+// ---------------------------------------------------------------------------
+static void build_tables(int ndim, std::vector<double>& w, std::vector<double>& gw, std::vector<double>& ggw,
+                         std::vector<double>& wd, std::vector<double>& gwd, double& dq2, double& ddq2)
+{
+    const double pi = 3.141592653589;
+    const double radkern = 2.0;
+    dq2 = radkern * radkern / (double)IKERN;
+    double cn = 0.0, cd = 0.0;
+    if (ndim == 1) { cn = 0.66666666666; cd = 2.0; }
+    if (ndim == 2) { cn = 10. / (7. * pi); cd = 70. / (31. * pi); }
+    if (ndim == 3) { cn = 1. / pi; cd = 10. / (9. * pi); }
+    w.assign(NTAB, 0.0); gw.assign(NTAB, 0.0); ggw.assign(NTAB, 0.0); wd.assign(NTAB, 0.0); gwd.assign(NTAB, 0.0);
+    for (int i = 0; i <= IKERN; i++) {
+        volatile double q2 = i * dq2;
+        double q = sqrt(q2);
+        double a = 0, b = 0, c = 0, da = 0, db = 0;
+        if (q < 1.0) {
+            volatile double t1 = 1.5 * q2;
+            volatile double t2 = 0.75 * q;
+            volatile double t3 = t2 * q2;
+            a = (1. - t1) + t3;
+            volatile double u1 = -3. * q;
+            volatile double u2 = 2.25 * q2;
+            b = u1 + u2;
+            volatile double v1 = 4.5 * q;
+            c = -3. + v1;
+            volatile double q4 = q2 * q2;
+            volatile double s1 = 1.5 * q4;
+            volatile double s2 = 0.75 * q4;
+            volatile double s3 = s2 * q;
+            da = (q2 - s1) + s3;
+            volatile double r1 = 2. * q;
+            volatile double r2 = 6. * q2;
+            volatile double r3 = r2 * q;
+            volatile double r4 = 3.75 * q4;
+            db = (r1 - r3) + r4;
+        } else if (q <= 2.0) {
+            volatile double tt = 2. - q;
+            volatile double t2 = tt * tt;
+            volatile double t3 = t2 * tt;
+            a = 0.25 * t3;
+            b = -0.75 * t2;
+            c = 1.5 * tt;
+            volatile double x1 = 0.25 * q2;
+            da = x1 * t3;
+            volatile double y1 = 0.5 * q;
+            volatile double y2 = y1 * t3;
+            volatile double y3 = 0.75 * q2;
+            volatile double y4 = y3 * t2;
+            db = y2 - y4;
+        }
+        w[i] = cn * a; gw[i] = cn * b; ggw[i] = cn * c; wd[i] = cd * da; gwd[i] = cd * db;
+    }
+    ddq2 = 1. / dq2;
+}
+
+static void pack_tab(const std::vector<double>& t, double ddq2, double2* out64, float2* out32)
+{
+    for (int i = 0; i <= IKERN; i++) {
+        int i1 = std::min(i + 1, IKERN);
+        volatile double diff = t[i1] - t[i];
+        double slope = diff * ddq2;
+        out64[i] = make_double2(t[i], slope);
+        out32[i] = make_float2((float)t[i], (float)slope);
+    }
+}
+
+extern "C" int ndsph_kernel_tables(int32_t ndim, double* out)
+{
+    if (ndim < 1 || ndim > 3 || !out) return NDSPH_E_ARG;
+    std::vector<double> w, gw, ggw, wd, gwd;
+    double dq2, ddq2;
+    build_tables(ndim, w, gw, ggw, wd, gwd, dq2, ddq2);
+    memcpy(out + 0 * NTAB, w.data(), NTAB * 8);
+    memcpy(out + 1 * NTAB, gw.data(), NTAB * 8);
+    memcpy(out + 2 * NTAB, ggw.data(), NTAB * 8);
+    memcpy(out + 3 * NTAB, wd.data(), NTAB * 8);
+    memcpy(out + 4 * NTAB, gwd.data(), NTAB * 8);
+    return 0;
+}
+
+extern "C" void ndsph_default_opts(ndsph_opts* o, int32_t ndim)
+{
+    memset(o, 0, sizeof(*o));
+    o->ndim = ndim;
+    o->xmax[0] = o->xmax[1] = o->xmax[2] = 1.0;
+    o->hfact = 1.2; o->tolh = 1.e-3; o->psep = 0.01; o->maxdensits = 250;
+    o->imhd = 0; o->imagforce = 2; o->iener = 2; o->iav = 2;
+    o->iavlim[0] = 2; o->iavlim[1] = 1; o->iavlim[2] = 0;
+    o->alphamin = 0.1; o->alphaumin = 0.0; o->alphaBmin = 1.0; o->beta = 2.0; o->avdecayconst = 0.1;
+    o->gamma = 5. / 3.; o->polyk = 1.0; o->C_cour = 0.3; o->C_force = 0.25;
+}
+
+extern "C" const char* ndsph_last_error(ndsph_ctx* ctx)
+{
+    return ctx ? ctx->err.c_str() : g_err.c_str();
+}
+
+static int check_opts(const ndsph_opts* p, std::string& why)
+{
+    if (p->ndim < 1 || p->ndim > 3) { why = "ndim must be 1..3"; return NDSPH_E_ARG; }
+    for (int d = 0; d < p->ndim; d++) {
+        if (p->ibound[d] != 0 && p->ibound[d] != 1 && p->ibound[d] != 3) {
+            why = "ibound must be 0, 1 or 3 (reflective/shearing ghosts are out of scope)";
+            return NDSPH_E_ARG;
+        }
+        if (p->ibound[d] == 3 && !(p->xmax[d] > p->xmin[d])) { why = "periodic box with xmax <= xmin"; return NDSPH_E_ARG; }
+    }
+    if (!(p->imhd == 0 || p->imhd == 1 || p->imhd == 11)) { why = "imhd must be 0, 1 or 11"; return NDSPH_E_ARG; }
+    if (p->imhd != 0 && p->imagforce != 2) { why = "imagforce must be 2"; return NDSPH_E_ARG; }
+    if (!(p->iener == 0 || p->iener == 2)) { why = "iener must be 0 or 2"; return NDSPH_E_ARG; }
+    if (!(p->iav == 2)) { why = "iav must be 2"; return NDSPH_E_ARG; }
+    if (!(p->idust == 0 || p->idust == 2)) { why = "idust must be 0 or 2"; return NDSPH_E_ARG; }
+    if (p->idust == 2 && p->idrag_nature != 1) { why = "idrag_nature must be 1"; return NDSPH_E_ARG; }
+    if (p->iavlim[0] == 3 || p->iavlim[2] != 0) { why = "iavlim must be (0|1|2, *, 0)"; return NDSPH_E_ARG; }
+    if (p->precision != NDSPH_PREC_FP64 && p->precision != NDSPH_PREC_FP32) { why = "bad precision"; return NDSPH_E_ARG; }
+    return 0;
+}
+
+static void set_devopts(ndsph_ctx* ctx)
+{
+    const ndsph_opts& p = ctx->opts;
+    DevOpts& o = ctx->o;
+    memset(&o, 0, sizeof(o));
+    o.ndim = p.ndim;
+    o.has_fixed = 0;
+    for (int d = 0; d < 3; d++) {
+        o.ibound[d] = (d < p.ndim) ? p.ibound[d] : 0;
+        o.periodic[d] = (d < p.ndim && p.ibound[d] == 3) ? 1 : 0;
+        o.xmin[d] = p.xmin[d]; o.xmax[d] = p.xmax[d];
+        o.L[d] = p.xmax[d] - p.xmin[d];
+        if (d < p.ndim && p.ibound[d] == 1) o.has_fixed = 1;
+    }
+    o.hfact = p.hfact; o.tolh = p.tolh; o.psep = p.psep; o.maxdensits = p.maxdensits;
+    o.imhd = p.imhd; o.imagforce = p.imagforce; o.iener = p.iener; o.iav = p.iav;
+    for (int k = 0; k < 3; k++) o.iavlim[k] = p.iavlim[k];
+    o.alphamin = p.alphamin; o.alphaumin = p.alphaumin; o.alphaBmin = p.alphaBmin;
+    o.beta = p.beta; o.avdecayconst = p.avdecayconst;
+    o.gamma = p.gamma; o.polyk = p.polyk;
+    // initialiseND_mhd.f90:168-172
+    o.avfact = (fabs(p.gamma - 1.) > 1.e-3) ? log(4.) / (log((p.gamma + 1.) / (p.gamma - 1.))) : 1.0;
+    o.idust = p.idust; o.idrag_nature = p.idrag_nature; o.Kdrag = p.Kdrag;
+    o.C_cour = p.C_cour; o.C_force = p.C_force; o.precision = p.precision;
+}
+
+static void free_particles(ndsph_ctx* ctx)
+{
+    void* ptrs[] = {ctx->slab[0], ctx->slab[1], ctx->S.itype, ctx->S.id, ctx->S.ireal, ctx->S.pos_of_id,
+                    ctx->S.numneigh, ctx->S.cell, ctx->S.xs, ctx->S.h1, ctx->S.active, ctx->S.active_next,
+                    ctx->S.flag, ctx->itype2, ctx->id2, ctx->ireal2, ctx->srt.key, ctx->srt.slot, ctx->srt.perm,
+                    ctx->d_stage, ctx->d_istage};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    ctx->slab[0] = ctx->slab[1] = nullptr;
+    memset(&ctx->S, 0, sizeof(ctx->S));
+    ctx->itype2 = ctx->id2 = ctx->ireal2 = nullptr;
+    ctx->srt.key = ctx->srt.slot = ctx->srt.perm = nullptr;
+    ctx->d_stage = nullptr; ctx->d_istage = nullptr;
+    ctx->cap = 0;
+}
+
+static void set_field_ptrs(ndsph_ctx* ctx)
+{
+    for (int f = 0; f < NF; f++) ctx->F.f[f] = ctx->slab[ctx->cur] + (size_t)f * ctx->cap;
+}
+
+static int ensure_capacity(ndsph_ctx* ctx, int n)
+{
+    if (n <= ctx->cap) return 0;
+    free_particles(ctx);
+    int cap = std::max(n, 1024);
+    size_t sz = (size_t)NF * cap * sizeof(double);
+    CK(cudaMalloc(&ctx->slab[0], sz));
+    CK(cudaMalloc(&ctx->slab[1], sz));
+    CK(cudaMemsetAsync(ctx->slab[0], 0, sz, ctx->st));
+    CK(cudaMemsetAsync(ctx->slab[1], 0, sz, ctx->st));
+    size_t ib = sizeof(int) * (size_t)cap;
+    CK(cudaMalloc(&ctx->S.itype, ib)); CK(cudaMalloc(&ctx->S.id, ib)); CK(cudaMalloc(&ctx->S.ireal, ib));
+    CK(cudaMalloc(&ctx->S.pos_of_id, ib)); CK(cudaMalloc(&ctx->S.numneigh, ib)); CK(cudaMalloc(&ctx->S.cell, ib));
+    CK(cudaMalloc(&ctx->S.xs, sizeof(float4) * (size_t)cap)); CK(cudaMalloc(&ctx->S.h1, sizeof(double) * (size_t)cap));
+    CK(cudaMalloc(&ctx->S.active, ib)); CK(cudaMalloc(&ctx->S.active_next, ib)); CK(cudaMalloc(&ctx->S.flag, ib));
+    CK(cudaMalloc(&ctx->itype2, ib)); CK(cudaMalloc(&ctx->id2, ib)); CK(cudaMalloc(&ctx->ireal2, ib));
+    CK(cudaMalloc(&ctx->srt.key, ib)); CK(cudaMalloc(&ctx->srt.slot, ib)); CK(cudaMalloc(&ctx->srt.perm, ib));
+    CK(cudaMalloc(&ctx->d_stage, sizeof(double) * 3 * (size_t)cap));
+    CK(cudaMalloc(&ctx->d_istage, ib));
+    CK(cudaMemsetAsync(ctx->S.numneigh, 0, ib, ctx->st));
+    ctx->cap = cap;
+    ctx->cur = 0;
+    set_field_ptrs(ctx);
+    ctx->linked = false;
+    return 0;
+}
+
+static int ensure_cells(ndsph_ctx* ctx, int ncells)
+{
+    if (ncells + 1 <= ctx->srt.cap_cells) return 0;
+    if (ctx->srt.count) cudaFree(ctx->srt.count);
+    if (ctx->srt.start) cudaFree(ctx->srt.start);
+    if (ctx->srt.blocksums) cudaFree(ctx->srt.blocksums);
+    int cap = std::max(ncells + 1, 4096);
+    cap = cap + cap / 4;
+    CK(cudaMalloc(&ctx->srt.count, sizeof(int) * (size_t)cap));
+    CK(cudaMalloc(&ctx->srt.start, sizeof(int) * (size_t)(cap + 1)));
+    int nb = (cap + 4095) / 4096 + 1;
+    CK(cudaMalloc(&ctx->srt.blocksums, sizeof(int) * (size_t)nb));
+    ctx->srt.cap_cells = cap;
+    ctx->srt.cap_blocks = nb;
+    return 0;
+}
+
+extern "C" int ndsph_init(ndsph_ctx** out, const ndsph_opts* opts, int32_t nmax)
+{
+    if (!out || !opts) return NDSPH_E_ARG;
+    std::string why;
+    int rc = check_opts(opts, why);
+    if (rc) { g_err = why; return rc; }
+    ndsph_ctx* ctx = new ndsph_ctx();
+    ctx->opts = *opts;
+    set_devopts(ctx);
+    memset(&ctx->S, 0, sizeof(ctx->S));
+    memset(&ctx->srt, 0, sizeof(ctx->srt));
+    memset(&ctx->timing, 0, sizeof(ctx->timing));
+    memset(&ctx->last_dt, 0, sizeof(ctx->last_dt));
+    cudaError_t e = cudaGetDevice(&ctx->device);
+    if (e != cudaSuccess) { g_err = cudaGetErrorString(e); delete ctx; return NDSPH_E_CUDA; }
+    e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { g_err = cudaGetErrorString(e); delete ctx; return NDSPH_E_CUDA; }
+    for (int k = 0; k < 16; k++) cudaEventCreate(&ctx->ev[k]);
+    // tables (setkernels / setkerndrag)
+    std::vector<double> w, gw, ggw, wd, gwd;
+    double dq2, ddq2;
+    build_tables(opts->ndim, w, gw, ggw, wd, gwd, dq2, ddq2);
+    std::vector<double2> h64(4 * NTAB);
+    std::vector<float2> h32(4 * NTAB);
+    pack_tab(w, ddq2, &h64[0 * NTAB], &h32[0 * NTAB]);
+    pack_tab(gw, ddq2, &h64[1 * NTAB], &h32[1 * NTAB]);
+    pack_tab(ggw, ddq2, &h64[2 * NTAB], &h32[2 * NTAB]);
+    pack_tab(wd, ddq2, &h64[3 * NTAB], &h32[3 * NTAB]);
+    if (cudaMalloc(&ctx->tab64, sizeof(double2) * 4 * NTAB) != cudaSuccess ||
+        cudaMalloc(&ctx->tab32, sizeof(float2) * 4 * NTAB) != cudaSuccess ||
+        cudaMalloc(&ctx->red, sizeof(Reduce)) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_red, sizeof(Reduce)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_dtout, sizeof(double) * 8) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_dtout, sizeof(double) * 8) != cudaSuccess ||
+        cudaMalloc(&ctx->d_ncalc, sizeof(int) * 4) != cudaSuccess ||
+        cudaMalloc(&ctx->d_fields, sizeof(int) * NF) != cudaSuccess) {
+        g_err = "cudaMalloc failed in ndsph_init";
+        ndsph_finalize(ctx);
+        return NDSPH_E_CUDA;
+    }
+    cudaMemcpy(ctx->tab64, h64.data(), sizeof(double2) * 4 * NTAB, cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->tab32, h32.data(), sizeof(float2) * 4 * NTAB, cudaMemcpyHostToDevice);
+    cudaMemset(ctx->red, 0, sizeof(Reduce));
+    ctx->t.w = ctx->tab64 + 0 * NTAB; ctx->t.gw = ctx->tab64 + 1 * NTAB;
+    ctx->t.ggw = ctx->tab64 + 2 * NTAB; ctx->t.wdrag = ctx->tab64 + 3 * NTAB;
+    ctx->t.wf = ctx->tab32 + 0 * NTAB; ctx->t.gwf = ctx->tab32 + 1 * NTAB;
+    ctx->t.ggwf = ctx->tab32 + 2 * NTAB; ctx->t.wdragf = ctx->tab32 + 3 * NTAB;
+    ctx->t.dq2table = dq2; ctx->t.ddq2table = ddq2;
+    ctx->t.dq2tablef = (float)dq2; ctx->t.ddq2tablef = (float)ddq2;
+    if (nmax > 0 && ensure_capacity(ctx, nmax)) {
+        g_err = ctx->err;
+        ndsph_finalize(ctx);
+        return NDSPH_E_CUDA;
+    }
+    *out = ctx;
+    return 0;
+}
+
+extern "C" int ndsph_finalize(ndsph_ctx* ctx)
+{
+    if (!ctx) return 0;
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    free_particles(ctx);
+    void* ptrs[] = {ctx->tab64, ctx->tab32, ctx->red, ctx->d_dtout, ctx->d_ncalc, ctx->d_fields,
+                    ctx->srt.count, ctx->srt.start, ctx->srt.blocksums};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    if (ctx->h_red) cudaFreeHost(ctx->h_red);
+    if (ctx->h_dtout) cudaFreeHost(ctx->h_dtout);
+    for (int k = 0; k < 16; k++) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+static int sync_red(ndsph_ctx* ctx)
+{
+    CK(cudaMemcpyAsync(ctx->h_red, ctx->red, sizeof(Reduce), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if (ctx->h_red->err) {
+        int code = ctx->h_red->err;
+        char buf[160];
+        snprintf(buf, sizeof buf, "device error %d at particle %d", code, ctx->h_red->err_index + 1);
+        ctx->err = buf;
+        return code;
+    }
+    return 0;
+}
+
+static int upload_aos(ndsph_ctx* ctx, const double* host, int f0, int ncomp, int stride, int n)
+{
+    if (!host) return 0;
+    CK(cudaMemcpyAsync(ctx->d_stage, host, sizeof(double) * (size_t)stride * n, cudaMemcpyHostToDevice, ctx->st));
+    launch_aos_to_slab(ctx->F, f0, ncomp, ctx->d_stage, stride, nullptr, n, ctx->st);
+    return 0;
+}
+static int download_aos(ndsph_ctx* ctx, double* host, int f0, int ncomp, int stride, int n)
+{
+    if (!host) return 0;
+    launch_slab_to_aos(ctx->d_stage, stride, ctx->F, f0, ncomp, ctx->S.id, n, ctx->st);
+    CK(cudaMemcpyAsync(host, ctx->d_stage, sizeof(double) * (size_t)stride * n, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+static int download_int(ndsph_ctx* ctx, int* host, const int* dsrc, int n, bool is_index)
+{
+    if (!host) return 0;
+    launch_slab_to_int(ctx->d_istage, dsrc, ctx->S.id, n, ctx->st);
+    CK(cudaMemcpyAsync(host, ctx->d_istage, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if (is_index) for (int i = 0; i < n; i++) host[i] = host[i] + 1;
+    return 0;
+}
+
+static void tmark(ndsph_ctx* ctx, int k)
+{
+    if (ctx->profiling) cudaEventRecord(ctx->ev[k], ctx->st);
+}
+static float tdiff(ndsph_ctx* ctx, int a, int b)
+{
+    float ms = 0.f;
+    if (ctx->profiling) cudaEventElapsedTime(&ms, ctx->ev[a], ctx->ev[b]);
+    return ms;
+}
+
+// state fields the host hands over (x, vel, Bevol, en, hh, pmass, alpha)
+static const int STATE_FIELDS[] = {X0, X1, X2, V0, V1, V2, BE0, BE1, BE2, EN, HH, PM, AL0, AL1, AL2};
+static const int INCOPY_FIELDS[] = {XIN0, XIN1, XIN2, VIN0, VIN1, VIN2, BIN0, BIN1, BIN2, HIN, ENIN, RHOIN,
+                                    ALIN0, ALIN1, ALIN2, FIN0, FIN1, FIN2, DBIN0, DBIN1, DBIN2, DHIN, DENIN,
+                                    DALIN0, DALIN1, DALIN2};
+
+// upload all inputs the drop-in entry points read (unsorted: slot = index)
+static int upload_inputs(ndsph_ctx* ctx, const ndsph_particles* p, int n, bool with_density, bool with_prim)
+{
+    const int nd = ctx->o.ndim;
+    int rc = ensure_capacity(ctx, n);
+    if (rc) return rc;
+    ctx->n = n;
+    rc |= upload_aos(ctx, p->x, X0, nd, nd, n);
+    rc |= upload_aos(ctx, p->vel, V0, 3, 3, n);
+    rc |= upload_aos(ctx, p->Bevol, BE0, 3, 3, n);
+    rc |= upload_aos(ctx, p->en, EN, 1, 1, n);
+    rc |= upload_aos(ctx, p->hh, HH, 1, 1, n);
+    rc |= upload_aos(ctx, p->pmass, PM, 1, 1, n);
+    rc |= upload_aos(ctx, p->alpha, AL0, 3, 3, n);
+    if (with_density) {
+        rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n);
+        rc |= upload_aos(ctx, p->rhoalt, RHOALT, 1, 1, n);
+        rc |= upload_aos(ctx, p->drhodt, DRHODT, 1, 1, n);
+        rc |= upload_aos(ctx, p->dhdt, DHDT, 1, 1, n);
+        rc |= upload_aos(ctx, p->gradh, GRADH, 1, 1, n);
+        rc |= upload_aos(ctx, p->gradhn, GRADHN, 1, 1, n);
+        rc |= upload_aos(ctx, p->gradgradh, GRADGRADH, 1, 1, n);
+    } else {
+        rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n);   // fixed particles keep rho
+    }
+    if (with_prim) {
+        rc |= upload_aos(ctx, p->dens, DENS, 1, 1, n);
+        rc |= upload_aos(ctx, p->uu, UU, 1, 1, n);
+        rc |= upload_aos(ctx, p->pr, PR, 1, 1, n);
+        rc |= upload_aos(ctx, p->spsound, CS, 1, 1, n);
+        rc |= upload_aos(ctx, p->Bfield, BF0, 3, 3, n);
+    }
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->S.itype, p->itype, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+    launch_iota(ctx->S.id, n, ctx->st);
+    launch_iota(ctx->S.pos_of_id, n, ctx->st);
+    // ireal: 1-based host index -> 0-based id (-1 none)
+    std::vector<int> ir(n, -1);
+    if (p->ireal)
+        for (int i = 0; i < n; i++) ir[i] = p->ireal[i] - 1;
+    CK(cudaMemcpyAsync(ctx->S.ireal, ir.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->linked = false;
+    return 0;
+}
+
+// cell grid for the current hmax: periodic dims tile [xmin,xmax] with
+// nc = floor(L/(2 hmax (1+1e-9))) >= 3 cells, open dims pad the bounding box
+// by one cell each side (like linkND.f90:80-89)
+static int build_grid(ndsph_ctx* ctx, double hmax, const double* lo, const double* hi)
+{
+    Grid& g = ctx->g;
+    const double cmin = 2.0 * hmax * (1.0 + 1.e-9);
+    long ncells = 1;
+    for (int d = 0; d < 3; d++) {
+        if (d >= ctx->o.ndim) {
+            g.nc[d] = 1; g.origin[d] = 0.0; g.cs[d] = 1.0;
+        } else if (ctx->o.periodic[d]) {
+            double L = ctx->o.L[d];
+            long nc = (long)floor(L / cmin);
+            if (nc < 3) {
+                ctx->err = "periodic box smaller than 3 cells of 2*hmax";
+                return NDSPH_E_CELLS;
+            }
+            if (nc > 4096) nc = 4096;
+            g.nc[d] = (int)nc;
+            g.origin[d] = ctx->o.xmin[d];
+            g.cs[d] = L / (double)nc;
+        } else {
+            double ext = (hi[d] - lo[d]) + 2.0 * cmin;
+            long nc = (long)floor(ext / cmin) + 1;
+            if (nc > 1 << 22) { ctx->err = "too many cells"; return NDSPH_E_CELLS; }
+            g.nc[d] = (int)std::max(nc, 1L);
+            g.cs[d] = cmin;
+            g.origin[d] = lo[d] - cmin;
+        }
+        g.inv_cs[d] = 1.0 / g.cs[d];
+        g.csf[d] = (float)g.cs[d];
+        ncells *= g.nc[d];
+    }
+    if (ncells > 200000000L) { ctx->err = "too many cells"; return NDSPH_E_CELLS; }
+    g.ncells = (int)ncells;
+    ctx->cell_hmax = hmax;
+    return ensure_cells(ctx, g.ncells);
+}
+
+// link: hmax + bbox, grid, counting sort by cell, permutation of `fields`
+static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hmax_ghost)
+{
+    const int n = ctx->n;
+    cudaStream_t st = ctx->st;
+    // reset bbox/hmax reduction slots
+    {
+        Reduce r0;
+        CK(cudaMemcpyAsync(ctx->h_red, ctx->red, sizeof(Reduce), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        r0 = *ctx->h_red;
+        for (int d = 0; d < 3; d++) { r0.xlo[d] = ~0ull; r0.xhi[d] = 0ull; }
+        r0.hmax = 0ull;
+        *ctx->h_red = r0;
+        CK(cudaMemcpyAsync(ctx->red, ctx->h_red, sizeof(Reduce), cudaMemcpyHostToDevice, st));
+    }
+    launch_hmax_bbox(ctx->F, ctx->o.ndim, n, ctx->red, &ctx->red->hmax, st);
+    CK(cudaMemcpyAsync(ctx->h_red, ctx->red, sizeof(Reduce), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double hmax = bitsd(ctx->h_red->hmax);
+    if (!(hmax > 0.0) || !std::isfinite(hmax)) {
+        ctx->err = "link: max h <= 0 or not finite";
+        return NDSPH_E_H_NONPOS;
+    }
+    double lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+        lo[d] = (d < ctx->o.ndim) ? unord_bits(ctx->h_red->xlo[d]) : 0.0;
+        hi[d] = (d < ctx->o.ndim) ? unord_bits(ctx->h_red->xhi[d]) : 0.0;
+        if (d < ctx->o.ndim && (!std::isfinite(lo[d]) || !std::isfinite(hi[d]))) {
+            ctx->err = "link: non-finite position";
+            return NDSPH_E_NAN;
+        }
+    }
+    int rc = build_grid(ctx, hmax, lo, hi);
+    if (rc) return rc;
+    if (!keep_hmax_ghost) {
+        ctx->h_red->hmax_ghost = dbits(hmax);
+        CK(cudaMemcpyAsync(&ctx->red->hmax_ghost, &ctx->h_red->hmax_ghost, sizeof(unsigned long long),
+                           cudaMemcpyHostToDevice, st));
+    }
+    launch_cell_key(ctx->F, ctx->g, ctx->o, n, ctx->srt, ctx->red, st);
+    launch_scan(ctx->srt, ctx->g.ncells, st);
+    launch_scatter_sort(ctx->srt, n, ctx->g.ncells, st);
+    // gather into the other slab, then swap
+    CK(cudaMemcpyAsync(ctx->d_fields, fields, sizeof(int) * (size_t)nfields, cudaMemcpyHostToDevice, st));
+    FieldPtrs dst;
+    double* other = ctx->slab[1 - ctx->cur];
+    for (int f = 0; f < NF; f++) {
+        // keep the HH/HNEXT swap state consistent across slabs
+        size_t off = (size_t)(ctx->F.f[f] - ctx->slab[ctx->cur]);
+        dst.f[f] = other + off;
+    }
+    launch_gather_fields(dst, ctx->F, ctx->d_fields, nfields, ctx->srt.perm, n, st);
+    launch_gather_int(ctx->itype2, ctx->S.itype, ctx->srt.perm, n, st);
+    launch_gather_int(ctx->id2, ctx->S.id, ctx->srt.perm, n, st);
+    launch_gather_int(ctx->ireal2, ctx->S.ireal, ctx->srt.perm, n, st);
+    std::swap(ctx->itype2, ctx->S.itype);
+    std::swap(ctx->id2, ctx->S.id);
+    std::swap(ctx->ireal2, ctx->S.ireal);
+    ctx->cur = 1 - ctx->cur;
+    ctx->F = dst;
+    launch_post_sort(ctx->S, ctx->srt, n, ctx->g.ncells, ctx->g, ctx->F, ctx->o, st);
+    ctx->linked = true;
+    CK(cudaGetLastError());
+    return 0;
+}
+
+static int link_all(ndsph_ctx* ctx, bool keep_hmax_ghost)
+{
+    std::vector<int> all(NF);
+    for (int f = 0; f < NF; f++) all[f] = f;
+    return do_link(ctx, all.data(), NF, keep_hmax_ghost);
+}
+
+static SweepArgs sweep_args(ndsph_ctx* ctx)
+{
+    SweepArgs a;
+    a.F = ctx->F;
+    a.S = ctx->S;
+    a.cell_start = ctx->srt.start;
+    a.g = ctx->g;
+    a.o = ctx->o;
+    a.t = ctx->t;
+    a.red = ctx->red;
+    a.n = ctx->n;
+    a.its = 0;
+    a.nlist = 0;
+    a.ncalc_next = ctx->d_ncalc;
+    return a;
+}
+
+// iterate_density iterate_density.f90:43-360 on the linked device state
+static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out, int* nrelink_out)
+{
+    const int n = ctx->n;
+    cudaStream_t st = ctx->st;
+    const int itsmax = ctx->o.maxdensits;
+    launch_density_init2(ctx->F, ctx->S, n, ctx->red, st);
+    int zero = 0;
+    CK(cudaMemcpyAsync(&ctx->red->redolink, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+    int its = 0, ncalc = n, ncalctotal = 0, nrelink = 0;
+    bool redolink = false;
+    // count fixed particles: a full pass is taken while ncalc == npart
+    float dens_ms = 0.f, pass1_ms = 0.f;
+    while (ncalc > 0 && its <= itsmax) {
+        its++;
+        if (redolink) {
+            // relink (iterate_density.f90:122-126): hhmax of the ghosts is the
+            // current max h; the cell grid is rebuilt if h outgrew the cells
+            CK(cudaMemcpyAsync(ctx->h_red, ctx->red, sizeof(Reduce), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            // active list -> ids
+            std::vector<int> act(ncalc), ids(n);
+            CK(cudaMemcpy(act.data(), ctx->S.active, sizeof(int) * (size_t)ncalc, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(ids.data(), ctx->S.id, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+            for (int k = 0; k < ncalc; k++) act[k] = ids[act[k]];
+            int rc = link_all(ctx, false);
+            if (rc) return rc;
+            std::vector<int> pos(n);
+            CK(cudaMemcpy(pos.data(), ctx->S.pos_of_id, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+            for (int k = 0; k < ncalc; k++) act[k] = pos[act[k]];
+            CK(cudaMemcpy(ctx->S.active, act.data(), sizeof(int) * (size_t)ncalc, cudaMemcpyHostToDevice));
+            nrelink++;
+        }
+        const bool full = (ncalc == n);
+        launch_h1(ctx->F, ctx->S, n, st);
+        if (full && its > 1) launch_copy(ctx->F.f[HNEXT], ctx->F.f[HH], n, st);
+        CK(cudaMemsetAsync(ctx->d_ncalc, 0, sizeof(int), st));
+        CK(cudaMemsetAsync(&ctx->red->redolink, 0, sizeof(int), st));
+        SweepArgs a = sweep_args(ctx);
+        a.its = its;
+        a.nlist = ncalc;
+        tmark(ctx, 2);
+        launch_density(a, full, st);
+        tmark(ctx, 3);
+        CK(cudaGetLastError());
+        if (full) std::swap(ctx->F.f[HH], ctx->F.f[HNEXT]);
+        if (ctx->o.has_fixed) launch_fixed_density_copy(ctx->F, ctx->S, n, st);
+        ncalctotal += ncalc;
+        int h_ncalc = 0;
+        CK(cudaMemcpyAsync(&h_ncalc, ctx->d_ncalc, sizeof(int), cudaMemcpyDeviceToHost, st));
+        int rc = sync_red(ctx);
+        if (rc) return rc;
+        if (ctx->profiling) {
+            float ms = tdiff(ctx, 2, 3);
+            dens_ms += ms;
+            if (its == 1) pass1_ms = ms;
+        }
+        redolink = ctx->h_red->redolink != 0;
+        ncalc = h_ncalc;
+        std::swap(ctx->S.active, ctx->S.active_next);
+    }
+    ctx->timing.density_ms = dens_ms;
+    ctx->timing.density_pass1_ms = pass1_ms;
+    ctx->timing.density_passes = its;
+    if (its_out) *its_out = its;
+    if (ncalctotal_out) *ncalctotal_out = ncalctotal;
+    if (nrelink_out) *nrelink_out = nrelink;
+    if (its > itsmax && itsmax > 0) {
+        char buf[128];
+        snprintf(buf, sizeof buf, "ERROR: DENSITY NOT CONVERGED ON %d PARTICLES", ncalc);
+        ctx->err = buf;
+        return NDSPH_E_NOT_CONVERGED;
+    }
+    return 0;
+}
+
+static int do_cons2prim(ndsph_ctx* ctx)
+{
+    launch_eos(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, ctx->st);
+    launch_fixed_copy(ctx->F, ctx->S, ctx->o, ctx->n, ctx->st);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+static int do_rates(ndsph_ctx* ctx)
+{
+    cudaStream_t st = ctx->st;
+    launch_h1(ctx->F, ctx->S, ctx->n, st);
+    SweepArgs a = sweep_args(ctx);
+    tmark(ctx, 4);
+    launch_rates(a, st);
+    tmark(ctx, 5);
+    launch_finalize_dt(ctx->red, ctx->o, ctx->d_dtout, st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ctx->h_dtout, ctx->d_dtout, sizeof(double) * 8, cudaMemcpyDeviceToHost, st));
+    int rc = sync_red(ctx);
+    if (rc) return rc;
+    ctx->timing.rates_ms = tdiff(ctx, 4, 5);
+    ndsph_dt& d = ctx->last_dt;
+    d.dtcourant = ctx->h_dtout[0];
+    d.dtforce = ctx->h_dtout[1];
+    d.dtav = ctx->h_dtout[2];
+    d.dtdrag = ctx->h_dtout[3];
+    d.dtvisc = 1.7976931348623157e308;
+    d.vsigmax = ctx->h_dtout[4];
+    d.stressmax = ctx->h_dtout[5];
+    d.hhmax = bitsd(ctx->h_red->hmax_ghost);
+    return 0;
+}
+
+// derivs: boundary, link, iterate_density, cons2prim, get_rates
+static int do_derivs(ndsph_ctx* ctx, const int* fields, int nfields)
+{
+    cudaStream_t st = ctx->st;
+    tmark(ctx, 0);
+    bool anyb = false;
+    for (int d = 0; d < ctx->o.ndim; d++) if (ctx->o.ibound[d] != 0) anyb = true;
+    if (anyb) launch_boundary_wrap(ctx->F, ctx->o, ctx->n, st);
+    int rc = do_link(ctx, fields, nfields, false);
+    if (rc) return rc;
+    tmark(ctx, 1);
+    launch_reduce_reset(ctx->red, st);
+    int its = 0, nct = 0, nrl = 0;
+    rc = do_iterate_density(ctx, &its, &nct, &nrl);
+    if (rc) return rc;
+    tmark(ctx, 6);
+    rc = do_cons2prim(ctx);
+    if (rc) return rc;
+    tmark(ctx, 7);
+    rc = do_rates(ctx);
+    if (rc) return rc;
+    ctx->last_dt.its = its;
+    ctx->last_dt.ncalctotal = nct;
+    ctx->last_dt.nrelink = nrl;
+    if (ctx->profiling) {
+        ctx->timing.link_ms = tdiff(ctx, 0, 1);
+        ctx->timing.eos_ms = tdiff(ctx, 6, 7);
+    }
+    return 0;
+}
+
+static int download_all(ndsph_ctx* ctx, ndsph_particles* p)
+{
+    const int n = ctx->n, nd = ctx->o.ndim;
+    int rc = 0;
+    rc |= download_aos(ctx, p->x, X0, nd, nd, n);
+    rc |= download_aos(ctx, p->vel, V0, 3, 3, n);
+    rc |= download_aos(ctx, p->Bevol, BE0, 3, 3, n);
+    rc |= download_aos(ctx, p->en, EN, 1, 1, n);
+    rc |= download_aos(ctx, p->hh, HH, 1, 1, n);
+    rc |= download_aos(ctx, p->pmass, PM, 1, 1, n);
+    rc |= download_aos(ctx, p->alpha, AL0, 3, 3, n);
+    rc |= download_aos(ctx, p->rho, RHO, 1, 1, n);
+    rc |= download_aos(ctx, p->rhoalt, RHOALT, 1, 1, n);
+    rc |= download_aos(ctx, p->drhodt, DRHODT, 1, 1, n);
+    rc |= download_aos(ctx, p->dhdt, DHDT, 1, 1, n);
+    rc |= download_aos(ctx, p->gradh, GRADH, 1, 1, n);
+    rc |= download_aos(ctx, p->gradhn, GRADHN, 1, 1, n);
+    rc |= download_aos(ctx, p->gradgradh, GRADGRADH, 1, 1, n);
+    rc |= download_aos(ctx, p->dens, DENS, 1, 1, n);
+    rc |= download_aos(ctx, p->uu, UU, 1, 1, n);
+    rc |= download_aos(ctx, p->pr, PR, 1, 1, n);
+    rc |= download_aos(ctx, p->spsound, CS, 1, 1, n);
+    rc |= download_aos(ctx, p->Bfield, BF0, 3, 3, n);
+    rc |= download_aos(ctx, p->force, F0, 3, 3, n);
+    rc |= download_aos(ctx, p->dBevoldt, DB0, 3, 3, n);
+    rc |= download_aos(ctx, p->dudt, DUDT, 1, 1, n);
+    rc |= download_aos(ctx, p->dendt, DENDT, 1, 1, n);
+    rc |= download_aos(ctx, p->daldt, DAL0, 3, 3, n);
+    rc |= download_aos(ctx, p->divB, DIVB, 1, 1, n);
+    rc |= download_aos(ctx, p->curlB, CB0, 3, 3, n);
+    rc |= download_aos(ctx, p->del2u, DEL2U, 1, 1, n);
+    rc |= download_aos(ctx, p->graddivv, GDV0, 3, 3, n);
+    if (rc) return rc;
+    rc = download_int(ctx, p->numneigh, ctx->S.numneigh, n, false);
+    return rc;
+}
+
+static void fill_dt(ndsph_ctx* ctx, ndsph_dt* d)
+{
+    if (!d) return;
+    ctx->last_dt.dt = ctx->dt;
+    ctx->last_dt.time = ctx->time;
+    ctx->last_dt.nsteps = ctx->nsteps;
+    *d = ctx->last_dt;
+}
+
+#define GUARD_CTX() do { if (!ctx) { g_err = "null context"; return NDSPH_E_ARG; } } while (0)
+#define GUARD_N() do { if (npart < 0 || !p) { ctx->err = "bad npart or particles"; return NDSPH_E_ARG; } } while (0)
+
+// ---------------------------------------------------------------------------
+// drop-in entry points
+// ---------------------------------------------------------------------------
+extern "C" int ndsph_set_linklist(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts)
+{
+    GUARD_CTX(); GUARD_N();
+    int rc = upload_inputs(ctx, p, npart, false, false);
+    if (rc) return rc;
+    rc = link_all(ctx, false);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->last_dt.hhmax = ctx->cell_hmax;
+    fill_dt(ctx, dts);
+    return 0;
+}
+
+extern "C" int ndsph_iterate_density(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts)
+{
+    GUARD_CTX(); GUARD_N();
+    int rc = upload_inputs(ctx, p, npart, false, false);
+    if (rc) return rc;
+    rc = link_all(ctx, false);
+    if (rc) return rc;
+    launch_reduce_reset(ctx->red, ctx->st);
+    int its = 0, nct = 0, nrl = 0;
+    rc = do_iterate_density(ctx, &its, &nct, &nrl);
+    ctx->last_dt.its = its; ctx->last_dt.ncalctotal = nct; ctx->last_dt.nrelink = nrl;
+    ctx->last_dt.hhmax = bitsd(ctx->h_red->hmax_ghost);
+    if (rc) return rc;
+    const int n = ctx->n;
+    rc |= download_aos(ctx, p->hh, HH, 1, 1, n);
+    rc |= download_aos(ctx, p->rho, RHO, 1, 1, n);
+    rc |= download_aos(ctx, p->rhoalt, RHOALT, 1, 1, n);
+    rc |= download_aos(ctx, p->drhodt, DRHODT, 1, 1, n);
+    rc |= download_aos(ctx, p->dhdt, DHDT, 1, 1, n);
+    rc |= download_aos(ctx, p->gradh, GRADH, 1, 1, n);
+    rc |= download_aos(ctx, p->gradhn, GRADHN, 1, 1, n);
+    rc |= download_aos(ctx, p->gradgradh, GRADGRADH, 1, 1, n);
+    if (rc) return rc;
+    rc = download_int(ctx, p->numneigh, ctx->S.numneigh, n, false);
+    fill_dt(ctx, dts);
+    return rc;
+}
+
+extern "C" int ndsph_conservative2primitive(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart)
+{
+    GUARD_CTX(); GUARD_N();
+    int rc = upload_inputs(ctx, p, npart, true, false);
+    if (rc) return rc;
+    launch_iota(ctx->S.pos_of_id, npart, ctx->st);
+    rc = do_cons2prim(ctx);
+    if (rc) return rc;
+    rc = sync_red(ctx);
+    if (rc) return rc;
+    const int n = ctx->n;
+    // unsorted state: id = iota, so download maps identity
+    rc |= download_aos(ctx, p->dens, DENS, 1, 1, n);
+    rc |= download_aos(ctx, p->uu, UU, 1, 1, n);
+    rc |= download_aos(ctx, p->pr, PR, 1, 1, n);
+    rc |= download_aos(ctx, p->spsound, CS, 1, 1, n);
+    rc |= download_aos(ctx, p->Bfield, BF0, 3, 3, n);
+    return rc;
+}
+
+extern "C" int ndsph_get_rates(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts)
+{
+    GUARD_CTX(); GUARD_N();
+    int rc = upload_inputs(ctx, p, npart, true, true);
+    if (rc) return rc;
+    rc = link_all(ctx, false);
+    if (rc) return rc;
+    launch_reduce_reset(ctx->red, ctx->st);
+    // stressmax from the given B and P (the EOS pass recomputes them from
+    // Bevol, rho, en exactly as conservative2primitive does)
+    rc = do_cons2prim(ctx);
+    if (rc) return rc;
+    rc = do_rates(ctx);
+    if (rc) return rc;
+    const int n = ctx->n;
+    rc |= download_aos(ctx, p->force, F0, 3, 3, n);
+    rc |= download_aos(ctx, p->dBevoldt, DB0, 3, 3, n);
+    rc |= download_aos(ctx, p->dudt, DUDT, 1, 1, n);
+    rc |= download_aos(ctx, p->dendt, DENDT, 1, 1, n);
+    rc |= download_aos(ctx, p->daldt, DAL0, 3, 3, n);
+    rc |= download_aos(ctx, p->divB, DIVB, 1, 1, n);
+    rc |= download_aos(ctx, p->curlB, CB0, 3, 3, n);
+    rc |= download_aos(ctx, p->del2u, DEL2U, 1, 1, n);
+    rc |= download_aos(ctx, p->graddivv, GDV0, 3, 3, n);
+    rc |= download_aos(ctx, p->drhodt, DRHODT, 1, 1, n);
+    rc |= download_aos(ctx, p->dhdt, DHDT, 1, 1, n);
+    rc |= download_aos(ctx, p->pr, PR, 1, 1, n);
+    rc |= download_aos(ctx, p->spsound, CS, 1, 1, n);
+    rc |= download_aos(ctx, p->Bfield, BF0, 3, 3, n);
+    rc |= download_aos(ctx, p->dens, DENS, 1, 1, n);
+    rc |= download_aos(ctx, p->uu, UU, 1, 1, n);
+    fill_dt(ctx, dts);
+    return rc;
+}
+
+extern "C" int ndsph_derivs(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts)
+{
+    GUARD_CTX(); GUARD_N();
+    int rc = upload_inputs(ctx, p, npart, false, false);
+    if (rc) return rc;
+    rc = do_derivs(ctx, STATE_FIELDS, (int)(sizeof(STATE_FIELDS) / sizeof(int)));
+    if (rc) return rc;
+    rc = download_all(ctx, p);
+    fill_dt(ctx, dts);
+    return rc;
+}
+
+extern "C" int ndsph_primitive2conservative(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts)
+{
+    GUARD_CTX(); GUARD_N();
+    int rc = upload_inputs(ctx, p, npart, false, false);
+    if (rc) return rc;
+    const int n = ctx->n;
+    rc |= upload_aos(ctx, p->dens, DENS, 1, 1, n);
+    rc |= upload_aos(ctx, p->uu, UU, 1, 1, n);
+    rc |= upload_aos(ctx, p->Bfield, BF0, 3, 3, n);
+    if (rc) return rc;
+    launch_p2c_init(ctx->F, ctx->S, ctx->o, n, ctx->st);
+    // polyk from the first gas particle when iener = 0 (conservative2primitive.f90:511-528)
+    if (ctx->o.iener == 0) {
+        for (int i = 0; i < n; i++) {
+            if (p->itype[i] != NDSPH_ITYPE_GAS) continue;
+            double g1 = ctx->o.gamma - 1.;
+            ctx->o.polyk = (ctx->o.gamma <= 1.0001) ? 2. / 3. * p->uu[i] : g1 * p->uu[i] / pow(p->dens[i], g1);
+            ctx->opts.polyk = ctx->o.polyk;
+            break;
+        }
+    }
+    rc = link_all(ctx, false);
+    if (rc) return rc;
+    launch_reduce_reset(ctx->red, ctx->st);
+    int its = 0;
+    rc = do_iterate_density(ctx, &its, nullptr, nullptr);
+    if (rc) return rc;
+    launch_p2c_post(ctx->F, ctx->S, ctx->o, n, ctx->st);
+    rc = do_derivs(ctx, STATE_FIELDS, (int)(sizeof(STATE_FIELDS) / sizeof(int)));
+    if (rc) return rc;
+    ctx->time = 0.0;
+    ctx->dt = 0.0;
+    ctx->nsteps = 0;
+    rc = download_all(ctx, p);
+    fill_dt(ctx, dts);
+    return rc;
+}
+
+// one leapfrog step on the device state (stepND_leapfrog_mhd.f90:31-275)
+static int dev_step_once(ndsph_ctx* ctx)
+{
+    cudaStream_t st = ctx->st;
+    // dt lives in the Reduce block
+    CK(cudaMemcpyAsync(&ctx->red->dt, &ctx->dt, sizeof(double), cudaMemcpyHostToDevice, st));
+    launch_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+    std::vector<int> live;
+    for (int f : STATE_FIELDS) live.push_back(f);
+    for (int f : INCOPY_FIELDS) live.push_back(f);
+    int rc = do_derivs(ctx, live.data(), (int)live.size());
+    if (rc) return rc;
+    launch_corrector(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+    rc = sync_red(ctx);
+    if (rc) return rc;
+    ctx->time += ctx->dt;
+    ctx->dt = ctx->h_dtout[6];
+    ctx->nsteps++;
+    return 0;
+}
+
+extern "C" int ndsph_dev_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
+{
+    GUARD_CTX();
+    if (npart < 0 || !p) { ctx->err = "bad npart or particles"; return NDSPH_E_ARG; }
+    int rc = upload_inputs(ctx, p, npart, true, true);
+    if (rc) return rc;
+    const int n = ctx->n;
+    rc |= upload_aos(ctx, p->force, F0, 3, 3, n);
+    rc |= upload_aos(ctx, p->dBevoldt, DB0, 3, 3, n);
+    rc |= upload_aos(ctx, p->dendt, DENDT, 1, 1, n);
+    rc |= upload_aos(ctx, p->dudt, DUDT, 1, 1, n);
+    rc |= upload_aos(ctx, p->daldt, DAL0, 3, 3, n);
+    rc |= upload_aos(ctx, p->divB, DIVB, 1, 1, n);
+    rc |= upload_aos(ctx, p->curlB, CB0, 3, 3, n);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->d_istage, p->numneigh, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+    launch_int_to_slab(ctx->S.numneigh, ctx->d_istage, nullptr, n, ctx->st);
+    rc = link_all(ctx, false);
+    CK(cudaStreamSynchronize(ctx->st));
+    return rc;
+}
+
+extern "C" int ndsph_dev_download(ndsph_ctx* ctx, ndsph_particles* p, ndsph_dt* dts)
+{
+    GUARD_CTX();
+    if (!p) return NDSPH_E_ARG;
+    int rc = download_all(ctx, p);
+    fill_dt(ctx, dts);
+    return rc;
+}
+
+extern "C" int ndsph_dev_step(ndsph_ctx* ctx, int32_t nsteps, ndsph_dt* dts)
+{
+    GUARD_CTX();
+    for (int k = 0; k < nsteps; k++) {
+        tmark(ctx, 8);
+        int rc = dev_step_once(ctx);
+        tmark(ctx, 9);
+        if (rc) return rc;
+        if (ctx->profiling) {
+            cudaEventSynchronize(ctx->ev[9]);
+            ctx->timing.step_ms = tdiff(ctx, 8, 9);
+        }
+    }
+    fill_dt(ctx, dts);
+    return 0;
+}
+
+extern "C" int ndsph_dev_set_time(ndsph_ctx* ctx, double dt, double time, int32_t nsteps)
+{
+    GUARD_CTX();
+    ctx->dt = dt;
+    ctx->time = time;
+    ctx->nsteps = nsteps;
+    return 0;
+}
+
+extern "C" int ndsph_dev_derivs(ndsph_ctx* ctx, ndsph_dt* dts)
+{
+    GUARD_CTX();
+    int rc = do_derivs(ctx, STATE_FIELDS, (int)(sizeof(STATE_FIELDS) / sizeof(int)));
+    fill_dt(ctx, dts);
+    return rc;
+}
+
+extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts)
+{
+    GUARD_CTX(); GUARD_N();
+    int rc = ndsph_dev_upload(ctx, p, npart);
+    if (rc) return rc;
+    if (dts) { ctx->dt = dts->dt; ctx->time = dts->time; ctx->nsteps = dts->nsteps; }
+    rc = dev_step_once(ctx);
+    if (rc) return rc;
+    rc = download_all(ctx, p);
+    fill_dt(ctx, dts);
+    return rc;
+}
+
+extern "C" int ndsph_neighbour_csr(ndsph_ctx* ctx, int32_t mode, int64_t* offsets, int32_t* neigh, int64_t cap)
+{
+    GUARD_CTX();
+    if (!ctx->linked || !offsets) { ctx->err = "call ndsph_set_linklist first"; return NDSPH_E_ARG; }
+    const int n = ctx->n;
+    cudaStream_t st = ctx->st;
+    launch_h1(ctx->F, ctx->S, n, st);
+    SweepArgs a = sweep_args(ctx);
+    long long* d_cnt = nullptr;
+    CK(cudaMalloc(&d_cnt, sizeof(long long) * (size_t)(n + 1)));
+    launch_neigh_count(a, mode, d_cnt, st);
+    std::vector<long long> cnt(n);
+    CK(cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(long long) * (size_t)n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    int64_t tot = 0;
+    for (int i = 0; i < n; i++) { offsets[i] = tot; tot += cnt[i]; }
+    offsets[n] = tot;
+    if (tot > cap || !neigh) { cudaFree(d_cnt); ctx->err = "neighbour buffer too small"; return NDSPH_E_CAPACITY; }
+    CK(cudaMemcpyAsync(d_cnt, offsets, sizeof(long long) * (size_t)n, cudaMemcpyHostToDevice, st));
+    int* d_out = nullptr;
+    CK(cudaMalloc(&d_out, sizeof(int) * (size_t)std::max<int64_t>(tot, 1)));
+    launch_neigh_fill(a, mode, d_cnt, d_out, st);
+    CK(cudaMemcpyAsync(neigh, d_out, sizeof(int) * (size_t)tot, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    cudaFree(d_out);
+    cudaFree(d_cnt);
+    for (int64_t k = 0; k < tot; k++) neigh[k] += 1;
+    return 0;
+}
+
+extern "C" int ndsph_get_timing(ndsph_ctx* ctx, ndsph_timing* t)
+{
+    GUARD_CTX();
+    if (t) *t = ctx->timing;
+    return 0;
+}
+
+extern "C" int ndsph_set_profiling(ndsph_ctx* ctx, int32_t on)
+{
+    GUARD_CTX();
+    ctx->profiling = on != 0;
+    return 0;
+}

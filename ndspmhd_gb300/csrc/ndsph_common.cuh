@@ -1,0 +1,143 @@
+// ndsph_common.cuh -- device-side types shared by the hot-path kernels.
+//
+// Layout in HBM: one structure-of-arrays per particle field, in cell-sorted
+// order (particles of one cell are contiguous, cells in row-major key order).
+// Every per-particle double field lives in one slab `F` of NF*cap doubles so
+// the cell sort can permute all live fields with one gather kernel.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "../../include/ndsph.h"
+
+namespace ndsph {
+
+constexpr int IKERN = 4000;            // kernelND.f90:37
+constexpr int NTAB = IKERN + 1;
+
+// double fields of the device slab
+enum Field : int {
+    X0, X1, X2, V0, V1, V2, BE0, BE1, BE2, EN, HH, PM, AL0, AL1, AL2,
+    RHO, RHOALT, DRHODT, DHDT, GRADH, GRADHN, GRADGRADH,
+    DENS, UU, PR, CS, BF0, BF1, BF2,
+    F0, F1, F2, DB0, DB1, DB2, DUDT, DENDT, DAL0, DAL1, DAL2, DIVB, CB0, CB1, CB2, DEL2U,
+    GDV0, GDV1, GDV2,
+    // leapfrog saves (part_in module, stepND_leapfrog_mhd.f90:70-101)
+    XIN0, XIN1, XIN2, VIN0, VIN1, VIN2, BIN0, BIN1, BIN2, HIN, ENIN, RHOIN, ALIN0, ALIN1, ALIN2,
+    FIN0, FIN1, FIN2, DBIN0, DBIN1, DBIN2, DHIN, DENIN, DALIN0, DALIN1, DALIN2,
+    HDEN0,      // h at entry of iterate_density (hhin, iterate_density.f90:87)
+    HNEXT,      // NR scratch: next h of the first pass
+    NF
+};
+
+// options + derived constants, passed by value to kernels
+struct DevOpts {
+    int ndim;
+    int ibound[3];
+    int periodic[3];
+    double xmin[3], xmax[3], L[3];
+    double hfact, tolh, psep;
+    int maxdensits;
+    int imhd, imagforce, iener, iav, iavlim[3];
+    double alphamin, alphaumin, alphaBmin, beta, avdecayconst, avfact;
+    double gamma, polyk;
+    int idust, idrag_nature;
+    double Kdrag;
+    double C_cour, C_force;
+    int precision;
+    int has_fixed;      // any ibound == 1 (fixed particles with ireal copies)
+};
+
+// cell grid (periodic dims wrap, the others are padded bounding boxes)
+struct Grid {
+    int nc[3];          // cells per dim (1 for unused dims)
+    int ncells;
+    double origin[3];   // lower corner
+    double cs[3];       // cell size per dim (>= 2 hmax)
+    double inv_cs[3];
+    float csf[3];
+};
+
+// kernel tables: value and slope per entry, slope(i) = (t(i+1)-t(i))*ddq2table
+// exactly as interpolate_kernel* form it (kernelND.f90:4382-4391)
+struct Tables {
+    const double2* w;       // W(q2)
+    const double2* gw;      // dW/dq
+    const double2* ggw;     // d2W/dq2
+    const double2* wdrag;   // double-hump drag kernel
+    const float2* wf;       // FP32 copies for the FP32 form
+    const float2* gwf;
+    const float2* ggwf;
+    const float2* wdragf;
+    double dq2table, ddq2table;
+    float dq2tablef, ddq2tablef;
+};
+
+// global reductions written by the sweeps (int64 bit patterns of
+// non-negative doubles so integer atomics order them)
+struct Reduce {
+    unsigned long long dtcourant;   // min
+    unsigned long long dtav;        // min
+    unsigned long long vsigmax;     // max
+    unsigned long long ts_min;      // min
+    unsigned long long fhmax;       // max
+    unsigned long long stressmax;   // max
+    unsigned long long hmax;        // max
+    unsigned long long hmax_ghost;  // max h of the last (re)link
+    int ncalc;                      // unconverged count of the current pass
+    int redolink;                   // NR asked for a relink
+    int err;                        // first error code raised on the device
+    int err_index;
+    int nclumped;
+    int pad;
+    unsigned long long pairs;       // accepted pairs (diagnostic)
+    double dt, time;                // leapfrog dt/time (device-resident form)
+    unsigned long long xlo[3];      // order-preserving bits of min x (bounding box)
+    unsigned long long xhi[3];      // order-preserving bits of max x
+    double h_on_csts_max;
+};
+
+__host__ __device__ inline unsigned long long dbits(double v)
+{
+#ifdef __CUDA_ARCH__
+    return (unsigned long long)__double_as_longlong(v);
+#else
+    union { double d; unsigned long long u; } c; c.d = v; return c.u;
+#endif
+}
+__host__ __device__ inline double bitsd(unsigned long long u)
+{
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)u);
+#else
+    union { double d; unsigned long long u; } c; c.u = u; return c.d;
+#endif
+}
+
+inline double unord_bits(unsigned long long u)
+{
+    u = (u & 0x8000000000000000ull) ? (u & ~0x8000000000000000ull) : ~u;
+    union { double d; unsigned long long u; } c; c.u = u; return c.d;
+}
+
+#ifdef __CUDACC__
+__device__ inline void atomic_min_pos(unsigned long long* a, double v)
+{
+    if (v >= 0.0) atomicMin(a, dbits(v));
+}
+__device__ inline void atomic_max_pos(unsigned long long* a, double v)
+{
+    if (v >= 0.0) atomicMax(a, dbits(v));
+}
+// order-preserving map of any double to uint64 (for signed min/max atomics)
+__device__ inline unsigned long long ord_bits(double v)
+{
+    unsigned long long u = dbits(v);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ inline void raise_err(Reduce* r, int code, int idx)
+{
+    if (atomicCAS(&r->err, 0, code) == 0) r->err_index = idx;
+}
+#endif
+
+}  // namespace ndsph

@@ -1,0 +1,672 @@
+// ndsph_kernels.cu -- link (cell keys, counting sort by cell, permutation
+// gather), host-layout conversion, EOS, fixed-particle copies and leapfrog.
+//
+// All kernels are HBM-bound streaming passes over per-particle SoA arrays:
+// one thread per particle, grid = ceil(n/256) blocks (a multiple of the 152 SMs
+// for any n above ~40k), coalesced 8-byte loads and stores.
+#include <cstdio>
+#include <cmath>
+#include "ndsph_launch.h"
+
+namespace ndsph {
+
+static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+// ---------------------------------------------------------------------------
+// boundary boundaryND.f90:30-90: periodic wrap (x > xmax -> (xmin + x) - xmax,
+// x < xmin -> xmax - (xmin - x)); fixed particles are wrapped as well because
+// the reference loops over all npart.
+// ---------------------------------------------------------------------------
+__global__ void k_boundary_wrap(FieldPtrs F, DevOpts o, int n)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int d = 0; d < o.ndim; d++) {
+        if (o.ibound[d] != 3) continue;
+        double x = F.f[X0 + d][i];
+        if (x > o.xmax[d]) x = __dsub_rn(__dadd_rn(o.xmin[d], x), o.xmax[d]);
+        else if (x < o.xmin[d]) x = __dsub_rn(o.xmax[d], __dsub_rn(o.xmin[d], x));
+        F.f[X0 + d][i] = x;
+    }
+}
+void launch_boundary_wrap(FieldPtrs F, DevOpts o, int n, cudaStream_t st)
+{
+    if (n > 0) k_boundary_wrap<<<nblk(n, 256), 256, 0, st>>>(F, o, n);
+}
+
+// max h (bound module hhmax, linkND.f90:70 / ghostND_mhd.f90:77) and the
+// particle bounding box (linkND.f90:80-89) in one pass
+__global__ void k_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double h = (i < n) ? F.f[HH][i] : 0.0;
+    unsigned long long lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+        if (i < n && d < ndim) {
+            unsigned long long b = ord_bits(F.f[X0 + d][i]);
+            lo[d] = b; hi[d] = b;
+        } else {
+            lo[d] = ~0ull; hi[d] = 0ull;
+        }
+    }
+    // warp reduce
+    for (int off = 16; off > 0; off >>= 1) {
+        h = fmax(h, __shfl_down_sync(0xffffffffu, h, off));
+        for (int d = 0; d < 3; d++) {
+            unsigned long long a = __shfl_down_sync(0xffffffffu, lo[d], off);
+            unsigned long long b = __shfl_down_sync(0xffffffffu, hi[d], off);
+            lo[d] = a < lo[d] ? a : lo[d];
+            hi[d] = b > hi[d] ? b : hi[d];
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(dst, dbits(h));
+        for (int d = 0; d < ndim; d++) {
+            atomicMin(&red->xlo[d], lo[d]);
+            atomicMax(&red->xhi[d], hi[d]);
+        }
+    }
+}
+void launch_hmax(const double* h, int n, Reduce* red, unsigned long long* dst, cudaStream_t st)
+{
+    (void)h; (void)n; (void)red; (void)dst; (void)st;
+}
+void launch_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, cudaStream_t st)
+{
+    if (n > 0) k_hmax_bbox<<<nblk(n, 256), 256, 0, st>>>(F, ndim, n, red, dst);
+}
+
+// ---------------------------------------------------------------------------
+// cell keys + counting: key = (cz*ny + cy)*nx + cx, row-major like the
+// reference's icell (linkND.f90:127-135).  The atomic slot is made
+// deterministic afterwards by sorting each cell's segment by index.
+// ---------------------------------------------------------------------------
+__device__ inline int cell_coord(double x, double origin, double inv_cs, int nc)
+{
+    int c = (int)floor((x - origin) * inv_cs);
+    c = c < 0 ? 0 : c;
+    c = c >= nc ? nc - 1 : c;
+    return c;
+}
+
+__global__ void k_cell_key(FieldPtrs F, Grid g, int ndim, int n, SortScratch s)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c[3] = {0, 0, 0};
+    for (int d = 0; d < ndim; d++) c[d] = cell_coord(F.f[X0 + d][i], g.origin[d], g.inv_cs[d], g.nc[d]);
+    int key = (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
+    s.key[i] = key;
+    s.slot[i] = atomicAdd(&s.count[key], 1);
+}
+void launch_cell_key(FieldPtrs F, Grid g, DevOpts o, int n, SortScratch s, Reduce* red, cudaStream_t st)
+{
+    (void)red;
+    cudaMemsetAsync(s.count, 0, sizeof(int) * (size_t)g.ncells, st);
+    if (n > 0) k_cell_key<<<nblk(n, 256), 256, 0, st>>>(F, g, o.ndim, n, s);
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan of the cell counts (three passes: block sums, scan of the
+// block sums in one CTA, block-local scan plus offset)
+// ---------------------------------------------------------------------------
+constexpr int SCAN_BS = 1024;
+constexpr int SCAN_IPT = 4;
+constexpr int SCAN_TILE = SCAN_BS * SCAN_IPT;
+
+__device__ inline int block_exclusive_scan(int v, int* smem, int* total)
+{
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) smem[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int nw = blockDim.x >> 5;
+        int w = (lane < nw) ? smem[lane] : 0;
+        for (int off = 1; off < 32; off <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += y;
+        }
+        if (lane < nw) smem[lane] = w;
+    }
+    __syncthreads();
+    int base = (warp > 0) ? smem[warp - 1] : 0;
+    if (total) *total = smem[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return base + x - v;
+}
+
+__global__ void k_scan_blocksum(const int* in, int n, int* bsum)
+{
+    __shared__ int sm[32];
+    int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_IPT;
+    int s = 0;
+    for (int k = 0; k < SCAN_IPT; k++) s += (base + k < n) ? in[base + k] : 0;
+    int tot;
+    block_exclusive_scan(s, sm, &tot);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_bsum(int* bsum, int nb)
+{
+    __shared__ int sm[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int b0 = 0; b0 < nb; b0 += blockDim.x) {
+        int i = b0 + threadIdx.x;
+        int v = (i < nb) ? bsum[i] : 0;
+        int tot;
+        int ex = block_exclusive_scan(v, sm, &tot);
+        if (i < nb) bsum[i] = ex + carry;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+}
+
+__global__ void k_scan_final(const int* in, int n, const int* bsum, int* out)
+{
+    __shared__ int sm[32];
+    int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_IPT;
+    int v[SCAN_IPT];
+    int s = 0;
+    for (int k = 0; k < SCAN_IPT; k++) { v[k] = (base + k < n) ? in[base + k] : 0; s += v[k]; }
+    int ex = block_exclusive_scan(s, sm, nullptr) + bsum[blockIdx.x];
+    for (int k = 0; k < SCAN_IPT; k++) {
+        if (base + k < n) out[base + k] = ex;
+        ex += v[k];
+    }
+    // out[n] = total (written by the last block's last thread)
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[n] = ex;
+}
+
+void launch_scan(SortScratch s, int ncells, cudaStream_t st)
+{
+    int nb = nblk(ncells, SCAN_TILE);
+    k_scan_blocksum<<<nb, SCAN_BS, 0, st>>>(s.count, ncells, s.blocksums);
+    k_scan_bsum<<<1, SCAN_BS, 0, st>>>(s.blocksums, nb);
+    k_scan_final<<<nb, SCAN_BS, 0, st>>>(s.count, ncells, s.blocksums, s.start);
+}
+
+__global__ void k_scatter(SortScratch s, int n)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    s.perm[s.start[s.key[i]] + s.slot[i]] = i;
+}
+
+// per-cell insertion sort of the (previous-order) indices: deterministic order
+__global__ void k_cell_sort(SortScratch s, int ncells)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    int a = s.start[c], b = s.start[c + 1];
+    for (int k = a + 1; k < b; k++) {
+        int v = s.perm[k];
+        int m = k - 1;
+        while (m >= a && s.perm[m] > v) { s.perm[m + 1] = s.perm[m]; m--; }
+        s.perm[m + 1] = v;
+    }
+}
+
+void launch_scatter_sort(SortScratch s, int n, int ncells, cudaStream_t st)
+{
+    if (n > 0) k_scatter<<<nblk(n, 256), 256, 0, st>>>(s, n);
+    k_cell_sort<<<nblk(ncells, 128), 128, 0, st>>>(s, ncells);
+}
+
+// permutation gather of the live fields: dst[f][k] = src[f][perm[k]]
+__global__ void k_gather_fields(FieldPtrs dst, FieldPtrs src, const int* __restrict__ fields, int nfields,
+                                const int* __restrict__ perm, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int p = perm[k];
+    for (int q = 0; q < nfields; q++) {
+        int f = fields[q];
+        dst.f[f][k] = src.f[f][p];
+    }
+}
+void launch_gather_fields(FieldPtrs dst, FieldPtrs src, const int* fields, int nfields, const int* perm, int n,
+                          cudaStream_t st)
+{
+    if (n > 0) k_gather_fields<<<nblk(n, 256), 256, 0, st>>>(dst, src, fields, nfields, perm, n);
+}
+
+__global__ void k_gather_int(int* dst, const int* src, const int* perm, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[k] = src[perm[k]];
+}
+void launch_gather_int(int* dst, const int* src, const int* perm, int n, cudaStream_t st)
+{
+    if (n > 0) k_gather_int<<<nblk(n, 256), 256, 0, st>>>(dst, src, perm, n);
+}
+
+// after the gather: cell id per slot, inverse of id
+__global__ void k_post_sort(Side S, SortScratch s, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    S.cell[k] = s.key[s.perm[k]];
+    S.pos_of_id[S.id[k]] = k;
+}
+
+// FP32 position of each particle relative to its cell's lower corner, and h
+__global__ void k_xs(FieldPtrs F, Side S, Grid g, int ndim, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int c = S.cell[k];
+    int cc[3];
+    cc[0] = c % g.nc[0];
+    cc[1] = (c / g.nc[0]) % g.nc[1];
+    cc[2] = c / (g.nc[0] * g.nc[1]);
+    float r[3] = {0.f, 0.f, 0.f};
+    for (int d = 0; d < ndim; d++) r[d] = (float)(F.f[X0 + d][k] - (g.origin[d] + cc[d] * g.cs[d]));
+    S.xs[k] = make_float4(r[0], r[1], r[2], (float)F.f[HH][k]);
+}
+
+void launch_post_sort(Side S, SortScratch s, int n, int ncells, Grid g, FieldPtrs F, DevOpts o, cudaStream_t st)
+{
+    (void)ncells;
+    if (n > 0) k_post_sort<<<nblk(n, 256), 256, 0, st>>>(S, s, n);
+    if (n > 0) k_xs<<<nblk(n, 256), 256, 0, st>>>(F, S, g, o.ndim, n);
+}
+void launch_xs(FieldPtrs F, Side S, Grid g, DevOpts o, int n, cudaStream_t st)
+{
+    if (n > 0) k_xs<<<nblk(n, 256), 256, 0, st>>>(F, S, g, o.ndim, n);
+}
+
+// ---------------------------------------------------------------------------
+// host layout <-> slab
+// ---------------------------------------------------------------------------
+__global__ void k_aos_to_slab(FieldPtrs F, int f0, int ncomp, const double* __restrict__ aos, int stride,
+                             const int* __restrict__ id, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int src = id ? id[k] : k;
+    for (int c = 0; c < ncomp; c++) F.f[f0 + c][k] = aos[(size_t)src * stride + c];
+}
+void launch_aos_to_slab(FieldPtrs F, int f0, int ncomp, const double* aos, int stride, const int* id, int n,
+                        cudaStream_t st)
+{
+    if (n > 0) k_aos_to_slab<<<nblk(n, 256), 256, 0, st>>>(F, f0, ncomp, aos, stride, id, n);
+}
+
+__global__ void k_slab_to_aos(double* __restrict__ aos, int stride, FieldPtrs F, int f0, int ncomp,
+                              const int* __restrict__ id, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int dst = id ? id[k] : k;
+    for (int c = 0; c < ncomp; c++) aos[(size_t)dst * stride + c] = F.f[f0 + c][k];
+}
+void launch_slab_to_aos(double* aos, int stride, FieldPtrs F, int f0, int ncomp, const int* id, int n,
+                        cudaStream_t st)
+{
+    if (n > 0) k_slab_to_aos<<<nblk(n, 256), 256, 0, st>>>(aos, stride, F, f0, ncomp, id, n);
+}
+
+__global__ void k_int_to_slab(int* dst, const int* src, const int* id, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[k] = src[id ? id[k] : k];
+}
+void launch_int_to_slab(int* dst, const int* src, const int* id, int n, cudaStream_t st)
+{
+    if (n > 0) k_int_to_slab<<<nblk(n, 256), 256, 0, st>>>(dst, src, id, n);
+}
+__global__ void k_slab_to_int(int* dst, const int* src, const int* id, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[id ? id[k] : k] = src[k];
+}
+void launch_slab_to_int(int* dst, const int* src, const int* id, int n, cudaStream_t st)
+{
+    if (n > 0) k_slab_to_int<<<nblk(n, 256), 256, 0, st>>>(dst, src, id, n);
+}
+__global__ void k_iota(int* a, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) a[k] = k;
+}
+void launch_iota(int* a, int n, cudaStream_t st)
+{
+    if (n > 0) k_iota<<<nblk(n, 256), 256, 0, st>>>(a, n);
+}
+__global__ void k_fill(double* a, double v, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) a[k] = v;
+}
+void launch_fill(double* a, double v, int n, cudaStream_t st)
+{
+    if (n > 0) k_fill<<<nblk(n, 256), 256, 0, st>>>(a, v, n);
+}
+__global__ void k_copy(double* dst, const double* src, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[k] = src[k];
+}
+void launch_copy(double* dst, const double* src, int n, cudaStream_t st)
+{
+    if (n > 0) k_copy<<<nblk(n, 256), 256, 0, st>>>(dst, src, n);
+}
+
+// ---------------------------------------------------------------------------
+// density pass set-up
+// ---------------------------------------------------------------------------
+__global__ void k_h1(FieldPtrs F, Side S, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double h = F.f[HH][k];
+    S.h1[k] = 1.0 / h;
+    float4 x = S.xs[k];
+    x.w = (float)h;
+    S.xs[k] = x;
+}
+void launch_h1(FieldPtrs F, Side S, int n, cudaStream_t st)
+{
+    if (n > 0) k_h1<<<nblk(n, 256), 256, 0, st>>>(F, S, n);
+}
+
+// iterate_density.f90:79-86 (zero gradh.. on non-fixed particles) and
+// hhin = hh (:87); h <= 0 check (:99-102)
+__global__ void k_density_init(FieldPtrs F, Side S, int n, Reduce* red)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    if (S.itype[k] != NDSPH_ITYPE_BND) {
+        F.f[GRADH][k] = 0.0; F.f[GRADHN][k] = 0.0; F.f[GRADGRADH][k] = 0.0;
+        F.f[DRHODT][k] = 0.0; F.f[DHDT][k] = 0.0;
+    }
+    double h = F.f[HH][k];
+    F.f[HNEXT][k] = h;
+    F.f[HDEN0][k] = h;
+    if (!(h > 2.2250738585072014e-308)) raise_err(red, NDSPH_E_H_NONPOS, S.id[k]);
+}
+void launch_density_init(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st)
+{
+    (void)o; (void)F; (void)S; (void)n; (void)st;
+}
+void launch_density_init2(FieldPtrs F, Side S, int n, Reduce* red, cudaStream_t st)
+{
+    if (n > 0) k_density_init<<<nblk(n, 256), 256, 0, st>>>(F, S, n, red);
+}
+
+// fixed particles take rho.. from their source after each NR pass
+// (iterate_density.f90:312-328)
+__global__ void k_fixed_density_copy(FieldPtrs F, Side S, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    if (S.itype[k] != NDSPH_ITYPE_BND) return;
+    int src_id = S.ireal[k];
+    if (src_id < 0) return;
+    int j = S.pos_of_id[src_id];
+    const int fl[7] = {RHO, RHOALT, DRHODT, DHDT, HH, GRADH, GRADHN};
+    for (int q = 0; q < 7; q++) F.f[fl[q]][k] = F.f[fl[q]][j];
+}
+void launch_fixed_density_copy(FieldPtrs F, Side S, int n, cudaStream_t st)
+{
+    if (n > 0) k_fixed_density_copy<<<nblk(n, 256), 256, 0, st>>>(F, S, n);
+}
+
+// ---------------------------------------------------------------------------
+// conservative2primitive (in-scope part) + equation_of_state eos.f90:40-106;
+// also the stressmax reduction of get_rates (ratesND_mhd.f90:232-245)
+// ---------------------------------------------------------------------------
+__global__ void k_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double st = 0.0;
+    if (k < n) {
+        double rho = F.f[RHO][k];
+        F.f[DENS][k] = rho;
+        double B[3] = {0.0, 0.0, 0.0};
+        if (o.imhd >= 11) {
+            for (int d = 0; d < 3; d++) B[d] = F.f[BE0 + d][k];
+        } else if (o.imhd >= 1 && o.imhd <= 9) {
+            for (int d = 0; d < 3; d++) B[d] = F.f[BE0 + d][k] * rho;
+        }
+        if (o.imhd != 0)
+            for (int d = 0; d < 3; d++) F.f[BF0 + d][k] = B[d];
+        double uu = F.f[EN][k];
+        double pr = F.f[PR][k], cs = F.f[CS][k];
+        int it = S.itype[k];
+        if (o.iener == 0) {
+            if (rho > 0.0 && it == NDSPH_ITYPE_GAS) {
+                pr = o.polyk * pow(rho, o.gamma);
+                cs = sqrt(o.gamma * pr / rho);
+            } else if (it != NDSPH_ITYPE_BND) {
+                pr = 0.0;
+            }
+            if (fabs(o.gamma - 1.0) > 1.e-3 && rho > 0.0) uu = pr / ((o.gamma - 1.0) * rho);
+        } else {
+            if (rho > 0.0) {
+                pr = (o.gamma - 1.0) * uu * rho;
+                cs = sqrt(o.gamma * pr / rho);
+            }
+        }
+        F.f[UU][k] = uu;
+        F.f[PR][k] = pr;
+        F.f[CS][k] = cs;
+        if (o.imhd != 0 && o.imagforce == 2) {
+            double B2 = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+            st = fmax(0.5 * B2 - pr, 0.0);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) st = fmax(st, __shfl_down_sync(0xffffffffu, st, off));
+    if ((threadIdx.x & 31) == 0 && st > 0.0) atomic_max_pos(&red->stressmax, st);
+}
+void launch_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st)
+{
+    if (n > 0) k_eos<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+}
+
+// copy_particle copy_particle.f90:28-80 for fixed particles
+// (conservative2primitive.f90:430-441): everything but x and vel
+__global__ void k_fixed_copy(FieldPtrs F, Side S, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    if (S.itype[k] != NDSPH_ITYPE_BND && S.itype[k] != NDSPH_ITYPE_BNDDUST) return;
+    int src_id = S.ireal[k];
+    if (src_id < 0) return;
+    int j = S.pos_of_id[src_id];
+    const int fl[] = {PM, RHO, RHOALT, HH, UU, EN, BE0, BE1, BE2, BF0, BF1, BF2, AL0, AL1, AL2, GRADH, GRADHN,
+                      GRADGRADH, CS, PR, DENS, F0, F1, F2, DRHODT, DUDT, DENDT, DB0, DB1, DB2, DHDT, DAL0, DAL1,
+                      DAL2, DIVB, CB0, CB1, CB2};
+    for (unsigned q = 0; q < sizeof(fl) / sizeof(fl[0]); q++) F.f[fl[q]][k] = F.f[fl[q]][j];
+}
+void launch_fixed_copy(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st)
+{
+    if (o.has_fixed && n > 0) k_fixed_copy<<<nblk(n, 256), 256, 0, st>>>(F, S, n);
+}
+
+// ---------------------------------------------------------------------------
+// leapfrog stepND_leapfrog_mhd.f90:31-275
+// ---------------------------------------------------------------------------
+__global__ void k_predictor(FieldPtrs F, Side S, DevOpts o, int n, const Reduce* red)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double dt = red->dt;
+    // save (:70-101)
+    for (int d = 0; d < o.ndim; d++) F.f[XIN0 + d][i] = F.f[X0 + d][i];
+    for (int d = 0; d < 3; d++) {
+        F.f[VIN0 + d][i] = F.f[V0 + d][i];
+        F.f[BIN0 + d][i] = F.f[BE0 + d][i];
+        F.f[ALIN0 + d][i] = F.f[AL0 + d][i];
+        F.f[FIN0 + d][i] = F.f[F0 + d][i];
+        F.f[DBIN0 + d][i] = F.f[DB0 + d][i];
+        F.f[DALIN0 + d][i] = F.f[DAL0 + d][i];
+    }
+    F.f[HIN][i] = F.f[HH][i];
+    F.f[ENIN][i] = F.f[EN][i];
+    F.f[RHOIN][i] = F.f[RHO][i];
+    F.f[DHIN][i] = F.f[DHDT][i];
+    F.f[DENIN][i] = F.f[DENDT][i];
+}
+
+__global__ void k_predictor2(FieldPtrs F, Side S, DevOpts o, int n, const Reduce* red)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double dt = red->dt;
+    int t = S.itype[i];
+    if (t == NDSPH_ITYPE_BND || t == NDSPH_ITYPE_BNDDUST) {
+        int j = (S.ireal[i] >= 0) ? S.pos_of_id[S.ireal[i]] : i;
+        for (int d = 0; d < o.ndim; d++)
+            F.f[X0 + d][i] = F.f[XIN0 + d][i] + dt * F.f[VIN0 + d][j] + 0.5 * dt * dt * F.f[FIN0 + d][j];
+        for (int d = 0; d < 3; d++) F.f[BE0 + d][i] = F.f[BIN0 + d][i];
+        F.f[RHO][i] = F.f[RHOIN][i];
+        F.f[HH][i] = F.f[HIN][i];
+        F.f[EN][i] = F.f[ENIN][i];
+        for (int d = 0; d < 3; d++) F.f[AL0 + d][i] = F.f[ALIN0 + d][i];
+    } else {
+        for (int d = 0; d < o.ndim; d++)
+            F.f[X0 + d][i] = F.f[XIN0 + d][i] + dt * F.f[VIN0 + d][i] + 0.5 * dt * dt * F.f[FIN0 + d][i];
+        for (int d = 0; d < 3; d++) F.f[V0 + d][i] = (F.f[VIN0 + d][i] + dt * F.f[FIN0 + d][i]) / (1.0 + 0.0);
+        if (o.imhd != 0)
+            for (int d = 0; d < 3; d++) F.f[BE0 + d][i] = F.f[BIN0 + d][i] + dt * F.f[DBIN0 + d][i];
+        F.f[HH][i] = F.f[HIN][i] + dt * F.f[DHIN][i];
+        if (o.iener != 0) F.f[EN][i] = F.f[ENIN][i] + dt * F.f[DENIN][i];
+        for (int d = 0; d < 3; d++)
+            if (o.iavlim[d] != 0) F.f[AL0 + d][i] = fmin(F.f[ALIN0 + d][i] + dt * F.f[DALIN0 + d][i], 1.0);
+    }
+}
+void launch_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st)
+{
+    if (n <= 0) return;
+    k_predictor<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+    k_predictor2<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+}
+
+__global__ void k_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double dt = red->dt;
+    const double hdt = 0.5 * dt;
+    int t = S.itype[i];
+    if (t == NDSPH_ITYPE_BND || t == NDSPH_ITYPE_BNDDUST) {
+        for (int d = 0; d < 3; d++) F.f[V0 + d][i] = F.f[VIN0 + d][i];
+        for (int d = 0; d < 3; d++) F.f[BE0 + d][i] = F.f[BIN0 + d][i];
+        F.f[RHO][i] = F.f[RHOIN][i];
+        F.f[HH][i] = F.f[HIN][i];
+        F.f[EN][i] = F.f[ENIN][i];
+        for (int d = 0; d < 3; d++) F.f[AL0 + d][i] = F.f[ALIN0 + d][i];
+    } else {
+        for (int d = 0; d < 3; d++)
+            F.f[V0 + d][i] = (F.f[VIN0 + d][i] + hdt * (F.f[F0 + d][i] + F.f[FIN0 + d][i])) / (1.0 + 0.0);
+        if (o.imhd != 0)
+            for (int d = 0; d < 3; d++)
+                F.f[BE0 + d][i] = F.f[BIN0 + d][i] + hdt * (F.f[DB0 + d][i] + F.f[DBIN0 + d][i]);
+        double h = F.f[HIN][i] + hdt * (F.f[DHDT][i] + F.f[DHIN][i]);
+        F.f[HH][i] = h;
+        if (!(h > 0.0)) raise_err(red, NDSPH_E_H_NONPOS, S.id[i]);
+        if (o.iener != 0) F.f[EN][i] = F.f[ENIN][i] + hdt * (F.f[DENDT][i] + F.f[DENIN][i]);
+        for (int d = 0; d < 3; d++)
+            if (o.iavlim[d] != 0)
+                F.f[AL0 + d][i] = fmin(F.f[ALIN0 + d][i] + hdt * (F.f[DAL0 + d][i] + F.f[DALIN0 + d][i]), 1.0);
+    }
+    // boundary after the corrector (:221)
+    for (int d = 0; d < o.ndim; d++) {
+        if (o.ibound[d] != 3) continue;
+        double x = F.f[X0 + d][i];
+        if (x > o.xmax[d]) x = __dsub_rn(__dadd_rn(o.xmin[d], x), o.xmax[d]);
+        else if (x < o.xmin[d]) x = __dsub_rn(o.xmax[d], __dsub_rn(o.xmin[d], x));
+        F.f[X0 + d][i] = x;
+    }
+}
+void launch_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st)
+{
+    if (n > 0) k_corrector<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+}
+
+// dt = min(C_force*dtforce, C_cour*dtcourant, 0.9*dtdrag, C_force*dtvisc)
+// (stepND_leapfrog_mhd.f90:252); out = {dtcourant, dtforce, dtav, dtdrag,
+// vsigmax, stressmax, dtnext}
+__global__ void k_finalize_dt(Reduce* red, DevOpts o, double* out)
+{
+    double dtcourant = bitsd(red->dtcourant);
+    double dtav = bitsd(red->dtav);
+    double fhmax = bitsd(red->fhmax);
+    double dtforce = 1.7976931348623157e308;
+    if (fhmax > 0.0) dtforce = fmin(dtforce, sqrt(1.0 / fhmax));
+    double dtdrag = 1.7976931348623157e308;
+    if (o.idust == 2 && o.idrag_nature != 0 && (o.Kdrag > 0.0 || o.idrag_nature > 1))
+        dtdrag = fmin(dtdrag, bitsd(red->ts_min));
+    double dtvisc = 1.7976931348623157e308;
+    double dtn = o.C_force * dtforce;
+    dtn = fmin(dtn, o.C_cour * dtcourant);
+    dtn = fmin(dtn, 0.9 * dtdrag);
+    dtn = fmin(dtn, o.C_force * dtvisc);
+    out[0] = dtcourant; out[1] = dtforce; out[2] = dtav; out[3] = dtdrag;
+    out[4] = bitsd(red->vsigmax); out[5] = bitsd(red->stressmax); out[6] = dtn;
+}
+void launch_finalize_dt(Reduce* red, DevOpts o, double* out, cudaStream_t st)
+{
+    k_finalize_dt<<<1, 1, 0, st>>>(red, o, out);
+}
+
+__global__ void k_reduce_reset(Reduce* red)
+{
+    red->dtcourant = dbits(1.e6);
+    red->dtav = dbits(1.7976931348623157e308);
+    red->vsigmax = 0ull;
+    red->ts_min = dbits(1.7976931348623157e308);
+    red->fhmax = 0ull;
+    red->stressmax = 0ull;
+    red->pairs = 0ull;
+    red->nclumped = 0;
+}
+void launch_reduce_reset(Reduce* red, cudaStream_t st)
+{
+    k_reduce_reset<<<1, 1, 0, st>>>(red);
+}
+
+// primitive2conservative (conservative2primitive.f90:488-509): rho = dens,
+// h = hfact*(m/rho)^(1/ndim)
+__global__ void k_p2c_init(FieldPtrs F, DevOpts o, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double rho = F.f[DENS][k];
+    F.f[RHO][k] = rho;
+    F.f[HH][k] = o.hfact * pow(F.f[PM][k] / (rho + 0.0), 1.0 / o.ndim);
+}
+void launch_p2c_init(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st)
+{
+    (void)S;
+    if (n > 0) k_p2c_init<<<nblk(n, 256), 256, 0, st>>>(F, o, n);
+}
+// after the density iteration: Bevol from Bfield (:608-619), en = uu (:743)
+__global__ void k_p2c_post(FieldPtrs F, DevOpts o, int n)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double rho = F.f[RHO][k];
+    if (o.imhd >= 11) {
+        for (int d = 0; d < 3; d++) F.f[BE0 + d][k] = F.f[BF0 + d][k];
+    } else if (o.imhd >= 1 && o.imhd <= 9) {
+        for (int d = 0; d < 3; d++) F.f[BE0 + d][k] = F.f[BF0 + d][k] / rho;
+    }
+    F.f[EN][k] = F.f[UU][k];
+}
+void launch_p2c_post(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st)
+{
+    (void)S;
+    if (n > 0) k_p2c_post<<<nblk(n, 256), 256, 0, st>>>(F, o, n);
+}
+
+}  // namespace ndsph

@@ -1,0 +1,97 @@
+// ndsph_launch.h -- host-side launch wrappers of the device kernels.
+#pragma once
+#include "ndsph_common.cuh"
+
+namespace ndsph {
+
+// pointer table of the field slab (passed by value to kernels)
+struct FieldPtrs {
+    double* f[NF];
+};
+
+// per-particle int / float side arrays (sorted order unless noted)
+struct Side {
+    int* itype;       // particle type
+    int* id;          // original (host) index of the particle in this slot
+    int* ireal;       // original index of the source particle of a fixed particle (-1 none)
+    int* pos_of_id;   // inverse of id
+    int* numneigh;
+    int* cell;        // cell id of the slot
+    float4* xs;       // FP32 cell-relative position + h (screen / FP32 form)
+    double* h1;       // 1/h of the pass
+    int* active;      // NR active list (current pass)
+    int* active_next; // NR active list (next pass)
+    int* flag;        // NR converged flag scratch
+};
+
+struct SortScratch {
+    int* key;         // cell id per particle (unsorted order)
+    int* slot;        // rank inside the cell from the atomic count
+    int* count;       // per-cell counts (ncells)
+    int* start;       // exclusive scan (ncells + 1)
+    int* perm;        // sorted slot -> unsorted index
+    int* blocksums;   // scan scratch
+    int cap_cells;
+    int cap_blocks;
+};
+
+struct SweepArgs {
+    FieldPtrs F;
+    Side S;
+    const int* cell_start;   // ncells + 1
+    Grid g;
+    DevOpts o;
+    Tables t;
+    Reduce* red;
+    int n;
+    int its;                 // NR pass number (1-based)
+    int nlist;               // partial pass: entries in S.active
+    int* ncalc_next;         // partial: counter of the next active list
+};
+
+// ---- link / sort (ndsph_kernels.cu) ------------------------------------------
+void launch_boundary_wrap(FieldPtrs F, DevOpts o, int n, cudaStream_t st);
+void launch_hmax(const double* h, int n, Reduce* red, unsigned long long* dst, cudaStream_t st);
+void launch_cell_key(FieldPtrs F, Grid g, DevOpts o, int n, SortScratch s, Reduce* red, cudaStream_t st);
+void launch_scan(SortScratch s, int ncells, cudaStream_t st);
+void launch_scatter_sort(SortScratch s, int n, int ncells, cudaStream_t st);
+void launch_gather_fields(FieldPtrs dst, FieldPtrs src, const int* fields, int nfields, const int* perm,
+                          int n, cudaStream_t st);
+void launch_gather_int(int* dst, const int* src, const int* perm, int n, cudaStream_t st);
+void launch_post_sort(Side S, SortScratch s, int n, int ncells, Grid g, FieldPtrs F, DevOpts o,
+                      cudaStream_t st);
+void launch_xs(FieldPtrs F, Side S, Grid g, DevOpts o, int n, cudaStream_t st);
+
+// ---- host layout <-> device slab ------------------------------------------
+// AoS host-layout staging buffer (one field: stride comps) -> sorted slab fields
+void launch_aos_to_slab(FieldPtrs F, int f0, int ncomp, const double* aos, int stride, const int* id, int n,
+                        cudaStream_t st);
+void launch_slab_to_aos(double* aos, int stride, FieldPtrs F, int f0, int ncomp, const int* id, int n,
+                        cudaStream_t st);
+void launch_int_to_slab(int* dst, const int* src, const int* id, int n, cudaStream_t st);
+void launch_slab_to_int(int* dst, const int* src, const int* id, int n, cudaStream_t st);
+void launch_iota(int* a, int n, cudaStream_t st);
+void launch_fill(double* a, double v, int n, cudaStream_t st);
+void launch_copy(double* dst, const double* src, int n, cudaStream_t st);
+
+// ---- per-particle physics (ndsph_kernels.cu) --------------------------------
+void launch_h1(FieldPtrs F, Side S, int n, cudaStream_t st);
+void launch_density_init(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
+void launch_fixed_density_copy(FieldPtrs F, Side S, int n, cudaStream_t st);
+void launch_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st);
+void launch_fixed_copy(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
+void launch_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st);
+void launch_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st);
+void launch_finalize_dt(Reduce* red, DevOpts o, double* out, cudaStream_t st);
+void launch_reduce_reset(Reduce* red, cudaStream_t st);
+void launch_p2c_init(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
+void launch_p2c_post(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
+
+// ---- sweeps (ndsph_sweeps.cu) --------------------------------------------
+void launch_density(const SweepArgs& a, bool full, cudaStream_t st);
+void launch_rates(const SweepArgs& a, cudaStream_t st);
+// neighbour CSR for parity tests: counts (mode) then fill
+void launch_neigh_count(const SweepArgs& a, int mode, long long* counts, cudaStream_t st);
+void launch_neigh_fill(const SweepArgs& a, int mode, const long long* offsets, int* out, cudaStream_t st);
+
+}  // namespace ndsph

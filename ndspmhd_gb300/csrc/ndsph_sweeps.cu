@@ -1,0 +1,883 @@
+// ndsph_sweeps.cu -- the two O(N n_neigh) pair sweeps of the hot path.
+//
+//  k_density<NDIM, FULL, PREC>: density (density_sums.f90:38-379) as a gather
+//    when FULL (first NR pass: union criterion q_i<2 or q_j<2 for numneigh),
+//    density_partial (:396-658) otherwise (q_i<2 over the active list), with
+//    the Newton-Raphson update of iterate_density.f90:163-278 fused as the
+//    per-particle epilogue.
+//  k_rates<NDIM, PREC>: get_rates (ratesND_mhd.f90:29-979) as a gather over
+//    every pair with q_i<2 or q_j<2: rates_core (:1175-1690),
+//    artificial_dissipation (:1700-1894), mhd_terms (:2377-2720),
+//    drag_forces (:1074-1169); the per-particle post pass (:532-965) is the
+//    epilogue.
+//
+// The reference scatters each unordered pair to both particles; here every
+// particle gathers its own side of every pair (H6 in the design notes), so no
+// atomics touch per-particle sums and results are deterministic.  The
+// j-side formulas of the reference equal the i-side formulas evaluated from
+// j's point of view (checked term by term in the design notes), so the
+// gather is the same sum in a different order.
+//
+// Neighbour search: particle slots are cell-sorted; each thread walks the
+// 3^NDIM stencil of its own cell.  Candidates are screened in FP32 with a
+// conservative margin on cell-relative coordinates; in the FP64 form the
+// survivors are re-tested exactly in FP64 with the reference's own rounding
+// (dx = x_i - x_j' with periodic images placed as ghostND_mhd.f90:224-225
+// places ghosts, rij2 = dx.dx without FMA, q2 = rij2*h^-2), so the neighbour
+// sets match the reference bit for bit.
+#include <cstdio>
+#include <type_traits>
+#include "ndsph_launch.h"
+
+namespace ndsph {
+
+static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+__device__ __forceinline__ bool type_match(int ti, int tj)
+{
+    return (tj == ti) || (ti == NDSPH_ITYPE_GAS && tj == NDSPH_ITYPE_BND) ||
+           (tj == NDSPH_ITYPE_GAS && ti == NDSPH_ITYPE_BND) ||
+           (ti == NDSPH_ITYPE_DUST && tj == NDSPH_ITYPE_BNDDUST) ||
+           (tj == NDSPH_ITYPE_DUST && ti == NDSPH_ITYPE_BNDDUST);
+}
+
+// interpolate_kernel* index logic (kernelND.f90:4382-4391) in FP64:
+// index = int(q2*ddq2table) clamped to ikern, value + slope*(q2 - index*dq2table)
+struct TabIdx {
+    int i0;
+    double dxx;
+};
+__device__ __forceinline__ TabIdx tab_index(const Tables& t, double q2)
+{
+    int idx = (int)__dmul_rn(q2, t.ddq2table);
+    if (idx > IKERN || idx < 0) idx = IKERN;
+    TabIdx r;
+    r.i0 = idx;
+    r.dxx = __dsub_rn(q2, __dmul_rn((double)idx, t.dq2table));
+    return r;
+}
+__device__ __forceinline__ double tab_val(const double2* tab, const TabIdx& ix)
+{
+    double2 e = __ldg(&tab[ix.i0]);
+    return e.x + e.y * ix.dxx;
+}
+struct TabIdxF {
+    int i0;
+    float dxx;
+};
+__device__ __forceinline__ TabIdxF tab_indexf(const Tables& t, float q2)
+{
+    int idx = (int)(q2 * t.ddq2tablef);
+    if (idx > IKERN || idx < 0) idx = IKERN;
+    TabIdxF r;
+    r.i0 = idx;
+    r.dxx = q2 - (float)idx * t.dq2tablef;
+    return r;
+}
+__device__ __forceinline__ float tab_valf(const float2* tab, const TabIdxF& ix)
+{
+    float2 e = __ldg(&tab[ix.i0]);
+    return fmaf(e.y, ix.dxx, e.x);
+}
+
+// stencil cell with periodic wrap; returns false if outside (open dims)
+template <int NDIM>
+struct Stencil {
+    int cc[3];
+    __device__ Stencil(int cell, const Grid& g)
+    {
+        cc[0] = cell % g.nc[0];
+        cc[1] = (cell / g.nc[0]) % g.nc[1];
+        cc[2] = cell / (g.nc[0] * g.nc[1]);
+    }
+    // offset index o in [0, 3^NDIM): d = (o%3-1, (o/3)%3-1, o/9-1)
+    __device__ __forceinline__ bool cell_at(int o, const Grid& g, const DevOpts& op, int& cid, int d[3],
+                                            int w[3]) const
+    {
+        int c[3];
+        d[0] = o % 3 - 1;
+        d[1] = (NDIM >= 2) ? (o / 3) % 3 - 1 : 0;
+        d[2] = (NDIM >= 3) ? o / 9 - 1 : 0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            w[k] = 0;
+            c[k] = cc[k] + d[k];
+            if (k < NDIM) {
+                if (c[k] < 0) {
+                    if (!op.periodic[k]) return false;
+                    c[k] += g.nc[k];
+                    w[k] = -1;
+                } else if (c[k] >= g.nc[k]) {
+                    if (!op.periodic[k]) return false;
+                    c[k] -= g.nc[k];
+                    w[k] = 1;
+                }
+            }
+        }
+        cid = (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
+        return true;
+    }
+};
+
+// periodic image of x_j as the reference's ghost would place it, and the
+// ghost-existence test (0 < distance-to-boundary < radkern*hhmax,
+// ghostND_mhd.f90:218).  w = +1: image beyond xmax, w = -1: below xmin.
+__device__ __forceinline__ bool image_coord(double xj, int w, int d, const DevOpts& o, double dxbound,
+                                            double& xim)
+{
+    if (w == 0) { xim = xj; return true; }
+    if (w > 0) {
+        double dist = __dsub_rn(xj, o.xmin[d]);
+        xim = __dadd_rn(o.xmax[d], dist);
+        return (dist < dxbound) && (dist > 0.0);
+    }
+    double dist = __dsub_rn(o.xmax[d], xj);
+    xim = __dadd_rn(o.xmin[d], __dsub_rn(xj, o.xmax[d]));
+    return (dist < dxbound) && (dist > 0.0);
+}
+
+// exact FP64 separation and rij2 for slot j seen from x_i
+template <int NDIM>
+__device__ __forceinline__ bool exact_dx(const FieldPtrs& F, int j, const double xi[3], const int w[3],
+                                         const DevOpts& o, double dxbound, double dx[3], double& rij2)
+{
+    bool exists = true;
+#pragma unroll
+    for (int d = 0; d < 3; d++) dx[d] = 0.0;
+#pragma unroll
+    for (int d = 0; d < NDIM; d++) {
+        double xim;
+        exists &= image_coord(F.f[X0 + d][j], w[d], d, o, dxbound, xim);
+        dx[d] = __dsub_rn(xi[d], xim);
+    }
+    double r = __dmul_rn(dx[0], dx[0]);
+    if (NDIM >= 2) r = __dadd_rn(r, __dmul_rn(dx[1], dx[1]));
+    if (NDIM >= 3) r = __dadd_rn(r, __dmul_rn(dx[2], dx[2]));
+    rij2 = r;
+    return exists;
+}
+
+// FP32 screen on cell-relative coordinates
+template <int NDIM>
+__device__ __forceinline__ float screen_r2(const float4& xsi, const float4& xsj, const int d[3], const Grid& g,
+                                           float dxf[3])
+{
+    dxf[0] = (xsi.x - xsj.x) - (float)d[0] * g.csf[0];
+    dxf[1] = (NDIM >= 2) ? (xsi.y - xsj.y) - (float)d[1] * g.csf[1] : 0.f;
+    dxf[2] = (NDIM >= 3) ? (xsi.z - xsj.z) - (float)d[2] * g.csf[2] : 0.f;
+    return dxf[0] * dxf[0] + dxf[1] * dxf[1] + dxf[2] * dxf[2];
+}
+
+// compensated FP32 accumulator (Neumaier)
+struct KSum {
+    float s, c;
+    __device__ KSum() : s(0.f), c(0.f) {}
+    __device__ __forceinline__ void add(float v)
+    {
+        float t = s + v;
+        if (fabsf(s) >= fabsf(v)) c += (s - t) + v;
+        else c += (v - t) + s;
+        s = t;
+    }
+    __device__ __forceinline__ double val() const { return (double)s + (double)c; }
+};
+
+// ===========================================================================
+// density + Newton-Raphson
+// ===========================================================================
+template <int NDIM, bool FULL, int PREC>
+__global__ void __launch_bounds__(128) k_density(SweepArgs a)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int i;
+    if (FULL) {
+        if (t >= a.n) return;
+        i = t;
+    } else {
+        if (t >= a.nlist) return;
+        i = a.S.active[t];
+    }
+    const FieldPtrs& F = a.F;
+    const DevOpts& o = a.o;
+    const Grid& g = a.g;
+    const int typei = a.S.itype[i];
+    const bool fixed_i = (typei == NDSPH_ITYPE_BND || typei == NDSPH_ITYPE_BNDDUST);
+    if (!FULL && typei == NDSPH_ITYPE_BND) return;
+    double xi[3] = {0.0, 0.0, 0.0}, vi[3];
+#pragma unroll
+    for (int d = 0; d < NDIM; d++) xi[d] = F.f[X0 + d][i];
+#pragma unroll
+    for (int d = 0; d < 3; d++) vi[d] = F.f[V0 + d][i];
+    const double hi = F.f[HH][i];
+    const double hi1 = a.S.h1[i];
+    const double hi21 = __dmul_rn(hi1, hi1);
+    const float4 xsi = a.S.xs[i];
+    const float hif = (float)hi;
+    const double dxbound = 2.0 * bitsd(a.red->hmax_ghost);
+    const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
+
+    // FP64 sums (PREC 0) or compensated FP32 sums (PREC 1), in kernel units
+    double sw = 0.0, sn = 0.0, sg = 0.0, sgn = 0.0, sgg = 0.0, sd = 0.0;
+    KSum fw, fn, fg, fgn, fgg, fd;
+    int nn = 0;
+
+    Stencil<NDIM> stn(a.S.cell[i], g);
+    constexpr int NST = (NDIM == 1) ? 3 : (NDIM == 2 ? 9 : 27);
+    for (int so = 0; so < NST; so++) {
+        int cid, d[3], w[3];
+        if (!stn.cell_at(so, g, o, cid, d, w)) continue;
+        const int jb = a.cell_start[cid], je = a.cell_start[cid + 1];
+        for (int j = jb; j < je; j++) {
+            const float4 xsj = a.S.xs[j];
+            float dxf[3];
+            const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
+            const float hm = FULL ? fmaxf(hif, xsj.w) : hif;
+            if (PREC == NDSPH_PREC_FP64) {
+                const float rc = 2.0f * hm * 1.0002f + abs_tol;
+                if (r2f > rc * rc) continue;
+            } else {
+                if (r2f >= 4.0f * hm * hm) continue;
+            }
+            const int typej = a.S.itype[j];
+            if (!type_match(typei, typej)) continue;
+            if (PREC == NDSPH_PREC_FP64) {
+                double dx[3], rij2;
+                if (!exact_dx<NDIM>(F, j, xi, w, o, dxbound, dx, rij2)) continue;
+                const double q2i = __dmul_rn(rij2, hi21);
+                bool inc;
+                if (FULL) {
+                    const double hj1 = a.S.h1[j];
+                    const double q2j = __dmul_rn(__dmul_rn(rij2, hj1), hj1);
+                    inc = (q2i < 4.0) || (q2j < 4.0);
+                } else {
+                    inc = q2i < 4.0;
+                }
+                if (!inc) continue;
+                nn++;
+                if (q2i >= 4.0 || fixed_i) continue;
+                const double mj = F.f[PM][j];
+                const TabIdx ix = tab_index(a.t, q2i);
+                const double wv = tab_val(a.t.w, ix);
+                const double gw = tab_val(a.t.gw, ix);
+                const double ggw = tab_val(a.t.ggw, ix);
+                const double q = sqrt(q2i);
+                sw += mj * wv;
+                sn += wv;
+                const double tg = q * gw + (double)NDIM * wv;
+                sg += mj * tg;
+                sgn += tg;
+                sgg += mj * ((double)(NDIM * (NDIM + 1)) * wv + (double)(2 * (NDIM + 1)) * q * gw + q2i * ggw);
+                if (j != i) {
+                    const double rij = sqrt(rij2);
+                    double dvr = (vi[0] - F.f[V0][j]) * dx[0];
+                    if (NDIM >= 2) dvr += (vi[1] - F.f[V1][j]) * dx[1];
+                    if (NDIM >= 3) dvr += (vi[2] - F.f[V2][j]) * dx[2];
+                    sd += mj * dvr * gw / (rij + 2.220446049250313e-16);
+                }
+            } else {
+                // FP32 form: separation from the FP32 cell-relative coordinates
+                const float q2i = r2f / (hif * hif);
+                nn++;
+                if (fixed_i || !(q2i < 4.0f)) continue;
+                const float mj = (float)F.f[PM][j];
+                const TabIdxF ix = tab_indexf(a.t, q2i);
+                const float wv = tab_valf(a.t.wf, ix);
+                const float gw = tab_valf(a.t.gwf, ix);
+                const float ggw = tab_valf(a.t.ggwf, ix);
+                const float q = sqrtf(q2i);
+                fw.add(mj * wv);
+                fn.add(wv);
+                const float tg = q * gw + (float)NDIM * wv;
+                fg.add(mj * tg);
+                fgn.add(tg);
+                fgg.add(mj * ((float)(NDIM * (NDIM + 1)) * wv + (float)(2 * (NDIM + 1)) * q * gw + q2i * ggw));
+                if (j != i) {
+                    const float rij = q * hif;
+                    float dvr = (float)(vi[0] - F.f[V0][j]) * dxf[0];
+                    if (NDIM >= 2) dvr += (float)(vi[1] - F.f[V1][j]) * dxf[1];
+                    if (NDIM >= 3) dvr += (float)(vi[2] - F.f[V2][j]) * dxf[2];
+                    fd.add(mj * dvr * gw / (rij + 1e-30f));
+                }
+            }
+        }
+    }
+    if (PREC == NDSPH_PREC_FP32) {
+        sw = fw.val(); sn = fn.val(); sg = fg.val(); sgn = fgn.val(); sgg = fgg.val(); sd = fd.val();
+    }
+    a.S.numneigh[i] = nn;
+    if (fixed_i) return;
+
+    // ---- sums in reference units ----
+    double hfac = hi1;
+    if (NDIM >= 2) hfac *= hi1;
+    if (NDIM >= 3) hfac *= hi1;
+    const double rho = hfac * sw;
+    const double rhoalt = hfac * sn;
+    double gradh = -hfac * hi1 * sg;
+    const double gradhn = -hfac * hi1 * sgn;
+    double gradgradh = hfac * hi1 * hi1 * sgg;
+    double drhodt = hfac * hi1 * sd;
+
+    // ---- Newton-Raphson update, iterate_density.f90:163-278 ----
+    const double pm = F.f[PM][i];
+    const double hfact = o.hfact;
+    if (rho <= 1.e-6 && rho <= 0.0) {
+        raise_err(a.red, NDSPH_E_RHO_NONPOS, a.S.id[i]);
+        return;
+    }
+    double hb = hi / hfact;
+    double hpow = hb;
+    if (NDIM >= 2) hpow = hpow * hb;
+    if (NDIM >= 3) hpow = hpow * hb;
+    const double rhoi = pm / hpow;
+    const double dhdrhoi = -hi / ((double)NDIM * rho);
+    const double dwdhsumi = gradh;
+    double omegai = 1.0 - dhdrhoi * gradh;
+    if (omegai < 1.e-5 && fabs(omegai) == 0.0) omegai = 1.0;
+    gradh = 1.0 / omegai;
+    const double func = rhoi - rho;
+    const double dfdh = omegai / dhdrhoi;
+    const double rn = rho * (double)NDIM;
+    const double d2hdrho2i = hi * (double)(NDIM + 1) / (rn * rn);
+    gradgradh = rho * (d2hdrho2i * dwdhsumi + dhdrhoi * dhdrhoi * gradgradh);
+    double hnew = hi - func / dfdh;
+    if (hnew > 1.2 * hi) hnew = 1.2 * hi;
+    else if (hnew < 0.8 * hi) hnew = 0.8 * hi;
+    if (hnew <= 0.0 || gradh <= 2.2250738585072014e-308) {
+        hnew = hfact * pow(pm / rho, 1.0 / (double)NDIM);
+    } else if (a.its > 100) {
+        hnew = hfact * pow(pm / rho, 1.0 / (double)NDIM);
+    }
+    bool relink = false;
+    if (nn <= 1) {
+        hnew = hi + o.psep;
+        relink = true;
+    }
+    const double hin = F.f[HDEN0][i];
+    const bool converged = (fabs((hnew - hi) / hin) < o.tolh && omegai > 0.0) || o.maxdensits == 0;
+    double* hdst = FULL ? F.f[HNEXT] : F.f[HH];
+    if (!converged) {
+        const int k = atomicAdd(a.ncalc_next, 1);
+        a.S.active_next[k] = i;
+        if (a.its <= o.maxdensits) hdst[i] = hnew;
+        if (hnew > bitsd(a.red->hmax_ghost)) relink = true;
+    } else {
+        drhodt = drhodt * gradh;
+        F.f[DHDT][i] = dhdrhoi * drhodt;
+    }
+    if (relink) a.red->redolink = 1;
+    F.f[RHO][i] = rho;
+    F.f[RHOALT][i] = rhoalt;
+    F.f[DRHODT][i] = drhodt;
+    F.f[GRADH][i] = gradh;
+    F.f[GRADHN][i] = gradhn;
+    F.f[GRADGRADH][i] = gradgradh;
+}
+
+void launch_density(const SweepArgs& a, bool full, cudaStream_t st)
+{
+    const int bs = 128;
+    const int nthreads = full ? a.n : a.nlist;
+    if (nthreads <= 0) return;
+    const int nb = nblk(nthreads, bs);
+#define DLAUNCH(ND, FU, PR) k_density<ND, FU, PR><<<nb, bs, 0, st>>>(a)
+    if (a.o.precision == NDSPH_PREC_FP64) {
+        if (a.o.ndim == 1) { if (full) DLAUNCH(1, true, 0); else DLAUNCH(1, false, 0); }
+        else if (a.o.ndim == 2) { if (full) DLAUNCH(2, true, 0); else DLAUNCH(2, false, 0); }
+        else { if (full) DLAUNCH(3, true, 0); else DLAUNCH(3, false, 0); }
+    } else {
+        if (a.o.ndim == 1) { if (full) DLAUNCH(1, true, 1); else DLAUNCH(1, false, 1); }
+        else if (a.o.ndim == 2) { if (full) DLAUNCH(2, true, 1); else DLAUNCH(2, false, 1); }
+        else { if (full) DLAUNCH(3, true, 1); else DLAUNCH(3, false, 1); }
+    }
+#undef DLAUNCH
+}
+
+// ===========================================================================
+// rates
+// ===========================================================================
+template <typename R>
+struct Acc;
+template <>
+struct Acc<double> {
+    double v = 0.0;
+    __device__ __forceinline__ void add(double x) { v += x; }
+    __device__ __forceinline__ double val() const { return v; }
+};
+template <>
+struct Acc<float> {
+    KSum k;
+    __device__ __forceinline__ void add(float x) { k.add(x); }
+    __device__ __forceinline__ double val() const { return k.val(); }
+};
+
+template <int NDIM, int PREC>
+__global__ void __launch_bounds__(128) k_rates(SweepArgs a)
+{
+    typedef typename std::conditional<PREC == NDSPH_PREC_FP64, double, float>::type R;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const FieldPtrs& F = a.F;
+    const DevOpts& o = a.o;
+    const Grid& g = a.g;
+    const int typei = a.S.itype[i];
+    double xi[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int d = 0; d < NDIM; d++) xi[d] = F.f[X0 + d][i];
+    const double hi_d = F.f[HH][i];
+    const double hi1_d = a.S.h1[i];
+    const double hi21_d = __dmul_rn(hi1_d, hi1_d);
+    const float4 xsi = a.S.xs[i];
+    const float hif = (float)hi_d;
+    const double dxbound = 2.0 * bitsd(a.red->hmax_ghost);
+    const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
+
+    const R hi = (R)hi_d, hi1 = (R)hi1_d;
+    R hfacgrki = hi1 * hi1;
+    if (NDIM >= 2) hfacgrki *= hi1;
+    if (NDIM >= 3) hfacgrki *= hi1;
+    const R vi[3] = {(R)F.f[V0][i], (R)F.f[V1][i], (R)F.f[V2][i]};
+    const R rhoi = (R)F.f[RHO][i];
+    const R rho1i = (R)1 / rhoi;
+    const R rho21i = rho1i * rho1i;
+    const R pri = (R)fmax(F.f[PR][i], 0.0);
+    const R Prho2i = pri * rho21i;
+    const R csi = (R)F.f[CS][i];
+    const R ui = (R)F.f[UU][i];
+    const R mi = (R)F.f[PM][i];
+    const R alphai = (R)F.f[AL0][i], alphaui = (R)F.f[AL1][i], alphaBi = (R)F.f[AL2][i];
+    const R gradhi = (R)F.f[GRADH][i];
+    const bool mhd = (o.imhd != 0);
+    R Bi[3] = {0, 0, 0}, Brhoi[3] = {0, 0, 0};
+    R B2i = 0, Brho2i = 0, va2i = 0;
+    if (mhd) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) { Bi[d] = (R)F.f[BF0 + d][i]; Brhoi[d] = Bi[d] * rho1i; }
+        B2i = Bi[0] * Bi[0] + Bi[1] * Bi[1] + Bi[2] * Bi[2];
+        Brho2i = B2i * rho21i;
+        va2i = B2i * rho1i;
+    }
+    const R vsig2i = csi * csi + va2i;
+    const R stressmax = (R)bitsd(a.red->stressmax);
+    const R beta = (R)o.beta;
+    const bool i_dust = (typei == NDSPH_ITYPE_DUST);
+
+    Acc<R> fx, fy, fz, dbx, dby, dbz, du, dvb, cbx, cby, cbz, d2u, gx, gy, gz;
+    double dtc = 1.e6, dtav = 1.7976931348623157e308, vsmax = 0.0, tsmin = 1.7976931348623157e308;
+    double hcsts = 0.0;
+
+    Stencil<NDIM> stn(a.S.cell[i], g);
+    constexpr int NST = (NDIM == 1) ? 3 : (NDIM == 2 ? 9 : 27);
+    for (int so = 0; so < NST; so++) {
+        int cid, d[3], w[3];
+        if (!stn.cell_at(so, g, o, cid, d, w)) continue;
+        const int jb = a.cell_start[cid], je = a.cell_start[cid + 1];
+        for (int j = jb; j < je; j++) {
+            if (j == i) continue;
+            const float4 xsj = a.S.xs[j];
+            float dxf[3];
+            const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
+            const float hm = fmaxf(hif, xsj.w);
+            R dr[3], rij, q2i, q2j, hj1;
+            if (PREC == NDSPH_PREC_FP64) {
+                const float rc = 2.0f * hm * 1.0002f + abs_tol;
+                if (r2f > rc * rc) continue;
+                double dx[3], rij2;
+                if (!exact_dx<NDIM>(F, j, xi, w, o, dxbound, dx, rij2)) continue;
+                const double hj1d = a.S.h1[j];
+                const double q2id = __dmul_rn(rij2, hi21_d);
+                const double q2jd = __dmul_rn(rij2, __dmul_rn(hj1d, hj1d));
+                if (!(q2id < 4.0 || q2jd < 4.0)) continue;
+                const double rijd = sqrt(rij2);
+                if (rijd <= 2.220446049250313e-16) {
+                    if (a.S.itype[j] == typei && rijd < 2.2250738585072014e-308 && typei != 2)
+                        raise_err(a.red, NDSPH_E_CLUMP, a.S.id[i]);
+                    dr[0] = dr[1] = dr[2] = 0;
+                } else {
+                    const double ir = 1.0 / rijd;
+                    dr[0] = (R)(dx[0] * ir);
+                    dr[1] = (R)(dx[1] * ir);
+                    dr[2] = (R)(dx[2] * ir);
+                }
+                rij = (R)rijd; q2i = (R)q2id; q2j = (R)q2jd; hj1 = (R)hj1d;
+            } else {
+                const float hjf = xsj.w;
+                if (!(r2f < 4.0f * hm * hm)) continue;
+                const float rr = sqrtf(r2f);
+                if (rr <= 1e-30f) {
+                    if (a.S.itype[j] == typei && typei != 2) raise_err(a.red, NDSPH_E_CLUMP, a.S.id[i]);
+                    dr[0] = dr[1] = dr[2] = 0;
+                } else {
+                    const float ir = 1.0f / rr;
+                    dr[0] = (R)(dxf[0] * ir); dr[1] = (R)(dxf[1] * ir); dr[2] = (R)(dxf[2] * ir);
+                }
+                rij = (R)rr;
+                hj1 = (R)(1.0f / hjf);
+                q2i = (R)(r2f / (hif * hif));
+                q2j = (R)(r2f * (float)hj1 * (float)hj1);
+            }
+            const int typej = a.S.itype[j];
+            const R mj = (R)F.f[PM][j];
+            const R vj[3] = {(R)F.f[V0][j], (R)F.f[V1][j], (R)F.f[V2][j]};
+            const R dvel[3] = {vi[0] - vj[0], vi[1] - vj[1], vi[2] - vj[2]};
+            const R rhoj = (R)F.f[RHO][j];
+            if (type_match(typei, typej)) {
+                // ---------------- rates_core ----------------
+                R hfacgrkj = hj1 * hj1;
+                if (NDIM >= 2) hfacgrkj *= hj1;
+                if (NDIM >= 3) hfacgrkj *= hj1;
+                R gwi, gwj;
+                if (PREC == NDSPH_PREC_FP64) {
+                    gwi = (R)tab_val(a.t.gw, tab_index(a.t, (double)q2i));
+                    gwj = (R)tab_val(a.t.gw, tab_index(a.t, (double)q2j));
+                } else {
+                    gwi = (R)tab_valf(a.t.gwf, tab_indexf(a.t, (float)q2i));
+                    gwj = (R)tab_valf(a.t.gwf, tab_indexf(a.t, (float)q2j));
+                }
+                const R grkerni = gwi * hfacgrki * gradhi;
+                const R grkernj = gwj * hfacgrkj * (R)F.f[GRADH][j];
+                const R grkern = (R)0.5 * (grkerni + grkernj);
+                const R dvdotr = dvel[0] * dr[0] + dvel[1] * dr[1] + dvel[2] * dr[2];
+                const R rho1j = (R)1 / rhoj;
+                const R rho21j = rho1j * rho1j;
+                const R rhoav1 = (R)0.5 * (rho1i + rho1j);
+                const R prj = (R)fmax(F.f[PR][j], 0.0);
+                const R Prho2j = prj * rho21j;
+                const R csj = (R)F.f[CS][j];
+                R vsigi, vsigj, vsigB;
+                R dB[3] = {0, 0, 0}, Brhoj[3] = {0, 0, 0};
+                R projBrhoi = 0, projBrhoj = 0, projdB = 0, Brho2j = 0;
+                if (mhd) {
+                    R Bj[3];
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        Bj[c] = (R)F.f[BF0 + c][j];
+                        Brhoj[c] = Bj[c] * rho1j;
+                        dB[c] = Bi[c] - Bj[c];
+                    }
+                    const R projBi = Bi[0] * dr[0] + Bi[1] * dr[1] + Bi[2] * dr[2];
+                    const R projBj = Bj[0] * dr[0] + Bj[1] * dr[1] + Bj[2] * dr[2];
+                    projdB = dB[0] * dr[0] + dB[1] * dr[1] + dB[2] * dr[2];
+                    projBrhoi = Brhoi[0] * dr[0] + Brhoi[1] * dr[1] + Brhoi[2] * dr[2];
+                    projBrhoj = Brhoj[0] * dr[0] + Brhoj[1] * dr[1] + Brhoj[2] * dr[2];
+                    const R B2j = Bj[0] * Bj[0] + Bj[1] * Bj[1] + Bj[2] * Bj[2];
+                    const R va2j = B2j * rho1j;
+                    Brho2j = B2j * rho21j;
+                    const R vsig2j = csj * csj + va2j;
+                    const R ti = csi * projBi, tj = csj * projBj;
+                    const R vpi = vsig2i * vsig2i - (R)4 * (ti * ti) * rho1i;
+                    const R vpj = vsig2j * vsig2j - (R)4 * (tj * tj) * rho1j;
+                    if (vpi < (R)0 || vpj < (R)0) raise_err(a.red, NDSPH_E_VSIG_DET, a.S.id[i]);
+                    vsigi = sqrt((R)0.5 * (vsig2i + sqrt(fmax(vpi, (R)0))));
+                    vsigj = sqrt((R)0.5 * (vsig2j + sqrt(fmax(vpj, (R)0))));
+                    vsigB = sqrt(dvel[0] * dvel[0] + dvel[1] * dvel[1] + dvel[2] * dvel[2]);
+                } else {
+                    vsigi = csi; vsigj = csj; vsigB = 0;
+                }
+                R vsig = (R)0.5 * fmax(vsigi + vsigj - beta * dvdotr, (R)0);
+                const R prj_net = prj;
+                R vsigu = sqrt(fabs(pri - prj_net) * rhoav1);
+                R vsigdtc = fmax(vsig, (R)0.5 * (vsigi + vsigj + beta * fabs(dvdotr)));
+                vsigdtc = fmax(vsigdtc, vsigB);
+                if (i_dust) {
+                    vsig = 0; vsigu = 0;
+                } else {
+                    vsmax = fmax(vsmax, (double)vsigdtc);
+                    if ((double)vsigdtc > 1.e-10) {
+                        const double hj_d = F.f[HH][j];
+                        dtc = fmin(dtc, fmin(hi_d, hj_d) / (double)vsigdtc);
+                    }
+                }
+                R fxi = 0, fyi = 0, fzi = 0;
+                // ---------------- artificial_dissipation ----------------
+                if (o.iav > 0) {
+                    const R alphaav = (R)0.5 * (alphai + (R)F.f[AL0][j]);
+                    const R alphau = (R)0.5 * (alphaui + (R)F.f[AL1][j]);
+                    const R alphaB = (R)0.5 * (alphaBi + (R)F.f[AL2][j]);
+                    const R vsigav = fmax(fmax(alphaav, alphau), alphaB) * vsig;
+                    const R term = vsig * rhoav1 * grkern;
+                    const R termu = vsigu * rhoav1 * grkern;
+                    const R termB = vsigB * rhoav1 * grkern;
+                    if (dvdotr < (R)0 && o.iav <= 3) {
+                        const R visc = alphaav * term * (-dvdotr);
+                        fxi -= mj * visc * dr[0]; fyi -= mj * visc * dr[1]; fzi -= mj * visc * dr[2];
+                    }
+                    if (o.imhd > 0 && o.imhd != 10 && o.iav >= 2) {
+                        const R fb = rhoi * mj * alphaB * termB * rhoav1;
+                        dbx.add(fb * dB[0]); dby.add(fb * dB[1]); dbz.add(fb * dB[2]);
+                    }
+                    if (o.iener > 0 && o.iener != 3) {
+                        R vissv = 0;
+                        if (dvdotr < (R)0 && o.iav <= 3) {
+                            const R tt = (vi[0] * dr[0] + vi[1] * dr[1] + vi[2] * dr[2]) -
+                                         (vj[0] * dr[0] + vj[1] * dr[1] + vj[2] * dr[2]);
+                            vissv = -alphaav * (R)0.5 * (tt * tt);
+                        }
+                        const R vissu = (o.iener == 1) ? (R)0 : alphau * (ui - (R)F.f[UU][j]);
+                        R vissB = 0;
+                        if (o.imhd > 0 && o.imhd != 10 && o.iav >= 2)
+                            vissB = -alphaB * (R)0.5 * (dB[0] * dB[0] + dB[1] * dB[1] + dB[2] * dB[2]) * rhoav1;
+                        du.add(mj * (term * vissv + termu * vissu + termB * vissB));
+                    }
+                    if ((double)vsigav > 1.e-10) {
+                        const double hj_d = F.f[HH][j];
+                        dtav = fmin(dtav, fmin(hi_d, hj_d) / (double)vsigav);
+                    }
+                }
+                // ---------------- pressure ----------------
+                const R prterm = Prho2i * grkerni + Prho2j * grkernj;
+                fxi -= mj * prterm * dr[0]; fyi -= mj * prterm * dr[1]; fzi -= mj * prterm * dr[2];
+                // ---------------- mhd_terms ----------------
+                if (mhd) {
+                    const R fiso = (R)0.5 * (Brho2i * grkerni + Brho2j * grkernj);
+                    R fm[3];
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        const R fan = (Brhoi[c] * projBrhoi - stressmax * dr[c] * rho21i) * grkerni +
+                                      (Brhoj[c] * projBrhoj - stressmax * dr[c] * rho21j) * grkernj;
+                        fm[c] = fan - fiso * dr[c];
+                    }
+                    fxi += mj * fm[0]; fyi += mj * fm[1]; fzi += mj * fm[2];
+                    dvb.add(-mj * projdB * grkern);
+                    if (o.imhd > 0) {
+                        const R c0 = dB[1] * dr[2] - dB[2] * dr[1];
+                        const R c1 = dB[2] * dr[0] - dB[0] * dr[2];
+                        const R c2 = dB[0] * dr[1] - dB[1] * dr[0];
+                        cbx.add(mj * c0 * grkern); cby.add(mj * c1 * grkern); cbz.add(mj * c2 * grkern);
+                    }
+                    if (o.imhd == 1 || o.imhd == 11) {
+                        const R fb = mj * projBrhoi * grkerni;
+                        dbx.add(-fb * dvel[0]); dby.add(-fb * dvel[1]); dbz.add(-fb * dvel[2]);
+                    }
+                }
+                fx.add(fxi); fy.add(fyi); fz.add(fzi);
+                if (o.iav > 0) {
+                    if (o.iavlim[1] > 0) {
+                        const R graduterm = (ui - (R)F.f[UU][j]) / rij;
+                        d2u.add(mj * rho1j * graduterm * grkerni);
+                    }
+                    if (o.iavlim[0] != 3) {
+                        gx.add(mj * (dvel[0] - dvdotr) * grkerni);
+                        gy.add(mj * (dvel[1] - dvdotr) * grkerni);
+                        gz.add(mj * (dvel[2] - dvdotr) * grkerni);
+                    }
+                }
+            } else if (o.idust == 2 && o.idrag_nature > 0) {
+                // ---------------- drag_forces ----------------
+                const R dv2 = dvel[0] * dvel[0] + dvel[1] * dvel[1] + dvel[2] * dvel[2];
+                R drd[3];
+                if ((double)rij <= 2.220446049250313e-16) {
+                    if ((double)dv2 <= 2.220446049250313e-16) continue;
+                    const R vij = sqrt(dv2);
+                    drd[0] = dvel[0] / vij; drd[1] = dvel[1] / vij; drd[2] = dvel[2] / vij;
+                } else {
+                    drd[0] = dr[0]; drd[1] = dr[1]; drd[2] = dr[2];
+                }
+                R wgas, ts, csg;
+                R rsum = rhoi + rhoj;
+                ts = rhoj * rhoi / ((R)o.Kdrag * rsum);
+                if (typei == NDSPH_ITYPE_GAS || typei == NDSPH_ITYPE_BND) {
+                    R wdi;
+                    if (PREC == 0) wdi = (R)tab_val(a.t.wdrag, tab_index(a.t, (double)q2i));
+                    else wdi = (R)tab_valf(a.t.wdragf, tab_indexf(a.t, (float)q2i));
+                    R hfw = hi1;
+                    if (NDIM >= 2) hfw *= hi1;
+                    if (NDIM >= 3) hfw *= hi1;
+                    wgas = wdi * hfw;
+                    csg = csi;
+                    hcsts = fmax(hcsts, (double)(hi / (csg * ts)));
+                } else {
+                    if (typej != NDSPH_ITYPE_GAS && typej != NDSPH_ITYPE_BND) continue;
+                    R wdj;
+                    if (PREC == 0) wdj = (R)tab_val(a.t.wdrag, tab_index(a.t, (double)q2j));
+                    else wdj = (R)tab_valf(a.t.wdragf, tab_indexf(a.t, (float)q2j));
+                    R hfw = hj1;
+                    if (NDIM >= 2) hfw *= hj1;
+                    if (NDIM >= 3) hfw *= hj1;
+                    wgas = wdj * hfw;
+                    csg = (R)F.f[CS][j];
+                    hcsts = fmax(hcsts, (double)((R)1 / (hj1 * csg * ts)));
+                }
+                tsmin = fmin(tsmin, (double)ts);
+                const R projv = dvel[0] * drd[0] + dvel[1] * drd[1] + dvel[2] * drd[2];
+                const R dragterm = (R)NDIM * wgas / (rsum * ts) * projv;
+                const R dragterm_en = dragterm * projv;
+                fx.add(-dragterm * mj * drd[0]);
+                fy.add(-dragterm * mj * drd[1]);
+                fz.add(-dragterm * mj * drd[2]);
+                if (typei == NDSPH_ITYPE_GAS) du.add(mj * dragterm_en);
+            }
+        }
+    }
+
+    // ---- global reductions (warp first) ----
+    for (int off = 16; off > 0; off >>= 1) {
+        dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
+        dtav = fmin(dtav, __shfl_down_sync(0xffffffffu, dtav, off));
+        vsmax = fmax(vsmax, __shfl_down_sync(0xffffffffu, vsmax, off));
+        tsmin = fmin(tsmin, __shfl_down_sync(0xffffffffu, tsmin, off));
+    }
+
+    // ---- per-particle post pass ratesND_mhd.f90:532-965 ----
+    const double rhoi_d = F.f[RHO][i];
+    const double rho1 = 1.0 / rhoi_d;
+    double force[3] = {fx.val(), fy.val(), fz.val()};
+    double dBe[3] = {dbx.val(), dby.val(), dbz.val()};
+    double dudt = du.val();
+    double divB = dvb.val();
+    double curlB[3] = {cbx.val(), cby.val(), cbz.val()};
+    const double del2u = d2u.val();
+    double gdv[3] = {gx.val(), gy.val(), gz.val()};
+    if (mhd) {
+        if (o.imhd > 0)
+            for (int c = 0; c < 3; c++) curlB[c] *= rho1;
+        divB *= rho1;
+    }
+    const double fmag = sqrt(force[0] * force[0] + force[1] * force[1] + force[2] * force[2]);
+    double fonh = fmag / hi_d;
+    if (typei == 1) fonh = 0.0;
+    double va2 = 0.0;
+    if (mhd) {
+        const double b0 = F.f[BF0][i], b1 = F.f[BF1][i], b2 = F.f[BF2][i];
+        va2 = (b0 * b0 + b1 * b1 + b2 * b2) / F.f[DENS][i];
+    }
+    const double csd = F.f[CS][i];
+    const double vsig = sqrt(csd * csd + va2);
+    const double drhodt = F.f[DRHODT][i];
+    if (o.imhd >= 11 && o.imhd <= 19) {
+        for (int c = 0; c < 3; c++) dBe[c] = dBe[c] + F.f[BE0 + c][i] * rho1 * drhodt;
+    } else if (o.imhd >= 1 && o.imhd <= 9) {
+        for (int c = 0; c < 3; c++) dBe[c] = dBe[c] * rho1;
+    } else {
+        dBe[0] = dBe[1] = dBe[2] = 0.0;
+    }
+    double dendt;
+    if (o.iener > 0 && o.iav >= 0 && o.iener != 3 && o.iener != 10 && o.iener != 11) {
+        dudt = dudt + F.f[PR][i] * (rho1 * rho1) * drhodt;
+        dendt = dudt;
+    } else {
+        dendt = dudt;
+    }
+    if (typei == NDSPH_ITYPE_DUST) dendt = 0.0;
+    double daldt[3] = {0.0, 0.0, 0.0};
+    if (o.iavlim[0] != 0 || o.iavlim[1] != 0 || o.iavlim[2] != 0) {
+        const double tdecay1 = (o.avdecayconst * vsig) / hi_d;
+        const double a0 = F.f[AL0][i];
+        if (o.iavlim[0] == 1 || o.iavlim[0] == 2) {
+            double source = fmax(drhodt * rho1, 0.0);
+            if (o.iavlim[0] == 2) source = source * (2.0 - a0);
+            daldt[0] = (o.alphamin - a0) * tdecay1 + o.avfact * source;
+        }
+        if (o.iener > 0 && o.iavlim[1] > 0) {
+            const double uu = F.f[UU][i];
+            double sourceu = 0.0;
+            if (uu > 2.220446049250313e-16) sourceu = hi_d * fabs(del2u) / sqrt(uu);
+            daldt[1] = (o.alphaumin - F.f[AL1][i]) * tdecay1 + sourceu;
+        }
+    }
+    double dhdt = F.f[DHDT][i];
+    double drhodt_out = drhodt;
+    if (typei == NDSPH_ITYPE_BND || typei == NDSPH_ITYPE_BNDDUST) {
+        for (int c = 0; c < 3; c++) { force[c] = 0.0; dBe[c] = 0.0; daldt[c] = 0.0; curlB[c] = 0.0; }
+        drhodt_out = 0.0; dhdt = 0.0; dudt = 0.0; dendt = 0.0; divB = 0.0;
+    }
+    for (int c = 0; c < 3; c++) {
+        F.f[F0 + c][i] = force[c];
+        F.f[DB0 + c][i] = dBe[c];
+        F.f[DAL0 + c][i] = daldt[c];
+        F.f[GDV0 + c][i] = gdv[c];
+        if (o.imhd > 0) F.f[CB0 + c][i] = curlB[c];
+    }
+    F.f[DRHODT][i] = drhodt_out;
+    F.f[DHDT][i] = dhdt;
+    F.f[DUDT][i] = dudt;
+    F.f[DENDT][i] = dendt;
+    F.f[DIVB][i] = divB;
+    F.f[DEL2U][i] = del2u;
+
+    for (int off = 16; off > 0; off >>= 1) {
+        fonh = fmax(fonh, __shfl_down_sync(0xffffffffu, fonh, off));
+        hcsts = fmax(hcsts, __shfl_down_sync(0xffffffffu, hcsts, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomic_min_pos(&a.red->dtcourant, dtc);
+        atomic_min_pos(&a.red->dtav, dtav);
+        atomic_max_pos(&a.red->vsigmax, vsmax);
+        atomic_min_pos(&a.red->ts_min, tsmin);
+        atomic_max_pos(&a.red->fhmax, fonh);
+    }
+}
+
+void launch_rates(const SweepArgs& a, cudaStream_t st)
+{
+    const int bs = 128;
+    if (a.n <= 0) return;
+    const int nb = nblk(a.n, bs);
+    if (a.o.precision == NDSPH_PREC_FP64) {
+        if (a.o.ndim == 1) k_rates<1, 0><<<nb, bs, 0, st>>>(a);
+        else if (a.o.ndim == 2) k_rates<2, 0><<<nb, bs, 0, st>>>(a);
+        else k_rates<3, 0><<<nb, bs, 0, st>>>(a);
+    } else {
+        if (a.o.ndim == 1) k_rates<1, 1><<<nb, bs, 0, st>>>(a);
+        else if (a.o.ndim == 2) k_rates<2, 1><<<nb, bs, 0, st>>>(a);
+        else k_rates<3, 1><<<nb, bs, 0, st>>>(a);
+    }
+}
+
+// ===========================================================================
+// neighbour CSR for the parity tests (check_neighbourlist.f90 replacement).
+// mode 0: q_i<2; mode 1: q_i<2 or q_j<2 with q2 = rij2*(h1*h1); type filter
+// as density; self excluded; indices are original (0-based) ids.
+// ===========================================================================
+template <int NDIM>
+__global__ void k_neigh(SweepArgs a, int mode, const long long* offsets, long long* counts, int* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const FieldPtrs& F = a.F;
+    double xi[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < NDIM; d++) xi[d] = F.f[X0 + d][i];
+    const double hi1 = a.S.h1[i];
+    const double hi21 = __dmul_rn(hi1, hi1);
+    const int typei = a.S.itype[i];
+    const double dxbound = 2.0 * bitsd(a.red->hmax_ghost);
+    Stencil<NDIM> stn(a.S.cell[i], a.g);
+    constexpr int NST = (NDIM == 1) ? 3 : (NDIM == 2 ? 9 : 27);
+    long long k = offsets ? offsets[a.S.id[i]] : 0;
+    long long cnt = 0;
+    for (int so = 0; so < NST; so++) {
+        int cid, d[3], w[3];
+        if (!stn.cell_at(so, a.g, a.o, cid, d, w)) continue;
+        for (int j = a.cell_start[cid]; j < a.cell_start[cid + 1]; j++) {
+            if (j == i) continue;
+            if (!type_match(typei, a.S.itype[j])) continue;
+            double dx[3], rij2;
+            if (!exact_dx<NDIM>(F, j, xi, w, a.o, dxbound, dx, rij2)) continue;
+            const double q2i = __dmul_rn(rij2, hi21);
+            const double hj1 = a.S.h1[j];
+            const double q2j = __dmul_rn(rij2, __dmul_rn(hj1, hj1));
+            const bool ok = (mode == 0) ? (q2i < 4.0) : (q2i < 4.0 || q2j < 4.0);
+            if (!ok) continue;
+            if (out) out[k++] = a.S.id[j];
+            cnt++;
+        }
+    }
+    if (counts) counts[a.S.id[i]] = cnt;
+}
+
+void launch_neigh_count(const SweepArgs& a, int mode, long long* counts, cudaStream_t st)
+{
+    const int nb = nblk(a.n, 128);
+    if (a.o.ndim == 1) k_neigh<1><<<nb, 128, 0, st>>>(a, mode, nullptr, counts, nullptr);
+    else if (a.o.ndim == 2) k_neigh<2><<<nb, 128, 0, st>>>(a, mode, nullptr, counts, nullptr);
+    else k_neigh<3><<<nb, 128, 0, st>>>(a, mode, nullptr, counts, nullptr);
+}
+void launch_neigh_fill(const SweepArgs& a, int mode, const long long* offsets, int* out, cudaStream_t st)
+{
+    const int nb = nblk(a.n, 128);
+    if (a.o.ndim == 1) k_neigh<1><<<nb, 128, 0, st>>>(a, mode, offsets, nullptr, out);
+    else if (a.o.ndim == 2) k_neigh<2><<<nb, 128, 0, st>>>(a, mode, offsets, nullptr, out);
+    else k_neigh<3><<<nb, 128, 0, st>>>(a, mode, offsets, nullptr, out);
+}
+
+}  // namespace ndsph
