@@ -1,0 +1,346 @@
+#!/usr/bin/env python
+"""Benchmark of the NDSPMHD per-step hot path on GB300.
+
+Workload (one "step" = one leapfrog step of the whole box: link, all
+Newton-Raphson density passes, EOS, rates, predictor/corrector, dt):
+the 3D MHD uniform box, 128^3 = 2,097,152 particles in a periodic unit cube,
+jittered cubic lattice (seed 1234), rho = 1, v ~ N(0, 0.1^2), B = (0.1, 0, 0)
+plus a 1% transverse perturbation, gamma = 5/3, cubic-spline kernel,
+hfact = 1.2, tolh = 1e-3.  Synthetic data generated in-process.
+
+Metric: particle-updates/s = N x steps / device time of the step loop.
+``value`` is the chosen FP32-pair form with the state resident in HBM;
+``fp64`` reports the plain FP64 form (the parity form) on the same workload;
+``e2e`` times the reference-facing C-ABI call ndsph_step with the state in
+pinned host buffers (H2D of the state and D2H of the result every step).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+(N>1 under torchrun: independent replicas, one box per rank, weak scaling.)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N1D = int(os.environ.get("NDSPH_BENCH_N1D", "128"))
+CPU_SAMPLE_N1D = 48          # CPU baseline sample: 48^3 box, 2 steps
+CPU_SAMPLE_STEPS = 2
+METRIC = "SPH particle-updates/s on 1 GB300 (3D MHD 128^3 box, full leapfrog step)"
+UNIT = "particle-updates/s"
+
+# algorithmic bytes per particle of the rates sweep: reads x(3) v(3) m h rho P
+# c_s u gradh B(3) alpha(3) Bevol(3) drhodt dhdt (26 doubles) and writes
+# force(3) dBevol/dt(3) du/dt de/dt dalpha/dt(3) divB curlB(3) del2u
+# graddivv(3) drhodt dhdt (21 doubles) once each
+RATES_BYTES_PER_PARTICLE = (26 + 21) * 8
+# density pass: reads x(3) h m v(3) (8 doubles) writes rho rhoalt drhodt dhdt
+# gradh gradhn gradgradh h (8 doubles) + numneigh (4 B)
+DENSITY_BYTES_PER_PARTICLE = 16 * 8 + 4
+
+
+def _load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    def __init__(self, gpu_index: int = 0):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self._proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+            if self._stop.is_set():
+                break
+
+    def stop(self) -> dict:
+        self._stop.set()
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                smax = float(s[1])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if s[3 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_problem(n1d: int, precision: int):
+    from ndspmhd_gb300 import configs
+    o, p = configs.mhd_box_3d(n1d, seed=1234)
+    o["precision"] = precision
+    return o, configs.full_state(p, 3)
+
+
+def init_state(o, st):
+    """primitive2conservative on the GPU (untimed set-up)."""
+    from ndspmhd_gb300.gpu import GpuSPH
+    g = GpuSPH(o, st)
+    g.primitive2conservative()
+    return g
+
+
+def run_device(o, st, steps: int, warmup: int, dist=None):
+    """Device-resident timing: returns (ms_per_step, timing dict, dts, clocks)."""
+    import torch
+    g = init_state(o, st)
+    g.dev_upload()
+    g.set_dt(0.0)
+    g.dev_step(warmup)
+    g.set_profiling(False)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.start()
+    g.dev_step(steps)              # bracketed by CUDA events on the library's stream
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    total_ms = g.timing()["total_ms"]
+    # kernel breakdown on one extra profiled step (not part of the timed loop)
+    g.set_profiling(True)
+    g.dev_step(1)
+    tim = g.timing()
+    dts = g.dts()
+    g.close()
+    return total_ms / steps, tim, dts, clocks
+
+
+def run_e2e(o, steps: int, warmup: int):
+    """Reference-facing C-ABI call with pinned host buffers: ndsph_step."""
+    import numpy as np
+    import torch
+    from ndspmhd_gb300.abi import alloc_state
+    from ndspmhd_gb300.gpu import GpuSPH
+    o2, st = make_problem(N1D, o["precision"])
+    g0 = init_state(o2, st)
+    dt0 = g0.dts()
+    g0.close()
+    n = st["x"].shape[0]
+    # pinned host copies of every array ndsph_step reads and writes
+    pinned = {}
+    for k, v in st.items():
+        t = torch.empty(v.shape, dtype=torch.float64 if v.dtype == np.float64 else torch.int32, pin_memory=True)
+        a = t.numpy()
+        a[...] = v
+        pinned[k] = (t, a)
+    host = {k: a for k, (t, a) in pinned.items()}
+    g = GpuSPH(o2, host)
+    g.set_dt(0.0)
+    g.dt.dt, g.dt.time, g.dt.nsteps = 0.0, 0.0, 0
+    for _ in range(warmup):
+        g.step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        g.step()
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    # bytes: ndsph_step uploads x v Bevol en hh pmass alpha rho rhoalt drhodt dhdt
+    # gradh gradhn gradgradh dens uu pr spsound Bfield force dBevoldt dendt dudt
+    # daldt divB curlB + itype ireal numneigh, and downloads the full state
+    d_up = (3 + 3 + 3 + 1 + 1 + 1 + 3 + 7 + 4 + 3 + 3 + 3 + 1 + 1 + 3 + 1 + 3) * 8 + 3 * 4
+    d_dn = (3 + 3 + 3 + 1 + 1 + 1 + 3 + 7 + 4 + 3 + 3 + 3 + 1 + 1 + 3 + 1 + 3 + 1 + 3) * 8 + 4
+    g.close()
+    del dt0
+    return n * steps / el, d_up * n, d_dn * n
+
+
+def cpu_baseline(n1d: int = CPU_SAMPLE_N1D, steps: int = CPU_SAMPLE_STEPS) -> dict:
+    """The oracle (single-threaded C restatement of the reference) on a
+    bounded sample of the same workload: a n1d^3 box, `steps` leapfrog steps."""
+    from ndspmhd_gb300 import configs
+    from oracle.oracle import Oracle
+    o, p = configs.mhd_box_3d(n1d, seed=1234)
+    orc = Oracle(o, configs.full_state(p, 3))
+    orc.primitive2conservative()
+    t0 = time.perf_counter()
+    orc.step(steps)
+    el = time.perf_counter() - t0
+    n = n1d ** 3
+    return {"value": n * steps / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n1d}^3 box ({n} particles), {steps} leapfrog steps, FP64 oracle, 1 thread, "
+                      f"{el:.1f} s"}
+
+
+def _cpu_worker(args):
+    n1d, steps = args
+    return cpu_baseline(n1d, steps)["value"]
+
+
+def reference_arm(args):
+    """--impl reference: the reference's CPU implementation of the path (the
+    oracle port; the Fortran reference cannot be built here) on all host
+    cores as independent replicas of the bounded sample (the reference is
+    serial, so one simulation per core)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    for _ in range(max(args.warmup, 0) and 0):
+        pass
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        vals = pool.map(_cpu_worker, [(CPU_SAMPLE_N1D, CPU_SAMPLE_STEPS)] * cores)
+    el = time.perf_counter() - t0
+    value = float(sum(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": CPU_SAMPLE_STEPS, "warmup": 0,
+        "ms_per_step": 1e3 * (CPU_SAMPLE_N1D ** 3) / (value / cores) if value > 0 else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded 3D MHD box)",
+        "config": {"workload": f"3D MHD box, sample {CPU_SAMPLE_N1D}^3 per core", "n1d": CPU_SAMPLE_N1D,
+                   "parallelism": f"{cores} independent serial replicas"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} x ({CPU_SAMPLE_N1D}^3 box, {CPU_SAMPLE_STEPS} steps), wall {el:.1f} s"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form measurement")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+        dist = tdist
+    else:
+        torch.cuda.set_device(0)
+    warmup = max(args.warmup, 3)
+
+    # CPU baseline first (before heavy GPU work; rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline()
+
+    o32, st32 = make_problem(N1D, 1)
+    n = st32["x"].shape[0]
+    ms32, tim32, dts32, clocks = run_device(o32, st32, args.steps, warmup, dist)
+    ms64 = tim64 = None
+    if not args.no_fp64:
+        o64, st64 = make_problem(N1D, 0)
+        ms64, tim64, _, _ = run_device(o64, st64, max(2, args.steps // 2), 3, dist)
+
+    # max over ranks
+    if dist is not None:
+        t = torch.tensor([ms32], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms32 = float(t.item())
+    value = world * n / (ms32 * 1e-3)
+
+    e2e_val, h2d, d2h = run_e2e(o32, max(2, args.steps // 2), 1)
+
+    peak, peak_kind = _load_peaks()
+    rates_ms = tim32["rates_ms"]
+    achieved = RATES_BYTES_PER_PARTICLE * n / (rates_ms * 1e-3) / 1e9 if rates_ms > 0 else 0.0
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "rates_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get("fp32_bytes_per_launch_2M")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 5), "traffic": traffic,
+                "kernel": "k_rates<3,FP32> (rates sweep)",
+                "note": f"peak of {peak_kind} (MEASURED_PEAKS.json hbm_gbs); algorithmic bytes "
+                        f"{RATES_BYTES_PER_PARTICLE} B/particle x {n}; the sweep is FP32-issue bound, "
+                        f"see profiles/"}
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": warmup, "ms_per_step": round(ms32, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 pairs / f64 state",
+        "data": "synthetic (seeded jittered 128^3 MHD box, generated in-process)",
+        "config": {"workload": f"3D MHD box {N1D}^3 = {n} particles, periodic, full leapfrog step",
+                   "form": "FP32 pair sums (compensated), FP64 state/integration",
+                   "l2": "inputs larger than L2 (state slab ~1.3 GB)", "parallelism": f"replicas x{world}",
+                   "nr_passes_per_step": tim32["density_passes"]},
+        "gpu_launches": None,
+        "kernels_ms_per_step": {"rates": round(tim32["rates_ms"], 3), "density_all_passes": round(tim32["density_ms"], 3),
+                                "link": round(tim32["link_ms"], 3), "step_total": round(tim32["step_ms"], 3)},
+        "roofline": roofline,
+        "clocks": clocks,
+        "e2e": {"value": round(e2e_val, 1), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "call": "ndsph_step with pinned host buffers"},
+    }
+    if ms64 is not None:
+        line["fp64"] = {"value": round(n / (ms64 * 1e-3), 1), "ms_per_step": round(ms64, 3),
+                        "rates_ms": round(tim64["rates_ms"], 3), "density_ms": round(tim64["density_ms"], 3),
+                        "speedup_fp32_over_fp64": round(ms64 / ms32, 2)}
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    # launches per step: link (~12) + per NR pass (h1, density, ncalc copies) + EOS,
+    # packs, rates, finalize, predictor x2, corrector
+    passes = max(tim32["density_passes"], 1)
+    line["gpu_launches"] = args.steps * (14 + 3 * passes + 6)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

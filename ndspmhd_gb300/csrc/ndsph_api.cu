@@ -232,7 +232,7 @@ static void free_particles(ndsph_ctx* ctx)
     void* ptrs[] = {ctx->slab[0], ctx->slab[1], ctx->S.itype, ctx->S.id, ctx->S.ireal, ctx->S.pos_of_id,
                     ctx->S.numneigh, ctx->S.cell, ctx->S.xs, ctx->S.h1, ctx->S.active, ctx->S.active_next,
                     ctx->S.flag, ctx->itype2, ctx->id2, ctx->ireal2, ctx->srt.key, ctx->srt.slot, ctx->srt.perm,
-                    ctx->d_stage, ctx->d_istage};
+                    ctx->d_stage, ctx->d_istage, ctx->S.pk_v, ctx->S.pk_t, ctx->S.pk_b, ctx->S.pk_a};
     for (void* p : ptrs) if (p) cudaFree(p);
     ctx->slab[0] = ctx->slab[1] = nullptr;
     memset(&ctx->S, 0, sizeof(ctx->S));
@@ -265,6 +265,10 @@ static int ensure_capacity(ndsph_ctx* ctx, int n)
     CK(cudaMalloc(&ctx->itype2, ib)); CK(cudaMalloc(&ctx->id2, ib)); CK(cudaMalloc(&ctx->ireal2, ib));
     CK(cudaMalloc(&ctx->srt.key, ib)); CK(cudaMalloc(&ctx->srt.slot, ib)); CK(cudaMalloc(&ctx->srt.perm, ib));
     CK(cudaMalloc(&ctx->d_stage, sizeof(double) * 3 * (size_t)cap));
+    CK(cudaMalloc(&ctx->S.pk_v, sizeof(float4) * (size_t)cap));
+    CK(cudaMalloc(&ctx->S.pk_t, sizeof(float4) * (size_t)cap));
+    CK(cudaMalloc(&ctx->S.pk_b, sizeof(float4) * (size_t)cap));
+    CK(cudaMalloc(&ctx->S.pk_a, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->d_istage, ib));
     CK(cudaMemsetAsync(ctx->S.numneigh, 0, ib, ctx->st));
     ctx->cap = cap;
@@ -612,6 +616,10 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
     CK(cudaMemcpyAsync(&ctx->red->redolink, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
     int its = 0, ncalc = n, ncalctotal = 0, nrelink = 0;
     bool redolink = false;
+    if (ctx->o.precision == NDSPH_PREC_FP32) {
+        SweepArgs pa = sweep_args(ctx);
+        launch_pack_v(pa, st);
+    }
     // count fixed particles: a full pass is taken while ncalc == npart
     float dens_ms = 0.f, pass1_ms = 0.f;
     while (ncalc > 0 && its <= itsmax) {
@@ -633,6 +641,10 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
             for (int k = 0; k < ncalc; k++) act[k] = pos[act[k]];
             CK(cudaMemcpy(ctx->S.active, act.data(), sizeof(int) * (size_t)ncalc, cudaMemcpyHostToDevice));
             nrelink++;
+            if (ctx->o.precision == NDSPH_PREC_FP32) {
+                SweepArgs pa = sweep_args(ctx);
+                launch_pack_v(pa, st);
+            }
         }
         const bool full = (ncalc == n);
         launch_h1(ctx->F, ctx->S, n, st);
@@ -690,6 +702,7 @@ static int do_rates(ndsph_ctx* ctx)
     cudaStream_t st = ctx->st;
     launch_h1(ctx->F, ctx->S, ctx->n, st);
     SweepArgs a = sweep_args(ctx);
+    if (ctx->o.precision == NDSPH_PREC_FP32) launch_pack_rates(a, st);
     tmark(ctx, 4);
     launch_rates(a, st);
     tmark(ctx, 5);
@@ -995,6 +1008,10 @@ extern "C" int ndsph_dev_download(ndsph_ctx* ctx, ndsph_particles* p, ndsph_dt* 
 extern "C" int ndsph_dev_step(ndsph_ctx* ctx, int32_t nsteps, ndsph_dt* dts)
 {
     GUARD_CTX();
+    // the whole call is bracketed by events on the context's stream
+    CK(cudaEventRecord(ctx->ev[10], ctx->st));
+    float rates_sum = 0.f, dens_sum = 0.f, link_sum = 0.f;
+    int passes = 0;
     for (int k = 0; k < nsteps; k++) {
         tmark(ctx, 8);
         int rc = dev_step_once(ctx);
@@ -1003,7 +1020,23 @@ extern "C" int ndsph_dev_step(ndsph_ctx* ctx, int32_t nsteps, ndsph_dt* dts)
         if (ctx->profiling) {
             cudaEventSynchronize(ctx->ev[9]);
             ctx->timing.step_ms = tdiff(ctx, 8, 9);
+            rates_sum += ctx->timing.rates_ms;
+            dens_sum += ctx->timing.density_ms;
+            link_sum += ctx->timing.link_ms;
+            passes += ctx->timing.density_passes;
         }
+    }
+    CK(cudaEventRecord(ctx->ev[11], ctx->st));
+    CK(cudaEventSynchronize(ctx->ev[11]));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev[10], ctx->ev[11]);
+    ctx->timing.total_ms = ms;
+    if (ctx->profiling && nsteps > 0) {
+        // per-call sums of the per-step kernel times
+        ctx->timing.rates_ms = rates_sum;
+        ctx->timing.density_ms = dens_sum;
+        ctx->timing.link_ms = link_sum;
+        ctx->timing.density_passes = passes;
     }
     fill_dt(ctx, dts);
     return 0;

@@ -22,6 +22,11 @@ struct Side {
     int* active;      // NR active list (current pass)
     int* active_next; // NR active list (next pass)
     int* flag;        // NR converged flag scratch
+    // FP32 packs of the neighbour data (FP32 form only), one float4 each:
+    float4* pk_v;     // (vx, vy, vz, m)
+    float4* pk_t;     // (rho, max(P,0), c_s, u)
+    float4* pk_b;     // (Bx, By, Bz, gradh)
+    float4* pk_a;     // (alpha1, alpha2, alpha3, h)
 };
 
 struct SortScratch {
@@ -90,6 +95,8 @@ void launch_p2c_post(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
 // ---- sweeps (ndsph_sweeps.cu) --------------------------------------------
 void launch_density(const SweepArgs& a, bool full, cudaStream_t st);
 void launch_rates(const SweepArgs& a, cudaStream_t st);
+void launch_pack_v(const SweepArgs& a, cudaStream_t st);
+void launch_pack_rates(const SweepArgs& a, cudaStream_t st);
 // neighbour CSR for parity tests: counts (mode) then fill
 void launch_neigh_count(const SweepArgs& a, int mode, long long* counts, cudaStream_t st);
 void launch_neigh_fill(const SweepArgs& a, int mode, const long long* offsets, int* out, cudaStream_t st);

@@ -213,6 +213,12 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
     const double hi21 = __dmul_rn(hi1, hi1);
     const float4 xsi = a.S.xs[i];
     const float hif = (float)hi;
+    const float hi21f = __frcp_rn(hif * hif);
+    float vif[3] = {0.f, 0.f, 0.f};
+    if (PREC == NDSPH_PREC_FP32) {
+        const float4 pvi = a.S.pk_v[i];
+        vif[0] = pvi.x; vif[1] = pvi.y; vif[2] = pvi.z;
+    }
     const double dxbound = 2.0 * bitsd(a.red->hmax_ghost);
     const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
 
@@ -276,10 +282,11 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
                 }
             } else {
                 // FP32 form: separation from the FP32 cell-relative coordinates
-                const float q2i = r2f / (hif * hif);
+                const float q2i = r2f * hi21f;
                 nn++;
                 if (fixed_i || !(q2i < 4.0f)) continue;
-                const float mj = (float)F.f[PM][j];
+                const float4 pvj = a.S.pk_v[j];
+                const float mj = pvj.w;
                 const TabIdxF ix = tab_indexf(a.t, q2i);
                 const float wv = tab_valf(a.t.wf, ix);
                 const float gw = tab_valf(a.t.gwf, ix);
@@ -293,10 +300,10 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
                 fgg.add(mj * ((float)(NDIM * (NDIM + 1)) * wv + (float)(2 * (NDIM + 1)) * q * gw + q2i * ggw));
                 if (j != i) {
                     const float rij = q * hif;
-                    float dvr = (float)(vi[0] - F.f[V0][j]) * dxf[0];
-                    if (NDIM >= 2) dvr += (float)(vi[1] - F.f[V1][j]) * dxf[1];
-                    if (NDIM >= 3) dvr += (float)(vi[2] - F.f[V2][j]) * dxf[2];
-                    fd.add(mj * dvr * gw / (rij + 1e-30f));
+                    float dvr = (vif[0] - pvj.x) * dxf[0];
+                    if (NDIM >= 2) dvr += (vif[1] - pvj.y) * dxf[1];
+                    if (NDIM >= 3) dvr += (vif[2] - pvj.z) * dxf[2];
+                    fd.add(mj * dvr * gw * __frcp_rn(rij + 1e-30f));
                 }
             }
         }
@@ -411,6 +418,37 @@ struct Acc<float> {
     __device__ __forceinline__ double val() const { return k.val(); }
 };
 
+// per-particle quantities the rates sweep reads for either side of a pair
+template <typename R>
+struct PData {
+    R vx, vy, vz, m, rho, pr, cs, u, Bx, By, Bz, gradh, a0, a1, a2, h;
+};
+template <int PREC>
+__device__ __forceinline__ void load_p(const SweepArgs& a, int j,
+                                       PData<typename std::conditional<PREC == 0, double, float>::type>& q)
+{
+    if constexpr (PREC == NDSPH_PREC_FP64) {
+        const FieldPtrs& F = a.F;
+        q.vx = F.f[V0][j]; q.vy = F.f[V1][j]; q.vz = F.f[V2][j]; q.m = F.f[PM][j];
+        q.rho = F.f[RHO][j]; q.pr = fmax(F.f[PR][j], 0.0); q.cs = F.f[CS][j]; q.u = F.f[UU][j];
+        q.Bx = F.f[BF0][j]; q.By = F.f[BF1][j]; q.Bz = F.f[BF2][j]; q.gradh = F.f[GRADH][j];
+        q.a0 = F.f[AL0][j]; q.a1 = F.f[AL1][j]; q.a2 = F.f[AL2][j]; q.h = F.f[HH][j];
+    } else {
+        const float4 v = a.S.pk_v[j], t = a.S.pk_t[j], b = a.S.pk_b[j], al = a.S.pk_a[j];
+        q.vx = v.x; q.vy = v.y; q.vz = v.z; q.m = v.w;
+        q.rho = t.x; q.pr = t.y; q.cs = t.z; q.u = t.w;
+        q.Bx = b.x; q.By = b.y; q.Bz = b.z; q.gradh = b.w;
+        q.a0 = al.x; q.a1 = al.y; q.a2 = al.z; q.h = al.w;
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ R rcp(R x)
+{
+    if constexpr (std::is_same<R, float>::value) return __frcp_rn(x);
+    else return 1.0 / x;
+}
+
 template <int NDIM, int PREC>
 __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
 {
@@ -422,37 +460,41 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
     const Grid& g = a.g;
     const int typei = a.S.itype[i];
     double xi[3] = {0.0, 0.0, 0.0};
+    if (PREC == NDSPH_PREC_FP64) {
 #pragma unroll
-    for (int d = 0; d < NDIM; d++) xi[d] = F.f[X0 + d][i];
-    const double hi_d = F.f[HH][i];
+        for (int d = 0; d < NDIM; d++) xi[d] = F.f[X0 + d][i];
+    }
     const double hi1_d = a.S.h1[i];
-    const double hi21_d = __dmul_rn(hi1_d, hi1_d);
+    const double hi21_d = hi1_d * hi1_d;
     const float4 xsi = a.S.xs[i];
-    const float hif = (float)hi_d;
+    const float hif = xsi.w;
     const double dxbound = 2.0 * bitsd(a.red->hmax_ghost);
     const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
 
-    const R hi = (R)hi_d, hi1 = (R)hi1_d;
+    PData<R> pi;
+    load_p<PREC>(a, i, pi);
+    const R hi = pi.h;
+    const R hi1 = (PREC == 0) ? (R)hi1_d : rcp(hi);
     R hfacgrki = hi1 * hi1;
     if (NDIM >= 2) hfacgrki *= hi1;
     if (NDIM >= 3) hfacgrki *= hi1;
-    const R vi[3] = {(R)F.f[V0][i], (R)F.f[V1][i], (R)F.f[V2][i]};
-    const R rhoi = (R)F.f[RHO][i];
-    const R rho1i = (R)1 / rhoi;
+    const R vi[3] = {pi.vx, pi.vy, pi.vz};
+    const R rhoi = pi.rho;
+    const R rho1i = rcp(rhoi);
     const R rho21i = rho1i * rho1i;
-    const R pri = (R)fmax(F.f[PR][i], 0.0);
+    const R pri = pi.pr;
     const R Prho2i = pri * rho21i;
-    const R csi = (R)F.f[CS][i];
-    const R ui = (R)F.f[UU][i];
-    const R mi = (R)F.f[PM][i];
-    const R alphai = (R)F.f[AL0][i], alphaui = (R)F.f[AL1][i], alphaBi = (R)F.f[AL2][i];
-    const R gradhi = (R)F.f[GRADH][i];
+    const R csi = pi.cs;
+    const R ui = pi.u;
+    const R alphai = pi.a0, alphaui = pi.a1, alphaBi = pi.a2;
+    const R gradhi = pi.gradh;
     const bool mhd = (o.imhd != 0);
     R Bi[3] = {0, 0, 0}, Brhoi[3] = {0, 0, 0};
     R B2i = 0, Brho2i = 0, va2i = 0;
     if (mhd) {
+        Bi[0] = pi.Bx; Bi[1] = pi.By; Bi[2] = pi.Bz;
 #pragma unroll
-        for (int d = 0; d < 3; d++) { Bi[d] = (R)F.f[BF0 + d][i]; Brhoi[d] = Bi[d] * rho1i; }
+        for (int d = 0; d < 3; d++) Brhoi[d] = Bi[d] * rho1i;
         B2i = Bi[0] * Bi[0] + Bi[1] * Bi[1] + Bi[2] * Bi[2];
         Brho2i = B2i * rho21i;
         va2i = B2i * rho1i;
@@ -460,11 +502,11 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
     const R vsig2i = csi * csi + va2i;
     const R stressmax = (R)bitsd(a.red->stressmax);
     const R beta = (R)o.beta;
+    const R Kdrag = (R)o.Kdrag;
     const bool i_dust = (typei == NDSPH_ITYPE_DUST);
 
     Acc<R> fx, fy, fz, dbx, dby, dbz, du, dvb, cbx, cby, cbz, d2u, gx, gy, gz;
-    double dtc = 1.e6, dtav = 1.7976931348623157e308, vsmax = 0.0, tsmin = 1.7976931348623157e308;
-    double hcsts = 0.0;
+    R dtc = (R)1.e6, dtav = (R)3.0e38, vsmax = 0, tsmin = (R)3.0e38, hcsts = 0;
 
     Stencil<NDIM> stn(a.S.cell[i], g);
     constexpr int NST = (NDIM == 1) ? 3 : (NDIM == 2 ? 9 : 27);
@@ -479,7 +521,7 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
             const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
             const float hm = fmaxf(hif, xsj.w);
             R dr[3], rij, q2i, q2j, hj1;
-            if (PREC == NDSPH_PREC_FP64) {
+            if constexpr (PREC == NDSPH_PREC_FP64) {
                 const float rc = 2.0f * hm * 1.0002f + abs_tol;
                 if (r2f > rc * rc) continue;
                 double dx[3], rij2;
@@ -495,71 +537,69 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
                     dr[0] = dr[1] = dr[2] = 0;
                 } else {
                     const double ir = 1.0 / rijd;
-                    dr[0] = (R)(dx[0] * ir);
-                    dr[1] = (R)(dx[1] * ir);
-                    dr[2] = (R)(dx[2] * ir);
+                    dr[0] = dx[0] * ir; dr[1] = dx[1] * ir; dr[2] = dx[2] * ir;
                 }
-                rij = (R)rijd; q2i = (R)q2id; q2j = (R)q2jd; hj1 = (R)hj1d;
+                rij = rijd; q2i = q2id; q2j = q2jd; hj1 = hj1d;
             } else {
-                const float hjf = xsj.w;
                 if (!(r2f < 4.0f * hm * hm)) continue;
-                const float rr = sqrtf(r2f);
+                const float ir = rsqrtf(fmaxf(r2f, 1e-37f));
+                const float rr = r2f * ir;
                 if (rr <= 1e-30f) {
                     if (a.S.itype[j] == typei && typei != 2) raise_err(a.red, NDSPH_E_CLUMP, a.S.id[i]);
                     dr[0] = dr[1] = dr[2] = 0;
                 } else {
-                    const float ir = 1.0f / rr;
-                    dr[0] = (R)(dxf[0] * ir); dr[1] = (R)(dxf[1] * ir); dr[2] = (R)(dxf[2] * ir);
+                    dr[0] = dxf[0] * ir; dr[1] = dxf[1] * ir; dr[2] = dxf[2] * ir;
                 }
-                rij = (R)rr;
-                hj1 = (R)(1.0f / hjf);
-                q2i = (R)(r2f / (hif * hif));
-                q2j = (R)(r2f * (float)hj1 * (float)hj1);
+                rij = rr;
+                hj1 = rcp(xsj.w);
+                q2i = r2f * (hi1 * hi1);
+                q2j = r2f * (hj1 * hj1);
             }
             const int typej = a.S.itype[j];
-            const R mj = (R)F.f[PM][j];
-            const R vj[3] = {(R)F.f[V0][j], (R)F.f[V1][j], (R)F.f[V2][j]};
+            PData<R> pj;
+            load_p<PREC>(a, j, pj);
+            const R mj = pj.m;
+            const R vj[3] = {pj.vx, pj.vy, pj.vz};
             const R dvel[3] = {vi[0] - vj[0], vi[1] - vj[1], vi[2] - vj[2]};
-            const R rhoj = (R)F.f[RHO][j];
+            const R rhoj = pj.rho;
             if (type_match(typei, typej)) {
                 // ---------------- rates_core ----------------
                 R hfacgrkj = hj1 * hj1;
                 if (NDIM >= 2) hfacgrkj *= hj1;
                 if (NDIM >= 3) hfacgrkj *= hj1;
                 R gwi, gwj;
-                if (PREC == NDSPH_PREC_FP64) {
-                    gwi = (R)tab_val(a.t.gw, tab_index(a.t, (double)q2i));
-                    gwj = (R)tab_val(a.t.gw, tab_index(a.t, (double)q2j));
+                if constexpr (PREC == NDSPH_PREC_FP64) {
+                    gwi = tab_val(a.t.gw, tab_index(a.t, q2i));
+                    gwj = tab_val(a.t.gw, tab_index(a.t, q2j));
                 } else {
-                    gwi = (R)tab_valf(a.t.gwf, tab_indexf(a.t, (float)q2i));
-                    gwj = (R)tab_valf(a.t.gwf, tab_indexf(a.t, (float)q2j));
+                    gwi = tab_valf(a.t.gwf, tab_indexf(a.t, q2i));
+                    gwj = tab_valf(a.t.gwf, tab_indexf(a.t, q2j));
                 }
                 const R grkerni = gwi * hfacgrki * gradhi;
-                const R grkernj = gwj * hfacgrkj * (R)F.f[GRADH][j];
+                const R grkernj = gwj * hfacgrkj * pj.gradh;
                 const R grkern = (R)0.5 * (grkerni + grkernj);
                 const R dvdotr = dvel[0] * dr[0] + dvel[1] * dr[1] + dvel[2] * dr[2];
-                const R rho1j = (R)1 / rhoj;
+                const R rho1j = rcp(rhoj);
                 const R rho21j = rho1j * rho1j;
                 const R rhoav1 = (R)0.5 * (rho1i + rho1j);
-                const R prj = (R)fmax(F.f[PR][j], 0.0);
+                const R prj = pj.pr;
                 const R Prho2j = prj * rho21j;
-                const R csj = (R)F.f[CS][j];
+                const R csj = pj.cs;
                 R vsigi, vsigj, vsigB;
                 R dB[3] = {0, 0, 0}, Brhoj[3] = {0, 0, 0};
                 R projBrhoi = 0, projBrhoj = 0, projdB = 0, Brho2j = 0;
                 if (mhd) {
-                    R Bj[3];
+                    const R Bj[3] = {pj.Bx, pj.By, pj.Bz};
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
-                        Bj[c] = (R)F.f[BF0 + c][j];
                         Brhoj[c] = Bj[c] * rho1j;
                         dB[c] = Bi[c] - Bj[c];
                     }
                     const R projBi = Bi[0] * dr[0] + Bi[1] * dr[1] + Bi[2] * dr[2];
                     const R projBj = Bj[0] * dr[0] + Bj[1] * dr[1] + Bj[2] * dr[2];
                     projdB = dB[0] * dr[0] + dB[1] * dr[1] + dB[2] * dr[2];
-                    projBrhoi = Brhoi[0] * dr[0] + Brhoi[1] * dr[1] + Brhoi[2] * dr[2];
-                    projBrhoj = Brhoj[0] * dr[0] + Brhoj[1] * dr[1] + Brhoj[2] * dr[2];
+                    projBrhoi = projBi * rho1i;
+                    projBrhoj = projBj * rho1j;
                     const R B2j = Bj[0] * Bj[0] + Bj[1] * Bj[1] + Bj[2] * Bj[2];
                     const R va2j = B2j * rho1j;
                     Brho2j = B2j * rho21j;
@@ -575,25 +615,22 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
                     vsigi = csi; vsigj = csj; vsigB = 0;
                 }
                 R vsig = (R)0.5 * fmax(vsigi + vsigj - beta * dvdotr, (R)0);
-                const R prj_net = prj;
-                R vsigu = sqrt(fabs(pri - prj_net) * rhoav1);
+                R vsigu = sqrt(fabs(pri - prj) * rhoav1);
                 R vsigdtc = fmax(vsig, (R)0.5 * (vsigi + vsigj + beta * fabs(dvdotr)));
                 vsigdtc = fmax(vsigdtc, vsigB);
+                const R hmin = fmin(hi, pj.h);
                 if (i_dust) {
                     vsig = 0; vsigu = 0;
                 } else {
-                    vsmax = fmax(vsmax, (double)vsigdtc);
-                    if ((double)vsigdtc > 1.e-10) {
-                        const double hj_d = F.f[HH][j];
-                        dtc = fmin(dtc, fmin(hi_d, hj_d) / (double)vsigdtc);
-                    }
+                    vsmax = fmax(vsmax, vsigdtc);
+                    if (vsigdtc > (R)1.e-10) dtc = fmin(dtc, hmin / vsigdtc);
                 }
                 R fxi = 0, fyi = 0, fzi = 0;
                 // ---------------- artificial_dissipation ----------------
                 if (o.iav > 0) {
-                    const R alphaav = (R)0.5 * (alphai + (R)F.f[AL0][j]);
-                    const R alphau = (R)0.5 * (alphaui + (R)F.f[AL1][j]);
-                    const R alphaB = (R)0.5 * (alphaBi + (R)F.f[AL2][j]);
+                    const R alphaav = (R)0.5 * (alphai + pj.a0);
+                    const R alphau = (R)0.5 * (alphaui + pj.a1);
+                    const R alphaB = (R)0.5 * (alphaBi + pj.a2);
                     const R vsigav = fmax(fmax(alphaav, alphau), alphaB) * vsig;
                     const R term = vsig * rhoav1 * grkern;
                     const R termu = vsigu * rhoav1 * grkern;
@@ -613,16 +650,13 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
                                          (vj[0] * dr[0] + vj[1] * dr[1] + vj[2] * dr[2]);
                             vissv = -alphaav * (R)0.5 * (tt * tt);
                         }
-                        const R vissu = (o.iener == 1) ? (R)0 : alphau * (ui - (R)F.f[UU][j]);
+                        const R vissu = (o.iener == 1) ? (R)0 : alphau * (ui - pj.u);
                         R vissB = 0;
                         if (o.imhd > 0 && o.imhd != 10 && o.iav >= 2)
                             vissB = -alphaB * (R)0.5 * (dB[0] * dB[0] + dB[1] * dB[1] + dB[2] * dB[2]) * rhoav1;
                         du.add(mj * (term * vissv + termu * vissu + termB * vissB));
                     }
-                    if ((double)vsigav > 1.e-10) {
-                        const double hj_d = F.f[HH][j];
-                        dtav = fmin(dtav, fmin(hi_d, hj_d) / (double)vsigav);
-                    }
+                    if (vsigav > (R)1.e-10) dtav = fmin(dtav, hmin / vsigav);
                 }
                 // ---------------- pressure ----------------
                 const R prterm = Prho2i * grkerni + Prho2j * grkernj;
@@ -630,14 +664,13 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
                 // ---------------- mhd_terms ----------------
                 if (mhd) {
                     const R fiso = (R)0.5 * (Brho2i * grkerni + Brho2j * grkernj);
-                    R fm[3];
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         const R fan = (Brhoi[c] * projBrhoi - stressmax * dr[c] * rho21i) * grkerni +
                                       (Brhoj[c] * projBrhoj - stressmax * dr[c] * rho21j) * grkernj;
-                        fm[c] = fan - fiso * dr[c];
+                        const R fm = mj * (fan - fiso * dr[c]);
+                        if (c == 0) fxi += fm; else if (c == 1) fyi += fm; else fzi += fm;
                     }
-                    fxi += mj * fm[0]; fyi += mj * fm[1]; fzi += mj * fm[2];
                     dvb.add(-mj * projdB * grkern);
                     if (o.imhd > 0) {
                         const R c0 = dB[1] * dr[2] - dB[2] * dr[1];
@@ -653,7 +686,7 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
                 fx.add(fxi); fy.add(fyi); fz.add(fzi);
                 if (o.iav > 0) {
                     if (o.iavlim[1] > 0) {
-                        const R graduterm = (ui - (R)F.f[UU][j]) / rij;
+                        const R graduterm = (ui - pj.u) * rcp(rij);
                         d2u.add(mj * rho1j * graduterm * grkerni);
                     }
                     if (o.iavlim[0] != 3) {
@@ -666,39 +699,39 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
                 // ---------------- drag_forces ----------------
                 const R dv2 = dvel[0] * dvel[0] + dvel[1] * dvel[1] + dvel[2] * dvel[2];
                 R drd[3];
-                if ((double)rij <= 2.220446049250313e-16) {
-                    if ((double)dv2 <= 2.220446049250313e-16) continue;
-                    const R vij = sqrt(dv2);
-                    drd[0] = dvel[0] / vij; drd[1] = dvel[1] / vij; drd[2] = dvel[2] / vij;
+                if (rij <= (R)2.220446049250313e-16) {
+                    if (dv2 <= (R)2.220446049250313e-16) continue;
+                    const R ivij = rcp(sqrt(dv2));
+                    drd[0] = dvel[0] * ivij; drd[1] = dvel[1] * ivij; drd[2] = dvel[2] * ivij;
                 } else {
                     drd[0] = dr[0]; drd[1] = dr[1]; drd[2] = dr[2];
                 }
-                R wgas, ts, csg;
-                R rsum = rhoi + rhoj;
-                ts = rhoj * rhoi / ((R)o.Kdrag * rsum);
+                const R rsum = rhoi + rhoj;
+                const R ts = rhoj * rhoi / (Kdrag * rsum);
+                R wgas, csg;
                 if (typei == NDSPH_ITYPE_GAS || typei == NDSPH_ITYPE_BND) {
                     R wdi;
-                    if (PREC == 0) wdi = (R)tab_val(a.t.wdrag, tab_index(a.t, (double)q2i));
-                    else wdi = (R)tab_valf(a.t.wdragf, tab_indexf(a.t, (float)q2i));
+                    if constexpr (PREC == 0) wdi = tab_val(a.t.wdrag, tab_index(a.t, q2i));
+                    else wdi = tab_valf(a.t.wdragf, tab_indexf(a.t, q2i));
                     R hfw = hi1;
                     if (NDIM >= 2) hfw *= hi1;
                     if (NDIM >= 3) hfw *= hi1;
                     wgas = wdi * hfw;
                     csg = csi;
-                    hcsts = fmax(hcsts, (double)(hi / (csg * ts)));
+                    hcsts = fmax(hcsts, hi / (csg * ts));
                 } else {
                     if (typej != NDSPH_ITYPE_GAS && typej != NDSPH_ITYPE_BND) continue;
                     R wdj;
-                    if (PREC == 0) wdj = (R)tab_val(a.t.wdrag, tab_index(a.t, (double)q2j));
-                    else wdj = (R)tab_valf(a.t.wdragf, tab_indexf(a.t, (float)q2j));
+                    if constexpr (PREC == 0) wdj = tab_val(a.t.wdrag, tab_index(a.t, q2j));
+                    else wdj = tab_valf(a.t.wdragf, tab_indexf(a.t, q2j));
                     R hfw = hj1;
                     if (NDIM >= 2) hfw *= hj1;
                     if (NDIM >= 3) hfw *= hj1;
                     wgas = wdj * hfw;
-                    csg = (R)F.f[CS][j];
-                    hcsts = fmax(hcsts, (double)((R)1 / (hj1 * csg * ts)));
+                    csg = pj.cs;
+                    hcsts = fmax(hcsts, pj.h / (csg * ts));
                 }
-                tsmin = fmin(tsmin, (double)ts);
+                tsmin = fmin(tsmin, ts);
                 const R projv = dvel[0] * drd[0] + dvel[1] * drd[1] + dvel[2] * drd[2];
                 const R dragterm = (R)NDIM * wgas / (rsum * ts) * projv;
                 const R dragterm_en = dragterm * projv;
@@ -710,15 +743,8 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
         }
     }
 
-    // ---- global reductions (warp first) ----
-    for (int off = 16; off > 0; off >>= 1) {
-        dtc = fmin(dtc, __shfl_down_sync(0xffffffffu, dtc, off));
-        dtav = fmin(dtav, __shfl_down_sync(0xffffffffu, dtav, off));
-        vsmax = fmax(vsmax, __shfl_down_sync(0xffffffffu, vsmax, off));
-        tsmin = fmin(tsmin, __shfl_down_sync(0xffffffffu, tsmin, off));
-    }
-
     // ---- per-particle post pass ratesND_mhd.f90:532-965 ----
+    const double hi_d = F.f[HH][i];
     const double rhoi_d = F.f[RHO][i];
     const double rho1 = 1.0 / rhoi_d;
     double force[3] = {fx.val(), fy.val(), fz.val()};
@@ -795,17 +821,55 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
     F.f[DIVB][i] = divB;
     F.f[DEL2U][i] = del2u;
 
-    for (int off = 16; off > 0; off >>= 1) {
-        fonh = fmax(fonh, __shfl_down_sync(0xffffffffu, fonh, off));
-        hcsts = fmax(hcsts, __shfl_down_sync(0xffffffffu, hcsts, off));
+    // ---- global reductions (warp first, then one atomic per warp) ----
+    double rdtc = (double)dtc, rdtav = (double)dtav, rvs = (double)vsmax, rts = (double)tsmin;
+    if (PREC != 0) {
+        if (rdtav > 1e37) rdtav = 1.7976931348623157e308;
+        if (rts > 1e37) rts = 1.7976931348623157e308;
     }
+    for (int off = 16; off > 0; off >>= 1) {
+        rdtc = fmin(rdtc, __shfl_down_sync(0xffffffffu, rdtc, off));
+        rdtav = fmin(rdtav, __shfl_down_sync(0xffffffffu, rdtav, off));
+        rvs = fmax(rvs, __shfl_down_sync(0xffffffffu, rvs, off));
+        rts = fmin(rts, __shfl_down_sync(0xffffffffu, rts, off));
+        fonh = fmax(fonh, __shfl_down_sync(0xffffffffu, fonh, off));
+    }
+    (void)hcsts;
     if ((threadIdx.x & 31) == 0) {
-        atomic_min_pos(&a.red->dtcourant, dtc);
-        atomic_min_pos(&a.red->dtav, dtav);
-        atomic_max_pos(&a.red->vsigmax, vsmax);
-        atomic_min_pos(&a.red->ts_min, tsmin);
+        atomic_min_pos(&a.red->dtcourant, rdtc);
+        atomic_min_pos(&a.red->dtav, rdtav);
+        atomic_max_pos(&a.red->vsigmax, rvs);
+        atomic_min_pos(&a.red->ts_min, rts);
         atomic_max_pos(&a.red->fhmax, fonh);
     }
+}
+
+// FP32 packs (FP32 form): velocities + masses before the density passes,
+// everything the rates sweep reads after the EOS
+__global__ void k_pack_v(SweepArgs a)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    const FieldPtrs& F = a.F;
+    a.S.pk_v[k] = make_float4((float)F.f[V0][k], (float)F.f[V1][k], (float)F.f[V2][k], (float)F.f[PM][k]);
+}
+__global__ void k_pack_rates(SweepArgs a)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    const FieldPtrs& F = a.F;
+    a.S.pk_v[k] = make_float4((float)F.f[V0][k], (float)F.f[V1][k], (float)F.f[V2][k], (float)F.f[PM][k]);
+    a.S.pk_t[k] = make_float4((float)F.f[RHO][k], (float)fmax(F.f[PR][k], 0.0), (float)F.f[CS][k], (float)F.f[UU][k]);
+    a.S.pk_b[k] = make_float4((float)F.f[BF0][k], (float)F.f[BF1][k], (float)F.f[BF2][k], (float)F.f[GRADH][k]);
+    a.S.pk_a[k] = make_float4((float)F.f[AL0][k], (float)F.f[AL1][k], (float)F.f[AL2][k], (float)F.f[HH][k]);
+}
+void launch_pack_v(const SweepArgs& a, cudaStream_t st)
+{
+    if (a.n > 0) k_pack_v<<<nblk(a.n, 256), 256, 0, st>>>(a);
+}
+void launch_pack_rates(const SweepArgs& a, cudaStream_t st)
+{
+    if (a.n > 0) k_pack_rates<<<nblk(a.n, 256), 256, 0, st>>>(a);
 }
 
 void launch_rates(const SweepArgs& a, cudaStream_t st)
