@@ -198,7 +198,7 @@ def _gaussian_field(n1d: int, rng, kmin: float, kmax: float, slope: float) -> np
     band = (kk >= kmin) & (kk <= kmax)
     amp[band] = kk[band] ** (slope / 2.0)
     noise = rng.normal(size=kk.shape) + 1j * rng.normal(size=kk.shape)
-    f = np.fft.irfftn(noise * amp, s=(n1d, n1d, n1d))
+    f = np.fft.irfftn(noise * amp, s=(n1d, n1d, n1d), axes=(0, 1, 2))
     f -= f.mean()
     s = f.std()
     return f / s if s > 0 else f
@@ -232,9 +232,9 @@ def turbulent_box_3d(n1d: int = 128, seed1: int = 11, seed2: int = 12,
     k2[0, 0, 0] = 1.0
     dk = np.fft.rfftn(delta)
     phi = dk / k2                       # s = grad(phi) ... div s = -k2 phi = -delta
-    sx = np.fft.irfftn(1j * kx * phi, s=(n1d,) * 3)
-    sy = np.fft.irfftn(1j * ky * phi, s=(n1d,) * 3)
-    sz = np.fft.irfftn(1j * kz * phi, s=(n1d,) * 3)
+    sx = np.fft.irfftn(1j * kx * phi, s=(n1d,) * 3, axes=(0, 1, 2))
+    sy = np.fft.irfftn(1j * ky * phi, s=(n1d,) * 3, axes=(0, 1, 2))
+    sz = np.fft.irfftn(1j * kz * phi, s=(n1d,) * 3, axes=(0, 1, 2))
     smax = 0.45 * dx * 4.0
     scale = min(1.0, smax / max(np.abs(sx).max(), np.abs(sy).max(), np.abs(sz).max(), 1e-30))
     g = (np.arange(n1d, dtype=np.float64) + 0.5) * dx
@@ -248,9 +248,9 @@ def turbulent_box_3d(n1d: int = 128, seed1: int = 11, seed2: int = 12,
     ay = _gaussian_field(n1d, rng2, 2.0, 32.0, -2.0)
     az = _gaussian_field(n1d, rng2, 2.0, 32.0, -2.0)
     fx, fy, fz = np.fft.rfftn(ax), np.fft.rfftn(ay), np.fft.rfftn(az)
-    vx = np.fft.irfftn(1j * (ky * fz - kz * fy), s=(n1d,) * 3)
-    vy = np.fft.irfftn(1j * (kz * fx - kx * fz), s=(n1d,) * 3)
-    vz = np.fft.irfftn(1j * (kx * fy - ky * fx), s=(n1d,) * 3)
+    vx = np.fft.irfftn(1j * (ky * fz - kz * fy), s=(n1d,) * 3, axes=(0, 1, 2))
+    vy = np.fft.irfftn(1j * (kz * fx - kx * fz), s=(n1d,) * 3, axes=(0, 1, 2))
+    vz = np.fft.irfftn(1j * (kx * fy - ky * fx), s=(n1d,) * 3, axes=(0, 1, 2))
     vrms = math.sqrt(np.mean(vx ** 2 + vy ** 2 + vz ** 2))
     cs = 1.0
     f = mach * cs / vrms if vrms > 0 else 0.0

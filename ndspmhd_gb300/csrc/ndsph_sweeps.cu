@@ -453,8 +453,11 @@ template <int NDIM, int PREC>
 __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
 {
     typedef typename std::conditional<PREC == NDSPH_PREC_FP64, double, float>::type R;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
+    // no early return: every lane of the warp takes part in the final
+    // shuffle reductions; lanes past n run an empty stencil on slot 0
+    const int ithread = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = ithread < a.n;
+    const int i = live ? ithread : 0;
     const FieldPtrs& F = a.F;
     const DevOpts& o = a.o;
     const Grid& g = a.g;
@@ -510,7 +513,7 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
 
     Stencil<NDIM> stn(a.S.cell[i], g);
     constexpr int NST = (NDIM == 1) ? 3 : (NDIM == 2 ? 9 : 27);
-    for (int so = 0; so < NST; so++) {
+    for (int so = 0; so < (live ? NST : 0); so++) {
         int cid, d[3], w[3];
         if (!stn.cell_at(so, g, o, cid, d, w)) continue;
         const int jb = a.cell_start[cid], je = a.cell_start[cid + 1];
@@ -807,19 +810,22 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
         for (int c = 0; c < 3; c++) { force[c] = 0.0; dBe[c] = 0.0; daldt[c] = 0.0; curlB[c] = 0.0; }
         drhodt_out = 0.0; dhdt = 0.0; dudt = 0.0; dendt = 0.0; divB = 0.0;
     }
-    for (int c = 0; c < 3; c++) {
+    if (!live) fonh = 0.0;
+    for (int c = 0; c < 3 && live; c++) {
         F.f[F0 + c][i] = force[c];
         F.f[DB0 + c][i] = dBe[c];
         F.f[DAL0 + c][i] = daldt[c];
         F.f[GDV0 + c][i] = gdv[c];
         if (o.imhd > 0) F.f[CB0 + c][i] = curlB[c];
     }
-    F.f[DRHODT][i] = drhodt_out;
-    F.f[DHDT][i] = dhdt;
-    F.f[DUDT][i] = dudt;
-    F.f[DENDT][i] = dendt;
-    F.f[DIVB][i] = divB;
-    F.f[DEL2U][i] = del2u;
+    if (live) {
+        F.f[DRHODT][i] = drhodt_out;
+        F.f[DHDT][i] = dhdt;
+        F.f[DUDT][i] = dudt;
+        F.f[DENDT][i] = dendt;
+        F.f[DIVB][i] = divB;
+        F.f[DEL2U][i] = del2u;
+    }
 
     // ---- global reductions (warp first, then one atomic per warp) ----
     double rdtc = (double)dtc, rdtav = (double)dtav, rvs = (double)vsmax, rts = (double)tsmin;

@@ -77,11 +77,12 @@ def test_iterate_density(initialised):
     ref.iterate_density()
     g = GpuSPH(o, {k: v.copy() for k, v in st.items()})
     g.iterate_density()
-    assert g.dts()["its"] == ref.dts()["its"], (g.dts(), ref.dts())
+    assert g.dts()["its"] == ref.dts()["its"], (name, g.dts(), ref.dts())
     got = g.state
     errs, bad = compare_fields(got, ref.state, DENS_FIELDS, 1e-12)
     assert not bad, f"{name}: {errs}"
-    assert np.array_equal(got["numneigh"], ref.state["numneigh"]), name
+    nd = np.nonzero(got["numneigh"] != ref.state["numneigh"])[0]
+    assert len(nd) == 0, (name, nd[:10], got["numneigh"][nd[:10]], ref.state["numneigh"][nd[:10]])
     g.close()
 
 
@@ -99,7 +100,7 @@ def test_derivs(initialised):
     assert np.array_equal(g.state["numneigh"], ref.state["numneigh"]), name
     gd, rd = g.dts(), ref.dts()
     for k in ("dtcourant", "dtforce", "dtav", "vsigmax", "stressmax"):
-        assert abs(gd[k] - rd[k]) <= 1e-12 * max(abs(rd[k]), 1e-300), (k, gd[k], rd[k])
+        assert abs(gd[k] - rd[k]) <= 1e-12 * max(abs(rd[k]), 1e-300), (name, k, gd[k], rd[k])
     if o["idust"]:
         assert abs(gd["dtdrag"] - rd["dtdrag"]) <= 1e-12 * rd["dtdrag"]
     g.close()
