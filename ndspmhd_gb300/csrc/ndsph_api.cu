@@ -56,6 +56,9 @@ struct ndsph_ctx {
     // host staging
     double* d_stage = nullptr;   // n*3 doubles
     int* d_istage = nullptr;
+    // neighbour lists
+    int nl_stride = 0;
+    float nl_skin = 1.1f;
     // timing
     bool profiling = false;
     cudaEvent_t ev[16];
@@ -67,6 +70,7 @@ struct ndsph_ctx {
 };
 
 static thread_local std::string g_err;
+static int build_nlist(ndsph_ctx* ctx);
 
 #define CK(call)                                                                          \
     do {                                                                                  \
@@ -232,7 +236,8 @@ static void free_particles(ndsph_ctx* ctx)
     void* ptrs[] = {ctx->slab[0], ctx->slab[1], ctx->S.itype, ctx->S.id, ctx->S.ireal, ctx->S.pos_of_id,
                     ctx->S.numneigh, ctx->S.cell, ctx->S.xs, ctx->S.h1, ctx->S.active, ctx->S.active_next,
                     ctx->S.flag, ctx->itype2, ctx->id2, ctx->ireal2, ctx->srt.key, ctx->srt.slot, ctx->srt.perm,
-                    ctx->d_stage, ctx->d_istage, ctx->S.pk_v, ctx->S.pk_t, ctx->S.pk_b, ctx->S.pk_a};
+                    ctx->d_stage, ctx->d_istage, ctx->S.pk_v, ctx->S.pk_t, ctx->S.pk_b, ctx->S.pk_a,
+                    ctx->S.nl, ctx->S.nl_cnt, ctx->S.hb};
     for (void* p : ptrs) if (p) cudaFree(p);
     ctx->slab[0] = ctx->slab[1] = nullptr;
     memset(&ctx->S, 0, sizeof(ctx->S));
@@ -269,6 +274,10 @@ static int ensure_capacity(ndsph_ctx* ctx, int n)
     CK(cudaMalloc(&ctx->S.pk_t, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_b, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_a, sizeof(float4) * (size_t)cap));
+    CK(cudaMalloc(&ctx->S.nl_cnt, ib));
+    CK(cudaMalloc(&ctx->S.hb, sizeof(float) * (size_t)cap));
+    ctx->S.nl = nullptr;
+    ctx->nl_stride = 0;
     CK(cudaMalloc(&ctx->d_istage, ib));
     CK(cudaMemsetAsync(ctx->S.numneigh, 0, ib, ctx->st));
     ctx->cap = cap;
@@ -423,7 +432,8 @@ static float tdiff(ndsph_ctx* ctx, int a, int b)
 }
 
 // state fields the host hands over (x, vel, Bevol, en, hh, pmass, alpha)
-static const int STATE_FIELDS[] = {X0, X1, X2, V0, V1, V2, BE0, BE1, BE2, EN, HH, PM, AL0, AL1, AL2};
+static const int STATE_FIELDS[] = {X0, X1, X2, V0, V1, V2, BE0, BE1, BE2, EN, HH, PM, AL0, AL1, AL2,
+                                   RHO, RHOALT, DRHODT, DHDT, GRADH, GRADHN, GRADGRADH};
 static const int INCOPY_FIELDS[] = {XIN0, XIN1, XIN2, VIN0, VIN1, VIN2, BIN0, BIN1, BIN2, HIN, ENIN, RHOIN,
                                     ALIN0, ALIN1, ALIN2, FIN0, FIN1, FIN2, DBIN0, DBIN1, DBIN2, DHIN, DENIN,
                                     DALIN0, DALIN1, DALIN2};
@@ -442,17 +452,16 @@ static int upload_inputs(ndsph_ctx* ctx, const ndsph_particles* p, int n, bool w
     rc |= upload_aos(ctx, p->hh, HH, 1, 1, n);
     rc |= upload_aos(ctx, p->pmass, PM, 1, 1, n);
     rc |= upload_aos(ctx, p->alpha, AL0, 3, 3, n);
-    if (with_density) {
-        rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n);
-        rc |= upload_aos(ctx, p->rhoalt, RHOALT, 1, 1, n);
-        rc |= upload_aos(ctx, p->drhodt, DRHODT, 1, 1, n);
-        rc |= upload_aos(ctx, p->dhdt, DHDT, 1, 1, n);
-        rc |= upload_aos(ctx, p->gradh, GRADH, 1, 1, n);
-        rc |= upload_aos(ctx, p->gradhn, GRADHN, 1, 1, n);
-        rc |= upload_aos(ctx, p->gradgradh, GRADGRADH, 1, 1, n);
-    } else {
-        rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n);   // fixed particles keep rho
-    }
+    // the density outputs are module arrays in the reference: fixed particles
+    // (and any particle the NR loop does not touch) carry them through
+    (void)with_density;
+    rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n);
+    rc |= upload_aos(ctx, p->rhoalt, RHOALT, 1, 1, n);
+    rc |= upload_aos(ctx, p->drhodt, DRHODT, 1, 1, n);
+    rc |= upload_aos(ctx, p->dhdt, DHDT, 1, 1, n);
+    rc |= upload_aos(ctx, p->gradh, GRADH, 1, 1, n);
+    rc |= upload_aos(ctx, p->gradhn, GRADHN, 1, 1, n);
+    rc |= upload_aos(ctx, p->gradgradh, GRADGRADH, 1, 1, n);
     if (with_prim) {
         rc |= upload_aos(ctx, p->dens, DENS, 1, 1, n);
         rc |= upload_aos(ctx, p->uu, UU, 1, 1, n);
@@ -578,7 +587,7 @@ static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hma
     launch_post_sort(ctx->S, ctx->srt, n, ctx->g.ncells, ctx->g, ctx->F, ctx->o, st);
     ctx->linked = true;
     CK(cudaGetLastError());
-    return 0;
+    return build_nlist(ctx);
 }
 
 static int link_all(ndsph_ctx* ctx, bool keep_hmax_ghost)
@@ -602,7 +611,41 @@ static SweepArgs sweep_args(ndsph_ctx* ctx)
     a.its = 0;
     a.nlist = 0;
     a.ncalc_next = ctx->d_ncalc;
+    a.nl_ld = ctx->cap;
+    a.nl_stride = ctx->nl_stride;
+    a.nl_skin = ctx->nl_skin;
     return a;
+}
+
+// (re)build the neighbour lists of the current link; grows the stride and
+// rebuilds once if some particle had more candidates than the stride
+static int build_nlist(ndsph_ctx* ctx)
+{
+    cudaStream_t st = ctx->st;
+    if (ctx->nl_stride == 0) {
+        int s0 = ctx->o.ndim == 1 ? 32 : (ctx->o.ndim == 2 ? 64 : 160);
+        CK(cudaMalloc(&ctx->S.nl, sizeof(unsigned) * (size_t)s0 * ctx->cap));
+        ctx->nl_stride = s0;
+    }
+    for (int attempt = 0; attempt < 4; attempt++) {
+        int z[3] = {0, 0, 0};
+        CK(cudaMemcpyAsync(&ctx->red->nl_stale, z, sizeof(int) * 3, cudaMemcpyHostToDevice, st));
+        SweepArgs a = sweep_args(ctx);
+        launch_build_nlist(a, st);
+        CK(cudaGetLastError());
+        int h[3];
+        CK(cudaMemcpyAsync(h, &ctx->red->nl_stale, sizeof(int) * 3, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (!h[1]) return 0;
+        // overflow: grow to the largest count seen (+25%) and rebuild
+        int ns = h[2] + h[2] / 4 + 8;
+        CK(cudaFree(ctx->S.nl));
+        ctx->S.nl = nullptr;
+        CK(cudaMalloc(&ctx->S.nl, sizeof(unsigned) * (size_t)ns * ctx->cap));
+        ctx->nl_stride = ns;
+    }
+    ctx->err = "neighbour list stride did not converge";
+    return NDSPH_E_CAPACITY;
 }
 
 // iterate_density iterate_density.f90:43-360 on the linked device state
@@ -673,6 +716,11 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
         redolink = ctx->h_red->redolink != 0;
         ncalc = h_ncalc;
         std::swap(ctx->S.active, ctx->S.active_next);
+        if (ctx->h_red->nl_stale && !redolink) {
+            launch_h1(ctx->F, ctx->S, n, st);   // list radius from the current h
+            rc = build_nlist(ctx);
+            if (rc) return rc;
+        }
     }
     ctx->timing.density_ms = dens_ms;
     ctx->timing.density_pass1_ms = pass1_ms;

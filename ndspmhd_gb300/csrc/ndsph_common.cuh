@@ -94,6 +94,10 @@ struct Reduce {
     unsigned long long xlo[3];      // order-preserving bits of min x (bounding box)
     unsigned long long xhi[3];      // order-preserving bits of max x
     double h_on_csts_max;
+    int nl_stale;                   // some h outgrew the neighbour-list skin
+    int nl_overflow;                // some particle had more candidates than the list stride
+    int nl_maxcnt;                  // largest list length of the last build
+    int pad2;
 };
 
 __host__ __device__ inline unsigned long long dbits(double v)

@@ -27,6 +27,11 @@ struct Side {
     float4* pk_t;     // (rho, max(P,0), c_s, u)
     float4* pk_b;     // (Bx, By, Bz, gradh)
     float4* pk_a;     // (alpha1, alpha2, alpha3, h)
+    // neighbour lists (ELL layout: entry k of slot i at nl[k*nl_ld + i]);
+    // each entry packs (j << 5) | stencil offset of j's cell
+    unsigned* nl;
+    int* nl_cnt;
+    float* hb;        // h of each slot when its list was built
 };
 
 struct SortScratch {
@@ -52,6 +57,9 @@ struct SweepArgs {
     int its;                 // NR pass number (1-based)
     int nlist;               // partial pass: entries in S.active
     int* ncalc_next;         // partial: counter of the next active list
+    long long nl_ld;         // leading dimension of the list (>= n)
+    int nl_stride;           // entries per particle
+    float nl_skin;           // list radius = 2 max(h_i,h_j) skin (h may grow by skin before a rebuild)
 };
 
 // ---- link / sort (ndsph_kernels.cu) ------------------------------------------
@@ -96,6 +104,7 @@ void launch_p2c_post(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
 void launch_density(const SweepArgs& a, bool full, cudaStream_t st);
 void launch_rates(const SweepArgs& a, cudaStream_t st);
 void launch_pack_v(const SweepArgs& a, cudaStream_t st);
+void launch_build_nlist(const SweepArgs& a, cudaStream_t st);
 void launch_pack_rates(const SweepArgs& a, cudaStream_t st);
 // neighbour CSR for parity tests: counts (mode) then fill
 void launch_neigh_count(const SweepArgs& a, int mode, long long* counts, cudaStream_t st);

@@ -117,6 +117,18 @@ struct Stencil {
         cid = (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
         return true;
     }
+    // offsets and wrap flags of a stored stencil index (the cell exists)
+    __device__ __forceinline__ void offset(int o, const Grid& g, int d[3], int w[3]) const
+    {
+        d[0] = o % 3 - 1;
+        d[1] = (NDIM >= 2) ? (o / 3) % 3 - 1 : 0;
+        d[2] = (NDIM >= 3) ? o / 9 - 1 : 0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const int c = cc[k] + d[k];
+            w[k] = (k < NDIM) ? ((c < 0) ? -1 : ((c >= g.nc[k]) ? 1 : 0)) : 0;
+        }
+    }
 };
 
 // periodic image of x_j as the reference's ghost would place it, and the
@@ -228,12 +240,13 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
     int nn = 0;
 
     Stencil<NDIM> stn(a.S.cell[i], g);
-    constexpr int NST = (NDIM == 1) ? 3 : (NDIM == 2 ? 9 : 27);
-    for (int so = 0; so < NST; so++) {
-        int cid, d[3], w[3];
-        if (!stn.cell_at(so, g, o, cid, d, w)) continue;
-        const int jb = a.cell_start[cid], je = a.cell_start[cid + 1];
-        for (int j = jb; j < je; j++) {
+    const int ncand = a.S.nl_cnt[i];
+    {
+        for (int k = 0; k < ncand; k++) {
+            const unsigned pk = a.S.nl[(size_t)k * a.nl_ld + i];
+            const int j = (int)(pk >> 5);
+            int d[3], w[3];
+            stn.offset((int)(pk & 31u), g, d, w);
             const float4 xsj = a.S.xs[j];
             float dxf[3];
             const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
@@ -368,6 +381,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
         a.S.active_next[k] = i;
         if (a.its <= o.maxdensits) hdst[i] = hnew;
         if (hnew > bitsd(a.red->hmax_ghost)) relink = true;
+        if ((float)hnew > a.S.hb[i] * a.nl_skin) a.red->nl_stale = 1;
     } else {
         drhodt = drhodt * gradh;
         F.f[DHDT][i] = dhdrhoi * drhodt;
@@ -512,13 +526,14 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
     R dtc = (R)1.e6, dtav = (R)3.0e38, vsmax = 0, tsmin = (R)3.0e38, hcsts = 0;
 
     Stencil<NDIM> stn(a.S.cell[i], g);
-    constexpr int NST = (NDIM == 1) ? 3 : (NDIM == 2 ? 9 : 27);
-    for (int so = 0; so < (live ? NST : 0); so++) {
-        int cid, d[3], w[3];
-        if (!stn.cell_at(so, g, o, cid, d, w)) continue;
-        const int jb = a.cell_start[cid], je = a.cell_start[cid + 1];
-        for (int j = jb; j < je; j++) {
+    const int ncand = live ? a.S.nl_cnt[i] : 0;
+    {
+        for (int k = 0; k < ncand; k++) {
+            const unsigned pk = a.S.nl[(size_t)k * a.nl_ld + i];
+            const int j = (int)(pk >> 5);
             if (j == i) continue;
+            int d[3], w[3];
+            stn.offset((int)(pk & 31u), g, d, w);
             const float4 xsj = a.S.xs[j];
             float dxf[3];
             const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
@@ -892,6 +907,55 @@ void launch_rates(const SweepArgs& a, cudaStream_t st)
         else if (a.o.ndim == 2) k_rates<2, 1><<<nb, bs, 0, st>>>(a);
         else k_rates<3, 1><<<nb, bs, 0, st>>>(a);
     }
+}
+
+
+// ===========================================================================
+// neighbour lists: every candidate j (self included) of slot i with
+// |x_i - x_j| < 2 max(h_i, h_j) skin (+ FP32 margin), from the 3^NDIM stencil.
+// The sweeps then test only these; a list is rebuilt when some h grows by
+// more than `skin` (NR epilogue flag) and after every link.
+// ===========================================================================
+template <int NDIM>
+__global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const Grid& g = a.g;
+    const float4 xsi = a.S.xs[i];
+    const float hi = xsi.w;
+    const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
+    const float sk = 2.0f * a.nl_skin * 1.0002f;
+    Stencil<NDIM> stn(a.S.cell[i], g);
+    constexpr int NST = (NDIM == 1) ? 3 : (NDIM == 2 ? 9 : 27);
+    int cnt = 0;
+    for (int so = 0; so < NST; so++) {
+        int cid, d[3], w[3];
+        if (!stn.cell_at(so, g, a.o, cid, d, w)) continue;
+        const int jb = a.cell_start[cid], je = a.cell_start[cid + 1];
+        for (int j = jb; j < je; j++) {
+            const float4 xsj = a.S.xs[j];
+            float dxf[3];
+            const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
+            const float rc = sk * fmaxf(hi, xsj.w) + abs_tol;
+            if (r2f > rc * rc) continue;
+            if (cnt < a.nl_stride) a.S.nl[(size_t)cnt * a.nl_ld + i] = ((unsigned)j << 5) | (unsigned)so;
+            cnt++;
+        }
+    }
+    a.S.nl_cnt[i] = cnt < a.nl_stride ? cnt : a.nl_stride;
+    a.S.hb[i] = hi;
+    if (cnt > a.nl_stride) a.red->nl_overflow = 1;
+    atomicMax(&a.red->nl_maxcnt, cnt);
+}
+
+void launch_build_nlist(const SweepArgs& a, cudaStream_t st)
+{
+    if (a.n <= 0) return;
+    const int nb = nblk(a.n, 128);
+    if (a.o.ndim == 1) k_build_nlist<1><<<nb, 128, 0, st>>>(a);
+    else if (a.o.ndim == 2) k_build_nlist<2><<<nb, 128, 0, st>>>(a);
+    else k_build_nlist<3><<<nb, 128, 0, st>>>(a);
 }
 
 // ===========================================================================
