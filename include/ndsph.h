@@ -225,6 +225,30 @@ NDSPH_API int ndsph_neighbour_csr(ndsph_ctx* ctx, int32_t mode, int64_t* offsets
  * doubles: wij, grwij, grgrwij, wijdrag, grwijdrag.                            */
 NDSPH_API int ndsph_kernel_tables(int32_t ndim, double* out);
 
+/* ---- allocation-free entry point -------------------------------------------
+ * No counterpart in the reference: an added entry point for callers that may
+ * not allocate device memory when they call (device memory owned by another
+ * runtime's pool, e.g. an OpenACC/OpenMP-offload host that maps the module
+ * arrays itself; real-time loops that must not take cudaMalloc's implicit
+ * synchronisation; applications that reserve all device memory up front).
+ * It runs the first density pass of iterate_density with every particle
+ * treated as converged (the maxdensits = 0 case): rho, gradh (= 1/omega),
+ * drhodt (normalised by gradh) and numneigh for particles that are not fixed.
+ * All pointers are DEVICE pointers in the host layout of ndsph_particles
+ * (x(ndim,n), vel(3,n)); `stream` is a cudaStream_t (NULL = legacy stream);
+ * the call returns after the stream has finished its work.
+ * Scratch: one file-scope __device__ array of about 5 MB (held by every GPU
+ * that loads the library until exit); npart <= 262144 and cells <= 262144,
+ * larger sizes return NDSPH_E_CAPACITY (message on stderr).  Calls share
+ * the scratch, so calls that overlap on the GPU race; each call clears what
+ * must start at zero.  The first call on a device takes the scratch's device
+ * address (cudaGetSymbolAddress) and uploads the kernel table: make it before
+ * any stream capture.  No cudaMalloc, cudaFree or allocating library call.   */
+NDSPH_API int ndsph_density_noalloc(const ndsph_opts* opts, const double* d_x, const double* d_hh,
+                                    const double* d_pmass, const double* d_vel, const int32_t* d_itype,
+                                    int32_t npart, double* d_rho, double* d_drhodt, double* d_gradh,
+                                    int32_t* d_numneigh, void* stream);
+
 /* per-kernel device timings of the last call (ms), for the bench's roofline. */
 typedef struct ndsph_timing {
     float link_ms, density_ms, density_pass1_ms, eos_ms, rates_ms, post_ms, step_ms, total_ms;
