@@ -38,6 +38,9 @@ void launch_boundary_wrap(FieldPtrs F, DevOpts o, int n, cudaStream_t st)
 // particle bounding box (linkND.f90:80-89) in one pass
 __global__ void k_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst)
 {
+    // block-level reduction first: one set of atomics per block, not per warp
+    __shared__ double sh[8];
+    __shared__ unsigned long long slo[8][3], shi[8][3];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double h = (i < n) ? F.f[HH][i] : 0.0;
     unsigned long long lo[3], hi[3];
@@ -49,7 +52,6 @@ __global__ void k_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned 
             lo[d] = ~0ull; hi[d] = 0ull;
         }
     }
-    // warp reduce
     for (int off = 16; off > 0; off >>= 1) {
         h = fmax(h, __shfl_down_sync(0xffffffffu, h, off));
         for (int d = 0; d < 3; d++) {
@@ -59,7 +61,21 @@ __global__ void k_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned 
             hi[d] = b > hi[d] ? b : hi[d];
         }
     }
-    if ((threadIdx.x & 31) == 0) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sh[warp] = h;
+        for (int d = 0; d < 3; d++) { slo[warp][d] = lo[d]; shi[warp][d] = hi[d]; }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = blockDim.x >> 5;
+        for (int w = 1; w < nw; w++) {
+            h = fmax(h, sh[w]);
+            for (int d = 0; d < 3; d++) {
+                lo[d] = slo[w][d] < lo[d] ? slo[w][d] : lo[d];
+                hi[d] = shi[w][d] > hi[d] ? shi[w][d] : hi[d];
+            }
+        }
         atomicMax(dst, dbits(h));
         for (int d = 0; d < ndim; d++) {
             atomicMin(&red->xlo[d], lo[d]);

@@ -463,8 +463,11 @@ __device__ __forceinline__ R rcp(R x)
     else return 1.0 / x;
 }
 
+#ifndef NDSPH_RATES_FP32_MINB
+#define NDSPH_RATES_FP32_MINB 4
+#endif
 template <int NDIM, int PREC>
-__global__ void __launch_bounds__(128) k_rates(SweepArgs a)
+__global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_rates(SweepArgs a)
 {
     typedef typename std::conditional<PREC == NDSPH_PREC_FP64, double, float>::type R;
     // no early return: every lane of the warp takes part in the final
@@ -761,81 +764,77 @@ __global__ void __launch_bounds__(128) k_rates(SweepArgs a)
         }
     }
 
-    // ---- per-particle post pass ratesND_mhd.f90:532-965 ----
-    const double hi_d = F.f[HH][i];
-    const double rhoi_d = F.f[RHO][i];
-    const double rho1 = 1.0 / rhoi_d;
-    double force[3] = {fx.val(), fy.val(), fz.val()};
-    double dBe[3] = {dbx.val(), dby.val(), dbz.val()};
-    double dudt = du.val();
-    double divB = dvb.val();
-    double curlB[3] = {cbx.val(), cby.val(), cbz.val()};
-    const double del2u = d2u.val();
-    double gdv[3] = {gx.val(), gy.val(), gz.val()};
+    // ---- per-particle post pass ratesND_mhd.f90:532-965 (in the pair
+    // precision R: FP64 for the parity form, FP32 for the FP32 form) ----
+    const R hi_p = (PREC == 0) ? (R)F.f[HH][i] : hi;
+    const R rho1 = (PREC == 0) ? (R)(1.0 / F.f[RHO][i]) : rho1i;
+    R force[3] = {(R)fx.val(), (R)fy.val(), (R)fz.val()};
+    R dBe[3] = {(R)dbx.val(), (R)dby.val(), (R)dbz.val()};
+    R dudt = (R)du.val();
+    R divB = (R)dvb.val();
+    R curlB[3] = {(R)cbx.val(), (R)cby.val(), (R)cbz.val()};
+    const R del2u = (R)d2u.val();
+    const R gdv[3] = {(R)gx.val(), (R)gy.val(), (R)gz.val()};
     if (mhd) {
         if (o.imhd > 0)
             for (int c = 0; c < 3; c++) curlB[c] *= rho1;
         divB *= rho1;
     }
-    const double fmag = sqrt(force[0] * force[0] + force[1] * force[1] + force[2] * force[2]);
-    double fonh = fmag / hi_d;
-    if (typei == 1) fonh = 0.0;
-    double va2 = 0.0;
-    if (mhd) {
-        const double b0 = F.f[BF0][i], b1 = F.f[BF1][i], b2 = F.f[BF2][i];
-        va2 = (b0 * b0 + b1 * b1 + b2 * b2) / F.f[DENS][i];
-    }
-    const double csd = F.f[CS][i];
-    const double vsig = sqrt(csd * csd + va2);
-    const double drhodt = F.f[DRHODT][i];
+    const R fmag = sqrt(force[0] * force[0] + force[1] * force[1] + force[2] * force[2]);
+    R fonh_r = fmag / hi_p;
+    if (typei == 1) fonh_r = 0;
+    R va2 = 0;
+    if (mhd) va2 = B2i * rho1i;   // B^2/dens with dens = rho
+    const R vsig = sqrt(csi * csi + va2);
+    const R drhodt = (R)F.f[DRHODT][i];
     if (o.imhd >= 11 && o.imhd <= 19) {
-        for (int c = 0; c < 3; c++) dBe[c] = dBe[c] + F.f[BE0 + c][i] * rho1 * drhodt;
+        for (int c = 0; c < 3; c++) dBe[c] = dBe[c] + (R)F.f[BE0 + c][i] * rho1 * drhodt;
     } else if (o.imhd >= 1 && o.imhd <= 9) {
         for (int c = 0; c < 3; c++) dBe[c] = dBe[c] * rho1;
     } else {
-        dBe[0] = dBe[1] = dBe[2] = 0.0;
+        dBe[0] = dBe[1] = dBe[2] = 0;
     }
-    double dendt;
+    R dendt;
     if (o.iener > 0 && o.iav >= 0 && o.iener != 3 && o.iener != 10 && o.iener != 11) {
-        dudt = dudt + F.f[PR][i] * (rho1 * rho1) * drhodt;
+        dudt = dudt + pri * (rho1 * rho1) * drhodt;
         dendt = dudt;
     } else {
         dendt = dudt;
     }
-    if (typei == NDSPH_ITYPE_DUST) dendt = 0.0;
-    double daldt[3] = {0.0, 0.0, 0.0};
+    if (typei == NDSPH_ITYPE_DUST) dendt = 0;
+    R daldt[3] = {0, 0, 0};
     if (o.iavlim[0] != 0 || o.iavlim[1] != 0 || o.iavlim[2] != 0) {
-        const double tdecay1 = (o.avdecayconst * vsig) / hi_d;
-        const double a0 = F.f[AL0][i];
+        const R tdecay1 = ((R)o.avdecayconst * vsig) / hi_p;
         if (o.iavlim[0] == 1 || o.iavlim[0] == 2) {
-            double source = fmax(drhodt * rho1, 0.0);
-            if (o.iavlim[0] == 2) source = source * (2.0 - a0);
-            daldt[0] = (o.alphamin - a0) * tdecay1 + o.avfact * source;
+            R source = fmax(drhodt * rho1, (R)0);
+            if (o.iavlim[0] == 2) source = source * ((R)2 - alphai);
+            daldt[0] = ((R)o.alphamin - alphai) * tdecay1 + (R)o.avfact * source;
         }
         if (o.iener > 0 && o.iavlim[1] > 0) {
-            const double uu = F.f[UU][i];
-            double sourceu = 0.0;
-            if (uu > 2.220446049250313e-16) sourceu = hi_d * fabs(del2u) / sqrt(uu);
-            daldt[1] = (o.alphaumin - F.f[AL1][i]) * tdecay1 + sourceu;
+            R sourceu = 0;
+            if (ui > (R)2.220446049250313e-16) sourceu = hi_p * fabs(del2u) / sqrt(ui);
+            daldt[1] = ((R)o.alphaumin - alphaui) * tdecay1 + sourceu;
         }
     }
-    double dhdt = F.f[DHDT][i];
-    double drhodt_out = drhodt;
+    R drhodt_out = drhodt;
+    bool zero_dh = false;
     if (typei == NDSPH_ITYPE_BND || typei == NDSPH_ITYPE_BNDDUST) {
-        for (int c = 0; c < 3; c++) { force[c] = 0.0; dBe[c] = 0.0; daldt[c] = 0.0; curlB[c] = 0.0; }
-        drhodt_out = 0.0; dhdt = 0.0; dudt = 0.0; dendt = 0.0; divB = 0.0;
+        for (int c = 0; c < 3; c++) { force[c] = 0; dBe[c] = 0; daldt[c] = 0; curlB[c] = 0; }
+        drhodt_out = 0; dudt = 0; dendt = 0; divB = 0;
+        zero_dh = true;
     }
-    if (!live) fonh = 0.0;
-    for (int c = 0; c < 3 && live; c++) {
-        F.f[F0 + c][i] = force[c];
-        F.f[DB0 + c][i] = dBe[c];
-        F.f[DAL0 + c][i] = daldt[c];
-        F.f[GDV0 + c][i] = gdv[c];
-        if (o.imhd > 0) F.f[CB0 + c][i] = curlB[c];
-    }
+    double fonh = live ? (double)fonh_r : 0.0;
     if (live) {
-        F.f[DRHODT][i] = drhodt_out;
-        F.f[DHDT][i] = dhdt;
+        for (int c = 0; c < 3; c++) {
+            F.f[F0 + c][i] = force[c];
+            F.f[DB0 + c][i] = dBe[c];
+            F.f[DAL0 + c][i] = daldt[c];
+            F.f[GDV0 + c][i] = gdv[c];
+            if (o.imhd > 0) F.f[CB0 + c][i] = curlB[c];
+        }
+        if (zero_dh) { F.f[DRHODT][i] = 0.0; F.f[DHDT][i] = 0.0; }
+        else if (PREC != 0) { /* drhodt unchanged */ }
+        if (PREC == 0) F.f[DRHODT][i] = drhodt_out;
         F.f[DUDT][i] = dudt;
         F.f[DENDT][i] = dendt;
         F.f[DIVB][i] = divB;
