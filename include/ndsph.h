@@ -256,8 +256,22 @@ typedef struct ndsph_timing {
     int32_t launches;
     int64_t pairs_density;   /* accepted (i,j) pairs summed in pass 1          */
     int64_t pairs_rates;     /* accepted (i,j) pairs in the rates sweep        */
+    float   mlp_loss;        /* learned h: last minibatch loss (z units^2)     */
+    float   mlp_ms;          /* learned h: inference + training time per step  */
+    int32_t mlp_updates;     /* learned h: optimiser steps taken so far        */
+    int32_t pad;
 } ndsph_timing;
 NDSPH_API int ndsph_get_timing(ndsph_ctx* ctx, ndsph_timing* t);
+
+/* ---- learned-h predictor: standalone forward / gradient (tests) ------------
+ * params: the 1313 FP32 master weights (W1[32][6], b1[32], W2[32][32], b2[32],
+ * W3[32], b3); feats[n][6]; host buffers.  ndsph_mlp_forward runs the
+ * tensor-core inference (BF16 operands, FP32 accumulation); ndsph_mlp_grad
+ * the training kernel: grad of mean((out - target)^2) and that loss.  No
+ * reference counterpart (the learned part is new).                           */
+NDSPH_API int ndsph_mlp_forward(const float* params, const float* feats, int32_t n, float* out);
+NDSPH_API int ndsph_mlp_grad(const float* params, const float* feats, const float* targets, int32_t n,
+                             float* grad, float* loss);
 NDSPH_API int ndsph_set_profiling(ndsph_ctx* ctx, int32_t on);
 
 #ifdef __cplusplus

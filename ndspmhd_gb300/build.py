@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUTDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUTDIR, "libndsph_gpu.so")
-SOURCES = ["ndsph_api.cu", "ndsph_kernels.cu", "ndsph_sweeps.cu", "ndsph_noalloc.cu"]
+SOURCES = ["ndsph_api.cu", "ndsph_kernels.cu", "ndsph_sweeps.cu", "ndsph_noalloc.cu", "ndsph_mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr"]

@@ -13,6 +13,7 @@
 #include <vector>
 #include <algorithm>
 #include "ndsph_launch.h"
+#include "ndsph_mlp.h"
 
 namespace ndsph {
 void launch_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, cudaStream_t st);
@@ -59,6 +60,17 @@ struct ndsph_ctx {
     // neighbour lists
     int nl_stride = 0;
     float nl_skin = 1.1f;
+    // learned-h predictor
+    float* mlp_p = nullptr;      // FP32 master weights
+    float* mlp_m = nullptr;      // Adam moments
+    float* mlp_v = nullptr;
+    float* mlp_g = nullptr;      // gradient
+    float* mlp_loss = nullptr;
+    MlpFrag* mlp_frag = nullptr; // BF16 tensor-core operands
+    int mlp_step = 0;
+    float mlp_lr = 2.e-3f;
+    int mlp_batch = 16384;
+    int mlp_iters = 4;
     // timing
     bool profiling = false;
     cudaEvent_t ev[16];
@@ -353,6 +365,25 @@ extern "C" int ndsph_init(ndsph_ctx** out, const ndsph_opts* opts, int32_t nmax)
     ctx->t.ggwf = ctx->tab32 + 2 * NTAB; ctx->t.wdragf = ctx->tab32 + 3 * NTAB;
     ctx->t.dq2table = dq2; ctx->t.ddq2table = ddq2;
     ctx->t.dq2tablef = (float)dq2; ctx->t.ddq2tablef = (float)ddq2;
+    if (opts->learned_h) {
+        if (cudaMalloc(&ctx->mlp_p, sizeof(float) * MLP_NPARAM) != cudaSuccess ||
+            cudaMalloc(&ctx->mlp_m, sizeof(float) * MLP_NPARAM) != cudaSuccess ||
+            cudaMalloc(&ctx->mlp_v, sizeof(float) * MLP_NPARAM) != cudaSuccess ||
+            cudaMalloc(&ctx->mlp_g, sizeof(float) * MLP_NPARAM) != cudaSuccess ||
+            cudaMalloc(&ctx->mlp_loss, sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&ctx->mlp_frag, sizeof(MlpFrag)) != cudaSuccess) {
+            g_err = "cudaMalloc failed (learned h)";
+            ndsph_finalize(ctx);
+            return NDSPH_E_CUDA;
+        }
+        std::vector<float> p0;
+        mlp_init_params(p0, 12345u);
+        cudaMemcpy(ctx->mlp_p, p0.data(), sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice);
+        cudaMemset(ctx->mlp_m, 0, sizeof(float) * MLP_NPARAM);
+        cudaMemset(ctx->mlp_v, 0, sizeof(float) * MLP_NPARAM);
+        launch_mlp_pack(ctx->mlp_p, ctx->mlp_frag, ctx->st);
+        cudaStreamSynchronize(ctx->st);
+    }
     if (nmax > 0 && ensure_capacity(ctx, nmax)) {
         g_err = ctx->err;
         ndsph_finalize(ctx);
@@ -368,7 +399,8 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     free_particles(ctx);
     void* ptrs[] = {ctx->tab64, ctx->tab32, ctx->red, ctx->d_dtout, ctx->d_ncalc, ctx->d_fields,
-                    ctx->srt.count, ctx->srt.start, ctx->srt.blocksums};
+                    ctx->srt.count, ctx->srt.start, ctx->srt.blocksums, ctx->mlp_p, ctx->mlp_m, ctx->mlp_v,
+                    ctx->mlp_g, ctx->mlp_loss, ctx->mlp_frag};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (ctx->h_red) cudaFreeHost(ctx->h_red);
     if (ctx->h_dtout) cudaFreeHost(ctx->h_dtout);
@@ -1001,6 +1033,64 @@ extern "C" int ndsph_primitive2conservative(ndsph_ctx* ctx, ndsph_particles* p, 
     return rc;
 }
 
+static const int MLP_FIELDS[] = {HPRED, YPREV, FT0, FT1, FT2, FT3, FT4, FT5};
+
+// learned h, before the link: features of the previous step, h_pred -> h_init
+static void mlp_infer(ndsph_ctx* ctx)
+{
+    MlpInferArgs a;
+    memset(&a, 0, sizeof a);
+    a.n = ctx->n;
+    a.ndim = ctx->o.ndim;
+    a.dt = ctx->dt;
+    a.hfact = ctx->o.hfact;
+    const double pi = 3.141592653589793;
+    const double r = 2.0 * ctx->o.hfact;
+    a.nn_ref = (a.ndim == 3) ? 4.0 / 3.0 * pi * r * r * r : ((a.ndim == 2) ? pi * r * r : 2.0 * r);
+    a.zclip = 15.0;            // |log(h_init/h_pred)| <= 0.15
+    a.apply = 1;
+    a.fixed = ctx->o.has_fixed;
+    a.hin = ctx->F.f[HIN];
+    a.rho = ctx->F.f[RHO];
+    a.drhodt = ctx->F.f[DRHODT];
+    a.cs = ctx->F.f[CS];
+    a.pmass = ctx->F.f[PM];
+    a.yprev = ctx->F.f[YPREV];
+    a.numneigh = ctx->S.numneigh;
+    a.itype = ctx->S.itype;
+    a.hh = ctx->F.f[HH];
+    a.hpred = ctx->F.f[HPRED];
+    for (int k = 0; k < MLP_NIN; k++) a.feat[k] = ctx->F.f[FT0 + k];
+    launch_mlp_infer(ctx->mlp_frag, a, ctx->st);
+}
+
+// learned h, after the density iteration: train on (features, converged h)
+static void mlp_train(ndsph_ctx* ctx)
+{
+    cudaStream_t st = ctx->st;
+    const long long n = ctx->n;
+    for (int it = 0; it < ctx->mlp_iters; it++) {
+        MlpTrainArgs a;
+        memset(&a, 0, sizeof a);
+        a.nbatch = (int)std::min<long long>(ctx->mlp_batch, n);
+        a.n = n;
+        // strided sample: stride coprime with n, offset varies per update
+        long long stride = n / std::max(a.nbatch, 1);
+        if (stride < 1) stride = 1;
+        while (stride > 1 && std::__gcd(stride, n) != 1) stride--;
+        a.stride = stride;
+        a.offset = (long long)(ctx->mlp_step * 7919LL + it * 104729LL) % n;
+        for (int k = 0; k < MLP_NIN; k++) a.feat[k] = ctx->F.f[FT0 + k];
+        a.hconv = ctx->F.f[HH];
+        a.hpred = ctx->F.f[HPRED];
+        launch_mlp_grad(ctx->mlp_p, a, ctx->mlp_g, ctx->mlp_loss, st);
+        ctx->mlp_step++;
+        launch_mlp_adam(ctx->mlp_p, ctx->mlp_m, ctx->mlp_v, ctx->mlp_g, ctx->mlp_step, ctx->mlp_lr, st);
+    }
+    launch_mlp_pack(ctx->mlp_p, ctx->mlp_frag, st);
+    launch_mlp_store_y(ctx->F.f[HH], ctx->F.f[HPRED], ctx->F.f[YPREV], ctx->n, st);
+}
+
 // one leapfrog step on the device state (stepND_leapfrog_mhd.f90:31-275)
 static int dev_step_once(ndsph_ctx* ctx)
 {
@@ -1008,11 +1098,32 @@ static int dev_step_once(ndsph_ctx* ctx)
     // dt lives in the Reduce block
     CK(cudaMemcpyAsync(&ctx->red->dt, &ctx->dt, sizeof(double), cudaMemcpyHostToDevice, st));
     launch_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+    const bool learned = ctx->opts.learned_h && ctx->mlp_p;
+    if (learned) {
+        tmark(ctx, 12);
+        mlp_infer(ctx);
+        tmark(ctx, 13);
+    }
     std::vector<int> live;
     for (int f : STATE_FIELDS) live.push_back(f);
     for (int f : INCOPY_FIELDS) live.push_back(f);
+    if (learned)
+        for (int f : MLP_FIELDS) live.push_back(f);
     int rc = do_derivs(ctx, live.data(), (int)live.size());
     if (rc) return rc;
+    if (learned) {
+        tmark(ctx, 14);
+        mlp_train(ctx);
+        tmark(ctx, 15);
+        if (ctx->profiling) {
+            float loss = 0.f;
+            cudaMemcpyAsync(&loss, ctx->mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, st);
+            cudaStreamSynchronize(st);
+            ctx->timing.mlp_loss = loss;
+            ctx->timing.mlp_ms = tdiff(ctx, 12, 13) + tdiff(ctx, 14, 15);
+        }
+        ctx->timing.mlp_updates = ctx->mlp_step;
+    }
     launch_corrector(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
     rc = sync_red(ctx);
     if (rc) return rc;
@@ -1020,6 +1131,58 @@ static int dev_step_once(ndsph_ctx* ctx)
     ctx->dt = ctx->h_dtout[6];
     ctx->nsteps++;
     return 0;
+}
+
+// standalone MLP entry points for the tests (host buffers)
+extern "C" int ndsph_mlp_forward(const float* params, const float* feats, int32_t n, float* out)
+{
+    if (!params || n < 0 || (n > 0 && (!feats || !out))) return NDSPH_E_ARG;
+    if (n == 0) return 0;
+    float *dp = nullptr, *df = nullptr, *dout = nullptr;
+    MlpFrag* fr = nullptr;
+    int rc = 0;
+    if (cudaMalloc(&dp, sizeof(float) * MLP_NPARAM) != cudaSuccess || cudaMalloc(&fr, sizeof(MlpFrag)) != cudaSuccess ||
+        cudaMalloc(&df, sizeof(float) * (size_t)n * MLP_NIN) != cudaSuccess ||
+        cudaMalloc(&dout, sizeof(float) * (size_t)n) != cudaSuccess) {
+        rc = NDSPH_E_CUDA;
+    } else {
+        cudaMemcpy(dp, params, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice);
+        cudaMemcpy(df, feats, sizeof(float) * (size_t)n * MLP_NIN, cudaMemcpyHostToDevice);
+        launch_mlp_pack(dp, fr, 0);
+        launch_mlp_forward(fr, df, n, dout, 0);
+        if (cudaMemcpy(out, dout, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess) rc = NDSPH_E_CUDA;
+    }
+    cudaFree(dp); cudaFree(fr); cudaFree(df); cudaFree(dout);
+    return rc;
+}
+
+extern "C" int ndsph_mlp_grad(const float* params, const float* feats, const float* targets, int32_t n,
+                              float* grad, float* loss)
+{
+    if (!params || n <= 0 || !feats || !targets || !grad || !loss) return NDSPH_E_ARG;
+    float *dp = nullptr, *df = nullptr, *dt = nullptr, *dg = nullptr, *dl = nullptr;
+    int rc = 0;
+    if (cudaMalloc(&dp, sizeof(float) * MLP_NPARAM) != cudaSuccess ||
+        cudaMalloc(&df, sizeof(float) * (size_t)n * MLP_NIN) != cudaSuccess ||
+        cudaMalloc(&dt, sizeof(float) * (size_t)n) != cudaSuccess ||
+        cudaMalloc(&dg, sizeof(float) * MLP_NPARAM) != cudaSuccess || cudaMalloc(&dl, sizeof(float)) != cudaSuccess) {
+        rc = NDSPH_E_CUDA;
+    } else {
+        cudaMemcpy(dp, params, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice);
+        cudaMemcpy(df, feats, sizeof(float) * (size_t)n * MLP_NIN, cudaMemcpyHostToDevice);
+        cudaMemcpy(dt, targets, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice);
+        MlpTrainArgs a;
+        memset(&a, 0, sizeof a);
+        a.nbatch = n;
+        a.feats = df;
+        a.targets = dt;
+        launch_mlp_grad(dp, a, dg, dl, 0);
+        if (cudaMemcpy(grad, dg, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(loss, dl, sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = NDSPH_E_CUDA;
+    }
+    cudaFree(dp); cudaFree(df); cudaFree(dt); cudaFree(dg); cudaFree(dl);
+    return rc;
 }
 
 extern "C" int ndsph_dev_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)

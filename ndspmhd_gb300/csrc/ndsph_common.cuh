@@ -24,6 +24,7 @@ enum Field : int {
     // leapfrog saves (part_in module, stepND_leapfrog_mhd.f90:70-101)
     XIN0, XIN1, XIN2, VIN0, VIN1, VIN2, BIN0, BIN1, BIN2, HIN, ENIN, RHOIN, ALIN0, ALIN1, ALIN2,
     FIN0, FIN1, FIN2, DBIN0, DBIN1, DBIN2, DHIN, DENIN, DALIN0, DALIN1, DALIN2,
+    HPRED, YPREV, FT0, FT1, FT2, FT3, FT4, FT5,   // learned-h predictor: h_pred, last z, features
     HDEN0,      // h at entry of iterate_density (hhin, iterate_density.f90:87)
     HNEXT,      // NR scratch: next h of the first pass
     NF
