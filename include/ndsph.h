@@ -270,6 +270,9 @@ NDSPH_API int ndsph_get_timing(ndsph_ctx* ctx, ndsph_timing* t);
  * the training kernel: grad of mean((out - target)^2) and that loss.  No
  * reference counterpart (the learned part is new).                           */
 NDSPH_API int ndsph_mlp_forward(const float* params, const float* feats, int32_t n, float* out);
+/* training schedule of the learned-h predictor of a context (opts.learned_h):
+ * Adam learning rate, optimiser steps per leapfrog step, minibatch size.     */
+NDSPH_API int ndsph_set_learning(ndsph_ctx* ctx, float lr, int32_t iters_per_step, int32_t batch);
 NDSPH_API int ndsph_mlp_grad(const float* params, const float* feats, const float* targets, int32_t n,
                              float* grad, float* loss);
 NDSPH_API int ndsph_set_profiling(ndsph_ctx* ctx, int32_t on);

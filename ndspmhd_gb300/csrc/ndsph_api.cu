@@ -1133,6 +1133,16 @@ static int dev_step_once(ndsph_ctx* ctx)
     return 0;
 }
 
+extern "C" int ndsph_set_learning(ndsph_ctx* ctx, float lr, int32_t iters_per_step, int32_t batch)
+{
+    GUARD_CTX();
+    if (!(lr > 0.f) || iters_per_step < 0 || batch < 1) { ctx->err = "bad learning schedule"; return NDSPH_E_ARG; }
+    ctx->mlp_lr = lr;
+    ctx->mlp_iters = iters_per_step;
+    ctx->mlp_batch = batch;
+    return 0;
+}
+
 // standalone MLP entry points for the tests (host buffers)
 extern "C" int ndsph_mlp_forward(const float* params, const float* feats, int32_t n, float* out)
 {

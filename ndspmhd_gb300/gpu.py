@@ -75,6 +75,7 @@ def lib() -> C.CDLL:
     L.ndsph_kernel_tables.argtypes = [C.c_int32, C.POINTER(C.c_double)]
     L.ndsph_get_timing.argtypes = [P, C.POINTER(NdsphTiming)]
     L.ndsph_set_profiling.argtypes = [P, C.c_int32]
+    L.ndsph_set_learning.argtypes = [P, C.c_float, C.c_int32, C.c_int32]
     _lib = L
     return L
 
@@ -182,6 +183,9 @@ class GpuSPH:
                 continue
             self._check(rc)
             return offs, neigh[: offs[-1]]
+
+    def set_learning(self, lr: float = 2e-3, iters_per_step: int = 4, batch: int = 16384):
+        self._check(lib().ndsph_set_learning(self._h, lr, iters_per_step, batch))
 
     def set_profiling(self, on: bool = True):
         self._check(lib().ndsph_set_profiling(self._h, 1 if on else 0))
