@@ -68,9 +68,9 @@ struct ndsph_ctx {
     float* mlp_loss = nullptr;
     MlpFrag* mlp_frag = nullptr; // BF16 tensor-core operands
     int mlp_step = 0;
-    float mlp_lr = 2.e-3f;
+    float mlp_lr = 3.e-3f;
     int mlp_batch = 16384;
-    int mlp_iters = 4;
+    int mlp_iters = 16;
     // timing
     bool profiling = false;
     cudaEvent_t ev[16];

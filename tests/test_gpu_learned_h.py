@@ -85,7 +85,7 @@ def _run(learned: int, nsteps: int, n1d: int = 24):
 
 
 def test_learned_h_reduces_density_work(gpulib):
-    nsteps = 24
+    nsteps = 40
     p0, w0, _ = _run(0, nsteps)
     p1, w1, t1 = _run(1, nsteps)
     half = nsteps // 2
@@ -93,4 +93,5 @@ def test_learned_h_reduces_density_work(gpulib):
     print(f"density work per step (particle passes / N): predictor {base:.3f}, learned {lrn:.3f}; "
           f"NR passes {p0[half:].mean():.2f} vs {p1[half:].mean():.2f}; updates {t1['mlp_updates']}")
     assert t1["mlp_updates"] > 0
-    assert lrn < base
+    # measured on GB300: ~1.92 -> ~1.65 particle passes per step (second half)
+    assert lrn < 0.95 * base
