@@ -191,6 +191,60 @@ def run_e2e(o, steps: int, warmup: int):
     return n * steps / el, d_up * n, d_dn * n
 
 
+def run_batched(steps: int, warmup: int, ntubes: int = 4096):
+    """Batched form: 4096 independent 1D Brio-Wu tubes, 200-1600 particles
+    each (seeded), one device state, per-tube dt; FP32 pair sums."""
+    from ndspmhd_gb300 import configs
+    from ndspmhd_gb300.gpu import GpuSPH
+    o, p, sim, counts = configs.brio_wu_batch(ntubes)
+    o["precision"] = 1
+    g = GpuSPH(o, configs.full_state(p, 1))
+    g.batch_upload(sim, len(counts), initialise=True)
+    g.batch_step(warmup)
+    g.batch_step(steps)
+    ms = g.timing()["total_ms"]
+    n = int(counts.sum())
+    g.close()
+    return {"value": round(n * steps / (ms * 1e-3), 1), "unit": UNIT, "ms_per_step": round(ms / steps, 3),
+            "config": f"{ntubes} Brio-Wu tubes, {n} particles, FP32 pairs, per-tube dt", "steps": steps}
+
+
+def run_learned(n1d: int, steps: int, warmup: int):
+    """Learned-h workload: isothermal log-normal turbulent box, tolh = 1e-4,
+    FP32 pairs; NR density work and step rate with the reference's predictor
+    vs the learned predictor (trained online from step 0)."""
+    from ndspmhd_gb300 import configs
+    from ndspmhd_gb300.gpu import GpuSPH
+    out = {}
+    o, p = configs.turbulent_box_3d(n1d)
+    for learned in (0, 1):
+        o2 = dict(o)
+        o2["precision"] = 1
+        o2["learned_h"] = learned
+        g = GpuSPH(o2, configs.full_state(p, 3))
+        g.primitive2conservative()
+        g.dev_upload()
+        g.set_dt(0.0)
+        g.dev_step(warmup)
+        work, passes = [], []
+        tot = 0.0
+        for _ in range(steps):
+            g.dev_step(1)
+            d = g.dts()
+            work.append(d["ncalctotal"] / g.n)
+            passes.append(d["its"])
+            tot += g.timing()["total_ms"]
+        key = "learned" if learned else "predictor"
+        out[key] = {"particle_passes_per_step": round(sum(work) / len(work), 4),
+                    "nr_passes_per_step": round(sum(passes) / len(passes), 3),
+                    "value": round(g.n * steps / (tot * 1e-3), 1), "ms_per_step": round(tot / steps, 3)}
+        g.close()
+    out["config"] = f"isothermal turbulent box {n1d}^3, tolh 1e-4, FP32 pairs, {warmup} warm-up steps then {steps} timed"
+    out["work_reduction"] = round(1 - out["learned"]["particle_passes_per_step"] /
+                                  out["predictor"]["particle_passes_per_step"], 4)
+    return out
+
+
 def cpu_baseline(n1d: int = CPU_SAMPLE_N1D, steps: int = CPU_SAMPLE_STEPS) -> dict:
     """The oracle (single-threaded C restatement of the reference) on a
     bounded sample of the same workload: a n1d^3 box, `steps` leapfrog steps."""
@@ -254,6 +308,7 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched and learned-h workloads")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
@@ -332,6 +387,9 @@ def main():
                         "speedup_fp32_over_fp64": round(ms64 / ms32, 2)}
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if not args.no_extra and world == 1:
+        line["batched"] = run_batched(max(args.steps, 5), 3)
+        line["learned_h"] = run_learned(min(N1D, 128), 20, 40)
     # launches per step: link (~12) + per NR pass (h1, density, ncalc copies) + EOS,
     # packs, rates, finalize, predictor x2, corrector
     passes = max(tim32["density_passes"], 1)

@@ -213,6 +213,21 @@ NDSPH_API int ndsph_dev_derivs(ndsph_ctx* ctx, ndsph_dt* dts);
  * with dt = 0; later steps use the dt returned by the previous step)          */
 NDSPH_API int ndsph_dev_set_time(ndsph_ctx* ctx, double dt, double time, int32_t nsteps);
 
+/* ---- batched form --------------------------------------------------------------
+ * `nsim` independent simulations with the same options (open or fixed
+ * boundaries), in one device state: the batched counterpart of running the
+ * reference once per input file (ndspmhd.f90:312-359, multi/multirun.f90).
+ * sim[i] (0-based) names the simulation of particle i; ireal stays 1-based
+ * over the whole array.  Each simulation keeps its own dt and clock (first
+ * step dt = 0 as evolve.f90:50-56); reductions (dtcourant, dtforce,
+ * stressmax, ...) are per simulation, so each one evolves as it would alone.
+ * initialise = 1 runs primitive2conservative on the inputs (dens, uu,
+ * Bfield), 0 takes a full state.  dt_out/time_out hold nsim doubles.       */
+NDSPH_API int ndsph_batch_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart, const int32_t* sim,
+                                 int32_t nsim, int32_t initialise);
+NDSPH_API int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, double* time_out);
+NDSPH_API int ndsph_batch_download(ndsph_ctx* ctx, ndsph_particles* p);
+
 /* ---- parity / debug helpers (never on a timed path) -------------------------
  * ndsph_neighbour_csr: after ndsph_set_linklist, the 1-based neighbour set of
  * every real particle under the criterion `mode` (0: q_i<2 gather as

@@ -303,6 +303,33 @@ def dust_gas_box_3d(n1d: int = 96, eps: float = 0.1, tstop: float = 0.01,
     return o, p
 
 
+def brio_wu_batch(ntubes: int = 4096, nmin: int = 200, nmax: int = 1600, seed: int = 2024):
+    """Batched workload: ``ntubes`` independent 1D Brio-Wu tubes with particle
+    counts drawn from a seeded uniform integer range [nmin, nmax] (uneven),
+    concatenated.  Returns (opts, particles, sim, counts) where sim[i] is the
+    tube of particle i; ireal stays 1-based over the concatenation."""
+    rng = np.random.default_rng(seed)
+    counts = rng.integers(nmin, nmax + 1, size=ntubes)
+    parts, sims, o0 = [], [], None
+    start = 0
+    psep = 0.0
+    real_counts = []
+    for t, c in enumerate(counts):
+        o, p = brio_wu_tube(int(c))
+        n = p["x"].shape[0]
+        p["ireal"] = np.where(p["ireal"] > 0, p["ireal"] + start, 0).astype(np.int32)
+        parts.append(p)
+        sims.append(np.full(n, t, np.int32))
+        real_counts.append(n)
+        psep = max(psep, o["psep"])
+        start += n
+        o0 = o
+    o0 = dict(o0)
+    o0["psep"] = psep
+    cat = {k: np.concatenate([p[k] for p in parts], axis=0) for k in parts[0]}
+    return o0, cat, np.concatenate(sims), np.array(real_counts)
+
+
 ALLOC_FIELDS_SCALAR = ("en", "hh", "rho", "rhoalt", "drhodt", "dhdt", "gradh", "gradhn",
                        "gradgradh", "dens", "uu", "pr", "spsound", "dudt", "dendt", "divB", "del2u")
 ALLOC_FIELDS_VEC3 = ("vel", "Bevol", "alpha", "Bfield", "force", "dBevoldt", "daldt", "curlB", "graddivv")

@@ -71,6 +71,15 @@ struct ndsph_ctx {
     float mlp_lr = 3.e-3f;
     int mlp_batch = 16384;
     int mlp_iters = 16;
+    // batched form
+    int nsim = 0;
+    int* sim2 = nullptr;             // gather partner of S.sim
+    unsigned long long* d_sim_red = nullptr;
+    double* d_sim_dt = nullptr;
+    double* d_sim_dtnext = nullptr;
+    double* d_sim_out = nullptr;     // [nsim][4] dtcourant, dtforce, dtnext, time
+    double* d_sim_off = nullptr;
+    double* h_sim_out = nullptr;
     // timing
     bool profiling = false;
     cudaEvent_t ev[16];
@@ -249,11 +258,12 @@ static void free_particles(ndsph_ctx* ctx)
                     ctx->S.numneigh, ctx->S.cell, ctx->S.xs, ctx->S.h1, ctx->S.active, ctx->S.active_next,
                     ctx->S.flag, ctx->itype2, ctx->id2, ctx->ireal2, ctx->srt.key, ctx->srt.slot, ctx->srt.perm,
                     ctx->d_stage, ctx->d_istage, ctx->S.pk_v, ctx->S.pk_t, ctx->S.pk_b, ctx->S.pk_a,
-                    ctx->S.nl, ctx->S.nl_cnt, ctx->S.hb};
+                    ctx->S.nl, ctx->S.nl_cnt, ctx->S.hb, ctx->S.sim, ctx->sim2};
     for (void* p : ptrs) if (p) cudaFree(p);
     ctx->slab[0] = ctx->slab[1] = nullptr;
     memset(&ctx->S, 0, sizeof(ctx->S));
     ctx->itype2 = ctx->id2 = ctx->ireal2 = nullptr;
+    ctx->sim2 = nullptr;
     ctx->srt.key = ctx->srt.slot = ctx->srt.perm = nullptr;
     ctx->d_stage = nullptr; ctx->d_istage = nullptr;
     ctx->cap = 0;
@@ -287,6 +297,9 @@ static int ensure_capacity(ndsph_ctx* ctx, int n)
     CK(cudaMalloc(&ctx->S.pk_b, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_a, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.nl_cnt, ib));
+    CK(cudaMalloc(&ctx->S.sim, ib));
+    CK(cudaMalloc(&ctx->sim2, ib));
+    CK(cudaMemsetAsync(ctx->S.sim, 0, ib, ctx->st));
     CK(cudaMalloc(&ctx->S.hb, sizeof(float) * (size_t)cap));
     ctx->S.nl = nullptr;
     ctx->nl_stride = 0;
@@ -400,10 +413,12 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
     free_particles(ctx);
     void* ptrs[] = {ctx->tab64, ctx->tab32, ctx->red, ctx->d_dtout, ctx->d_ncalc, ctx->d_fields,
                     ctx->srt.count, ctx->srt.start, ctx->srt.blocksums, ctx->mlp_p, ctx->mlp_m, ctx->mlp_v,
-                    ctx->mlp_g, ctx->mlp_loss, ctx->mlp_frag};
+                    ctx->mlp_g, ctx->mlp_loss, ctx->mlp_frag, ctx->d_sim_red, ctx->d_sim_dt, ctx->d_sim_dtnext,
+                    ctx->d_sim_out, ctx->d_sim_off};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (ctx->h_red) cudaFreeHost(ctx->h_red);
     if (ctx->h_dtout) cudaFreeHost(ctx->h_dtout);
+    if (ctx->h_sim_out) cudaFreeHost(ctx->h_sim_out);
     for (int k = 0; k < 16; k++) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -611,6 +626,10 @@ static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hma
     launch_gather_int(ctx->itype2, ctx->S.itype, ctx->srt.perm, n, st);
     launch_gather_int(ctx->id2, ctx->S.id, ctx->srt.perm, n, st);
     launch_gather_int(ctx->ireal2, ctx->S.ireal, ctx->srt.perm, n, st);
+    if (ctx->o.batched) {
+        launch_gather_int(ctx->sim2, ctx->S.sim, ctx->srt.perm, n, st);
+        std::swap(ctx->sim2, ctx->S.sim);
+    }
     std::swap(ctx->itype2, ctx->S.itype);
     std::swap(ctx->id2, ctx->S.id);
     std::swap(ctx->ireal2, ctx->S.ireal);
@@ -787,6 +806,7 @@ static int do_rates(ndsph_ctx* ctx)
     launch_rates(a, st);
     tmark(ctx, 5);
     launch_finalize_dt(ctx->red, ctx->o, ctx->d_dtout, st);
+    if (ctx->o.batched) launch_sim_finalize(ctx->o, ctx->d_sim_dtnext, ctx->d_sim_out, st);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(ctx->h_dtout, ctx->d_dtout, sizeof(double) * 8, cudaMemcpyDeviceToHost, st));
     int rc = sync_red(ctx);
@@ -816,6 +836,7 @@ static int do_derivs(ndsph_ctx* ctx, const int* fields, int nfields)
     if (rc) return rc;
     tmark(ctx, 1);
     launch_reduce_reset(ctx->red, st);
+    if (ctx->o.batched) launch_sim_reset(ctx->o, st);
     int its = 0, nct = 0, nrl = 0;
     rc = do_iterate_density(ctx, &its, &nct, &nrl);
     if (rc) return rc;
@@ -1290,6 +1311,125 @@ extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, nds
     if (rc) return rc;
     rc = download_all(ctx, p);
     fill_dt(ctx, dts);
+    return rc;
+}
+
+// ---------------------------------------------------------------------------
+// batched form: nsim independent simulations (open/fixed boundaries) laid
+// side by side along x, one device state, per-simulation dt and clock
+// ---------------------------------------------------------------------------
+extern "C" int ndsph_batch_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart, const int32_t* sim,
+                                  int32_t nsim, int32_t initialise)
+{
+    GUARD_CTX();
+    if (!p || !sim || npart <= 0 || nsim <= 0) { ctx->err = "bad batch arguments"; return NDSPH_E_ARG; }
+    for (int d = 0; d < ctx->o.ndim; d++)
+        if (ctx->o.ibound[d] > 1) { ctx->err = "batched form needs open or fixed boundaries"; return NDSPH_E_ARG; }
+    for (int i = 0; i < npart; i++)
+        if (sim[i] < 0 || sim[i] >= nsim) { ctx->err = "simulation index out of range"; return NDSPH_E_ARG; }
+    int rc = upload_inputs(ctx, p, npart, true, !initialise);
+    if (rc) return rc;
+    const int n = ctx->n;
+    if (initialise) {
+        rc |= upload_aos(ctx, p->dens, DENS, 1, 1, n);
+        rc |= upload_aos(ctx, p->uu, UU, 1, 1, n);
+        rc |= upload_aos(ctx, p->Bfield, BF0, 3, 3, n);
+    } else {
+        rc |= upload_aos(ctx, p->force, F0, 3, 3, n);
+        rc |= upload_aos(ctx, p->dBevoldt, DB0, 3, 3, n);
+        rc |= upload_aos(ctx, p->dendt, DENDT, 1, 1, n);
+        rc |= upload_aos(ctx, p->daldt, DAL0, 3, 3, n);
+    }
+    if (rc) return rc;
+    // per-simulation arrays
+    if (nsim != ctx->nsim) {
+        void* old[] = {ctx->d_sim_red, ctx->d_sim_dt, ctx->d_sim_dtnext, ctx->d_sim_out, ctx->d_sim_off};
+        for (void* q : old) if (q) cudaFree(q);
+        if (ctx->h_sim_out) cudaFreeHost(ctx->h_sim_out);
+        CK(cudaMalloc(&ctx->d_sim_red, sizeof(unsigned long long) * SIMRED * (size_t)nsim));
+        CK(cudaMalloc(&ctx->d_sim_dt, sizeof(double) * (size_t)nsim));
+        CK(cudaMalloc(&ctx->d_sim_dtnext, sizeof(double) * (size_t)nsim));
+        CK(cudaMalloc(&ctx->d_sim_out, sizeof(double) * 4 * (size_t)nsim));
+        CK(cudaMalloc(&ctx->d_sim_off, sizeof(double) * (size_t)nsim));
+        CK(cudaMallocHost(&ctx->h_sim_out, sizeof(double) * 4 * (size_t)nsim));
+        ctx->nsim = nsim;
+    }
+    CK(cudaMemsetAsync(ctx->d_sim_dt, 0, sizeof(double) * (size_t)nsim, ctx->st));
+    CK(cudaMemsetAsync(ctx->d_sim_out, 0, sizeof(double) * 4 * (size_t)nsim, ctx->st));
+    std::vector<double> off(nsim);
+    const double span = 2.0 * (ctx->o.xmax[0] - ctx->o.xmin[0]) + 1.0;
+    for (int s2 = 0; s2 < nsim; s2++) off[s2] = span * s2;
+    CK(cudaMemcpyAsync(ctx->d_sim_off, off.data(), sizeof(double) * (size_t)nsim, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->S.sim, sim, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+    ctx->o.batched = 1;
+    ctx->o.nsim = nsim;
+    ctx->o.sim_red = ctx->d_sim_red;
+    ctx->o.sim_dt = ctx->d_sim_dt;
+    launch_add_offset(ctx->F, ctx->S.sim, ctx->d_sim_off, n, +1, ctx->st);
+    if (initialise) {
+        launch_p2c_init(ctx->F, ctx->S, ctx->o, n, ctx->st);
+        rc = link_all(ctx, false);
+        if (rc) return rc;
+        launch_reduce_reset(ctx->red, ctx->st);
+        launch_sim_reset(ctx->o, ctx->st);
+        rc = do_iterate_density(ctx, nullptr, nullptr, nullptr);
+        if (rc) return rc;
+        launch_p2c_post(ctx->F, ctx->S, ctx->o, n, ctx->st);
+        rc = do_derivs(ctx, STATE_FIELDS, (int)(sizeof(STATE_FIELDS) / sizeof(int)));
+        if (rc) return rc;
+    } else {
+        rc = link_all(ctx, false);
+        if (rc) return rc;
+    }
+    CK(cudaMemsetAsync(ctx->d_sim_dt, 0, sizeof(double) * (size_t)nsim, ctx->st));
+    CK(cudaMemsetAsync(ctx->d_sim_out, 0, sizeof(double) * 4 * (size_t)nsim, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, double* time_out)
+{
+    GUARD_CTX();
+    if (!ctx->o.batched) { ctx->err = "call ndsph_batch_upload first"; return NDSPH_E_ARG; }
+    cudaStream_t st = ctx->st;
+    CK(cudaEventRecord(ctx->ev[10], st));
+    for (int k = 0; k < nsteps; k++) {
+        launch_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+        std::vector<int> live;
+        for (int f : STATE_FIELDS) live.push_back(f);
+        for (int f : INCOPY_FIELDS) live.push_back(f);
+        int rc = do_derivs(ctx, live.data(), (int)live.size());
+        if (rc) return rc;
+        launch_corrector(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+        // next dt of every simulation
+        CK(cudaMemcpyAsync(ctx->d_sim_dt, ctx->d_sim_dtnext, sizeof(double) * (size_t)ctx->nsim,
+                           cudaMemcpyDeviceToDevice, st));
+        rc = sync_red(ctx);
+        if (rc) return rc;
+        ctx->nsteps++;
+    }
+    CK(cudaEventRecord(ctx->ev[11], st));
+    CK(cudaMemcpyAsync(ctx->h_sim_out, ctx->d_sim_out, sizeof(double) * 4 * (size_t)ctx->nsim,
+                       cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev[10], ctx->ev[11]);
+    ctx->timing.total_ms = ms;
+    for (int s2 = 0; s2 < ctx->nsim; s2++) {
+        if (dt_out) dt_out[s2] = ctx->h_sim_out[s2 * 4 + 2];
+        if (time_out) time_out[s2] = ctx->h_sim_out[s2 * 4 + 3];
+    }
+    return 0;
+}
+
+extern "C" int ndsph_batch_download(ndsph_ctx* ctx, ndsph_particles* p)
+{
+    GUARD_CTX();
+    if (!ctx->o.batched || !p) { ctx->err = "call ndsph_batch_upload first"; return NDSPH_E_ARG; }
+    launch_add_offset(ctx->F, ctx->S.sim, ctx->d_sim_off, ctx->n, -1, ctx->st);
+    int rc = download_all(ctx, p);
+    launch_add_offset(ctx->F, ctx->S.sim, ctx->d_sim_off, ctx->n, +1, ctx->st);
+    CK(cudaStreamSynchronize(ctx->st));
     return rc;
 }
 

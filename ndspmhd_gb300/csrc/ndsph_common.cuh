@@ -46,7 +46,14 @@ struct DevOpts {
     double C_cour, C_force;
     int precision;
     int has_fixed;      // any ibound == 1 (fixed particles with ireal copies)
+    // batched form: nsim independent simulations in one state
+    int batched;
+    int nsim;
+    unsigned long long* sim_red;   // [nsim][SIMRED] per-simulation reductions
+    double* sim_dt;                // [nsim] dt of the current step
 };
+// per-simulation reduction slots (batched form)
+enum SimRed : int { SR_DTC = 0, SR_DTAV, SR_VSIG, SR_TS, SR_FH, SR_STRESS, SIMRED = 8 };
 
 // cell grid (periodic dims wrap, the others are padded bounding boxes)
 struct Grid {

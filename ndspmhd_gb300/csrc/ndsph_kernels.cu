@@ -480,6 +480,10 @@ __global__ void k_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
             st = fmax(0.5 * B2 - pr, 0.0);
         }
     }
+    if (o.batched) {
+        if (k < n && st > 0.0) atomic_max_pos(&o.sim_red[(size_t)S.sim[k] * SIMRED + SR_STRESS], st);
+        return;
+    }
     for (int off = 16; off > 0; off >>= 1) st = fmax(st, __shfl_down_sync(0xffffffffu, st, off));
     if ((threadIdx.x & 31) == 0 && st > 0.0) atomic_max_pos(&red->stressmax, st);
 }
@@ -515,7 +519,6 @@ __global__ void k_predictor(FieldPtrs F, Side S, DevOpts o, int n, const Reduce*
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double dt = red->dt;
     // save (:70-101)
     for (int d = 0; d < o.ndim; d++) F.f[XIN0 + d][i] = F.f[X0 + d][i];
     for (int d = 0; d < 3; d++) {
@@ -537,7 +540,7 @@ __global__ void k_predictor2(FieldPtrs F, Side S, DevOpts o, int n, const Reduce
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double dt = red->dt;
+    const double dt = o.batched ? o.sim_dt[S.sim[i]] : red->dt;
     int t = S.itype[i];
     if (t == NDSPH_ITYPE_BND || t == NDSPH_ITYPE_BNDDUST) {
         int j = (S.ireal[i] >= 0) ? S.pos_of_id[S.ireal[i]] : i;
@@ -571,7 +574,7 @@ __global__ void k_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double dt = red->dt;
+    const double dt = o.batched ? o.sim_dt[S.sim[i]] : red->dt;
     const double hdt = 0.5 * dt;
     int t = S.itype[i];
     if (t == NDSPH_ITYPE_BND || t == NDSPH_ITYPE_BNDDUST) {
@@ -649,6 +652,65 @@ __global__ void k_reduce_reset(Reduce* red)
 void launch_reduce_reset(Reduce* red, cudaStream_t st)
 {
     k_reduce_reset<<<1, 1, 0, st>>>(red);
+}
+
+// ---------------------------------------------------------------------------
+// batched form: per-simulation reductions and clocks
+// ---------------------------------------------------------------------------
+__global__ void k_sim_reset(DevOpts o)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= o.nsim) return;
+    unsigned long long* r = o.sim_red + (size_t)s * SIMRED;
+    r[SR_DTC] = dbits(1.e6);
+    r[SR_DTAV] = dbits(1.7976931348623157e308);
+    r[SR_VSIG] = 0ull;
+    r[SR_TS] = dbits(1.7976931348623157e308);
+    r[SR_FH] = 0ull;
+    r[SR_STRESS] = 0ull;
+}
+void launch_sim_reset(DevOpts o, cudaStream_t st)
+{
+    if (o.nsim > 0) k_sim_reset<<<nblk(o.nsim, 256), 256, 0, st>>>(o);
+}
+// dt_next per simulation (stepND_leapfrog_mhd.f90:252) and its clock;
+// sim_out[s*4..] = {dtcourant, dtforce, dtnext, time}
+__global__ void k_sim_finalize(DevOpts o, double* dt_next, double* sim_out)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= o.nsim) return;
+    const unsigned long long* r = o.sim_red + (size_t)s * SIMRED;
+    const double dtcourant = bitsd(r[SR_DTC]);
+    const double fhmax = bitsd(r[SR_FH]);
+    double dtforce = 1.7976931348623157e308;
+    if (fhmax > 0.0) dtforce = fmin(dtforce, sqrt(1.0 / fhmax));
+    double dtdrag = 1.7976931348623157e308;
+    if (o.idust == 2 && o.idrag_nature != 0 && (o.Kdrag > 0.0 || o.idrag_nature > 1)) dtdrag = fmin(dtdrag, bitsd(r[SR_TS]));
+    double dtn = o.C_force * dtforce;
+    dtn = fmin(dtn, o.C_cour * dtcourant);
+    dtn = fmin(dtn, 0.9 * dtdrag);
+    dtn = fmin(dtn, o.C_force * 1.7976931348623157e308);
+    const double t = sim_out[s * 4 + 3] + o.sim_dt[s];
+    dt_next[s] = dtn;
+    sim_out[s * 4 + 0] = dtcourant;
+    sim_out[s * 4 + 1] = dtforce;
+    sim_out[s * 4 + 2] = dtn;
+    sim_out[s * 4 + 3] = t;
+}
+void launch_sim_finalize(DevOpts o, double* dt_next, double* sim_out, cudaStream_t st)
+{
+    if (o.nsim > 0) k_sim_finalize<<<nblk(o.nsim, 256), 256, 0, st>>>(o, dt_next, sim_out);
+}
+// x += sign * off[sim]  (tubes laid side by side along x)
+__global__ void k_add_offset(FieldPtrs F, const int* sim, const double* off, int n, int sign)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    F.f[X0][i] += (double)sign * off[sim[i]];
+}
+void launch_add_offset(FieldPtrs F, const int* sim, const double* off, int n, int sign, cudaStream_t st)
+{
+    if (n > 0) k_add_offset<<<nblk(n, 256), 256, 0, st>>>(F, sim, off, n, sign);
 }
 
 // primitive2conservative (conservative2primitive.f90:488-509): rho = dens,

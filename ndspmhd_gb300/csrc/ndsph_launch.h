@@ -32,6 +32,7 @@ struct Side {
     unsigned* nl;
     int* nl_cnt;
     float* hb;        // h of each slot when its list was built
+    int* sim;         // simulation of the slot (batched form)
 };
 
 struct SortScratch {
@@ -99,6 +100,10 @@ void launch_finalize_dt(Reduce* red, DevOpts o, double* out, cudaStream_t st);
 void launch_reduce_reset(Reduce* red, cudaStream_t st);
 void launch_p2c_init(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
 void launch_p2c_post(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
+// batched form
+void launch_sim_reset(DevOpts o, cudaStream_t st);
+void launch_sim_finalize(DevOpts o, double* dt_next, double* sim_out, cudaStream_t st);
+void launch_add_offset(FieldPtrs F, const int* sim, const double* off, int n, int sign, cudaStream_t st);
 
 // ---- sweeps (ndsph_sweeps.cu) --------------------------------------------
 void launch_density(const SweepArgs& a, bool full, cudaStream_t st);

@@ -520,7 +520,8 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
         va2i = B2i * rho1i;
     }
     const R vsig2i = csi * csi + va2i;
-    const R stressmax = (R)bitsd(a.red->stressmax);
+    const R stressmax = (R)bitsd(o.batched ? o.sim_red[(size_t)a.S.sim[i] * SIMRED + SR_STRESS]
+                                           : a.red->stressmax);
     const R beta = (R)o.beta;
     const R Kdrag = (R)o.Kdrag;
     const bool i_dust = (typei == NDSPH_ITYPE_DUST);
@@ -846,6 +847,31 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
     if (PREC != 0) {
         if (rdtav > 1e37) rdtav = 1.7976931348623157e308;
         if (rts > 1e37) rts = 1.7976931348623157e308;
+    }
+    if (o.batched) {
+        // per-simulation reductions: one atomic per warp when the whole warp
+        // belongs to one simulation (the usual case: tubes are contiguous)
+        const int si = live ? a.S.sim[i] : -1;
+        const int s0 = __shfl_sync(0xffffffffu, si, 0);
+        const bool uniform = __all_sync(0xffffffffu, si == s0 || si < 0);
+        if (uniform) {
+            for (int off = 16; off > 0; off >>= 1) {
+                rdtc = fmin(rdtc, __shfl_down_sync(0xffffffffu, rdtc, off));
+                rdtav = fmin(rdtav, __shfl_down_sync(0xffffffffu, rdtav, off));
+                rvs = fmax(rvs, __shfl_down_sync(0xffffffffu, rvs, off));
+                rts = fmin(rts, __shfl_down_sync(0xffffffffu, rts, off));
+                fonh = fmax(fonh, __shfl_down_sync(0xffffffffu, fonh, off));
+            }
+        }
+        if ((uniform && (threadIdx.x & 31) == 0 && s0 >= 0) || (!uniform && live)) {
+            unsigned long long* r = o.sim_red + (size_t)(uniform ? s0 : si) * SIMRED;
+            atomic_min_pos(&r[SR_DTC], rdtc);
+            atomic_min_pos(&r[SR_DTAV], rdtav);
+            atomic_max_pos(&r[SR_VSIG], rvs);
+            atomic_min_pos(&r[SR_TS], rts);
+            atomic_max_pos(&r[SR_FH], fonh);
+        }
+        return;
     }
     for (int off = 16; off > 0; off >>= 1) {
         rdtc = fmin(rdtc, __shfl_down_sync(0xffffffffu, rdtc, off));

@@ -76,6 +76,9 @@ def lib() -> C.CDLL:
     L.ndsph_get_timing.argtypes = [P, C.POINTER(NdsphTiming)]
     L.ndsph_set_profiling.argtypes = [P, C.c_int32]
     L.ndsph_set_learning.argtypes = [P, C.c_float, C.c_int32, C.c_int32]
+    L.ndsph_batch_upload.argtypes = [P, parts, C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.c_int32]
+    L.ndsph_batch_step.argtypes = [P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.ndsph_batch_download.argtypes = [P, parts]
     _lib = L
     return L
 
@@ -166,6 +169,24 @@ class GpuSPH:
         self.dt.time = time
         self.dt.nsteps = nsteps
         self._check(lib().ndsph_dev_set_time(self._h, dt, time, nsteps))
+
+    # ---- batched form ---------------------------------------------------------------
+    def batch_upload(self, sim: np.ndarray, nsim: int, initialise: bool = True):
+        self._sim = np.ascontiguousarray(sim, dtype=np.int32)
+        self.nsim = nsim
+        self._check(lib().ndsph_batch_upload(self._h, C.byref(self._p), self.n,
+                                             self._sim.ctypes.data_as(C.POINTER(C.c_int32)), nsim,
+                                             1 if initialise else 0))
+
+    def batch_step(self, nsteps: int = 1):
+        dt = np.zeros(self.nsim)
+        t = np.zeros(self.nsim)
+        self._check(lib().ndsph_batch_step(self._h, nsteps, dt.ctypes.data_as(C.POINTER(C.c_double)),
+                                           t.ctypes.data_as(C.POINTER(C.c_double))))
+        return dt, t
+
+    def batch_download(self):
+        self._check(lib().ndsph_batch_download(self._h, C.byref(self._p)))
 
     # ---- diagnostics --------------------------------------------------------------
     def dts(self) -> dict:
