@@ -274,7 +274,7 @@ typedef struct ndsph_timing {
     float   mlp_loss;        /* learned h: last minibatch loss (z units^2)     */
     float   mlp_ms;          /* learned h: inference + training time per step  */
     int32_t mlp_updates;     /* learned h: optimiser steps taken so far        */
-    int32_t pad;
+    int32_t nl_builds;       /* neighbour-list builds so far (link + rebuilds)  */
 } ndsph_timing;
 NDSPH_API int ndsph_get_timing(ndsph_ctx* ctx, ndsph_timing* t);
 

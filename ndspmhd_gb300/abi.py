@@ -64,7 +64,7 @@ class NdsphTiming(C.Structure):
         ("eos_ms", C.c_float), ("rates_ms", C.c_float), ("post_ms", C.c_float),
         ("step_ms", C.c_float), ("total_ms", C.c_float), ("density_passes", C.c_int32),
         ("launches", C.c_int32), ("pairs_density", C.c_int64), ("pairs_rates", C.c_int64),
-        ("mlp_loss", C.c_float), ("mlp_ms", C.c_float), ("mlp_updates", C.c_int32), ("pad", C.c_int32),
+        ("mlp_loss", C.c_float), ("mlp_ms", C.c_float), ("mlp_updates", C.c_int32), ("nl_builds", C.c_int32),
     ]
 
     def as_dict(self) -> dict:

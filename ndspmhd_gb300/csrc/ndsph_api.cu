@@ -92,6 +92,7 @@ struct ndsph_ctx {
 
 static thread_local std::string g_err;
 static int build_nlist(ndsph_ctx* ctx);
+#define CK_VOID(call) do { (void)(call); } while (0)
 
 #define CK(call)                                                                          \
     do {                                                                                  \
@@ -683,6 +684,7 @@ static int build_nlist(ndsph_ctx* ctx)
         CK(cudaMemcpyAsync(&ctx->red->nl_stale, z, sizeof(int) * 3, cudaMemcpyHostToDevice, st));
         SweepArgs a = sweep_args(ctx);
         launch_build_nlist(a, st);
+        ctx->timing.nl_builds++;
         CK(cudaGetLastError());
         int h[3];
         CK(cudaMemcpyAsync(h, &ctx->red->nl_stale, sizeof(int) * 3, cudaMemcpyDeviceToHost, st));
@@ -1068,7 +1070,8 @@ static void mlp_infer(ndsph_ctx* ctx)
     const double pi = 3.141592653589793;
     const double r = 2.0 * ctx->o.hfact;
     a.nn_ref = (a.ndim == 3) ? 4.0 / 3.0 * pi * r * r * r : ((a.ndim == 2) ? pi * r * r : 2.0 * r);
-    a.zclip = 15.0;            // |log(h_init/h_pred)| <= 0.15
+    a.zclip = 2.0;             // |log(h_init/h_pred)| <= 0.02: a poor prediction costs
+                               // NR passes, never a neighbour-list rebuild
     a.apply = 1;
     a.fixed = ctx->o.has_fixed;
     a.hin = ctx->F.f[HIN];
@@ -1090,6 +1093,10 @@ static void mlp_train(ndsph_ctx* ctx)
 {
     cudaStream_t st = ctx->st;
     const long long n = ctx->n;
+    if (ctx->mlp_iters > 0) {
+        CK_VOID(cudaMemsetAsync(ctx->mlp_g, 0, sizeof(float) * MLP_NPARAM, st));
+        CK_VOID(cudaMemsetAsync(ctx->mlp_loss, 0, sizeof(float), st));
+    }
     for (int it = 0; it < ctx->mlp_iters; it++) {
         MlpTrainArgs a;
         memset(&a, 0, sizeof a);
@@ -1104,6 +1111,7 @@ static void mlp_train(ndsph_ctx* ctx)
         for (int k = 0; k < MLP_NIN; k++) a.feat[k] = ctx->F.f[FT0 + k];
         a.hconv = ctx->F.f[HH];
         a.hpred = ctx->F.f[HPRED];
+        if (it == ctx->mlp_iters - 1) CK_VOID(cudaMemsetAsync(ctx->mlp_loss, 0, sizeof(float), st));
         launch_mlp_grad(ctx->mlp_p, a, ctx->mlp_g, ctx->mlp_loss, st);
         ctx->mlp_step++;
         launch_mlp_adam(ctx->mlp_p, ctx->mlp_m, ctx->mlp_v, ctx->mlp_g, ctx->mlp_step, ctx->mlp_lr, st);
@@ -1207,6 +1215,8 @@ extern "C" int ndsph_mlp_grad(const float* params, const float* feats, const flo
         a.nbatch = n;
         a.feats = df;
         a.targets = dt;
+        cudaMemset(dg, 0, sizeof(float) * MLP_NPARAM);
+        cudaMemset(dl, 0, sizeof(float));
         launch_mlp_grad(dp, a, dg, dl, 0);
         if (cudaMemcpy(grad, dg, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost) != cudaSuccess ||
             cudaMemcpy(loss, dl, sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)

@@ -185,27 +185,35 @@ __global__ void k_mlp_infer(const MlpFrag* __restrict__ frp, MlpInferArgs a)
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int tile = warp; tile * 16 < a.n; tile += nwarps) {
         const int r0 = tile * 16 + g, r1 = r0 + 8;
-        float fa[MLP_NIN] = {0, 0, 0, 0, 0, 0}, fb[MLP_NIN] = {0, 0, 0, 0, 0, 0};
-        if (r0 < a.n) slot_features(a, r0, fa);
-        if (r1 < a.n) slot_features(a, r1, fb);
-        // lane t holds features 2t, 2t+1 of rows g and g+8
+        // lanes t = 0 and 1 compute the features of rows g and g+8 once;
+        // every lane then picks its two columns by shuffle
+        float fa[MLP_NIN] = {0, 0, 0, 0, 0, 0};
+        const int myrow = (t == 0) ? r0 : r1;
+        if (t < 2 && myrow < a.n) slot_features(a, myrow, fa);
         float f00 = 0.f, f01 = 0.f, f10 = 0.f, f11 = 0.f;
-        if (t < 3) { f00 = fa[2 * t]; f01 = fa[2 * t + 1]; f10 = fb[2 * t]; f11 = fb[2 * t + 1]; }
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            // column pair (2k, 2k+1) belongs to lane t == k
+            const float ra0 = __shfl_sync(0xffffffffu, fa[2 * k], lane & ~3);
+            const float ra1 = __shfl_sync(0xffffffffu, fa[2 * k + 1], lane & ~3);
+            const float rb0 = __shfl_sync(0xffffffffu, fa[2 * k], (lane & ~3) | 1);
+            const float rb1 = __shfl_sync(0xffffffffu, fa[2 * k + 1], (lane & ~3) | 1);
+            if (t == k) { f00 = ra0; f01 = ra1; f10 = rb0; f11 = rb1; }
+        }
         float z0, z1;
         mlp_tile(fr, pack_bf16(f00, f01), pack_bf16(f10, f11), z0, z1);
-        if (t == 0) {
-            const int rows[2] = {r0, r1};
-            const float zs[2] = {z0, z1};
-            float* ff[2] = {fa, fb};
-            for (int q = 0; q < 2; q++) {
-                const int i = rows[q];
-                if (i >= a.n) continue;
-                for (int k = 0; k < MLP_NIN; k++) a.feat[k][i] = ff[q][k];
+        // lane t = 0 finishes row g, lane t = 1 row g+8
+        if (t < 2) {
+            const int i = myrow;
+            const float zz = (t == 0) ? z0 : z1;
+            if (i < a.n) {
+                for (int k = 0; k < MLP_NIN; k++) a.feat[k][i] = fa[k];
                 const double hpred = a.hh[i];
                 a.hpred[i] = hpred;
-                if (a.fixed && a.itype[i] == 1) continue;
-                const float z = fminf(fmaxf(zs[q], -(float)a.zclip), (float)a.zclip);
-                if (a.apply) a.hh[i] = hpred * (double)expf(0.01f * z);
+                if (!(a.fixed && a.itype[i] == 1)) {
+                    const float z = fminf(fmaxf(zz, -(float)a.zclip), (float)a.zclip);
+                    if (a.apply) a.hh[i] = hpred * (double)expf(0.01f * z);
+                }
             }
         }
     }
@@ -303,7 +311,7 @@ __global__ void __launch_bounds__(TRAIN_BS) k_mlp_grad(const float* __restrict__
 }
 
 // Adam (Kingma & Ba 2015) on the FP32 master weights
-__global__ void k_mlp_adam(float* p, float* m, float* v, const float* g, int step, float lr)
+__global__ void k_mlp_adam(float* p, float* m, float* v, float* g, int step, float lr)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= MLP_NPARAM) return;
@@ -316,6 +324,7 @@ __global__ void k_mlp_adam(float* p, float* m, float* v, const float* g, int ste
     const float mh = mq / (1.f - powf(b1, (float)step));
     const float vh = vq / (1.f - powf(b2, (float)step));
     p[q] -= lr * mh / (sqrtf(vh) + eps);
+    g[q] = 0.f;   // ready for the next minibatch without a memset
 }
 
 // y_prev <- 100 log(h_conv / h_pred) for the next step's features
@@ -360,12 +369,11 @@ void launch_mlp_infer(const MlpFrag* fr, const MlpInferArgs& a, cudaStream_t st)
 }
 void launch_mlp_grad(const float* p, const MlpTrainArgs& a, float* grad, float* loss, cudaStream_t st)
 {
-    cudaMemsetAsync(grad, 0, sizeof(float) * MLP_NPARAM, st);
-    cudaMemsetAsync(loss, 0, sizeof(float), st);
+    // grad must be zero on entry (the Adam kernel leaves it so); loss accumulates
     const int blocks = (a.nbatch + TRAIN_BS - 1) / TRAIN_BS;
     k_mlp_grad<<<blocks, TRAIN_BS, 0, st>>>(p, a, grad, loss);
 }
-void launch_mlp_adam(float* p, float* m, float* v, const float* g, int step, float lr, cudaStream_t st)
+void launch_mlp_adam(float* p, float* m, float* v, float* g, int step, float lr, cudaStream_t st)
 {
     k_mlp_adam<<<(MLP_NPARAM + 255) / 256, 256, 0, st>>>(p, m, v, g, step, lr);
 }

@@ -54,7 +54,7 @@ void launch_mlp_pack(const float* p, MlpFrag* fr, cudaStream_t st);
 void launch_mlp_forward(const MlpFrag* fr, const float* feats, int n, float* out, cudaStream_t st);
 void launch_mlp_infer(const MlpFrag* fr, const MlpInferArgs& a, cudaStream_t st);
 void launch_mlp_grad(const float* p, const MlpTrainArgs& a, float* grad, float* loss, cudaStream_t st);
-void launch_mlp_adam(float* p, float* m, float* v, const float* g, int step, float lr, cudaStream_t st);
+void launch_mlp_adam(float* p, float* m, float* v, float* g, int step, float lr, cudaStream_t st);
 void launch_mlp_store_y(const double* hconv, const double* hpred, double* yprev, int n, cudaStream_t st);
 
 }  // namespace ndsph
