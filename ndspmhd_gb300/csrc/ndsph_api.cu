@@ -69,8 +69,8 @@ struct ndsph_ctx {
     MlpFrag* mlp_frag = nullptr; // BF16 tensor-core operands
     int mlp_step = 0;
     float mlp_lr = 3.e-3f;
-    int mlp_batch = 16384;
-    int mlp_iters = 16;
+    int mlp_batch = 32768;
+    int mlp_iters = 4;
     // batched form
     int nsim = 0;
     int* sim2 = nullptr;             // gather partner of S.sim
@@ -721,26 +721,37 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
     while (ncalc > 0 && its <= itsmax) {
         its++;
         if (redolink) {
-            // relink (iterate_density.f90:122-126): hhmax of the ghosts is the
-            // current max h; the cell grid is rebuilt if h outgrew the cells
-            CK(cudaMemcpyAsync(ctx->h_red, ctx->red, sizeof(Reduce), cudaMemcpyDeviceToHost, st));
+            // relink (iterate_density.f90:122-126): the ghosts' hhmax becomes the
+            // current max h.  The cells and the neighbour lists only have to be
+            // rebuilt if h outgrew them; otherwise refreshing hhmax is enough.
+            CK(cudaMemsetAsync(&ctx->red->hmax, 0, sizeof(unsigned long long), st));
+            launch_hmax_bbox(ctx->F, ctx->o.ndim, n, ctx->red, &ctx->red->hmax, st);
+            unsigned long long hb = 0ull;
+            CK(cudaMemcpyAsync(&hb, &ctx->red->hmax, sizeof(hb), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
-            // active list -> ids
-            std::vector<int> act(ncalc), ids(n);
-            CK(cudaMemcpy(act.data(), ctx->S.active, sizeof(int) * (size_t)ncalc, cudaMemcpyDeviceToHost));
-            CK(cudaMemcpy(ids.data(), ctx->S.id, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
-            for (int k = 0; k < ncalc; k++) act[k] = ids[act[k]];
-            int rc = link_all(ctx, false);
-            if (rc) return rc;
-            std::vector<int> pos(n);
-            CK(cudaMemcpy(pos.data(), ctx->S.pos_of_id, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
-            for (int k = 0; k < ncalc; k++) act[k] = pos[act[k]];
-            CK(cudaMemcpy(ctx->S.active, act.data(), sizeof(int) * (size_t)ncalc, cudaMemcpyHostToDevice));
-            nrelink++;
-            if (ctx->o.precision == NDSPH_PREC_FP32) {
-                SweepArgs pa = sweep_args(ctx);
-                launch_pack_v(pa, st);
+            const double hmax_now = bitsd(hb);
+            double cap = 1e300;
+            for (int d = 0; d < ctx->o.ndim; d++) cap = std::min(cap, 0.5 * ctx->g.cs[d] / (1.0 + 1.e-9));
+            if (hmax_now <= cap) {
+                CK(cudaMemcpyAsync(&ctx->red->hmax_ghost, &hb, sizeof(hb), cudaMemcpyHostToDevice, st));
+            } else {
+                // active list -> ids
+                std::vector<int> act(ncalc), ids(n);
+                CK(cudaMemcpy(act.data(), ctx->S.active, sizeof(int) * (size_t)ncalc, cudaMemcpyDeviceToHost));
+                CK(cudaMemcpy(ids.data(), ctx->S.id, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+                for (int k = 0; k < ncalc; k++) act[k] = ids[act[k]];
+                int rc = link_all(ctx, false);
+                if (rc) return rc;
+                std::vector<int> pos(n);
+                CK(cudaMemcpy(pos.data(), ctx->S.pos_of_id, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+                for (int k = 0; k < ncalc; k++) act[k] = pos[act[k]];
+                CK(cudaMemcpy(ctx->S.active, act.data(), sizeof(int) * (size_t)ncalc, cudaMemcpyHostToDevice));
+                if (ctx->o.precision == NDSPH_PREC_FP32) {
+                    SweepArgs pa = sweep_args(ctx);
+                    launch_pack_v(pa, st);
+                }
             }
+            nrelink++;
         }
         const bool full = (ncalc == n);
         launch_h1(ctx->F, ctx->S, n, st);
