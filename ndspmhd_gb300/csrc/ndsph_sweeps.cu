@@ -180,18 +180,18 @@ __device__ __forceinline__ float screen_r2(const float4& xsi, const float4& xsj,
     return dxf[0] * dxf[0] + dxf[1] * dxf[1] + dxf[2] * dxf[2];
 }
 
-// compensated FP32 accumulator (Neumaier)
+// compensated FP32 accumulator (Kahan, branch-free)
 struct KSum {
     float s, c;
     __device__ KSum() : s(0.f), c(0.f) {}
     __device__ __forceinline__ void add(float v)
     {
-        float t = s + v;
-        if (fabsf(s) >= fabsf(v)) c += (s - t) + v;
-        else c += (v - t) + s;
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
         s = t;
     }
-    __device__ __forceinline__ double val() const { return (double)s + (double)c; }
+    __device__ __forceinline__ double val() const { return (double)s - (double)c; }
 };
 
 // ===========================================================================
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
                 const float wv = tab_valf(a.t.wf, ix);
                 const float gw = tab_valf(a.t.gwf, ix);
                 const float ggw = tab_valf(a.t.ggwf, ix);
-                const float q = sqrtf(q2i);
+                const float q = sqrtp(q2i);
                 fw.add(mj * wv);
                 fn.add(wv);
                 const float tg = q * gw + (float)NDIM * wv;
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
                     float dvr = (vif[0] - pvj.x) * dxf[0];
                     if (NDIM >= 2) dvr += (vif[1] - pvj.y) * dxf[1];
                     if (NDIM >= 3) dvr += (vif[2] - pvj.z) * dxf[2];
-                    fd.add(mj * dvr * gw * __frcp_rn(rij + 1e-30f));
+                    fd.add(mj * dvr * gw * __fdividef(1.0f, rij + 1e-30f));
                 }
             }
         }
@@ -456,11 +456,25 @@ __device__ __forceinline__ void load_p(const SweepArgs& a, int j,
     }
 }
 
+// reciprocal and square root in the pair precision: exact (IEEE) in FP64,
+// the hardware approximations (MUFU, ~1 ulp) in the FP32 form
 template <typename R>
 __device__ __forceinline__ R rcp(R x)
 {
-    if constexpr (std::is_same<R, float>::value) return __frcp_rn(x);
+    if constexpr (std::is_same<R, float>::value) return __fdividef(1.0f, x);
     else return 1.0 / x;
+}
+template <typename R>
+__device__ __forceinline__ R sqrtp(R x)
+{
+    if constexpr (std::is_same<R, float>::value) return x * rsqrtf(fmaxf(x, 1e-37f));
+    else return sqrt(x);
+}
+template <typename R>
+__device__ __forceinline__ R divp(R a, R b)
+{
+    if constexpr (std::is_same<R, float>::value) return __fdividef(a, b);
+    else return a / b;
 }
 
 #ifndef NDSPH_RATES_FP32_MINB
@@ -630,14 +644,14 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
                     const R vpi = vsig2i * vsig2i - (R)4 * (ti * ti) * rho1i;
                     const R vpj = vsig2j * vsig2j - (R)4 * (tj * tj) * rho1j;
                     if (vpi < (R)0 || vpj < (R)0) raise_err(a.red, NDSPH_E_VSIG_DET, a.S.id[i]);
-                    vsigi = sqrt((R)0.5 * (vsig2i + sqrt(fmax(vpi, (R)0))));
-                    vsigj = sqrt((R)0.5 * (vsig2j + sqrt(fmax(vpj, (R)0))));
-                    vsigB = sqrt(dvel[0] * dvel[0] + dvel[1] * dvel[1] + dvel[2] * dvel[2]);
+                    vsigi = sqrtp((R)0.5 * (vsig2i + sqrtp(fmax(vpi, (R)0))));
+                    vsigj = sqrtp((R)0.5 * (vsig2j + sqrtp(fmax(vpj, (R)0))));
+                    vsigB = sqrtp(dvel[0] * dvel[0] + dvel[1] * dvel[1] + dvel[2] * dvel[2]);
                 } else {
                     vsigi = csi; vsigj = csj; vsigB = 0;
                 }
                 R vsig = (R)0.5 * fmax(vsigi + vsigj - beta * dvdotr, (R)0);
-                R vsigu = sqrt(fabs(pri - prj) * rhoav1);
+                R vsigu = sqrtp(fabs(pri - prj) * rhoav1);
                 R vsigdtc = fmax(vsig, (R)0.5 * (vsigi + vsigj + beta * fabs(dvdotr)));
                 vsigdtc = fmax(vsigdtc, vsigB);
                 const R hmin = fmin(hi, pj.h);
@@ -645,7 +659,7 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
                     vsig = 0; vsigu = 0;
                 } else {
                     vsmax = fmax(vsmax, vsigdtc);
-                    if (vsigdtc > (R)1.e-10) dtc = fmin(dtc, hmin / vsigdtc);
+                    if (vsigdtc > (R)1.e-10) dtc = fmin(dtc, divp(hmin, vsigdtc));
                 }
                 R fxi = 0, fyi = 0, fzi = 0;
                 // ---------------- artificial_dissipation ----------------
@@ -678,7 +692,7 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
                             vissB = -alphaB * (R)0.5 * (dB[0] * dB[0] + dB[1] * dB[1] + dB[2] * dB[2]) * rhoav1;
                         du.add(mj * (term * vissv + termu * vissu + termB * vissB));
                     }
-                    if (vsigav > (R)1.e-10) dtav = fmin(dtav, hmin / vsigav);
+                    if (vsigav > (R)1.e-10) dtav = fmin(dtav, divp(hmin, vsigav));
                 }
                 // ---------------- pressure ----------------
                 const R prterm = Prho2i * grkerni + Prho2j * grkernj;
@@ -974,13 +988,74 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
     atomicMax(&a.red->nl_maxcnt, cnt);
 }
 
+// Warp-cooperative build: one warp per cell.  The cell's particles (up to 32
+// at a time, one per lane) share their 3^NDIM candidate cells, so each chunk
+// of 32 candidates is loaded once, coalesced, and broadcast by shuffle; the
+// per-particle build above walks the same cells divergently.  Same screen,
+// same order of entries (stencil cell, then slot), so the lists are equal.
+template <int NDIM>
+__global__ void __launch_bounds__(256) k_build_nlist_cell(SweepArgs a)
+{
+    const int c = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= a.g.ncells) return;                 // uniform per warp
+    const Grid& g = a.g;
+    const int hb0 = a.cell_start[c], he = a.cell_start[c + 1];
+    if (hb0 == he) return;
+    const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
+    const float sk = 2.0f * a.nl_skin * 1.0002f;
+    Stencil<NDIM> stn(c, g);
+    constexpr int NST = (NDIM == 1) ? 3 : (NDIM == 2 ? 9 : 27);
+    for (int h0 = hb0; h0 < he; h0 += 32) {
+        const int i = h0 + lane;
+        const bool home = i < he;
+        const float4 xsi = home ? a.S.xs[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        int cnt = 0;
+        for (int so = 0; so < NST; so++) {
+            int cid, d[3], w[3];
+            if (!stn.cell_at(so, g, a.o, cid, d, w)) continue;
+            const int jb = a.cell_start[cid], je = a.cell_start[cid + 1];
+            const float ox = (float)d[0] * g.csf[0];
+            const float oy = (NDIM >= 2) ? (float)d[1] * g.csf[1] : 0.f;
+            const float oz = (NDIM >= 3) ? (float)d[2] * g.csf[2] : 0.f;
+            for (int j0 = jb; j0 < je; j0 += 32) {
+                const int jj = j0 + lane;
+                const float4 xc = (jj < je) ? a.S.xs[jj] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const int m = min(32, je - j0);
+                for (int k = 0; k < m; k++) {
+                    const float cx = __shfl_sync(0xffffffffu, xc.x, k);
+                    const float cy = (NDIM >= 2) ? __shfl_sync(0xffffffffu, xc.y, k) : 0.f;
+                    const float cz = (NDIM >= 3) ? __shfl_sync(0xffffffffu, xc.z, k) : 0.f;
+                    const float cw = __shfl_sync(0xffffffffu, xc.w, k);
+                    const float dx0 = (xsi.x - cx) - ox;
+                    const float dx1 = (NDIM >= 2) ? (xsi.y - cy) - oy : 0.f;
+                    const float dx2 = (NDIM >= 3) ? (xsi.z - cz) - oz : 0.f;
+                    const float r2f = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
+                    const float rc = sk * fmaxf(xsi.w, cw) + abs_tol;
+                    if (home && !(r2f > rc * rc)) {
+                        if (cnt < a.nl_stride) a.S.nl[(size_t)cnt * a.nl_ld + i] = ((unsigned)(j0 + k) << 5) | (unsigned)so;
+                        cnt++;
+                    }
+                }
+            }
+        }
+        if (home) {
+            a.S.nl_cnt[i] = cnt < a.nl_stride ? cnt : a.nl_stride;
+            a.S.hb[i] = xsi.w;
+            if (cnt > a.nl_stride) a.red->nl_overflow = 1;
+            atomicMax(&a.red->nl_maxcnt, cnt);
+        }
+    }
+}
+
 void launch_build_nlist(const SweepArgs& a, cudaStream_t st)
 {
     if (a.n <= 0) return;
-    const int nb = nblk(a.n, 128);
-    if (a.o.ndim == 1) k_build_nlist<1><<<nb, 128, 0, st>>>(a);
-    else if (a.o.ndim == 2) k_build_nlist<2><<<nb, 128, 0, st>>>(a);
-    else k_build_nlist<3><<<nb, 128, 0, st>>>(a);
+    const long long threads = (long long)a.g.ncells * 32;
+    const int nb = (int)((threads + 255) / 256);
+    if (a.o.ndim == 1) k_build_nlist_cell<1><<<nb, 256, 0, st>>>(a);
+    else if (a.o.ndim == 2) k_build_nlist_cell<2><<<nb, 256, 0, st>>>(a);
+    else k_build_nlist_cell<3><<<nb, 256, 0, st>>>(a);
 }
 
 // ===========================================================================
