@@ -180,6 +180,27 @@ __device__ __forceinline__ float screen_r2(const float4& xsi, const float4& xsj,
     return dxf[0] * dxf[0] + dxf[1] * dxf[1] + dxf[2] * dxf[2];
 }
 
+// reciprocal and square root in the pair precision: exact (IEEE) in FP64,
+// the hardware approximations (MUFU, ~1 ulp) in the FP32 form
+template <typename R>
+__device__ __forceinline__ R rcp(R x)
+{
+    if constexpr (std::is_same<R, float>::value) return __fdividef(1.0f, x);
+    else return 1.0 / x;
+}
+template <typename R>
+__device__ __forceinline__ R sqrtp(R x)
+{
+    if constexpr (std::is_same<R, float>::value) return x * rsqrtf(fmaxf(x, 1e-37f));
+    else return sqrt(x);
+}
+template <typename R>
+__device__ __forceinline__ R divp(R a, R b)
+{
+    if constexpr (std::is_same<R, float>::value) return __fdividef(a, b);
+    else return a / b;
+}
+
 // compensated FP32 accumulator (Kahan, branch-free)
 struct KSum {
     float s, c;
@@ -456,26 +477,6 @@ __device__ __forceinline__ void load_p(const SweepArgs& a, int j,
     }
 }
 
-// reciprocal and square root in the pair precision: exact (IEEE) in FP64,
-// the hardware approximations (MUFU, ~1 ulp) in the FP32 form
-template <typename R>
-__device__ __forceinline__ R rcp(R x)
-{
-    if constexpr (std::is_same<R, float>::value) return __fdividef(1.0f, x);
-    else return 1.0 / x;
-}
-template <typename R>
-__device__ __forceinline__ R sqrtp(R x)
-{
-    if constexpr (std::is_same<R, float>::value) return x * rsqrtf(fmaxf(x, 1e-37f));
-    else return sqrt(x);
-}
-template <typename R>
-__device__ __forceinline__ R divp(R a, R b)
-{
-    if constexpr (std::is_same<R, float>::value) return __fdividef(a, b);
-    else return a / b;
-}
 
 #ifndef NDSPH_RATES_FP32_MINB
 #define NDSPH_RATES_FP32_MINB 4
