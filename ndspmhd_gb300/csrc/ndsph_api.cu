@@ -57,6 +57,9 @@ struct ndsph_ctx {
     // host staging
     double* d_stage = nullptr;   // n*3 doubles
     int* d_istage = nullptr;
+    double* d_arena = nullptr;   // download staging: every output field side by side
+    size_t arena_cap = 0;        // doubles
+    size_t arena_used = 0;
     // neighbour lists
     int nl_stride = 0;
     float nl_skin = 1.1f;
@@ -418,6 +421,7 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
                     ctx->d_sim_out, ctx->d_sim_off};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (ctx->h_red) cudaFreeHost(ctx->h_red);
+    if (ctx->d_arena) cudaFree(ctx->d_arena);
     if (ctx->h_dtout) cudaFreeHost(ctx->h_dtout);
     if (ctx->h_sim_out) cudaFreeHost(ctx->h_sim_out);
     for (int k = 0; k < 16; k++) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
@@ -450,20 +454,40 @@ static int upload_aos(ndsph_ctx* ctx, const double* host, int f0, int ncomp, int
     launch_aos_to_slab(ctx->F, f0, ncomp, ctx->d_stage, stride, nullptr, n, ctx->st);
     return 0;
 }
+// downloads are staged in an arena and copied out asynchronously; the
+// caller synchronises once (download_end)
 static int download_aos(ndsph_ctx* ctx, double* host, int f0, int ncomp, int stride, int n)
 {
     if (!host) return 0;
-    launch_slab_to_aos(ctx->d_stage, stride, ctx->F, f0, ncomp, ctx->S.id, n, ctx->st);
-    CK(cudaMemcpyAsync(host, ctx->d_stage, sizeof(double) * (size_t)stride * n, cudaMemcpyDeviceToHost, ctx->st));
+    const size_t need = (size_t)stride * n;
+    if (ctx->arena_used + need > ctx->arena_cap) {
+        // grow: finish pending copies first, then reallocate
+        CK(cudaStreamSynchronize(ctx->st));
+        if (ctx->d_arena) CK(cudaFree(ctx->d_arena));
+        size_t cap = std::max(ctx->arena_cap * 2, (size_t)ctx->cap * 80);
+        CK(cudaMalloc(&ctx->d_arena, sizeof(double) * cap));
+        ctx->arena_cap = cap;
+        ctx->arena_used = 0;
+    }
+    double* dst = ctx->d_arena + ctx->arena_used;
+    ctx->arena_used += need;
+    launch_slab_to_aos(dst, stride, ctx->F, f0, ncomp, ctx->S.id, n, ctx->st);
+    CK(cudaMemcpyAsync(host, dst, sizeof(double) * need, cudaMemcpyDeviceToHost, ctx->st));
+    return 0;
+}
+static int download_end(ndsph_ctx* ctx)
+{
     CK(cudaStreamSynchronize(ctx->st));
+    ctx->arena_used = 0;
     return 0;
 }
 static int download_int(ndsph_ctx* ctx, int* host, const int* dsrc, int n, bool is_index)
 {
-    if (!host) return 0;
+    if (!host) return download_end(ctx);
     launch_slab_to_int(ctx->d_istage, dsrc, ctx->S.id, n, ctx->st);
     CK(cudaMemcpyAsync(host, ctx->d_istage, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    ctx->arena_used = 0;
     if (is_index) for (int i = 0; i < n; i++) host[i] = host[i] + 1;
     return 0;
 }
@@ -979,7 +1003,8 @@ extern "C" int ndsph_conservative2primitive(ndsph_ctx* ctx, ndsph_particles* p, 
     rc |= download_aos(ctx, p->pr, PR, 1, 1, n);
     rc |= download_aos(ctx, p->spsound, CS, 1, 1, n);
     rc |= download_aos(ctx, p->Bfield, BF0, 3, 3, n);
-    return rc;
+    if (rc) return rc;
+    return download_end(ctx);
 }
 
 extern "C" int ndsph_get_rates(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts)
@@ -1013,6 +1038,8 @@ extern "C" int ndsph_get_rates(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart
     rc |= download_aos(ctx, p->Bfield, BF0, 3, 3, n);
     rc |= download_aos(ctx, p->dens, DENS, 1, 1, n);
     rc |= download_aos(ctx, p->uu, UU, 1, 1, n);
+    if (rc) return rc;
+    rc = download_end(ctx);
     fill_dt(ctx, dts);
     return rc;
 }
@@ -1237,10 +1264,8 @@ extern "C" int ndsph_mlp_grad(const float* params, const float* feats, const flo
     return rc;
 }
 
-extern "C" int ndsph_dev_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
+static int dev_upload_impl(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart, bool link)
 {
-    GUARD_CTX();
-    if (npart < 0 || !p) { ctx->err = "bad npart or particles"; return NDSPH_E_ARG; }
     int rc = upload_inputs(ctx, p, npart, true, true);
     if (rc) return rc;
     const int n = ctx->n;
@@ -1254,9 +1279,16 @@ extern "C" int ndsph_dev_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_
     if (rc) return rc;
     CK(cudaMemcpyAsync(ctx->d_istage, p->numneigh, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
     launch_int_to_slab(ctx->S.numneigh, ctx->d_istage, nullptr, n, ctx->st);
-    rc = link_all(ctx, false);
+    if (link) rc = link_all(ctx, false);
     CK(cudaStreamSynchronize(ctx->st));
     return rc;
+}
+
+extern "C" int ndsph_dev_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
+{
+    GUARD_CTX();
+    if (npart < 0 || !p) { ctx->err = "bad npart or particles"; return NDSPH_E_ARG; }
+    return dev_upload_impl(ctx, p, npart, true);
 }
 
 extern "C" int ndsph_dev_download(ndsph_ctx* ctx, ndsph_particles* p, ndsph_dt* dts)
@@ -1325,7 +1357,9 @@ extern "C" int ndsph_dev_derivs(ndsph_ctx* ctx, ndsph_dt* dts)
 extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts)
 {
     GUARD_CTX(); GUARD_N();
-    int rc = ndsph_dev_upload(ctx, p, npart);
+    // the predictor is per particle, so the state need not be cell-sorted
+    // before the step: derivs links after the predictor
+    int rc = dev_upload_impl(ctx, p, npart, false);
     if (rc) return rc;
     if (dts) { ctx->dt = dts->dt; ctx->time = dts->time; ctx->nsteps = dts->nsteps; }
     rc = dev_step_once(ctx);

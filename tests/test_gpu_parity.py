@@ -124,3 +124,22 @@ def test_leapfrog_steps(initialised):
     errs, bad = compare_fields(g.state, ref.state, ["x", "vel", "hh", "en", "Bevol", "rho", "force", "alpha"], 1e-9)
     assert not bad, f"{name}: {errs}"
     g.close()
+
+
+def test_host_buffer_step(initialised):
+    """ndsph_step: one leapfrog step per call with the state in host arrays
+    (the reference-facing form the bench's e2e number times)."""
+    from ndspmhd_gb300.gpu import GpuSPH
+    name, o, orc = initialised
+    st = orc.snapshot()
+    from oracle.oracle import Oracle
+    ref = Oracle(o, st)
+    ref.step(3)
+    g = GpuSPH(o, {k: v.copy() for k, v in st.items()})
+    g.set_dt(0.0)
+    for _ in range(3):
+        g.step()
+    assert g.dts()["nsteps"] == 3
+    errs, bad = compare_fields(g.state, ref.state, ["x", "vel", "hh", "en", "Bevol", "rho", "force", "alpha"], 1e-9)
+    assert not bad, f"{name}: {errs}"
+    g.close()
