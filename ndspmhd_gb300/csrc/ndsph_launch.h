@@ -27,7 +27,7 @@ struct Side {
     float4* pk_t;     // (rho, max(P,0), c_s, u)
     float4* pk_b;     // (Bx, By, Bz, gradh)
     float4* pk_a;     // (alpha1, alpha2, alpha3, h)
-    // neighbour lists (ELL layout: entry k of slot i at nl[k*nl_ld + i]);
+    // neighbour lists, one row per slot: entry k of slot i at nl[i*stride + k];
     // each entry packs (j << 5) | stencil offset of j's cell
     unsigned* nl;
     int* nl_cnt;

@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
     const int ncand = a.S.nl_cnt[i];
     {
         for (int k = 0; k < ncand; k++) {
-            const unsigned pk = a.S.nl[(size_t)k * a.nl_ld + i];
+            const unsigned pk = a.S.nl[(size_t)i * a.nl_stride + k];
             const int j = (int)(pk >> 5);
             int d[3], w[3];
             stn.offset((int)(pk & 31u), g, d, w);
@@ -548,7 +548,7 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
     const int ncand = live ? a.S.nl_cnt[i] : 0;
     {
         for (int k = 0; k < ncand; k++) {
-            const unsigned pk = a.S.nl[(size_t)k * a.nl_ld + i];
+            const unsigned pk = a.S.nl[(size_t)i * a.nl_stride + k];
             const int j = (int)(pk >> 5);
             if (j == i) continue;
             int d[3], w[3];
@@ -979,7 +979,7 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
             const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
             const float rc = sk * fmaxf(hi, xsj.w) + abs_tol;
             if (r2f > rc * rc) continue;
-            if (cnt < a.nl_stride) a.S.nl[(size_t)cnt * a.nl_ld + i] = ((unsigned)j << 5) | (unsigned)so;
+            if (cnt < a.nl_stride) a.S.nl[(size_t)i * a.nl_stride + cnt] = ((unsigned)j << 5) | (unsigned)so;
             cnt++;
         }
     }
@@ -1034,7 +1034,7 @@ __global__ void __launch_bounds__(256) k_build_nlist_cell(SweepArgs a)
                     const float r2f = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
                     const float rc = sk * fmaxf(xsi.w, cw) + abs_tol;
                     if (home && !(r2f > rc * rc)) {
-                        if (cnt < a.nl_stride) a.S.nl[(size_t)cnt * a.nl_ld + i] = ((unsigned)(j0 + k) << 5) | (unsigned)so;
+                        if (cnt < a.nl_stride) a.S.nl[(size_t)i * a.nl_stride + cnt] = ((unsigned)(j0 + k) << 5) | (unsigned)so;
                         cnt++;
                     }
                 }
