@@ -245,6 +245,35 @@ def run_learned(n1d: int, steps: int, warmup: int):
     return out
 
 
+def run_dust(n1d: int, steps: int, warmup: int, nset: int = 8):
+    """Two-fluid dust + gas MHD box (2 x n1d^3, periodic), a batch of `nset`
+    (dust-to-gas ratio, stopping time) settings run one after another;
+    FP32 pair sums, FP64 integration."""
+    import numpy as np
+    from ndspmhd_gb300 import configs
+    from ndspmhd_gb300.gpu import GpuSPH
+    rng = np.random.default_rng(99)
+    eps = np.exp(rng.uniform(np.log(0.01), np.log(1.0), nset))
+    ts = np.exp(rng.uniform(np.log(1e-3), np.log(1.0), nset))
+    tot_ms, tot_upd, dtdrag = 0.0, 0, []
+    for k in range(nset):
+        o, p = configs.dust_gas_box_3d(n1d, eps=float(eps[k]), tstop=float(ts[k]), seed=77 + k)
+        o["precision"] = 1
+        g = GpuSPH(o, configs.full_state(p, 3))
+        g.primitive2conservative()
+        g.dev_upload()
+        g.set_dt(0.0)
+        g.dev_step(warmup)
+        g.dev_step(steps)
+        tot_ms += g.timing()["total_ms"]
+        tot_upd += g.n * steps
+        dtdrag.append(g.dts()["dtdrag"])
+        g.close()
+    return {"value": round(tot_upd / (tot_ms * 1e-3), 1), "unit": UNIT, "ms_per_step_per_setting": round(tot_ms / (steps * nset), 3),
+            "config": f"gas+dust box 2x{n1d}^3, {nset} (eps, t_s) settings, eps in [0.01,1], t_s in [1e-3,1], FP32 pairs",
+            "dtdrag_range": [min(dtdrag), max(dtdrag)]}
+
+
 def cpu_baseline(n1d: int = CPU_SAMPLE_N1D, steps: int = CPU_SAMPLE_STEPS) -> dict:
     """The oracle (single-threaded C restatement of the reference) on a
     bounded sample of the same workload: a n1d^3 box, `steps` leapfrog steps."""
@@ -390,6 +419,7 @@ def main():
     if not args.no_extra and world == 1:
         line["batched"] = run_batched(max(args.steps, 5), 3)
         line["learned_h"] = run_learned(min(N1D, 128), 20, 40)
+        line["dust"] = run_dust(96 if N1D >= 128 else 32, 3, 2)
     # launches per step: link (~12) + per NR pass (h1, density, ncalc copies) + EOS,
     # packs, rates, finalize, predictor x2, corrector
     passes = max(tim32["density_passes"], 1)

@@ -1054,9 +1054,13 @@ void launch_build_nlist(const SweepArgs& a, cudaStream_t st)
     if (a.n <= 0) return;
     const long long threads = (long long)a.g.ncells * 32;
     const int nb = (int)((threads + 255) / 256);
-    if (a.o.ndim == 1) k_build_nlist_cell<1><<<nb, 256, 0, st>>>(a);
-    else if (a.o.ndim == 2) k_build_nlist_cell<2><<<nb, 256, 0, st>>>(a);
-    else k_build_nlist_cell<3><<<nb, 256, 0, st>>>(a);
+    (void)nb;
+    // per-particle build (rows are contiguous per particle, so its appends
+    // merge in L2); the warp-per-cell variant above is kept for comparison
+    const int nbp = nblk(a.n, 128);
+    if (a.o.ndim == 1) k_build_nlist<1><<<nbp, 128, 0, st>>>(a);
+    else if (a.o.ndim == 2) k_build_nlist<2><<<nbp, 128, 0, st>>>(a);
+    else k_build_nlist<3><<<nbp, 128, 0, st>>>(a);
 }
 
 // ===========================================================================
