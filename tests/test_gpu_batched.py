@@ -41,3 +41,29 @@ def test_batched_tubes_match_independent_oracle_runs(gpulib):
 def _npart_arg(c):
     # brio_wu_tube rounds npart to 9 n_R; c is already such a count
     return int(c)
+
+
+def test_sweep_from_infiles_matches_oracle(gpulib, tmp_path):
+    """Sweep driver: three tube runs given by options files, two sharing
+    their options (one batched launch) and one with another gamma."""
+    from ndspmhd_gb300.infile import read_infile, run_sweep, write_infile
+    from oracle.oracle import Oracle
+    runs = []
+    for k, (npart, gamma) in enumerate([(270, 2.0), (450, 2.0), (360, 1.4)]):
+        o, p = configs.brio_wu_tube(npart)
+        o = dict(o, gamma=gamma)
+        p["uu"][:] = np.where(p["dens"] == 1.0, 1.0, 0.1) / ((gamma - 1.0) * p["dens"])
+        path = tmp_path / f"tube{k}.in"
+        write_infile(str(path), o)
+        runs.append((read_infile(str(path), 1, base=o), configs.full_state(p, 1)))
+    nsteps = 3
+    out = run_sweep(runs, nsteps, precision=0)
+    for k, (o, st) in enumerate(runs):
+        orc = Oracle(o, configs.full_state({f: st[f] for f in st}, 1))
+        orc.primitive2conservative()
+        orc.step(nsteps)
+        got, t, dt = out[k]
+        errs, bad = compare_fields({f: got[f] for f in ("x", "vel", "hh", "en", "rho")},
+                                   orc.state, ["x", "vel", "hh", "en", "rho"], 1e-9)
+        assert not bad, (k, errs)
+        assert abs(t - orc.dts()["time"]) <= 1e-10 * orc.dts()["time"]
