@@ -141,11 +141,14 @@ def run_device(o, st, steps: int, warmup: int, dist=None):
     g.dev_step(steps)              # bracketed by CUDA events on the library's stream
     torch.cuda.synchronize()
     clocks = clk.stop()
-    total_ms = g.timing()["total_ms"]
+    t_timed = g.timing()
+    total_ms = t_timed["total_ms"]
+    launches = t_timed["launches"]
     # kernel breakdown on one extra profiled step (not part of the timed loop)
     g.set_profiling(True)
     g.dev_step(1)
     tim = g.timing()
+    tim["launches_timed"] = launches
     dts = g.dts()
     g.close()
     return total_ms / steps, tim, dts, clocks
@@ -420,10 +423,9 @@ def main():
         line["batched"] = run_batched(max(args.steps, 5), 3)
         line["learned_h"] = run_learned(min(N1D, 128), 20, 40)
         line["dust"] = run_dust(96 if N1D >= 128 else 32, 3, 2)
-    # launches per step: link (~12) + per NR pass (h1, density, ncalc copies) + EOS,
-    # packs, rates, finalize, predictor x2, corrector
-    passes = max(tim32["density_passes"], 1)
-    line["gpu_launches"] = args.steps * (14 + 3 * passes + 6)
+    # kernel launches the library issued inside the timed step loop (counted
+    # at every launch site)
+    line["gpu_launches"] = tim32["launches_timed"]
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

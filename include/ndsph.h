@@ -268,7 +268,7 @@ NDSPH_API int ndsph_density_noalloc(const ndsph_opts* opts, const double* d_x, c
 typedef struct ndsph_timing {
     float link_ms, density_ms, density_pass1_ms, eos_ms, rates_ms, post_ms, step_ms, total_ms;
     int32_t density_passes;
-    int32_t launches;
+    int32_t launches;        /* kernel launches issued by the last step call   */
     int64_t pairs_density;   /* accepted (i,j) pairs summed in pass 1          */
     int64_t pairs_rates;     /* accepted (i,j) pairs in the rates sweep        */
     float   mlp_loss;        /* learned h: last minibatch loss (z units^2)     */

@@ -1303,6 +1303,7 @@ extern "C" int ndsph_dev_download(ndsph_ctx* ctx, ndsph_particles* p, ndsph_dt* 
 extern "C" int ndsph_dev_step(ndsph_ctx* ctx, int32_t nsteps, ndsph_dt* dts)
 {
     GUARD_CTX();
+    const long long l0 = ndsph_launch_counter().load();
     // the whole call is bracketed by events on the context's stream
     CK(cudaEventRecord(ctx->ev[10], ctx->st));
     float rates_sum = 0.f, dens_sum = 0.f, link_sum = 0.f;
@@ -1333,6 +1334,7 @@ extern "C" int ndsph_dev_step(ndsph_ctx* ctx, int32_t nsteps, ndsph_dt* dts)
         ctx->timing.link_ms = link_sum;
         ctx->timing.density_passes = passes;
     }
+    ctx->timing.launches = (int32_t)(ndsph_launch_counter().load() - l0);
     fill_dt(ctx, dts);
     return 0;
 }
@@ -1359,12 +1361,14 @@ extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, nds
     GUARD_CTX(); GUARD_N();
     // the predictor is per particle, so the state need not be cell-sorted
     // before the step: derivs links after the predictor
+    const long long l0 = ndsph_launch_counter().load();
     int rc = dev_upload_impl(ctx, p, npart, false);
     if (rc) return rc;
     if (dts) { ctx->dt = dts->dt; ctx->time = dts->time; ctx->nsteps = dts->nsteps; }
     rc = dev_step_once(ctx);
     if (rc) return rc;
     rc = download_all(ctx, p);
+    ctx->timing.launches = (int32_t)(ndsph_launch_counter().load() - l0);
     fill_dt(ctx, dts);
     return rc;
 }
@@ -1447,6 +1451,7 @@ extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, 
     GUARD_CTX();
     if (!ctx->o.batched) { ctx->err = "call ndsph_batch_upload first"; return NDSPH_E_ARG; }
     cudaStream_t st = ctx->st;
+    const long long l0 = ndsph_launch_counter().load();
     CK(cudaEventRecord(ctx->ev[10], st));
     for (int k = 0; k < nsteps; k++) {
         launch_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
@@ -1470,6 +1475,7 @@ extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, 
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev[10], ctx->ev[11]);
     ctx->timing.total_ms = ms;
+    ctx->timing.launches = (int32_t)(ndsph_launch_counter().load() - l0);
     for (int s2 = 0; s2 < ctx->nsim; s2++) {
         if (dt_out) dt_out[s2] = ctx->h_sim_out[s2 * 4 + 2];
         if (time_out) time_out[s2] = ctx->h_sim_out[s2 * 4 + 3];

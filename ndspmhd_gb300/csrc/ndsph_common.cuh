@@ -5,9 +5,19 @@
 // Every per-particle double field lives in one slab `F` of NF*cap doubles so
 // the cell sort can permute all live fields with one gather kernel.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "../../include/ndsph.h"
+
+// Host-side count of every kernel launch this library issues (all contexts);
+// ndsph_get_timing reports the launches of the last ndsph_dev_step call.
+inline std::atomic<long long>& ndsph_launch_counter()
+{
+    static std::atomic<long long> c{0};
+    return c;
+}
+#define NDSPH_COUNT_LAUNCH (void)ndsph_launch_counter().fetch_add(1, std::memory_order_relaxed)
 
 namespace ndsph {
 

@@ -31,7 +31,7 @@ __global__ void k_boundary_wrap(FieldPtrs F, DevOpts o, int n)
 }
 void launch_boundary_wrap(FieldPtrs F, DevOpts o, int n, cudaStream_t st)
 {
-    if (n > 0) k_boundary_wrap<<<nblk(n, 256), 256, 0, st>>>(F, o, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_boundary_wrap<<<nblk(n, 256), 256, 0, st>>>(F, o, n);
 }
 
 // max h (bound module hhmax, linkND.f90:70 / ghostND_mhd.f90:77) and the
@@ -89,7 +89,7 @@ void launch_hmax(const double* h, int n, Reduce* red, unsigned long long* dst, c
 }
 void launch_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, cudaStream_t st)
 {
-    if (n > 0) k_hmax_bbox<<<nblk(n, 256), 256, 0, st>>>(F, ndim, n, red, dst);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_hmax_bbox<<<nblk(n, 256), 256, 0, st>>>(F, ndim, n, red, dst);
 }
 
 // ---------------------------------------------------------------------------
@@ -119,7 +119,7 @@ void launch_cell_key(FieldPtrs F, Grid g, DevOpts o, int n, SortScratch s, Reduc
 {
     (void)red;
     cudaMemsetAsync(s.count, 0, sizeof(int) * (size_t)g.ncells, st);
-    if (n > 0) k_cell_key<<<nblk(n, 256), 256, 0, st>>>(F, g, o.ndim, n, s);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_cell_key<<<nblk(n, 256), 256, 0, st>>>(F, g, o.ndim, n, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -204,9 +204,9 @@ __global__ void k_scan_final(const int* in, int n, const int* bsum, int* out)
 void launch_scan(SortScratch s, int ncells, cudaStream_t st)
 {
     int nb = nblk(ncells, SCAN_TILE);
-    k_scan_blocksum<<<nb, SCAN_BS, 0, st>>>(s.count, ncells, s.blocksums);
-    k_scan_bsum<<<1, SCAN_BS, 0, st>>>(s.blocksums, nb);
-    k_scan_final<<<nb, SCAN_BS, 0, st>>>(s.count, ncells, s.blocksums, s.start);
+    NDSPH_COUNT_LAUNCH, k_scan_blocksum<<<nb, SCAN_BS, 0, st>>>(s.count, ncells, s.blocksums);
+    NDSPH_COUNT_LAUNCH, k_scan_bsum<<<1, SCAN_BS, 0, st>>>(s.blocksums, nb);
+    NDSPH_COUNT_LAUNCH, k_scan_final<<<nb, SCAN_BS, 0, st>>>(s.count, ncells, s.blocksums, s.start);
 }
 
 __global__ void k_scatter(SortScratch s, int n)
@@ -232,8 +232,8 @@ __global__ void k_cell_sort(SortScratch s, int ncells)
 
 void launch_scatter_sort(SortScratch s, int n, int ncells, cudaStream_t st)
 {
-    if (n > 0) k_scatter<<<nblk(n, 256), 256, 0, st>>>(s, n);
-    k_cell_sort<<<nblk(ncells, 128), 128, 0, st>>>(s, ncells);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_scatter<<<nblk(n, 256), 256, 0, st>>>(s, n);
+    NDSPH_COUNT_LAUNCH, k_cell_sort<<<nblk(ncells, 128), 128, 0, st>>>(s, ncells);
 }
 
 // permutation gather of the live fields: dst[f][k] = src[f][perm[k]]
@@ -251,7 +251,7 @@ __global__ void k_gather_fields(FieldPtrs dst, FieldPtrs src, const int* __restr
 void launch_gather_fields(FieldPtrs dst, FieldPtrs src, const int* fields, int nfields, const int* perm, int n,
                           cudaStream_t st)
 {
-    if (n > 0) k_gather_fields<<<nblk(n, 256), 256, 0, st>>>(dst, src, fields, nfields, perm, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_gather_fields<<<nblk(n, 256), 256, 0, st>>>(dst, src, fields, nfields, perm, n);
 }
 
 __global__ void k_gather_int(int* dst, const int* src, const int* perm, int n)
@@ -261,7 +261,7 @@ __global__ void k_gather_int(int* dst, const int* src, const int* perm, int n)
 }
 void launch_gather_int(int* dst, const int* src, const int* perm, int n, cudaStream_t st)
 {
-    if (n > 0) k_gather_int<<<nblk(n, 256), 256, 0, st>>>(dst, src, perm, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_gather_int<<<nblk(n, 256), 256, 0, st>>>(dst, src, perm, n);
 }
 
 // after the gather: cell id per slot, inverse of id
@@ -291,12 +291,12 @@ __global__ void k_xs(FieldPtrs F, Side S, Grid g, int ndim, int n)
 void launch_post_sort(Side S, SortScratch s, int n, int ncells, Grid g, FieldPtrs F, DevOpts o, cudaStream_t st)
 {
     (void)ncells;
-    if (n > 0) k_post_sort<<<nblk(n, 256), 256, 0, st>>>(S, s, n);
-    if (n > 0) k_xs<<<nblk(n, 256), 256, 0, st>>>(F, S, g, o.ndim, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_post_sort<<<nblk(n, 256), 256, 0, st>>>(S, s, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_xs<<<nblk(n, 256), 256, 0, st>>>(F, S, g, o.ndim, n);
 }
 void launch_xs(FieldPtrs F, Side S, Grid g, DevOpts o, int n, cudaStream_t st)
 {
-    if (n > 0) k_xs<<<nblk(n, 256), 256, 0, st>>>(F, S, g, o.ndim, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_xs<<<nblk(n, 256), 256, 0, st>>>(F, S, g, o.ndim, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -313,7 +313,7 @@ __global__ void k_aos_to_slab(FieldPtrs F, int f0, int ncomp, const double* __re
 void launch_aos_to_slab(FieldPtrs F, int f0, int ncomp, const double* aos, int stride, const int* id, int n,
                         cudaStream_t st)
 {
-    if (n > 0) k_aos_to_slab<<<nblk(n, 256), 256, 0, st>>>(F, f0, ncomp, aos, stride, id, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_aos_to_slab<<<nblk(n, 256), 256, 0, st>>>(F, f0, ncomp, aos, stride, id, n);
 }
 
 __global__ void k_slab_to_aos(double* __restrict__ aos, int stride, FieldPtrs F, int f0, int ncomp,
@@ -327,7 +327,7 @@ __global__ void k_slab_to_aos(double* __restrict__ aos, int stride, FieldPtrs F,
 void launch_slab_to_aos(double* aos, int stride, FieldPtrs F, int f0, int ncomp, const int* id, int n,
                         cudaStream_t st)
 {
-    if (n > 0) k_slab_to_aos<<<nblk(n, 256), 256, 0, st>>>(aos, stride, F, f0, ncomp, id, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_slab_to_aos<<<nblk(n, 256), 256, 0, st>>>(aos, stride, F, f0, ncomp, id, n);
 }
 
 __global__ void k_int_to_slab(int* dst, const int* src, const int* id, int n)
@@ -337,7 +337,7 @@ __global__ void k_int_to_slab(int* dst, const int* src, const int* id, int n)
 }
 void launch_int_to_slab(int* dst, const int* src, const int* id, int n, cudaStream_t st)
 {
-    if (n > 0) k_int_to_slab<<<nblk(n, 256), 256, 0, st>>>(dst, src, id, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_int_to_slab<<<nblk(n, 256), 256, 0, st>>>(dst, src, id, n);
 }
 __global__ void k_slab_to_int(int* dst, const int* src, const int* id, int n)
 {
@@ -346,7 +346,7 @@ __global__ void k_slab_to_int(int* dst, const int* src, const int* id, int n)
 }
 void launch_slab_to_int(int* dst, const int* src, const int* id, int n, cudaStream_t st)
 {
-    if (n > 0) k_slab_to_int<<<nblk(n, 256), 256, 0, st>>>(dst, src, id, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_slab_to_int<<<nblk(n, 256), 256, 0, st>>>(dst, src, id, n);
 }
 __global__ void k_iota(int* a, int n)
 {
@@ -355,7 +355,7 @@ __global__ void k_iota(int* a, int n)
 }
 void launch_iota(int* a, int n, cudaStream_t st)
 {
-    if (n > 0) k_iota<<<nblk(n, 256), 256, 0, st>>>(a, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_iota<<<nblk(n, 256), 256, 0, st>>>(a, n);
 }
 __global__ void k_fill(double* a, double v, int n)
 {
@@ -364,7 +364,7 @@ __global__ void k_fill(double* a, double v, int n)
 }
 void launch_fill(double* a, double v, int n, cudaStream_t st)
 {
-    if (n > 0) k_fill<<<nblk(n, 256), 256, 0, st>>>(a, v, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_fill<<<nblk(n, 256), 256, 0, st>>>(a, v, n);
 }
 __global__ void k_copy(double* dst, const double* src, int n)
 {
@@ -373,7 +373,7 @@ __global__ void k_copy(double* dst, const double* src, int n)
 }
 void launch_copy(double* dst, const double* src, int n, cudaStream_t st)
 {
-    if (n > 0) k_copy<<<nblk(n, 256), 256, 0, st>>>(dst, src, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_copy<<<nblk(n, 256), 256, 0, st>>>(dst, src, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -391,7 +391,7 @@ __global__ void k_h1(FieldPtrs F, Side S, int n)
 }
 void launch_h1(FieldPtrs F, Side S, int n, cudaStream_t st)
 {
-    if (n > 0) k_h1<<<nblk(n, 256), 256, 0, st>>>(F, S, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_h1<<<nblk(n, 256), 256, 0, st>>>(F, S, n);
 }
 
 // iterate_density.f90:79-86 (zero gradh.. on non-fixed particles) and
@@ -415,7 +415,7 @@ void launch_density_init(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st)
 }
 void launch_density_init2(FieldPtrs F, Side S, int n, Reduce* red, cudaStream_t st)
 {
-    if (n > 0) k_density_init<<<nblk(n, 256), 256, 0, st>>>(F, S, n, red);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_density_init<<<nblk(n, 256), 256, 0, st>>>(F, S, n, red);
 }
 
 // fixed particles take rho.. from their source after each NR pass
@@ -433,7 +433,7 @@ __global__ void k_fixed_density_copy(FieldPtrs F, Side S, int n)
 }
 void launch_fixed_density_copy(FieldPtrs F, Side S, int n, cudaStream_t st)
 {
-    if (n > 0) k_fixed_density_copy<<<nblk(n, 256), 256, 0, st>>>(F, S, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_fixed_density_copy<<<nblk(n, 256), 256, 0, st>>>(F, S, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -489,7 +489,7 @@ __global__ void k_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
 }
 void launch_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st)
 {
-    if (n > 0) k_eos<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_eos<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
 }
 
 // copy_particle copy_particle.f90:28-80 for fixed particles
@@ -509,7 +509,7 @@ __global__ void k_fixed_copy(FieldPtrs F, Side S, int n)
 }
 void launch_fixed_copy(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st)
 {
-    if (o.has_fixed && n > 0) k_fixed_copy<<<nblk(n, 256), 256, 0, st>>>(F, S, n);
+    if (o.has_fixed && n > 0) NDSPH_COUNT_LAUNCH, k_fixed_copy<<<nblk(n, 256), 256, 0, st>>>(F, S, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -566,8 +566,8 @@ __global__ void k_predictor2(FieldPtrs F, Side S, DevOpts o, int n, const Reduce
 void launch_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st)
 {
     if (n <= 0) return;
-    k_predictor<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
-    k_predictor2<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+    NDSPH_COUNT_LAUNCH, k_predictor<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+    NDSPH_COUNT_LAUNCH, k_predictor2<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
 }
 
 __global__ void k_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
@@ -609,7 +609,7 @@ __global__ void k_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
 }
 void launch_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st)
 {
-    if (n > 0) k_corrector<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_corrector<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
 }
 
 // dt = min(C_force*dtforce, C_cour*dtcourant, 0.9*dtdrag, C_force*dtvisc)
@@ -635,7 +635,7 @@ __global__ void k_finalize_dt(Reduce* red, DevOpts o, double* out)
 }
 void launch_finalize_dt(Reduce* red, DevOpts o, double* out, cudaStream_t st)
 {
-    k_finalize_dt<<<1, 1, 0, st>>>(red, o, out);
+    NDSPH_COUNT_LAUNCH, k_finalize_dt<<<1, 1, 0, st>>>(red, o, out);
 }
 
 __global__ void k_reduce_reset(Reduce* red)
@@ -651,7 +651,7 @@ __global__ void k_reduce_reset(Reduce* red)
 }
 void launch_reduce_reset(Reduce* red, cudaStream_t st)
 {
-    k_reduce_reset<<<1, 1, 0, st>>>(red);
+    NDSPH_COUNT_LAUNCH, k_reduce_reset<<<1, 1, 0, st>>>(red);
 }
 
 // ---------------------------------------------------------------------------
@@ -671,7 +671,7 @@ __global__ void k_sim_reset(DevOpts o)
 }
 void launch_sim_reset(DevOpts o, cudaStream_t st)
 {
-    if (o.nsim > 0) k_sim_reset<<<nblk(o.nsim, 256), 256, 0, st>>>(o);
+    if (o.nsim > 0) NDSPH_COUNT_LAUNCH, k_sim_reset<<<nblk(o.nsim, 256), 256, 0, st>>>(o);
 }
 // dt_next per simulation (stepND_leapfrog_mhd.f90:252) and its clock;
 // sim_out[s*4..] = {dtcourant, dtforce, dtnext, time}
@@ -699,7 +699,7 @@ __global__ void k_sim_finalize(DevOpts o, double* dt_next, double* sim_out)
 }
 void launch_sim_finalize(DevOpts o, double* dt_next, double* sim_out, cudaStream_t st)
 {
-    if (o.nsim > 0) k_sim_finalize<<<nblk(o.nsim, 256), 256, 0, st>>>(o, dt_next, sim_out);
+    if (o.nsim > 0) NDSPH_COUNT_LAUNCH, k_sim_finalize<<<nblk(o.nsim, 256), 256, 0, st>>>(o, dt_next, sim_out);
 }
 // x += sign * off[sim]  (tubes laid side by side along x)
 __global__ void k_add_offset(FieldPtrs F, const int* sim, const double* off, int n, int sign)
@@ -710,7 +710,7 @@ __global__ void k_add_offset(FieldPtrs F, const int* sim, const double* off, int
 }
 void launch_add_offset(FieldPtrs F, const int* sim, const double* off, int n, int sign, cudaStream_t st)
 {
-    if (n > 0) k_add_offset<<<nblk(n, 256), 256, 0, st>>>(F, sim, off, n, sign);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_add_offset<<<nblk(n, 256), 256, 0, st>>>(F, sim, off, n, sign);
 }
 
 // primitive2conservative (conservative2primitive.f90:488-509): rho = dens,
@@ -726,7 +726,7 @@ __global__ void k_p2c_init(FieldPtrs F, DevOpts o, int n)
 void launch_p2c_init(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st)
 {
     (void)S;
-    if (n > 0) k_p2c_init<<<nblk(n, 256), 256, 0, st>>>(F, o, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_p2c_init<<<nblk(n, 256), 256, 0, st>>>(F, o, n);
 }
 // after the density iteration: Bevol from Bfield (:608-619), en = uu (:743)
 __global__ void k_p2c_post(FieldPtrs F, DevOpts o, int n)
@@ -744,7 +744,7 @@ __global__ void k_p2c_post(FieldPtrs F, DevOpts o, int n)
 void launch_p2c_post(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st)
 {
     (void)S;
-    if (n > 0) k_p2c_post<<<nblk(n, 256), 256, 0, st>>>(F, o, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_p2c_post<<<nblk(n, 256), 256, 0, st>>>(F, o, n);
 }
 
 }  // namespace ndsph

@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstring>
 #include <vector>
+#include "ndsph_common.cuh"
 #include "ndsph_mlp.h"
 
 namespace ndsph {
@@ -351,13 +352,13 @@ void mlp_init_params(std::vector<float>& p, unsigned seed)
     for (int k = 0; k < 32; k++) p[MLP_OFF_W3 + k] = 0.f;
 }
 
-void launch_mlp_pack(const float* p, MlpFrag* fr, cudaStream_t st) { k_mlp_pack<<<1, 32, 0, st>>>(p, fr); }
+void launch_mlp_pack(const float* p, MlpFrag* fr, cudaStream_t st) { NDSPH_COUNT_LAUNCH, k_mlp_pack<<<1, 32, 0, st>>>(p, fr); }
 void launch_mlp_forward(const MlpFrag* fr, const float* feats, int n, float* out, cudaStream_t st)
 {
     if (n <= 0) return;
     const int tiles = (n + 15) / 16;
     const int blocks = (tiles + 7) / 8;
-    k_mlp_forward<<<blocks, 256, 0, st>>>(fr, feats, n, out);
+    NDSPH_COUNT_LAUNCH, k_mlp_forward<<<blocks, 256, 0, st>>>(fr, feats, n, out);
 }
 void launch_mlp_infer(const MlpFrag* fr, const MlpInferArgs& a, cudaStream_t st)
 {
@@ -365,21 +366,21 @@ void launch_mlp_infer(const MlpFrag* fr, const MlpInferArgs& a, cudaStream_t st)
     const int tiles = (a.n + 15) / 16;
     int blocks = (tiles + 7) / 8;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_mlp_infer<<<blocks, 256, 0, st>>>(fr, a);
+    NDSPH_COUNT_LAUNCH, k_mlp_infer<<<blocks, 256, 0, st>>>(fr, a);
 }
 void launch_mlp_grad(const float* p, const MlpTrainArgs& a, float* grad, float* loss, cudaStream_t st)
 {
     // grad must be zero on entry (the Adam kernel leaves it so); loss accumulates
     const int blocks = (a.nbatch + TRAIN_BS - 1) / TRAIN_BS;
-    k_mlp_grad<<<blocks, TRAIN_BS, 0, st>>>(p, a, grad, loss);
+    NDSPH_COUNT_LAUNCH, k_mlp_grad<<<blocks, TRAIN_BS, 0, st>>>(p, a, grad, loss);
 }
 void launch_mlp_adam(float* p, float* m, float* v, float* g, int step, float lr, cudaStream_t st)
 {
-    k_mlp_adam<<<(MLP_NPARAM + 255) / 256, 256, 0, st>>>(p, m, v, g, step, lr);
+    NDSPH_COUNT_LAUNCH, k_mlp_adam<<<(MLP_NPARAM + 255) / 256, 256, 0, st>>>(p, m, v, g, step, lr);
 }
 void launch_mlp_store_y(const double* hconv, const double* hpred, double* yprev, int n, cudaStream_t st)
 {
-    if (n > 0) k_mlp_store_y<<<(n + 255) / 256, 256, 0, st>>>(hconv, hpred, yprev, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_mlp_store_y<<<(n + 255) / 256, 256, 0, st>>>(hconv, hpred, yprev, n);
 }
 
 }  // namespace ndsph

@@ -401,8 +401,8 @@ extern "C" int ndsph_density_noalloc(const ndsph_opts* opts, const double* d_x, 
     const int nd = opts->ndim;
     const int bs = 256, nb = (npart + bs - 1) / bs;
 
-    na_reset<<<1, 32, 0, st>>>(p);
-    na_hmax_bbox<<<nb, bs, 0, st>>>(d_x, d_hh, nd, npart, p);
+    NDSPH_COUNT_LAUNCH, na_reset<<<1, 32, 0, st>>>(p);
+    NDSPH_COUNT_LAUNCH, na_hmax_bbox<<<nb, bs, 0, st>>>(d_x, d_hh, nd, npart, p);
     unsigned long long red[7];
     cudaError_t e = cudaMemcpyAsync(red, p.red, sizeof(red), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -455,15 +455,15 @@ extern "C" int ndsph_density_noalloc(const ndsph_opts* opts, const double* d_x, 
     // the counts must start at zero on every call (the scratch keeps the last call's contents)
     e = cudaMemsetAsync(p.count, 0, sizeof(int) * (size_t)nc, st);
     if (e != cudaSuccess) { g_na_err = cudaGetErrorString(e); return NDSPH_E_CUDA; }
-    na_cell_key<<<nb, bs, 0, st>>>(d_x, nd, npart, g, p);
+    NDSPH_COUNT_LAUNCH, na_cell_key<<<nb, bs, 0, st>>>(d_x, nd, npart, g, p);
     const int ntiles = (nc + NA_TILE - 1) / NA_TILE;
-    na_scan_tiles<<<ntiles, NA_TILE, 0, st>>>(p, nc);
-    na_scan_bsum<<<1, NA_TILE, 0, st>>>(p, ntiles);
-    na_scan_final<<<ntiles, NA_TILE, 0, st>>>(p, nc, npart);
-    na_scatter<<<nb, bs, 0, st>>>(p, npart);
-    na_cell_sort<<<(nc + 127) / 128, 128, 0, st>>>(p, nc);
+    NDSPH_COUNT_LAUNCH, na_scan_tiles<<<ntiles, NA_TILE, 0, st>>>(p, nc);
+    NDSPH_COUNT_LAUNCH, na_scan_bsum<<<1, NA_TILE, 0, st>>>(p, ntiles);
+    NDSPH_COUNT_LAUNCH, na_scan_final<<<ntiles, NA_TILE, 0, st>>>(p, nc, npart);
+    NDSPH_COUNT_LAUNCH, na_scatter<<<nb, bs, 0, st>>>(p, npart);
+    NDSPH_COUNT_LAUNCH, na_cell_sort<<<(nc + 127) / 128, 128, 0, st>>>(p, nc);
     const double dq2 = 4.0 / (double)IKERN, ddq2 = 1.0 / dq2;
-    na_density<<<(npart + 127) / 128, 128, 0, st>>>(d_x, d_hh, d_pmass, d_vel, d_itype, npart, g, o, 2.0 * hmax,
+    NDSPH_COUNT_LAUNCH, na_density<<<(npart + 127) / 128, 128, 0, st>>>(d_x, d_hh, d_pmass, d_vel, d_itype, npart, g, o, 2.0 * hmax,
                                                     dq2, ddq2, p, su.tab, d_rho, d_drhodt, d_gradh, d_numneigh);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

@@ -422,7 +422,7 @@ void launch_density(const SweepArgs& a, bool full, cudaStream_t st)
     const int nthreads = full ? a.n : a.nlist;
     if (nthreads <= 0) return;
     const int nb = nblk(nthreads, bs);
-#define DLAUNCH(ND, FU, PR) k_density<ND, FU, PR><<<nb, bs, 0, st>>>(a)
+#define DLAUNCH(ND, FU, PR) NDSPH_COUNT_LAUNCH, k_density<ND, FU, PR><<<nb, bs, 0, st>>>(a)
     if (a.o.precision == NDSPH_PREC_FP64) {
         if (a.o.ndim == 1) { if (full) DLAUNCH(1, true, 0); else DLAUNCH(1, false, 0); }
         else if (a.o.ndim == 2) { if (full) DLAUNCH(2, true, 0); else DLAUNCH(2, false, 0); }
@@ -926,11 +926,11 @@ __global__ void k_pack_rates(SweepArgs a)
 }
 void launch_pack_v(const SweepArgs& a, cudaStream_t st)
 {
-    if (a.n > 0) k_pack_v<<<nblk(a.n, 256), 256, 0, st>>>(a);
+    if (a.n > 0) NDSPH_COUNT_LAUNCH, k_pack_v<<<nblk(a.n, 256), 256, 0, st>>>(a);
 }
 void launch_pack_rates(const SweepArgs& a, cudaStream_t st)
 {
-    if (a.n > 0) k_pack_rates<<<nblk(a.n, 256), 256, 0, st>>>(a);
+    if (a.n > 0) NDSPH_COUNT_LAUNCH, k_pack_rates<<<nblk(a.n, 256), 256, 0, st>>>(a);
 }
 
 void launch_rates(const SweepArgs& a, cudaStream_t st)
@@ -939,13 +939,13 @@ void launch_rates(const SweepArgs& a, cudaStream_t st)
     if (a.n <= 0) return;
     const int nb = nblk(a.n, bs);
     if (a.o.precision == NDSPH_PREC_FP64) {
-        if (a.o.ndim == 1) k_rates<1, 0><<<nb, bs, 0, st>>>(a);
-        else if (a.o.ndim == 2) k_rates<2, 0><<<nb, bs, 0, st>>>(a);
-        else k_rates<3, 0><<<nb, bs, 0, st>>>(a);
+        if (a.o.ndim == 1) NDSPH_COUNT_LAUNCH, k_rates<1, 0><<<nb, bs, 0, st>>>(a);
+        else if (a.o.ndim == 2) NDSPH_COUNT_LAUNCH, k_rates<2, 0><<<nb, bs, 0, st>>>(a);
+        else NDSPH_COUNT_LAUNCH, k_rates<3, 0><<<nb, bs, 0, st>>>(a);
     } else {
-        if (a.o.ndim == 1) k_rates<1, 1><<<nb, bs, 0, st>>>(a);
-        else if (a.o.ndim == 2) k_rates<2, 1><<<nb, bs, 0, st>>>(a);
-        else k_rates<3, 1><<<nb, bs, 0, st>>>(a);
+        if (a.o.ndim == 1) NDSPH_COUNT_LAUNCH, k_rates<1, 1><<<nb, bs, 0, st>>>(a);
+        else if (a.o.ndim == 2) NDSPH_COUNT_LAUNCH, k_rates<2, 1><<<nb, bs, 0, st>>>(a);
+        else NDSPH_COUNT_LAUNCH, k_rates<3, 1><<<nb, bs, 0, st>>>(a);
     }
 }
 
@@ -1058,9 +1058,9 @@ void launch_build_nlist(const SweepArgs& a, cudaStream_t st)
     // per-particle build (rows are contiguous per particle, so its appends
     // merge in L2); the warp-per-cell variant above is kept for comparison
     const int nbp = nblk(a.n, 128);
-    if (a.o.ndim == 1) k_build_nlist<1><<<nbp, 128, 0, st>>>(a);
-    else if (a.o.ndim == 2) k_build_nlist<2><<<nbp, 128, 0, st>>>(a);
-    else k_build_nlist<3><<<nbp, 128, 0, st>>>(a);
+    if (a.o.ndim == 1) NDSPH_COUNT_LAUNCH, k_build_nlist<1><<<nbp, 128, 0, st>>>(a);
+    else if (a.o.ndim == 2) NDSPH_COUNT_LAUNCH, k_build_nlist<2><<<nbp, 128, 0, st>>>(a);
+    else NDSPH_COUNT_LAUNCH, k_build_nlist<3><<<nbp, 128, 0, st>>>(a);
 }
 
 // ===========================================================================
@@ -1107,16 +1107,16 @@ __global__ void k_neigh(SweepArgs a, int mode, const long long* offsets, long lo
 void launch_neigh_count(const SweepArgs& a, int mode, long long* counts, cudaStream_t st)
 {
     const int nb = nblk(a.n, 128);
-    if (a.o.ndim == 1) k_neigh<1><<<nb, 128, 0, st>>>(a, mode, nullptr, counts, nullptr);
-    else if (a.o.ndim == 2) k_neigh<2><<<nb, 128, 0, st>>>(a, mode, nullptr, counts, nullptr);
-    else k_neigh<3><<<nb, 128, 0, st>>>(a, mode, nullptr, counts, nullptr);
+    if (a.o.ndim == 1) NDSPH_COUNT_LAUNCH, k_neigh<1><<<nb, 128, 0, st>>>(a, mode, nullptr, counts, nullptr);
+    else if (a.o.ndim == 2) NDSPH_COUNT_LAUNCH, k_neigh<2><<<nb, 128, 0, st>>>(a, mode, nullptr, counts, nullptr);
+    else NDSPH_COUNT_LAUNCH, k_neigh<3><<<nb, 128, 0, st>>>(a, mode, nullptr, counts, nullptr);
 }
 void launch_neigh_fill(const SweepArgs& a, int mode, const long long* offsets, int* out, cudaStream_t st)
 {
     const int nb = nblk(a.n, 128);
-    if (a.o.ndim == 1) k_neigh<1><<<nb, 128, 0, st>>>(a, mode, offsets, nullptr, out);
-    else if (a.o.ndim == 2) k_neigh<2><<<nb, 128, 0, st>>>(a, mode, offsets, nullptr, out);
-    else k_neigh<3><<<nb, 128, 0, st>>>(a, mode, offsets, nullptr, out);
+    if (a.o.ndim == 1) NDSPH_COUNT_LAUNCH, k_neigh<1><<<nb, 128, 0, st>>>(a, mode, offsets, nullptr, out);
+    else if (a.o.ndim == 2) NDSPH_COUNT_LAUNCH, k_neigh<2><<<nb, 128, 0, st>>>(a, mode, offsets, nullptr, out);
+    else NDSPH_COUNT_LAUNCH, k_neigh<3><<<nb, 128, 0, st>>>(a, mode, offsets, nullptr, out);
 }
 
 }  // namespace ndsph
