@@ -42,6 +42,7 @@ UNIT = "particle-updates/s"
 # force(3) dBevol/dt(3) du/dt de/dt dalpha/dt(3) divB curlB(3) del2u
 # graddivv(3) drhodt dhdt (21 doubles) once each
 RATES_BYTES_PER_PARTICLE = (26 + 21) * 8
+RATES_DRAM_BYTES_64 = 146.9e6
 # density pass: reads x(3) h m v(3) (8 doubles) writes rho rhoalt drhodt dhdt
 # gradh gradhn gradgradh h (8 doubles) + numneigh (4 B)
 DENSITY_BYTES_PER_PARTICLE = 16 * 8 + 4
@@ -385,13 +386,11 @@ def main():
     peak, peak_kind = _load_peaks()
     rates_ms = tim32["rates_ms"]
     achieved = RATES_BYTES_PER_PARTICLE * n / (rates_ms * 1e-3) / 1e9 if rates_ms > 0 else 0.0
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "rates_traffic.json")
-    if os.path.exists(tp):
-        with open(tp) as f:
-            traffic = json.load(f).get("fp32_bytes_per_launch_2M")
+    # DRAM bytes of one k_rates<3,FP32> launch from an ncu capture of the 64^3 box
+    # (127.8 MB read + 19.1 MB written), scaled by the particle count
+    traffic = round(RATES_DRAM_BYTES_64 * n / 64 ** 3)
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 5), "traffic": traffic,
+                "frac": round(achieved / peak, 5), "traffic": traffic, "traffic_note": "ncu dram bytes of the 64^3 launch x N/64^3",
                 "kernel": "k_rates<3,FP32> (rates sweep)",
                 "note": f"peak of {peak_kind} (MEASURED_PEAKS.json hbm_gbs); algorithmic bytes "
                         f"{RATES_BYTES_PER_PARTICLE} B/particle x {n}; the sweep is FP32-issue bound, "
