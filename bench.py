@@ -197,20 +197,32 @@ def run_e2e(o, steps: int, warmup: int):
 
 def run_batched(steps: int, warmup: int, ntubes: int = 4096):
     """Batched form: 4096 independent 1D Brio-Wu tubes, 200-1600 particles
-    each (seeded), one device state, per-tube dt; FP32 pair sums."""
+    each (seeded), one device state, per-tube dt; FP32 pair sums.  `steps`
+    timed steps as captured CUDA graphs (one launch per step), then the same
+    problem on the eager host loop for comparison."""
     from ndspmhd_gb300 import configs
     from ndspmhd_gb300.gpu import GpuSPH
     o, p, sim, counts = configs.brio_wu_batch(ntubes)
     o["precision"] = 1
-    g = GpuSPH(o, configs.full_state(p, 1))
-    g.batch_upload(sim, len(counts), initialise=True)
-    g.batch_step(warmup)
-    g.batch_step(steps)
-    ms = g.timing()["total_ms"]
     n = int(counts.sum())
-    g.close()
-    return {"value": round(n * steps / (ms * 1e-3), 1), "unit": UNIT, "ms_per_step": round(ms / steps, 3),
-            "config": f"{ntubes} Brio-Wu tubes, {n} particles, FP32 pairs, per-tube dt", "steps": steps}
+    out = {}
+    for mode, nst in ((1, steps), (0, max(steps // 4, 5))):
+        g = GpuSPH(o, configs.full_state(p, 1))
+        g.batch_upload(sim, len(counts), initialise=True)
+        g.batch_set_graph(mode)
+        g.batch_step(warmup)
+        g.batch_step(nst)
+        tim = g.timing()
+        ms = tim["total_ms"]
+        g.close()
+        out[mode] = {"value": round(n * nst / (ms * 1e-3), 1), "ms_per_step": round(ms / nst, 3), "steps": nst,
+                     "launches_per_step": round(tim["launches"] / nst, 1),
+                     "graph_steps": tim["graph_steps"], "graph_redos": tim["graph_redos"]}
+    res = dict(out[1])
+    res.update({"unit": UNIT, "config": f"{ntubes} Brio-Wu tubes, {n} particles, FP32 pairs, per-tube dt, "
+                                        f"one captured graph launch per step",
+                "eager": out[0]})
+    return res
 
 
 def run_learned(n1d: int, steps: int, warmup: int):
@@ -419,7 +431,7 @@ def main():
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if not args.no_extra and world == 1:
-        line["batched"] = run_batched(max(args.steps, 5), 3)
+        line["batched"] = run_batched(200, 3)
         line["learned_h"] = run_learned(min(N1D, 128), 20, 40)
         line["dust"] = run_dust(96 if N1D >= 128 else 32, 3, 2)
     # kernel launches the library issued inside the timed step loop (counted

@@ -227,6 +227,14 @@ NDSPH_API int ndsph_batch_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32
                                  int32_t nsim, int32_t initialise);
 NDSPH_API int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, double* time_out);
 NDSPH_API int ndsph_batch_download(ndsph_ctx* ctx, ndsph_particles* p);
+/* how ndsph_batch_step runs a step: 1 (default) one captured CUDA graph per
+ * step -- link, neighbour rows, the Newton-Raphson passes under a device-driven
+ * WHILE node, EOS, rates, leapfrog and the per-simulation dt in one launch, with
+ * steps the graph cannot finish (cells or rows outgrown, a relink, the pass
+ * limit) redone on the eager path; 0 the eager host loop (one host
+ * synchronisation per Newton-Raphson pass).  Replaces the one-run-per-input
+ * loop of multi/multirun.f90; no reference counterpart for the mode itself.  */
+NDSPH_API int ndsph_batch_set_graph(ndsph_ctx* ctx, int32_t mode);
 
 /* ---- parity / debug helpers (never on a timed path) -------------------------
  * ndsph_neighbour_csr: after ndsph_set_linklist, the 1-based neighbour set of
@@ -275,6 +283,8 @@ typedef struct ndsph_timing {
     float   mlp_ms;          /* learned h: inference + training time per step  */
     int32_t mlp_updates;     /* learned h: optimiser steps taken so far        */
     int32_t nl_builds;       /* neighbour-list builds so far (link + rebuilds)  */
+    int32_t graph_steps;     /* batched steps run as a captured CUDA graph      */
+    int32_t graph_redos;     /* of those, steps redone on the eager path        */
 } ndsph_timing;
 NDSPH_API int ndsph_get_timing(ndsph_ctx* ctx, ndsph_timing* t);
 

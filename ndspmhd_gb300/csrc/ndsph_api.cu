@@ -16,7 +16,6 @@
 #include "ndsph_mlp.h"
 
 namespace ndsph {
-void launch_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, cudaStream_t st);
 void launch_density_init2(FieldPtrs F, Side S, int n, Reduce* red, cudaStream_t st);
 }
 
@@ -83,6 +82,28 @@ struct ndsph_ctx {
     double* d_sim_out = nullptr;     // [nsim][4] dtcourant, dtforce, dtnext, time
     double* d_sim_off = nullptr;
     double* h_sim_out = nullptr;
+    // captured batched step: two CUDA graphs (the link swaps the slabs, so
+    // consecutive steps alternate between two pointer states)
+    struct PtrState {
+        int cur;
+        FieldPtrs F;
+        Side S;
+        int *itype2, *id2, *ireal2, *sim2;
+    };
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    PtrState gptr[2];
+    int gparity = 0;
+    bool gvalid = false;
+    int graph_mode = 1;          // 1: batched steps run as captured graphs when possible
+    int gredo = 0;               // captured steps redone on the eager path
+    int gsteps = 0;              // captured steps launched
+    double g_hmax = 0.0;         // max h the graph's cells were sized for
+    double gmargin = 1.05;       // cell size = 2 hmax gmargin at capture
+    long long gl_main[2] = {0, 0};  // kernel nodes of each graph outside the loop body
+    long long gl_body[2] = {0, 0};  // kernel nodes of the loop body
+    int* d_live = nullptr;       // field list of the captured gather
+    int nlive = 0;
+    cudaStream_t st2 = nullptr;  // capture stream of the Newton-Raphson loop body
     // timing
     bool profiling = false;
     cudaEvent_t ev[16];
@@ -95,6 +116,7 @@ struct ndsph_ctx {
 
 static thread_local std::string g_err;
 static int build_nlist(ndsph_ctx* ctx);
+static void link_sort_gather(ndsph_ctx* ctx, const int* d_fields, int nfields, cudaStream_t st);
 #define CK_VOID(call) do { (void)(call); } while (0)
 
 #define CK(call)                                                                          \
@@ -382,6 +404,7 @@ extern "C" int ndsph_init(ndsph_ctx** out, const ndsph_opts* opts, int32_t nmax)
     ctx->t.ggwf = ctx->tab32 + 2 * NTAB; ctx->t.wdragf = ctx->tab32 + 3 * NTAB;
     ctx->t.dq2table = dq2; ctx->t.ddq2table = ddq2;
     ctx->t.dq2tablef = (float)dq2; ctx->t.ddq2tablef = (float)ddq2;
+    ctx->t.cnormf = (float)w[0];
     if (opts->learned_h) {
         if (cudaMalloc(&ctx->mlp_p, sizeof(float) * MLP_NPARAM) != cudaSuccess ||
             cudaMalloc(&ctx->mlp_m, sizeof(float) * MLP_NPARAM) != cudaSuccess ||
@@ -425,6 +448,9 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
     if (ctx->h_dtout) cudaFreeHost(ctx->h_dtout);
     if (ctx->h_sim_out) cudaFreeHost(ctx->h_sim_out);
     for (int k = 0; k < 16; k++) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    for (int k = 0; k < 2; k++) if (ctx->gexec[k]) cudaGraphExecDestroy(ctx->gexec[k]);
+    if (ctx->d_live) cudaFree(ctx->d_live);
+    if (ctx->st2) cudaStreamDestroy(ctx->st2);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
     return 0;
@@ -600,17 +626,7 @@ static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hma
 {
     const int n = ctx->n;
     cudaStream_t st = ctx->st;
-    // reset bbox/hmax reduction slots
-    {
-        Reduce r0;
-        CK(cudaMemcpyAsync(ctx->h_red, ctx->red, sizeof(Reduce), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        r0 = *ctx->h_red;
-        for (int d = 0; d < 3; d++) { r0.xlo[d] = ~0ull; r0.xhi[d] = 0ull; }
-        r0.hmax = 0ull;
-        *ctx->h_red = r0;
-        CK(cudaMemcpyAsync(ctx->red, ctx->h_red, sizeof(Reduce), cudaMemcpyHostToDevice, st));
-    }
+    launch_link_reset(ctx->red, st);
     launch_hmax_bbox(ctx->F, ctx->o.ndim, n, ctx->red, &ctx->red->hmax, st);
     CK(cudaMemcpyAsync(ctx->h_red, ctx->red, sizeof(Reduce), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -635,11 +651,21 @@ static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hma
         CK(cudaMemcpyAsync(&ctx->red->hmax_ghost, &ctx->h_red->hmax_ghost, sizeof(unsigned long long),
                            cudaMemcpyHostToDevice, st));
     }
+    CK(cudaMemcpyAsync(ctx->d_fields, fields, sizeof(int) * (size_t)nfields, cudaMemcpyHostToDevice, st));
+    link_sort_gather(ctx, ctx->d_fields, nfields, st);
+    ctx->linked = true;
+    CK(cudaGetLastError());
+    return build_nlist(ctx);
+}
+
+// counting sort by cell on the current grid, then the permutation gather of
+// `d_fields` into the other slab and the swap of the slabs and side arrays
+static void link_sort_gather(ndsph_ctx* ctx, const int* d_fields, int nfields, cudaStream_t st)
+{
+    const int n = ctx->n;
     launch_cell_key(ctx->F, ctx->g, ctx->o, n, ctx->srt, ctx->red, st);
     launch_scan(ctx->srt, ctx->g.ncells, st);
     launch_scatter_sort(ctx->srt, n, ctx->g.ncells, st);
-    // gather into the other slab, then swap
-    CK(cudaMemcpyAsync(ctx->d_fields, fields, sizeof(int) * (size_t)nfields, cudaMemcpyHostToDevice, st));
     FieldPtrs dst;
     double* other = ctx->slab[1 - ctx->cur];
     for (int f = 0; f < NF; f++) {
@@ -647,7 +673,7 @@ static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hma
         size_t off = (size_t)(ctx->F.f[f] - ctx->slab[ctx->cur]);
         dst.f[f] = other + off;
     }
-    launch_gather_fields(dst, ctx->F, ctx->d_fields, nfields, ctx->srt.perm, n, st);
+    launch_gather_fields(dst, ctx->F, d_fields, nfields, ctx->srt.perm, n, st);
     launch_gather_int(ctx->itype2, ctx->S.itype, ctx->srt.perm, n, st);
     launch_gather_int(ctx->id2, ctx->S.id, ctx->srt.perm, n, st);
     launch_gather_int(ctx->ireal2, ctx->S.ireal, ctx->srt.perm, n, st);
@@ -661,9 +687,6 @@ static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hma
     ctx->cur = 1 - ctx->cur;
     ctx->F = dst;
     launch_post_sort(ctx->S, ctx->srt, n, ctx->g.ncells, ctx->g, ctx->F, ctx->o, st);
-    ctx->linked = true;
-    CK(cudaGetLastError());
-    return build_nlist(ctx);
 }
 
 static int link_all(ndsph_ctx* ctx, bool keep_hmax_ghost)
@@ -690,6 +713,10 @@ static SweepArgs sweep_args(ndsph_ctx* ctx)
     a.nl_ld = ctx->cap;
     a.nl_stride = ctx->nl_stride;
     a.nl_skin = ctx->nl_skin;
+    a.d_its = nullptr;
+    a.d_nlist = nullptr;
+    a.gate = nullptr;
+    a.graph = 0;
     return a;
 }
 
@@ -715,7 +742,7 @@ static int build_nlist(ndsph_ctx* ctx)
         CK(cudaStreamSynchronize(st));
         if (!h[1]) return 0;
         // overflow: grow to the largest count seen (+25%) and rebuild
-        int ns = h[2] + h[2] / 4 + 8;
+        int ns = (h[2] + h[2] / 4 + 8 + 3) & ~3;   // rows of whole 16-byte groups
         CK(cudaFree(ctx->S.nl));
         ctx->S.nl = nullptr;
         CK(cudaMalloc(&ctx->S.nl, sizeof(unsigned) * (size_t)ns * ctx->cap));
@@ -735,7 +762,7 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
     int zero = 0;
     CK(cudaMemcpyAsync(&ctx->red->redolink, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
     int its = 0, ncalc = n, ncalctotal = 0, nrelink = 0;
-    bool redolink = false;
+    bool redolink = false, h1_stale = true;
     if (ctx->o.precision == NDSPH_PREC_FP32) {
         SweepArgs pa = sweep_args(ctx);
         launch_pack_v(pa, st);
@@ -774,11 +801,15 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
                     SweepArgs pa = sweep_args(ctx);
                     launch_pack_v(pa, st);
                 }
+                h1_stale = true;
             }
             nrelink++;
         }
         const bool full = (ncalc == n);
-        launch_h1(ctx->F, ctx->S, n, st);
+        // 1/h: after the start, a full pass (every h changed) or a relink; a
+        // partial pass keeps it current for the particles it updates
+        if (h1_stale) launch_h1(ctx->F, ctx->S, n, st);
+        h1_stale = full;
         if (full && its > 1) launch_copy(ctx->F.f[HNEXT], ctx->F.f[HH], n, st);
         CK(cudaMemsetAsync(ctx->d_ncalc, 0, sizeof(int), st));
         CK(cudaMemsetAsync(&ctx->red->redolink, 0, sizeof(int), st));
@@ -805,7 +836,8 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
         ncalc = h_ncalc;
         std::swap(ctx->S.active, ctx->S.active_next);
         if (ctx->h_red->nl_stale && !redolink) {
-            launch_h1(ctx->F, ctx->S, n, st);   // list radius from the current h
+            if (h1_stale) launch_h1(ctx->F, ctx->S, n, st);   // list radius from the current h
+            h1_stale = false;
             rc = build_nlist(ctx);
             if (rc) return rc;
         }
@@ -1446,6 +1478,303 @@ extern "C" int ndsph_batch_upload(ndsph_ctx* ctx, const ndsph_particles* p, int3
     return 0;
 }
 
+// one eager batched step: predictor, derivs, corrector, next dt per simulation
+static int batch_step_eager(ndsph_ctx* ctx)
+{
+    cudaStream_t st = ctx->st;
+    launch_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+    std::vector<int> live;
+    for (int f : STATE_FIELDS) live.push_back(f);
+    for (int f : INCOPY_FIELDS) live.push_back(f);
+    int rc = do_derivs(ctx, live.data(), (int)live.size());
+    if (rc) return rc;
+    launch_corrector(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+    // next dt of every simulation
+    CK(cudaMemcpyAsync(ctx->d_sim_dt, ctx->d_sim_dtnext, sizeof(double) * (size_t)ctx->nsim,
+                       cudaMemcpyDeviceToDevice, st));
+    return sync_red(ctx);
+}
+
+// ---------------------------------------------------------------------------
+// captured batched step (CUDA graph).  One graph launch runs the whole step:
+// predictor, boundary, link on the cells fixed at capture, the neighbour-row
+// build, the Newton-Raphson passes (the first full pass, then a WHILE
+// conditional node over the partial passes whose condition a kernel sets from
+// the device-side counts), EOS, rates, corrector and the next dt.  The host
+// reads the reduction block once per step.  Cases the eager host loop handles
+// by reallocation or relinking set `gfail` on the device instead; the step is
+// then redone from the predicted state on the eager path (h back to its value
+// at the start of the iteration) and the graphs are captured again.
+// ---------------------------------------------------------------------------
+static ndsph_ctx::PtrState save_ptrs(const ndsph_ctx* c)
+{
+    ndsph_ctx::PtrState p;
+    memset(&p, 0, sizeof(p));   // padding too: states are compared bytewise
+    p.cur = c->cur; p.F = c->F; p.S = c->S;
+    p.itype2 = c->itype2; p.id2 = c->id2; p.ireal2 = c->ireal2; p.sim2 = c->sim2;
+    return p;
+}
+static void load_ptrs(ndsph_ctx* c, const ndsph_ctx::PtrState& p)
+{
+    c->cur = p.cur; c->F = p.F; c->S = p.S;
+    c->itype2 = p.itype2; c->id2 = p.id2; c->ireal2 = p.ireal2; c->sim2 = p.sim2;
+}
+static bool same_ptrs(const ndsph_ctx::PtrState& a, const ndsph_ctx::PtrState& b)
+{
+    return memcmp(&a, &b, sizeof(a)) == 0;
+}
+
+static void graph_drop(ndsph_ctx* ctx)
+{
+    for (int k = 0; k < 2; k++) {
+        if (ctx->gexec[k]) cudaGraphExecDestroy(ctx->gexec[k]);
+        ctx->gexec[k] = nullptr;
+    }
+    ctx->gvalid = false;
+}
+
+static bool graph_usable(const ndsph_ctx* ctx)
+{
+    return ctx->graph_mode == 1 && ctx->o.batched && !ctx->opts.learned_h && !ctx->profiling &&
+           ctx->o.maxdensits >= 1 && ctx->n > 0;
+}
+
+// h cap of the captured cells (the cheap relink's test)
+static double cell_cap(const ndsph_ctx* ctx)
+{
+    double cap = 1e300;
+    for (int d = 0; d < ctx->o.ndim; d++) cap = std::min(cap, 0.5 * ctx->g.cs[d] / (1.0 + 1.e-9));
+    return cap;
+}
+
+// one Newton-Raphson pass on stream s (full: the first pass of the step)
+static void capture_nr_pass(ndsph_ctx* ctx, bool full, cudaGraphConditionalHandle hc, int its_cap,
+                            cudaStream_t s)
+{
+    const int n = ctx->n;
+    launch_nr_pre(ctx->red, ctx->d_ncalc, s);
+    if (!full) {
+        // the relink check of iterate_density.f90:122-126 (the first pass never relinks)
+        launch_hmax_bbox(ctx->F, ctx->o.ndim, n, ctx->red, &ctx->red->hmax, s, &ctx->red->g_gate);
+        launch_nr_relink_apply(ctx->red, cell_cap(ctx), s);
+    }
+    SweepArgs a = sweep_args(ctx);
+    a.d_its = &ctx->red->g_its;
+    if (!full) a.d_nlist = &ctx->red->g_nlist;
+    launch_density(a, full, s);
+    if (full) std::swap(ctx->F.f[HH], ctx->F.f[HNEXT]);
+    if (ctx->o.has_fixed) launch_fixed_density_copy(ctx->F, ctx->S, n, s);
+    launch_nr_post(ctx->red, ctx->d_ncalc, n, its_cap, hc, s);
+    launch_copy_active(ctx->S.active, ctx->S.active_next, &ctx->red->g_nlist, n, s);
+    // after the full pass every h changed; partial passes keep 1/h current themselves
+    if (full) launch_h1(ctx->F, ctx->S, n, s);
+    SweepArgs b = sweep_args(ctx);
+    b.gate = &ctx->red->g_rebuild;
+    b.graph = 1;
+    launch_build_nlist(b, s);
+}
+
+#define GCK(call)                                                                          \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess && err == cudaSuccess) { err = e_; what = #call; }           \
+    } while (0)
+
+// capture one step from the current pointer state; leaves the pointers in the
+// state after the step
+static int capture_one(ndsph_ctx* ctx, cudaGraphExec_t* out, long long* nmain, long long* nbody)
+{
+    const long long c0 = ndsph_launch_counter().load();
+    long long b0 = 0, b1 = 0;
+    cudaStream_t st = ctx->st;
+    const int n = ctx->n;
+    cudaError_t err = cudaSuccess;
+    const char* what = "";
+    cudaGraph_t graph = nullptr;
+    bool anyb = false;
+    for (int d = 0; d < ctx->o.ndim; d++) if (ctx->o.ibound[d] != 0) anyb = true;
+    const int its_cap = std::min(ctx->o.maxdensits, 30);
+    GCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    if (err) { ctx->err = std::string("graph capture: ") + cudaGetErrorString(err); return NDSPH_E_CUDA; }
+    launch_graph_begin(ctx->red, st);
+    launch_predictor(ctx->F, ctx->S, ctx->o, n, ctx->red, st);
+    if (anyb) launch_boundary_wrap(ctx->F, ctx->o, n, st);
+    // link on the captured cells
+    launch_link_reset(ctx->red, st);
+    launch_hmax_bbox(ctx->F, ctx->o.ndim, n, ctx->red, &ctx->red->hmax, st);
+    launch_grid_check(ctx->red, ctx->g, ctx->o, st);
+    link_sort_gather(ctx, ctx->d_live, ctx->nlive, st);
+    GCK(cudaMemsetAsync(&ctx->red->nl_stale, 0, sizeof(int) * 3, st));
+    {
+        SweepArgs a = sweep_args(ctx);
+        a.graph = 1;
+        launch_build_nlist(a, st);
+    }
+    launch_reduce_reset(ctx->red, st);
+    launch_sim_reset(ctx->o, st);
+    // iterate_density
+    launch_density_init2(ctx->F, ctx->S, n, ctx->red, st);
+    GCK(cudaMemsetAsync(&ctx->red->redolink, 0, sizeof(int), st));
+    launch_h1(ctx->F, ctx->S, n, st);
+    if (ctx->o.precision == NDSPH_PREC_FP32) {
+        SweepArgs pa = sweep_args(ctx);
+        launch_pack_v(pa, st);
+    }
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cgraph = nullptr;
+    GCK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &cgraph, nullptr, nullptr, nullptr));
+    cudaGraphConditionalHandle hc = 0;
+    GCK(cudaGraphConditionalHandleCreate(&hc, cgraph, 0, cudaGraphCondAssignDefault));
+    capture_nr_pass(ctx, true, hc, its_cap, st);
+    // the partial passes: WHILE node
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    GCK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &cgraph, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = hc;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode = nullptr;
+    GCK(cudaGraphAddNode(&wnode, cgraph, deps, nullptr, ndeps, &cp));
+    if (err == cudaSuccess) {
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        GCK(cudaStreamUpdateCaptureDependencies(st, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+        GCK(cudaStreamBeginCaptureToGraph(ctx->st2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        b0 = ndsph_launch_counter().load();
+        capture_nr_pass(ctx, false, hc, its_cap, ctx->st2);
+        b1 = ndsph_launch_counter().load();
+        GCK(cudaStreamEndCapture(ctx->st2, &body));
+    }
+    // cons2prim, rates, corrector, next dt
+    launch_eos(ctx->F, ctx->S, ctx->o, n, ctx->red, st);
+    launch_fixed_copy(ctx->F, ctx->S, ctx->o, n, st);
+    launch_h1(ctx->F, ctx->S, n, st);
+    {
+        SweepArgs a = sweep_args(ctx);
+        if (ctx->o.precision == NDSPH_PREC_FP32) launch_pack_rates(a, st);
+        launch_rates(a, st);
+    }
+    launch_finalize_dt(ctx->red, ctx->o, ctx->d_dtout, st);
+    launch_sim_finalize(ctx->o, ctx->d_sim_dtnext, ctx->d_sim_out, st);
+    launch_corrector(ctx->F, ctx->S, ctx->o, n, ctx->red, st);
+    launch_sim_dt_advance(ctx->d_sim_dt, ctx->d_sim_dtnext, ctx->nsim, ctx->red, st);
+    GCK(cudaMemcpyAsync(ctx->h_red, ctx->red, sizeof(Reduce), cudaMemcpyDeviceToHost, st));
+    GCK(cudaGetLastError());
+    cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+    if (err == cudaSuccess && e2 != cudaSuccess) { err = e2; what = "cudaStreamEndCapture"; }
+    if (err == cudaSuccess) GCK(cudaGraphInstantiate(out, graph, 0));
+    if (graph) cudaGraphDestroy(graph);
+    // capturing launches nothing: the launches are counted when the graph runs
+    const long long c1 = ndsph_launch_counter().load();
+    ndsph_launch_counter().fetch_sub(c1 - c0);
+    *nbody = b1 - b0;
+    *nmain = (c1 - c0) - *nbody;
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        ctx->err = std::string("graph capture: ") + what + ": " + cudaGetErrorString(err);
+        return NDSPH_E_CUDA;
+    }
+    return 0;
+}
+#undef GCK
+
+static int capture_graphs(ndsph_ctx* ctx)
+{
+    cudaStream_t st = ctx->st;
+    graph_drop(ctx);
+    if (!ctx->st2) CK(cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking));
+    if (!ctx->d_live) CK(cudaMalloc(&ctx->d_live, sizeof(int) * NF));
+    std::vector<int> live;
+    for (int f : STATE_FIELDS) live.push_back(f);
+    for (int f : INCOPY_FIELDS) live.push_back(f);
+    ctx->nlive = (int)live.size();
+    CK(cudaMemcpyAsync(ctx->d_live, live.data(), sizeof(int) * live.size(), cudaMemcpyHostToDevice, st));
+    // cells of the captured link: 2 hmax gmargin wide, 3 spare layers on open sides
+    launch_link_reset(ctx->red, st);
+    launch_hmax_bbox(ctx->F, ctx->o.ndim, ctx->n, ctx->red, &ctx->red->hmax, st);
+    CK(cudaMemcpyAsync(ctx->h_red, ctx->red, sizeof(Reduce), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const double hmax = bitsd(ctx->h_red->hmax);
+    if (!(hmax > 0.0) || !std::isfinite(hmax)) { ctx->err = "link: max h <= 0 or not finite"; return NDSPH_E_H_NONPOS; }
+    const double hc = hmax * ctx->gmargin;
+    const double c = 2.0 * hc * (1.0 + 1.e-9);
+    double lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+        lo[d] = (d < ctx->o.ndim) ? unord_bits(ctx->h_red->xlo[d]) - 2.0 * c : 0.0;
+        hi[d] = (d < ctx->o.ndim) ? unord_bits(ctx->h_red->xhi[d]) + 2.0 * c : 0.0;
+        if (d < ctx->o.ndim && (!std::isfinite(lo[d]) || !std::isfinite(hi[d]))) {
+            ctx->err = "link: non-finite position";
+            return NDSPH_E_NAN;
+        }
+    }
+    int rc = build_grid(ctx, hc, lo, hi);
+    if (rc) return rc;
+    ctx->g_hmax = hmax;
+    const ndsph_ctx::PtrState s0 = save_ptrs(ctx);
+    ctx->gptr[0] = s0;
+    rc = capture_one(ctx, &ctx->gexec[0], &ctx->gl_main[0], &ctx->gl_body[0]);
+    if (rc) { load_ptrs(ctx, s0); graph_drop(ctx); return rc; }
+    ctx->gptr[1] = save_ptrs(ctx);
+    rc = capture_one(ctx, &ctx->gexec[1], &ctx->gl_main[1], &ctx->gl_body[1]);
+    const bool back = same_ptrs(save_ptrs(ctx), s0);
+    load_ptrs(ctx, s0);
+    if (rc) { graph_drop(ctx); return rc; }
+    if (!back) { graph_drop(ctx); ctx->err = "graph capture: pointer state did not return"; return NDSPH_E_CUDA; }
+    ctx->gparity = 0;
+    ctx->gvalid = true;
+    return 0;
+}
+
+// redo a step whose captured form set gfail: from the predicted state, with h
+// back to its value at the start of the iteration
+static int graph_redo(ndsph_ctx* ctx)
+{
+    cudaStream_t st = ctx->st;
+    launch_copy(ctx->F.f[HH], ctx->F.f[HDEN0], ctx->n, st);
+    CK(cudaMemsetAsync(&ctx->red->gfail, 0, sizeof(int), st));
+    std::vector<int> live;
+    for (int f : STATE_FIELDS) live.push_back(f);
+    for (int f : INCOPY_FIELDS) live.push_back(f);
+    int rc = do_derivs(ctx, live.data(), (int)live.size());
+    if (rc) return rc;
+    launch_corrector(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+    CK(cudaMemcpyAsync(ctx->d_sim_dt, ctx->d_sim_dtnext, sizeof(double) * (size_t)ctx->nsim,
+                       cudaMemcpyDeviceToDevice, st));
+    return sync_red(ctx);
+}
+
+static int batch_step_graph(ndsph_ctx* ctx)
+{
+    if (!ctx->gvalid) {
+        int rc = capture_graphs(ctx);
+        if (rc) return rc;
+    }
+    const int p = ctx->gparity;
+    CK(cudaGraphLaunch(ctx->gexec[p], ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    load_ptrs(ctx, ctx->gptr[1 - p]);
+    ctx->gparity = 1 - p;
+    ctx->gsteps++;
+    ndsph_launch_counter().fetch_add(ctx->gl_main[p] + (long long)std::max(ctx->h_red->g_its - 1, 0) * ctx->gl_body[p]);
+    if (ctx->h_red->err) {
+        char buf[160];
+        snprintf(buf, sizeof buf, "device error %d at particle %d", ctx->h_red->err, ctx->h_red->err_index + 1);
+        ctx->err = buf;
+        return ctx->h_red->err;
+    }
+    if (ctx->h_red->gfail) {
+        ctx->gredo++;
+        graph_drop(ctx);
+        int rc = graph_redo(ctx);
+        if (rc) return rc;
+        if (ctx->gredo > 8 && ctx->gredo * 4 > ctx->gsteps) ctx->graph_mode = 0;   // mostly redone: stay eager
+        return 0;
+    }
+    // cells much larger than h needs: capture again on the next step
+    if (bitsd(ctx->h_red->hmax_ghost) < 0.8 * ctx->g_hmax) graph_drop(ctx);
+    return 0;
+}
+
 extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, double* time_out)
 {
     GUARD_CTX();
@@ -1454,17 +1783,7 @@ extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, 
     const long long l0 = ndsph_launch_counter().load();
     CK(cudaEventRecord(ctx->ev[10], st));
     for (int k = 0; k < nsteps; k++) {
-        launch_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
-        std::vector<int> live;
-        for (int f : STATE_FIELDS) live.push_back(f);
-        for (int f : INCOPY_FIELDS) live.push_back(f);
-        int rc = do_derivs(ctx, live.data(), (int)live.size());
-        if (rc) return rc;
-        launch_corrector(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
-        // next dt of every simulation
-        CK(cudaMemcpyAsync(ctx->d_sim_dt, ctx->d_sim_dtnext, sizeof(double) * (size_t)ctx->nsim,
-                           cudaMemcpyDeviceToDevice, st));
-        rc = sync_red(ctx);
+        const int rc = graph_usable(ctx) ? batch_step_graph(ctx) : batch_step_eager(ctx);
         if (rc) return rc;
         ctx->nsteps++;
     }
@@ -1476,10 +1795,21 @@ extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, 
     cudaEventElapsedTime(&ms, ctx->ev[10], ctx->ev[11]);
     ctx->timing.total_ms = ms;
     ctx->timing.launches = (int32_t)(ndsph_launch_counter().load() - l0);
+    ctx->timing.graph_steps = ctx->gsteps;
+    ctx->timing.graph_redos = ctx->gredo;
     for (int s2 = 0; s2 < ctx->nsim; s2++) {
         if (dt_out) dt_out[s2] = ctx->h_sim_out[s2 * 4 + 2];
         if (time_out) time_out[s2] = ctx->h_sim_out[s2 * 4 + 3];
     }
+    return 0;
+}
+
+extern "C" int ndsph_batch_set_graph(ndsph_ctx* ctx, int32_t mode)
+{
+    GUARD_CTX();
+    if (mode != 0 && mode != 1) { ctx->err = "graph mode must be 0 or 1"; return NDSPH_E_ARG; }
+    graph_drop(ctx);
+    ctx->graph_mode = mode;
     return 0;
 }
 

@@ -88,6 +88,7 @@ struct Tables {
     const float2* wdragf;
     double dq2table, ddq2table;
     float dq2tablef, ddq2tablef;
+    float cnormf;           // W(0): the kernel's normalisation (FP32 form's analytic kernel)
 };
 
 // global reductions written by the sweeps (int64 bit patterns of
@@ -116,6 +117,13 @@ struct Reduce {
     int nl_overflow;                // some particle had more candidates than the list stride
     int nl_maxcnt;                  // largest list length of the last build
     int pad2;
+    // control words of the captured (CUDA graph) step
+    int gfail;                      // the captured step met a case it leaves to the host path
+    int g_its;                      // Newton-Raphson pass number
+    int g_nlist;                    // active entries of the next partial pass
+    int g_gate;                     // relink check of this pass (redolink of the previous pass)
+    int g_rebuild;                  // rebuild the neighbour rows after this pass
+    int g_pad;
 };
 
 __host__ __device__ inline unsigned long long dbits(double v)
@@ -135,10 +143,10 @@ __host__ __device__ inline double bitsd(unsigned long long u)
 #endif
 }
 
-inline double unord_bits(unsigned long long u)
+__host__ __device__ inline double unord_bits(unsigned long long u)
 {
     u = (u & 0x8000000000000000ull) ? (u & ~0x8000000000000000ull) : ~u;
-    union { double d; unsigned long long u; } c; c.u = u; return c.d;
+    return bitsd(u);
 }
 
 #ifdef __CUDACC__

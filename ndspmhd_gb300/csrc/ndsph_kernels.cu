@@ -36,8 +36,9 @@ void launch_boundary_wrap(FieldPtrs F, DevOpts o, int n, cudaStream_t st)
 
 // max h (bound module hhmax, linkND.f90:70 / ghostND_mhd.f90:77) and the
 // particle bounding box (linkND.f90:80-89) in one pass
-__global__ void k_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst)
+__global__ void k_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, const int* gate)
 {
+    if (gate && *gate == 0) return;
     // block-level reduction first: one set of atomics per block, not per warp
     __shared__ double sh[8];
     __shared__ unsigned long long slo[8][3], shi[8][3];
@@ -87,9 +88,10 @@ void launch_hmax(const double* h, int n, Reduce* red, unsigned long long* dst, c
 {
     (void)h; (void)n; (void)red; (void)dst; (void)st;
 }
-void launch_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, cudaStream_t st)
+void launch_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, cudaStream_t st,
+                      const int* gate)
 {
-    if (n > 0) NDSPH_COUNT_LAUNCH, k_hmax_bbox<<<nblk(n, 256), 256, 0, st>>>(F, ndim, n, red, dst);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_hmax_bbox<<<nblk(n, 256), 256, 0, st>>>(F, ndim, n, red, dst, gate);
 }
 
 // ---------------------------------------------------------------------------
@@ -430,6 +432,12 @@ __global__ void k_fixed_density_copy(FieldPtrs F, Side S, int n)
     int j = S.pos_of_id[src_id];
     const int fl[7] = {RHO, RHOALT, DRHODT, DHDT, HH, GRADH, GRADHN};
     for (int q = 0; q < 7; q++) F.f[fl[q]][k] = F.f[fl[q]][j];
+    // 1/h and the list's h follow the copied h
+    const double h = F.f[HH][k];
+    S.h1[k] = 1.0 / h;
+    float4 xw = S.xs[k];
+    xw.w = (float)h;
+    S.xs[k] = xw;
 }
 void launch_fixed_density_copy(FieldPtrs F, Side S, int n, cudaStream_t st)
 {
@@ -574,6 +582,7 @@ __global__ void k_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (red->gfail) return;   // a captured step that failed is redone from the predicted state
     const double dt = o.batched ? o.sim_dt[S.sim[i]] : red->dt;
     const double hdt = 0.5 * dt;
     int t = S.itype[i];
@@ -745,6 +754,132 @@ void launch_p2c_post(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st)
 {
     (void)S;
     if (n > 0) NDSPH_COUNT_LAUNCH, k_p2c_post<<<nblk(n, 256), 256, 0, st>>>(F, o, n);
+}
+
+
+// ---------------------------------------------------------------------------
+// Control kernels of the captured (CUDA graph) step.  The host loop of the
+// eager step reads the Newton-Raphson counts and flags back after every pass;
+// the captured step keeps those decisions on the device: a WHILE conditional
+// node runs the partial passes, and every case the eager host loop handles by
+// reallocating or relinking (a grid that no longer fits, a neighbour row that
+// overflows, a relink, another full pass, the pass limit) sets `gfail`; the
+// corrector and the dt update then skip, and the host redoes the step from the
+// predicted state on the eager path.
+// ---------------------------------------------------------------------------
+__global__ void k_link_reset(Reduce* red)
+{
+    for (int d = 0; d < 3; d++) { red->xlo[d] = ~0ull; red->xhi[d] = 0ull; }
+    red->hmax = 0ull;
+}
+void launch_link_reset(Reduce* red, cudaStream_t st)
+{
+    NDSPH_COUNT_LAUNCH, k_link_reset<<<1, 1, 0, st>>>(red);
+}
+
+__global__ void k_grid_check(Reduce* red, Grid g, DevOpts o)
+{
+    const double hmax = bitsd(red->hmax);
+    double cap = 1e300;
+    for (int d = 0; d < o.ndim; d++) cap = fmin(cap, 0.5 * g.cs[d] / (1.0 + 1.e-9));
+    bool ok = (hmax > 0.0) && (hmax <= cap);
+    for (int d = 0; d < o.ndim; d++) {
+        if (o.periodic[d]) continue;
+        const double lo = unord_bits(red->xlo[d]), hi = unord_bits(red->xhi[d]);
+        const double top = g.origin[d] + g.cs[d] * (double)g.nc[d];
+        if (!(lo >= g.origin[d] + g.cs[d]) || !(hi < top - g.cs[d])) ok = false;
+    }
+    if (!ok) red->gfail |= 1;
+    red->hmax_ghost = red->hmax;   // the ghosts' hhmax is the max h at the link
+}
+void launch_grid_check(Reduce* red, Grid g, DevOpts o, cudaStream_t st)
+{
+    NDSPH_COUNT_LAUNCH, k_grid_check<<<1, 1, 0, st>>>(red, g, o);
+}
+
+__global__ void k_graph_begin(Reduce* red)
+{
+    red->gfail = 0;
+    red->g_its = 0;
+    red->g_nlist = 0;
+    red->g_gate = 0;
+    red->g_rebuild = 0;
+}
+void launch_graph_begin(Reduce* red, cudaStream_t st)
+{
+    NDSPH_COUNT_LAUNCH, k_graph_begin<<<1, 1, 0, st>>>(red);
+}
+
+// start of a pass: count it; the relink check of iterate_density.f90:122-126
+// runs when the previous pass asked for a relink
+__global__ void k_nr_pre(Reduce* red, int* d_ncalc)
+{
+    red->g_its += 1;
+    red->g_gate = red->redolink;
+    red->redolink = 0;
+    red->hmax = 0ull;
+    *d_ncalc = 0;
+}
+void launch_nr_pre(Reduce* red, int* d_ncalc, cudaStream_t st)
+{
+    NDSPH_COUNT_LAUNCH, k_nr_pre<<<1, 1, 0, st>>>(red, d_ncalc);
+}
+
+// the relink refreshes the ghosts' hhmax when h still fits the cells; a
+// relink that needs new cells is left to the host path
+__global__ void k_nr_relink_apply(Reduce* red, double cap)
+{
+    if (!red->g_gate) return;
+    const double hmax_now = bitsd(red->hmax);
+    if (hmax_now <= cap) red->hmax_ghost = red->hmax;
+    else red->gfail |= 4;
+}
+void launch_nr_relink_apply(Reduce* red, double cap, cudaStream_t st)
+{
+    NDSPH_COUNT_LAUNCH, k_nr_relink_apply<<<1, 1, 0, st>>>(red, cap);
+}
+
+// end of a pass: the next active count, the row-rebuild gate, and the loop
+// condition (more unconverged particles, no failure, pass limit not reached)
+__global__ void k_nr_post(Reduce* red, const int* d_ncalc, int n, int its_cap, cudaGraphConditionalHandle h)
+{
+    const int nc = *d_ncalc;
+    red->g_nlist = nc;
+    const int rebuild = (red->nl_stale != 0 && red->redolink == 0) ? 1 : 0;
+    red->g_rebuild = rebuild;
+    if (rebuild) { red->nl_stale = 0; red->nl_overflow = 0; red->nl_maxcnt = 0; }
+    if (nc > 0 && nc == n) red->gfail |= 8;               // another full pass
+    if (nc > 0 && red->g_its >= its_cap) red->gfail |= 16; // pass limit of the captured loop
+    const bool more = nc > 0 && red->gfail == 0;
+    cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+void launch_nr_post(Reduce* red, const int* d_ncalc, int n, int its_cap, cudaGraphConditionalHandle h,
+                    cudaStream_t st)
+{
+    NDSPH_COUNT_LAUNCH, k_nr_post<<<1, 1, 0, st>>>(red, d_ncalc, n, its_cap, h);
+}
+
+__global__ void k_copy_active(int* dst, const int* src, const int* count, int n)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = *count;
+    if (k >= c || k >= n) return;
+    dst[k] = src[k];
+}
+void launch_copy_active(int* dst, const int* src, const int* count, int n, cudaStream_t st)
+{
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_copy_active<<<nblk(n, 256), 256, 0, st>>>(dst, src, count, n);
+}
+
+__global__ void k_sim_dt_advance(double* dt, const double* dtnext, int nsim, const Reduce* red)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsim || red->gfail) return;
+    dt[s] = dtnext[s];
+}
+void launch_sim_dt_advance(double* dt, const double* dtnext, int nsim, const Reduce* red, cudaStream_t st)
+{
+    if (nsim > 0) NDSPH_COUNT_LAUNCH, k_sim_dt_advance<<<nblk(nsim, 256), 256, 0, st>>>(dt, dtnext, nsim, red);
 }
 
 }  // namespace ndsph

@@ -61,11 +61,20 @@ struct SweepArgs {
     long long nl_ld;         // leading dimension of the list (>= n)
     int nl_stride;           // entries per particle
     float nl_skin;           // list radius = 2 max(h_i,h_j) skin (h may grow by skin before a rebuild)
+    // device-side control (captured step): when set, the pass number, the
+    // active count and the row-build gate are read from device memory
+    const int* d_its;
+    const int* d_nlist;
+    const int* gate;
+    int graph;               // captured step: a row overflow sets gfail
 };
 
 // ---- link / sort (ndsph_kernels.cu) ------------------------------------------
 void launch_boundary_wrap(FieldPtrs F, DevOpts o, int n, cudaStream_t st);
 void launch_hmax(const double* h, int n, Reduce* red, unsigned long long* dst, cudaStream_t st);
+// max h and bounding box; skipped when `gate` is set and points to 0
+void launch_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, cudaStream_t st,
+                      const int* gate = nullptr);
 void launch_cell_key(FieldPtrs F, Grid g, DevOpts o, int n, SortScratch s, Reduce* red, cudaStream_t st);
 void launch_scan(SortScratch s, int ncells, cudaStream_t st);
 void launch_scatter_sort(SortScratch s, int n, int ncells, cudaStream_t st);
@@ -104,6 +113,16 @@ void launch_p2c_post(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
 void launch_sim_reset(DevOpts o, cudaStream_t st);
 void launch_sim_finalize(DevOpts o, double* dt_next, double* sim_out, cudaStream_t st);
 void launch_add_offset(FieldPtrs F, const int* sim, const double* off, int n, int sign, cudaStream_t st);
+// captured step (CUDA graph) control kernels
+void launch_link_reset(Reduce* red, cudaStream_t st);
+void launch_grid_check(Reduce* red, Grid g, DevOpts o, cudaStream_t st);
+void launch_graph_begin(Reduce* red, cudaStream_t st);
+void launch_nr_pre(Reduce* red, int* d_ncalc, cudaStream_t st);
+void launch_nr_relink_apply(Reduce* red, double cap, cudaStream_t st);
+void launch_nr_post(Reduce* red, const int* d_ncalc, int n, int its_cap, cudaGraphConditionalHandle h,
+                    cudaStream_t st);
+void launch_copy_active(int* dst, const int* src, const int* count, int n, cudaStream_t st);
+void launch_sim_dt_advance(double* dt, const double* dtnext, int nsim, const Reduce* red, cudaStream_t st);
 
 // ---- sweeps (ndsph_sweeps.cu) --------------------------------------------
 void launch_density(const SweepArgs& a, bool full, cudaStream_t st);

@@ -80,6 +80,28 @@ __device__ __forceinline__ float tab_valf(const float2* tab, const TabIdxF& ix)
     return fmaf(e.y, ix.dxx, e.x);
 }
 
+// FP32 form: the cubic spline W, dW/dq and d2W/dq2 evaluated directly,
+// C (t^3/4 - u^3) with t = max(2-q, 0), u = max(1-q, 0) (kernelND.f90:4143-4192).
+// The reference interpolates them linearly in q^2 from its 4001-point tables;
+// for q^2 >= KERN_Q2_DIRECT the two agree within 1.4e-7 C (W) and 7.5e-7 C
+// (dW/dq), well inside the form's 1e-5 budget, and no table is read.  Below
+// it (a few per cent of pairs) the table is used: there the linear
+// interpolation in q^2 departs from the polynomial (dW/dq ~ q ~ sqrt(q^2)).
+constexpr float KERN_Q2_DIRECT = 0.25f;
+struct KerF {
+    float w, gw, ggw;
+};
+__device__ __forceinline__ KerF kern_cubic(float q, float c)
+{
+    const float t = fmaxf(2.0f - q, 0.0f), u = fmaxf(1.0f - q, 0.0f);
+    const float t2 = t * t, u2 = u * u;
+    KerF k;
+    k.w = c * (0.25f * t2 * t - u2 * u);
+    k.gw = c * (3.0f * u2 - 0.75f * t2);
+    k.ggw = c * (1.5f * t - 6.0f * u);
+    return k;
+}
+
 // stencil cell with periodic wrap; returns false if outside (open dims)
 template <int NDIM>
 struct Stencil {
@@ -227,7 +249,8 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
         if (t >= a.n) return;
         i = t;
     } else {
-        if (t >= a.nlist) return;
+        const int nlist = a.d_nlist ? *a.d_nlist : a.nlist;
+        if (t >= nlist) return;
         i = a.S.active[t];
     }
     const FieldPtrs& F = a.F;
@@ -262,84 +285,118 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
 
     Stencil<NDIM> stn(a.S.cell[i], g);
     const int ncand = a.S.nl_cnt[i];
-    {
-        for (int k = 0; k < ncand; k++) {
-            const unsigned pk = a.S.nl[(size_t)i * a.nl_stride + k];
-            const int j = (int)(pk >> 5);
-            int d[3], w[3];
-            stn.offset((int)(pk & 31u), g, d, w);
-            const float4 xsj = a.S.xs[j];
-            float dxf[3];
-            const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
-            const float hm = FULL ? fmaxf(hif, xsj.w) : hif;
-            if (PREC == NDSPH_PREC_FP64) {
-                const float rc = 2.0f * hm * 1.0002f + abs_tol;
-                if (r2f > rc * rc) continue;
+    const unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
+    // one candidate: its list entry, position and type, and (FP32 form) its
+    // velocity/mass pack, loaded by the caller
+    auto pair = [&](unsigned pk, const float4& xsj, int typej, const float4& pvj) {
+        const int j = (int)(pk >> 5);
+        int d[3], w[3];
+        stn.offset((int)(pk & 31u), g, d, w);
+        float dxf[3];
+        const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
+        const float hm = FULL ? fmaxf(hif, xsj.w) : hif;
+        if (PREC == NDSPH_PREC_FP64) {
+            const float rc = 2.0f * hm * 1.0002f + abs_tol;
+            if (r2f > rc * rc) return;
+        } else {
+            if (r2f >= 4.0f * hm * hm) return;
+        }
+        if (!type_match(typei, typej)) return;
+        if (PREC == NDSPH_PREC_FP64) {
+            double dx[3], rij2;
+            if (!exact_dx<NDIM>(F, j, xi, w, o, dxbound, dx, rij2)) return;
+            const double q2i = __dmul_rn(rij2, hi21);
+            bool inc;
+            if (FULL) {
+                const double hj1 = a.S.h1[j];
+                const double q2j = __dmul_rn(__dmul_rn(rij2, hj1), hj1);
+                inc = (q2i < 4.0) || (q2j < 4.0);
             } else {
-                if (r2f >= 4.0f * hm * hm) continue;
+                inc = q2i < 4.0;
             }
-            const int typej = a.S.itype[j];
-            if (!type_match(typei, typej)) continue;
-            if (PREC == NDSPH_PREC_FP64) {
-                double dx[3], rij2;
-                if (!exact_dx<NDIM>(F, j, xi, w, o, dxbound, dx, rij2)) continue;
-                const double q2i = __dmul_rn(rij2, hi21);
-                bool inc;
-                if (FULL) {
-                    const double hj1 = a.S.h1[j];
-                    const double q2j = __dmul_rn(__dmul_rn(rij2, hj1), hj1);
-                    inc = (q2i < 4.0) || (q2j < 4.0);
-                } else {
-                    inc = q2i < 4.0;
-                }
-                if (!inc) continue;
-                nn++;
-                if (q2i >= 4.0 || fixed_i) continue;
-                const double mj = F.f[PM][j];
-                const TabIdx ix = tab_index(a.t, q2i);
-                const double wv = tab_val(a.t.w, ix);
-                const double gw = tab_val(a.t.gw, ix);
-                const double ggw = tab_val(a.t.ggw, ix);
-                const double q = sqrt(q2i);
-                sw += mj * wv;
-                sn += wv;
-                const double tg = q * gw + (double)NDIM * wv;
-                sg += mj * tg;
-                sgn += tg;
-                sgg += mj * ((double)(NDIM * (NDIM + 1)) * wv + (double)(2 * (NDIM + 1)) * q * gw + q2i * ggw);
-                if (j != i) {
-                    const double rij = sqrt(rij2);
-                    double dvr = (vi[0] - F.f[V0][j]) * dx[0];
-                    if (NDIM >= 2) dvr += (vi[1] - F.f[V1][j]) * dx[1];
-                    if (NDIM >= 3) dvr += (vi[2] - F.f[V2][j]) * dx[2];
-                    sd += mj * dvr * gw / (rij + 2.220446049250313e-16);
-                }
+            if (!inc) return;
+            nn++;
+            if (q2i >= 4.0 || fixed_i) return;
+            const double mj = F.f[PM][j];
+            const TabIdx ix = tab_index(a.t, q2i);
+            const double wv = tab_val(a.t.w, ix);
+            const double gw = tab_val(a.t.gw, ix);
+            const double ggw = tab_val(a.t.ggw, ix);
+            const double q = sqrt(q2i);
+            sw += mj * wv;
+            sn += wv;
+            const double tg = q * gw + (double)NDIM * wv;
+            sg += mj * tg;
+            sgn += tg;
+            sgg += mj * ((double)(NDIM * (NDIM + 1)) * wv + (double)(2 * (NDIM + 1)) * q * gw + q2i * ggw);
+            if (j != i) {
+                const double rij = sqrt(rij2);
+                double dvr = (vi[0] - F.f[V0][j]) * dx[0];
+                if (NDIM >= 2) dvr += (vi[1] - F.f[V1][j]) * dx[1];
+                if (NDIM >= 3) dvr += (vi[2] - F.f[V2][j]) * dx[2];
+                sd += mj * dvr * gw / (rij + 2.220446049250313e-16);
+            }
+        } else {
+            // FP32 form: separation from the FP32 cell-relative coordinates
+            const float q2i = r2f * hi21f;
+            nn++;
+            if (fixed_i || !(q2i < 4.0f)) return;
+            const float mj = pvj.w;
+            const float q = sqrtp(q2i);
+            float wv, gw, ggw;
+            if (q2i >= KERN_Q2_DIRECT) {
+                const KerF kf = kern_cubic(q, a.t.cnormf);
+                wv = kf.w; gw = kf.gw; ggw = kf.ggw;
             } else {
-                // FP32 form: separation from the FP32 cell-relative coordinates
-                const float q2i = r2f * hi21f;
-                nn++;
-                if (fixed_i || !(q2i < 4.0f)) continue;
-                const float4 pvj = a.S.pk_v[j];
-                const float mj = pvj.w;
                 const TabIdxF ix = tab_indexf(a.t, q2i);
-                const float wv = tab_valf(a.t.wf, ix);
-                const float gw = tab_valf(a.t.gwf, ix);
-                const float ggw = tab_valf(a.t.ggwf, ix);
-                const float q = sqrtp(q2i);
-                fw.add(mj * wv);
-                fn.add(wv);
-                const float tg = q * gw + (float)NDIM * wv;
-                fg.add(mj * tg);
-                fgn.add(tg);
-                fgg.add(mj * ((float)(NDIM * (NDIM + 1)) * wv + (float)(2 * (NDIM + 1)) * q * gw + q2i * ggw));
-                if (j != i) {
-                    const float rij = q * hif;
-                    float dvr = (vif[0] - pvj.x) * dxf[0];
-                    if (NDIM >= 2) dvr += (vif[1] - pvj.y) * dxf[1];
-                    if (NDIM >= 3) dvr += (vif[2] - pvj.z) * dxf[2];
-                    fd.add(mj * dvr * gw * __fdividef(1.0f, rij + 1e-30f));
-                }
+                wv = tab_valf(a.t.wf, ix);
+                gw = tab_valf(a.t.gwf, ix);
+                ggw = tab_valf(a.t.ggwf, ix);
             }
+            fw.add(mj * wv);
+            fn.add(wv);
+            const float tg = q * gw + (float)NDIM * wv;
+            fg.add(mj * tg);
+            fgn.add(tg);
+            fgg.add(mj * ((float)(NDIM * (NDIM + 1)) * wv + (float)(2 * (NDIM + 1)) * q * gw + q2i * ggw));
+            if (j != i) {
+                const float rij = q * hif;
+                float dvr = (vif[0] - pvj.x) * dxf[0];
+                if (NDIM >= 2) dvr += (vif[1] - pvj.y) * dxf[1];
+                if (NDIM >= 3) dvr += (vif[2] - pvj.z) * dxf[2];
+                fd.add(mj * dvr * gw * __fdividef(1.0f, rij + 1e-30f));
+            }
+        }
+    };
+    if (PREC == NDSPH_PREC_FP64) {
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = 0; k < ncand; k++) {
+            const unsigned pk = row[k];
+            const int j = (int)(pk >> 5);
+            pair(pk, a.S.xs[j], a.S.itype[j], z4);
+        }
+    } else {
+        // FP32 form: four candidates' loads in flight at once (the pair work
+        // is short, so the loop is bound by load latency otherwise)
+        // rows are 16-byte aligned with a stride of a multiple of 4 entries
+        const bool typed = (o.idust != 0);   // without dust every type pair matches
+        for (int k0 = 0; k0 < ncand; k0 += 4) {
+            const uint4 r4 = *reinterpret_cast<const uint4*>(row + k0);
+            unsigned pk[4] = {r4.x, r4.y, r4.z, r4.w};
+            float4 xj[4], vj[4];
+            int tj[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) if (k0 + u >= ncand) pk[u] = (unsigned)i << 5;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int j = (int)(pk[u] >> 5);
+                xj[u] = a.S.xs[j];
+                tj[u] = typed ? a.S.itype[j] : typei;
+                vj[u] = a.S.pk_v[j];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (k0 + u < ncand) pair(pk[u], xj[u], tj[u], vj[u]);
         }
     }
     if (PREC == NDSPH_PREC_FP32) {
@@ -362,31 +419,54 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
     // ---- Newton-Raphson update, iterate_density.f90:163-278 ----
     const double pm = F.f[PM][i];
     const double hfact = o.hfact;
+    const int its = a.d_its ? *a.d_its : a.its;
     if (rho <= 1.e-6 && rho <= 0.0) {
         raise_err(a.red, NDSPH_E_RHO_NONPOS, a.S.id[i]);
         return;
     }
-    double hb = hi / hfact;
-    double hpow = hb;
-    if (NDIM >= 2) hpow = hpow * hb;
-    if (NDIM >= 3) hpow = hpow * hb;
-    const double rhoi = pm / hpow;
-    const double dhdrhoi = -hi / ((double)NDIM * rho);
     const double dwdhsumi = gradh;
-    double omegai = 1.0 - dhdrhoi * gradh;
-    if (omegai < 1.e-5 && fabs(omegai) == 0.0) omegai = 1.0;
-    gradh = 1.0 / omegai;
-    const double func = rhoi - rho;
-    const double dfdh = omegai / dhdrhoi;
-    const double rn = rho * (double)NDIM;
-    const double d2hdrho2i = hi * (double)(NDIM + 1) / (rn * rn);
+    double rhoi, dhdrhoi, omegai, d2hdrho2i, hnew;
+    if (PREC == NDSPH_PREC_FP64) {
+        // the reference's expressions and association (parity form)
+        double hb = hi / hfact;
+        double hpow = hb;
+        if (NDIM >= 2) hpow = hpow * hb;
+        if (NDIM >= 3) hpow = hpow * hb;
+        rhoi = pm / hpow;
+        dhdrhoi = -hi / ((double)NDIM * rho);
+        omegai = 1.0 - dhdrhoi * gradh;
+        if (omegai < 1.e-5 && fabs(omegai) == 0.0) omegai = 1.0;
+        gradh = 1.0 / omegai;
+        const double func = rhoi - rho;
+        const double dfdh = omegai / dhdrhoi;
+        const double rn = rho * (double)NDIM;
+        d2hdrho2i = hi * (double)(NDIM + 1) / (rn * rn);
+        hnew = hi - func / dfdh;
+    } else {
+        // FP32 form: the same FP64 residual and Newton step with two FP64
+        // divisions instead of six (an FP64 division costs ~16 FP32 issue
+        // slots per operation on this part): 1/h comes from h1, 1/rho once,
+        // f/f' = f dh/drho / omega
+        const double rho1 = 1.0 / rho;
+        const double hb1 = hfact * hi1;
+        double hpow1 = hb1;
+        if (NDIM >= 2) hpow1 = hpow1 * hb1;
+        if (NDIM >= 3) hpow1 = hpow1 * hb1;
+        rhoi = pm * hpow1;
+        dhdrhoi = -hi * rho1 * (1.0 / (double)NDIM);
+        omegai = 1.0 - dhdrhoi * gradh;
+        if (omegai < 1.e-5 && fabs(omegai) == 0.0) omegai = 1.0;
+        gradh = 1.0 / omegai;
+        const double func = rhoi - rho;
+        d2hdrho2i = hi * (double)(NDIM + 1) * (rho1 * rho1) * (1.0 / (double)(NDIM * NDIM));
+        hnew = hi - func * dhdrhoi * gradh;
+    }
     gradgradh = rho * (d2hdrho2i * dwdhsumi + dhdrhoi * dhdrhoi * gradgradh);
-    double hnew = hi - func / dfdh;
     if (hnew > 1.2 * hi) hnew = 1.2 * hi;
     else if (hnew < 0.8 * hi) hnew = 0.8 * hi;
     if (hnew <= 0.0 || gradh <= 2.2250738585072014e-308) {
         hnew = hfact * pow(pm / rho, 1.0 / (double)NDIM);
-    } else if (a.its > 100) {
+    } else if (its > 100) {
         hnew = hfact * pow(pm / rho, 1.0 / (double)NDIM);
     }
     bool relink = false;
@@ -395,12 +475,24 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
         relink = true;
     }
     const double hin = F.f[HDEN0][i];
-    const bool converged = (fabs((hnew - hi) / hin) < o.tolh && omegai > 0.0) || o.maxdensits == 0;
+    const bool converged =
+        ((PREC == NDSPH_PREC_FP64 ? fabs((hnew - hi) / hin) < o.tolh : fabs(hnew - hi) < o.tolh * hin) &&
+         omegai > 0.0) ||
+        o.maxdensits == 0;
     double* hdst = FULL ? F.f[HNEXT] : F.f[HH];
     if (!converged) {
         const int k = atomicAdd(a.ncalc_next, 1);
         a.S.active_next[k] = i;
-        if (a.its <= o.maxdensits) hdst[i] = hnew;
+        if (its <= o.maxdensits) {
+            hdst[i] = hnew;
+            if (!FULL) {
+                // a partial pass reads only its own h: keep 1/h and the list's h current
+                a.S.h1[i] = 1.0 / hnew;
+                float4 xw = a.S.xs[i];
+                xw.w = (float)hnew;
+                a.S.xs[i] = xw;
+            }
+        }
         if (hnew > bitsd(a.red->hmax_ghost)) relink = true;
         if ((float)hnew > a.S.hb[i] * a.nl_skin) a.red->nl_stale = 1;
     } else {
@@ -419,7 +511,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
 void launch_density(const SweepArgs& a, bool full, cudaStream_t st)
 {
     const int bs = 128;
-    const int nthreads = full ? a.n : a.nlist;
+    const int nthreads = full ? a.n : (a.d_nlist ? a.n : a.nlist);
     if (nthreads <= 0) return;
     const int nb = nblk(nthreads, bs);
 #define DLAUNCH(ND, FU, PR) NDSPH_COUNT_LAUNCH, k_density<ND, FU, PR><<<nb, bs, 0, st>>>(a)
@@ -592,7 +684,8 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
                 q2i = r2f * (hi1 * hi1);
                 q2j = r2f * (hj1 * hj1);
             }
-            const int typej = a.S.itype[j];
+            // without dust every type pair matches and no drag applies
+            const int typej = (PREC == NDSPH_PREC_FP64 || o.idust != 0) ? a.S.itype[j] : typei;
             PData<R> pj;
             load_p<PREC>(a, j, pj);
             const R mj = pj.m;
@@ -609,8 +702,21 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
                     gwi = tab_val(a.t.gw, tab_index(a.t, q2i));
                     gwj = tab_val(a.t.gw, tab_index(a.t, q2j));
                 } else {
-                    gwi = tab_valf(a.t.gwf, tab_indexf(a.t, q2i));
-                    gwj = tab_valf(a.t.gwf, tab_indexf(a.t, q2j));
+                    const float c = a.t.cnormf;
+                    if (q2i >= KERN_Q2_DIRECT) {
+                        const float qi = rij * hi1;
+                        const float t = fmaxf(2.0f - qi, 0.0f), u = fmaxf(1.0f - qi, 0.0f);
+                        gwi = c * (3.0f * u * u - 0.75f * t * t);
+                    } else {
+                        gwi = tab_valf(a.t.gwf, tab_indexf(a.t, q2i));
+                    }
+                    if (q2j >= KERN_Q2_DIRECT) {
+                        const float qj = rij * hj1;
+                        const float t = fmaxf(2.0f - qj, 0.0f), u = fmaxf(1.0f - qj, 0.0f);
+                        gwj = c * (3.0f * u * u - 0.75f * t * t);
+                    } else {
+                        gwj = tab_valf(a.t.gwf, tab_indexf(a.t, q2j));
+                    }
                 }
                 const R grkerni = gwi * hfacgrki * gradhi;
                 const R grkernj = gwj * hfacgrkj * pj.gradh;
@@ -956,36 +1062,81 @@ void launch_rates(const SweepArgs& a, cudaStream_t st)
 // The sweeps then test only these; a list is rebuilt when some h grows by
 // more than `skin` (NR epilogue flag) and after every link.
 // ===========================================================================
+// candidates of slot i in the slot range [jb, je); the x offset of the cell
+// of j steps at b1 and b2 (a merged run of three x-adjacent cells) or stays
+// at d0 (b1 = b2 = je); stencil index so0 + 0/1/2 accordingly.  Loads are
+// issued four at a time so that their latencies overlap.
+template <int NDIM>
+__device__ __forceinline__ void nl_scan_range(const SweepArgs& a, const float4& xsi, float hi, float sk,
+                                              float abs_tol, int jb, int je, int b1, int b2, int d0,
+                                              float oy, float oz, int so0, unsigned* row, int& cnt)
+{
+    const Grid& g = a.g;
+    for (int j0 = jb; j0 < je; j0 += 4) {
+        float4 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) q[u] = (j0 + u < je) ? a.S.xs[j0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int j = j0 + u;
+            if (j >= je) break;
+            const int dx = (j < b1) ? d0 : ((j < b2) ? d0 + 1 : d0 + 2);
+            float r2 = (xsi.x - q[u].x) - (float)dx * g.csf[0];
+            r2 = r2 * r2;
+            if (NDIM >= 2) { const float t = (xsi.y - q[u].y) - oy; r2 += t * t; }
+            if (NDIM >= 3) { const float t = (xsi.z - q[u].z) - oz; r2 += t * t; }
+            const float rc = sk * fmaxf(hi, q[u].w) + abs_tol;
+            if (r2 > rc * rc) continue;
+            if (cnt < a.nl_stride) row[cnt] = ((unsigned)j << 5) | (unsigned)(so0 + dx - d0);
+            cnt++;
+        }
+    }
+}
+
 template <int NDIM>
 __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
+    if (a.gate && *a.gate == 0) return;
     const Grid& g = a.g;
     const float4 xsi = a.S.xs[i];
     const float hi = xsi.w;
     const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
     const float sk = 2.0f * a.nl_skin * 1.0002f;
     Stencil<NDIM> stn(a.S.cell[i], g);
-    constexpr int NST = (NDIM == 1) ? 3 : (NDIM == 2 ? 9 : 27);
+    constexpr int NYZ = (NDIM == 1) ? 1 : (NDIM == 2 ? 3 : 9);
+    unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
     int cnt = 0;
-    for (int so = 0; so < NST; so++) {
-        int cid, d[3], w[3];
-        if (!stn.cell_at(so, g, a.o, cid, d, w)) continue;
-        const int jb = a.cell_start[cid], je = a.cell_start[cid + 1];
-        for (int j = jb; j < je; j++) {
-            const float4 xsj = a.S.xs[j];
-            float dxf[3];
-            const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
-            const float rc = sk * fmaxf(hi, xsj.w) + abs_tol;
-            if (r2f > rc * rc) continue;
-            if (cnt < a.nl_stride) a.S.nl[(size_t)i * a.nl_stride + cnt] = ((unsigned)j << 5) | (unsigned)so;
-            cnt++;
+    for (int yz = 0; yz < NYZ; yz++) {
+        // the three x-neighbours at this (dy, dz): one slot range when they are
+        // consecutive cells (no x wrap), else cell by cell
+        int cid[3], dd[3][3], ww[3][3];
+        bool ok[3];
+#pragma unroll
+        for (int ox = 0; ox < 3; ox++) ok[ox] = stn.cell_at(3 * yz + ox, g, a.o, cid[ox], dd[ox], ww[ox]);
+        const int so0 = 3 * yz;
+        const float oy = (NDIM >= 2) ? (float)(yz % 3 - 1) * g.csf[1] : 0.f;
+        const float oz = (NDIM >= 3) ? (float)(yz / 3 - 1) * g.csf[2] : 0.f;
+        if (ok[0] && ok[1] && ok[2] && cid[1] == cid[0] + 1 && cid[2] == cid[0] + 2) {
+            const int jb = a.cell_start[cid[0]];
+            const int b1 = a.cell_start[cid[1]];
+            const int b2 = a.cell_start[cid[2]];
+            const int je = a.cell_start[cid[2] + 1];
+            nl_scan_range<NDIM>(a, xsi, hi, sk, abs_tol, jb, je, b1, b2, -1, oy, oz, so0, row, cnt);
+        } else {
+#pragma unroll
+            for (int ox = 0; ox < 3; ox++) {
+                if (!ok[ox]) continue;
+                const int jb = a.cell_start[cid[ox]], je = a.cell_start[cid[ox] + 1];
+                nl_scan_range<NDIM>(a, xsi, hi, sk, abs_tol, jb, je, je, je, ox - 1, oy, oz, so0 + ox, row,
+                                    cnt);
+            }
         }
     }
     a.S.nl_cnt[i] = cnt < a.nl_stride ? cnt : a.nl_stride;
     a.S.hb[i] = hi;
-    if (cnt > a.nl_stride) a.red->nl_overflow = 1;
+    if (cnt > a.nl_stride) { a.red->nl_overflow = 1; if (a.graph) a.red->gfail |= 2; }
     atomicMax(&a.red->nl_maxcnt, cnt);
 }
 

@@ -185,6 +185,9 @@ class GpuSPH:
                                            t.ctypes.data_as(C.POINTER(C.c_double))))
         return dt, t
 
+    def batch_set_graph(self, mode: int):
+        self._check(lib().ndsph_batch_set_graph(self._h, int(mode)))
+
     def batch_download(self):
         self._check(lib().ndsph_batch_download(self._h, C.byref(self._p)))
 

@@ -67,3 +67,50 @@ def test_sweep_from_infiles_matches_oracle(gpulib, tmp_path):
                                    orc.state, ["x", "vel", "hh", "en", "rho"], 1e-9)
         assert not bad, (k, errs)
         assert abs(t - orc.dts()["time"]) <= 1e-10 * orc.dts()["time"]
+
+
+def _batch_run(o, p, sim, nsim, mode, nsteps):
+    from ndspmhd_gb300.gpu import GpuSPH
+    g = GpuSPH(o, configs.full_state(p, 1))
+    g.batch_upload(sim, nsim, initialise=True)
+    g.batch_set_graph(mode)
+    dt, t = g.batch_step(nsteps)
+    g.batch_download()
+    out = ({f: v.copy() for f, v in g.state.items()}, dt, t, g.timing())
+    g.close()
+    return out
+
+
+FIELDS = ["x", "vel", "hh", "en", "Bevol", "rho", "force"]
+
+
+def test_graph_step_matches_eager_step(gpulib):
+    """Captured steps (one CUDA graph launch each, Newton-Raphson passes under
+    a device-driven WHILE node) against the eager host loop on the same tubes,
+    FP64 form.  The captured link uses wider cells, so only the order of each
+    particle's neighbour sum differs: 1e-11 after 12 steps."""
+    o, p, sim, counts = configs.brio_wu_batch(ntubes=24, nmin=200, nmax=900, seed=9)
+    eager = _batch_run(o, p, sim, len(counts), 0, 12)
+    graph = _batch_run(o, p, sim, len(counts), 1, 12)
+    assert eager[3]["graph_steps"] == 0
+    assert graph[3]["graph_steps"] >= 12
+    assert graph[3]["graph_redos"] <= graph[3]["graph_steps"]
+    errs, bad = compare_fields(graph[0], eager[0], FIELDS, 1e-11)
+    assert not bad, errs
+    np.testing.assert_allclose(graph[1], eager[1], rtol=1e-11)
+    np.testing.assert_allclose(graph[2], eager[2], rtol=1e-11)
+
+
+def test_graph_step_fp32_error_unchanged(gpulib):
+    """FP32 form: the captured step's cells differ from the eager step's, so
+    the FP32 cell-relative coordinates round differently; its error against
+    the FP64 eager run must stay at the eager FP32 run's level (within 2x)."""
+    o, p, sim, counts = configs.brio_wu_batch(ntubes=24, nmin=200, nmax=900, seed=9)
+    ref = _batch_run(o, p, sim, len(counts), 0, 3)
+    o32 = dict(o, precision=1)
+    eager = _batch_run(o32, p, sim, len(counts), 0, 3)
+    graph = _batch_run(o32, p, sim, len(counts), 1, 3)
+    e_eager, _ = compare_fields(eager[0], ref[0], FIELDS, 1.0)
+    e_graph, _ = compare_fields(graph[0], ref[0], FIELDS, 1.0)
+    for f in FIELDS:
+        assert e_graph[f] <= 2.0 * e_eager[f] + 1e-7, (f, e_graph, e_eager)
