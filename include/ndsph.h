@@ -227,6 +227,12 @@ NDSPH_API int ndsph_batch_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32
                                  int32_t nsim, int32_t initialise);
 NDSPH_API int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, double* time_out);
 NDSPH_API int ndsph_batch_download(ndsph_ctx* ctx, ndsph_particles* p);
+/* how the host-buffer entry points move the caller's arrays: 1 (default) the
+ * layout kernels read and write them in place when the device can address
+ * them (pinned memory, or pageable memory on systems where the device reads
+ * it, as Grace over NVLink-C2C does), else through staging copies; 0 always
+ * staging copies.  The results are the same either way.                      */
+NDSPH_API int ndsph_set_host_access(ndsph_ctx* ctx, int32_t mode);
 /* how ndsph_batch_step runs a step: 1 (default) one captured CUDA graph per
  * step -- link, neighbour rows, the Newton-Raphson passes under a device-driven
  * WHILE node, EOS, rates, leapfrog and the per-simulation dt in one launch, with

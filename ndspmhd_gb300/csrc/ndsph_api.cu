@@ -56,6 +56,18 @@ struct ndsph_ctx {
     // host staging
     double* d_stage = nullptr;   // n*3 doubles
     int* d_istage = nullptr;
+    // host arrays the kernels read and write in place (no staging copy):
+    // 1 when possible (pinned memory, or any memory where the device reads
+    // pageable host memory), 0 always stage through device buffers
+    int host_access = 0;
+    bool pageable_access = false;
+    // copy stream: staging copies overlap the layout kernels (two staging
+    // buffers), and outputs final before the rates sweep go back under it
+    cudaStream_t st_cp = nullptr;
+    cudaEvent_t ev_cp[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr}, ev_dl = nullptr;
+    int stage_k = 0;
+    ndsph_particles* dl_early = nullptr;   // ndsph_step: where the early outputs go
+    bool dl_density_done = false, dl_prim_done = false;
     double* d_arena = nullptr;   // download staging: every output field side by side
     size_t arena_cap = 0;        // doubles
     size_t arena_used = 0;
@@ -117,6 +129,8 @@ struct ndsph_ctx {
 static thread_local std::string g_err;
 static int build_nlist(ndsph_ctx* ctx);
 static void link_sort_gather(ndsph_ctx* ctx, const int* d_fields, int nfields, cudaStream_t st);
+static int download_density_group(ndsph_ctx* ctx, ndsph_particles* p);
+static int download_prim_group(ndsph_ctx* ctx, ndsph_particles* p);
 #define CK_VOID(call) do { (void)(call); } while (0)
 
 #define CK(call)                                                                          \
@@ -317,7 +331,7 @@ static int ensure_capacity(ndsph_ctx* ctx, int n)
     CK(cudaMalloc(&ctx->S.active, ib)); CK(cudaMalloc(&ctx->S.active_next, ib)); CK(cudaMalloc(&ctx->S.flag, ib));
     CK(cudaMalloc(&ctx->itype2, ib)); CK(cudaMalloc(&ctx->id2, ib)); CK(cudaMalloc(&ctx->ireal2, ib));
     CK(cudaMalloc(&ctx->srt.key, ib)); CK(cudaMalloc(&ctx->srt.slot, ib)); CK(cudaMalloc(&ctx->srt.perm, ib));
-    CK(cudaMalloc(&ctx->d_stage, sizeof(double) * 3 * (size_t)cap));
+    CK(cudaMalloc(&ctx->d_stage, sizeof(double) * 6 * (size_t)cap));   // two staging buffers
     CK(cudaMalloc(&ctx->S.pk_v, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_t, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_b, sizeof(float4) * (size_t)cap));
@@ -370,6 +384,22 @@ extern "C" int ndsph_init(ndsph_ctx** out, const ndsph_opts* opts, int32_t nmax)
     memset(&ctx->last_dt, 0, sizeof(ctx->last_dt));
     cudaError_t e = cudaGetDevice(&ctx->device);
     if (e != cudaSuccess) { g_err = cudaGetErrorString(e); delete ctx; return NDSPH_E_CUDA; }
+    {
+        int pa = 0;
+        if (cudaDeviceGetAttribute(&pa, cudaDevAttrPageableMemoryAccess, ctx->device) == cudaSuccess)
+            ctx->pageable_access = pa != 0;
+        cudaGetLastError();
+    }
+    if (cudaStreamCreateWithFlags(&ctx->st_cp, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_cp[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_cp[1], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_used[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_used[1], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_dl, cudaEventDisableTiming) != cudaSuccess) {
+        g_err = "stream/event creation failed";
+        delete ctx;
+        return NDSPH_E_CUDA;
+    }
     e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) { g_err = cudaGetErrorString(e); delete ctx; return NDSPH_E_CUDA; }
     for (int k = 0; k < 16; k++) cudaEventCreate(&ctx->ev[k]);
@@ -449,6 +479,9 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
     if (ctx->h_sim_out) cudaFreeHost(ctx->h_sim_out);
     for (int k = 0; k < 16; k++) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     for (int k = 0; k < 2; k++) if (ctx->gexec[k]) cudaGraphExecDestroy(ctx->gexec[k]);
+    if (ctx->st_cp) { cudaStreamSynchronize(ctx->st_cp); cudaStreamDestroy(ctx->st_cp); }
+    for (cudaEvent_t ev : {ctx->ev_cp[0], ctx->ev_cp[1], ctx->ev_used[0], ctx->ev_used[1], ctx->ev_dl})
+        if (ev) cudaEventDestroy(ev);
     if (ctx->d_live) cudaFree(ctx->d_live);
     if (ctx->st2) cudaStreamDestroy(ctx->st2);
     if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -473,11 +506,43 @@ static int sync_red(ndsph_ctx* ctx)
     return 0;
 }
 
+// Device address of a host array the kernels may access in place: pinned
+// memory (cudaHostAlloc / cudaHostRegister) is mapped into the device's
+// address space, and where the device reads pageable memory (Grace with
+// NVLink-C2C and address translation) any host pointer is; the layout
+// kernels then read and write the caller's arrays directly over the
+// coherent link.  nullptr: stage through a device buffer.
+static const void* host_view(ndsph_ctx* ctx, const void* host)
+{
+    if (!ctx->host_access || !host) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) == cudaSuccess) {
+        if (at.type == cudaMemoryTypeHost && at.devicePointer) return at.devicePointer;
+        if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return host;
+    } else {
+        cudaGetLastError();
+    }
+    return ctx->pageable_access ? host : nullptr;
+}
+
 static int upload_aos(ndsph_ctx* ctx, const double* host, int f0, int ncomp, int stride, int n)
 {
     if (!host) return 0;
-    CK(cudaMemcpyAsync(ctx->d_stage, host, sizeof(double) * (size_t)stride * n, cudaMemcpyHostToDevice, ctx->st));
-    launch_aos_to_slab(ctx->F, f0, ncomp, ctx->d_stage, stride, nullptr, n, ctx->st);
+    const double* src = (const double*)host_view(ctx, host);
+    if (src) {
+        launch_aos_to_slab(ctx->F, f0, ncomp, src, stride, nullptr, n, ctx->st);
+        return 0;
+    }
+    // copy into one staging buffer on the copy stream while the layout kernel
+    // of the previous array reads the other one
+    const int b = (ctx->stage_k++) & 1;
+    double* buf = ctx->d_stage + (size_t)b * 3 * ctx->cap;
+    CK(cudaStreamWaitEvent(ctx->st_cp, ctx->ev_used[b], 0));
+    CK(cudaMemcpyAsync(buf, host, sizeof(double) * (size_t)stride * n, cudaMemcpyHostToDevice, ctx->st_cp));
+    CK(cudaEventRecord(ctx->ev_cp[b], ctx->st_cp));
+    CK(cudaStreamWaitEvent(ctx->st, ctx->ev_cp[b], 0));
+    launch_aos_to_slab(ctx->F, f0, ncomp, buf, stride, nullptr, n, ctx->st);
+    CK(cudaEventRecord(ctx->ev_used[b], ctx->st));
     return 0;
 }
 // downloads are staged in an arena and copied out asynchronously; the
@@ -485,10 +550,15 @@ static int upload_aos(ndsph_ctx* ctx, const double* host, int f0, int ncomp, int
 static int download_aos(ndsph_ctx* ctx, double* host, int f0, int ncomp, int stride, int n)
 {
     if (!host) return 0;
+    if (double* direct = (double*)host_view(ctx, host)) {
+        launch_slab_to_aos(direct, stride, ctx->F, f0, ncomp, ctx->S.id, n, ctx->st);
+        return 0;
+    }
     const size_t need = (size_t)stride * n;
     if (ctx->arena_used + need > ctx->arena_cap) {
         // grow: finish pending copies first, then reallocate
         CK(cudaStreamSynchronize(ctx->st));
+        CK(cudaStreamSynchronize(ctx->st_cp));
         if (ctx->d_arena) CK(cudaFree(ctx->d_arena));
         size_t cap = std::max(ctx->arena_cap * 2, (size_t)ctx->cap * 80);
         CK(cudaMalloc(&ctx->d_arena, sizeof(double) * cap));
@@ -498,21 +568,29 @@ static int download_aos(ndsph_ctx* ctx, double* host, int f0, int ncomp, int str
     double* dst = ctx->d_arena + ctx->arena_used;
     ctx->arena_used += need;
     launch_slab_to_aos(dst, stride, ctx->F, f0, ncomp, ctx->S.id, n, ctx->st);
-    CK(cudaMemcpyAsync(host, dst, sizeof(double) * need, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaEventRecord(ctx->ev_dl, ctx->st));
+    CK(cudaStreamWaitEvent(ctx->st_cp, ctx->ev_dl, 0));
+    CK(cudaMemcpyAsync(host, dst, sizeof(double) * need, cudaMemcpyDeviceToHost, ctx->st_cp));
     return 0;
 }
 static int download_end(ndsph_ctx* ctx)
 {
     CK(cudaStreamSynchronize(ctx->st));
+    CK(cudaStreamSynchronize(ctx->st_cp));
     ctx->arena_used = 0;
     return 0;
 }
 static int download_int(ndsph_ctx* ctx, int* host, const int* dsrc, int n, bool is_index)
 {
     if (!host) return download_end(ctx);
-    launch_slab_to_int(ctx->d_istage, dsrc, ctx->S.id, n, ctx->st);
-    CK(cudaMemcpyAsync(host, ctx->d_istage, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, ctx->st));
+    if (int* direct = (int*)host_view(ctx, host)) {
+        launch_slab_to_int(direct, dsrc, ctx->S.id, n, ctx->st);
+    } else {
+        launch_slab_to_int(ctx->d_istage, dsrc, ctx->S.id, n, ctx->st);
+        CK(cudaMemcpyAsync(host, ctx->d_istage, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, ctx->st));
+    }
     CK(cudaStreamSynchronize(ctx->st));
+    CK(cudaStreamSynchronize(ctx->st_cp));
     ctx->arena_used = 0;
     if (is_index) for (int i = 0; i < n; i++) host[i] = host[i] + 1;
     return 0;
@@ -568,14 +646,21 @@ static int upload_inputs(ndsph_ctx* ctx, const ndsph_particles* p, int n, bool w
         rc |= upload_aos(ctx, p->Bfield, BF0, 3, 3, n);
     }
     if (rc) return rc;
-    CK(cudaMemcpyAsync(ctx->S.itype, p->itype, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+    if (const int* v = (const int*)host_view(ctx, p->itype))
+        launch_int_shift(ctx->S.itype, v, n, 0, ctx->st);
+    else
+        CK(cudaMemcpyAsync(ctx->S.itype, p->itype, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
     launch_iota(ctx->S.id, n, ctx->st);
     launch_iota(ctx->S.pos_of_id, n, ctx->st);
     // ireal: 1-based host index -> 0-based id (-1 none)
-    std::vector<int> ir(n, -1);
-    if (p->ireal)
-        for (int i = 0; i < n; i++) ir[i] = p->ireal[i] - 1;
-    CK(cudaMemcpyAsync(ctx->S.ireal, ir.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+    if (!p->ireal) {
+        CK(cudaMemsetAsync(ctx->S.ireal, 0xff, sizeof(int) * (size_t)n, ctx->st));
+    } else if (const int* v = (const int*)host_view(ctx, p->ireal)) {
+        launch_int_shift(ctx->S.ireal, v, n, -1, ctx->st);
+    } else {
+        CK(cudaMemcpyAsync(ctx->d_istage, p->ireal, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+        launch_int_shift(ctx->S.ireal, ctx->d_istage, n, -1, ctx->st);
+    }
     CK(cudaStreamSynchronize(ctx->st));
     ctx->linked = false;
     return 0;
@@ -909,9 +994,19 @@ static int do_derivs(ndsph_ctx* ctx, const int* fields, int nfields)
     int its = 0, nct = 0, nrl = 0;
     rc = do_iterate_density(ctx, &its, &nct, &nrl);
     if (rc) return rc;
+    if (ctx->dl_early) {
+        rc = download_density_group(ctx, ctx->dl_early);
+        if (rc) return rc;
+        ctx->dl_density_done = true;
+    }
     tmark(ctx, 6);
     rc = do_cons2prim(ctx);
     if (rc) return rc;
+    if (ctx->dl_early) {
+        rc = download_prim_group(ctx, ctx->dl_early);
+        if (rc) return rc;
+        ctx->dl_prim_done = true;
+    }
     tmark(ctx, 7);
     rc = do_rates(ctx);
     if (rc) return rc;
@@ -925,6 +1020,44 @@ static int do_derivs(ndsph_ctx* ctx, const int* fields, int nfields)
     return 0;
 }
 
+// outputs final once the Newton-Raphson iteration ends (rates and the
+// corrector leave them alone when no particle is fixed) and once the EOS ran
+static int download_density_group(ndsph_ctx* ctx, ndsph_particles* p)
+{
+    const int n = ctx->n;
+    int rc = 0;
+    rc |= download_aos(ctx, p->rho, RHO, 1, 1, n);
+    rc |= download_aos(ctx, p->rhoalt, RHOALT, 1, 1, n);
+    rc |= download_aos(ctx, p->gradh, GRADH, 1, 1, n);
+    rc |= download_aos(ctx, p->gradhn, GRADHN, 1, 1, n);
+    rc |= download_aos(ctx, p->gradgradh, GRADGRADH, 1, 1, n);
+    if (ctx->dl_early && p->numneigh) {
+        int* dst = (int*)(ctx->d_arena + ctx->arena_used);   // int staging in the arena
+        const size_t need = ((size_t)n * sizeof(int) + sizeof(double) - 1) / sizeof(double);
+        if (ctx->arena_used + need <= ctx->arena_cap) {
+            ctx->arena_used += need;
+            launch_slab_to_int(dst, ctx->S.numneigh, ctx->S.id, n, ctx->st);
+            CK(cudaEventRecord(ctx->ev_dl, ctx->st));
+            CK(cudaStreamWaitEvent(ctx->st_cp, ctx->ev_dl, 0));
+            CK(cudaMemcpyAsync(p->numneigh, dst, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, ctx->st_cp));
+        } else {
+            rc |= download_int(ctx, p->numneigh, ctx->S.numneigh, n, false);
+        }
+    }
+    return rc;
+}
+static int download_prim_group(ndsph_ctx* ctx, ndsph_particles* p)
+{
+    const int n = ctx->n;
+    int rc = 0;
+    rc |= download_aos(ctx, p->dens, DENS, 1, 1, n);
+    rc |= download_aos(ctx, p->uu, UU, 1, 1, n);
+    rc |= download_aos(ctx, p->pr, PR, 1, 1, n);
+    rc |= download_aos(ctx, p->spsound, CS, 1, 1, n);
+    rc |= download_aos(ctx, p->Bfield, BF0, 3, 3, n);
+    return rc;
+}
+
 static int download_all(ndsph_ctx* ctx, ndsph_particles* p)
 {
     const int n = ctx->n, nd = ctx->o.ndim;
@@ -934,20 +1067,12 @@ static int download_all(ndsph_ctx* ctx, ndsph_particles* p)
     rc |= download_aos(ctx, p->Bevol, BE0, 3, 3, n);
     rc |= download_aos(ctx, p->en, EN, 1, 1, n);
     rc |= download_aos(ctx, p->hh, HH, 1, 1, n);
-    rc |= download_aos(ctx, p->pmass, PM, 1, 1, n);
+    if (!ctx->dl_early) rc |= download_aos(ctx, p->pmass, PM, 1, 1, n);   // ndsph_step: unchanged, not copied
     rc |= download_aos(ctx, p->alpha, AL0, 3, 3, n);
-    rc |= download_aos(ctx, p->rho, RHO, 1, 1, n);
-    rc |= download_aos(ctx, p->rhoalt, RHOALT, 1, 1, n);
     rc |= download_aos(ctx, p->drhodt, DRHODT, 1, 1, n);
     rc |= download_aos(ctx, p->dhdt, DHDT, 1, 1, n);
-    rc |= download_aos(ctx, p->gradh, GRADH, 1, 1, n);
-    rc |= download_aos(ctx, p->gradhn, GRADHN, 1, 1, n);
-    rc |= download_aos(ctx, p->gradgradh, GRADGRADH, 1, 1, n);
-    rc |= download_aos(ctx, p->dens, DENS, 1, 1, n);
-    rc |= download_aos(ctx, p->uu, UU, 1, 1, n);
-    rc |= download_aos(ctx, p->pr, PR, 1, 1, n);
-    rc |= download_aos(ctx, p->spsound, CS, 1, 1, n);
-    rc |= download_aos(ctx, p->Bfield, BF0, 3, 3, n);
+    if (!ctx->dl_density_done) rc |= download_density_group(ctx, p);
+    if (!ctx->dl_prim_done) rc |= download_prim_group(ctx, p);
     rc |= download_aos(ctx, p->force, F0, 3, 3, n);
     rc |= download_aos(ctx, p->dBevoldt, DB0, 3, 3, n);
     rc |= download_aos(ctx, p->dudt, DUDT, 1, 1, n);
@@ -958,6 +1083,7 @@ static int download_all(ndsph_ctx* ctx, ndsph_particles* p)
     rc |= download_aos(ctx, p->del2u, DEL2U, 1, 1, n);
     rc |= download_aos(ctx, p->graddivv, GDV0, 3, 3, n);
     if (rc) return rc;
+    if (ctx->dl_early) return download_end(ctx);   // numneigh went with the density group
     rc = download_int(ctx, p->numneigh, ctx->S.numneigh, n, false);
     return rc;
 }
@@ -1309,8 +1435,12 @@ static int dev_upload_impl(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npa
     rc |= upload_aos(ctx, p->divB, DIVB, 1, 1, n);
     rc |= upload_aos(ctx, p->curlB, CB0, 3, 3, n);
     if (rc) return rc;
-    CK(cudaMemcpyAsync(ctx->d_istage, p->numneigh, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
-    launch_int_to_slab(ctx->S.numneigh, ctx->d_istage, nullptr, n, ctx->st);
+    if (const int* v = (const int*)host_view(ctx, p->numneigh)) {
+        launch_int_to_slab(ctx->S.numneigh, v, nullptr, n, ctx->st);
+    } else {
+        CK(cudaMemcpyAsync(ctx->d_istage, p->numneigh, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+        launch_int_to_slab(ctx->S.numneigh, ctx->d_istage, nullptr, n, ctx->st);
+    }
     if (link) rc = link_all(ctx, false);
     CK(cudaStreamSynchronize(ctx->st));
     return rc;
@@ -1388,18 +1518,69 @@ extern "C" int ndsph_dev_derivs(ndsph_ctx* ctx, ndsph_dt* dts)
     return rc;
 }
 
+// inputs of one leapfrog step: the state, the previous rates the predictor
+// reads (force, dBevol/dt, de/dt, dalpha/dt, dh/dt) and rho.  Every other
+// array the step returns is recomputed for every particle -- except with
+// fixed particles (whose gradgradh and rates the reference carries through)
+// or maxdensits = 0 (no density pass), where everything is uploaded.
+static int step_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
+{
+    if (ctx->o.has_fixed || ctx->o.maxdensits < 1) return dev_upload_impl(ctx, p, npart, false);
+    int rc = ensure_capacity(ctx, npart);
+    if (rc) return rc;
+    ctx->n = npart;
+    const int n = npart, nd = ctx->o.ndim;
+    rc |= upload_aos(ctx, p->x, X0, nd, nd, n);
+    rc |= upload_aos(ctx, p->vel, V0, 3, 3, n);
+    rc |= upload_aos(ctx, p->Bevol, BE0, 3, 3, n);
+    rc |= upload_aos(ctx, p->en, EN, 1, 1, n);
+    rc |= upload_aos(ctx, p->hh, HH, 1, 1, n);
+    rc |= upload_aos(ctx, p->pmass, PM, 1, 1, n);
+    rc |= upload_aos(ctx, p->alpha, AL0, 3, 3, n);
+    rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n);
+    rc |= upload_aos(ctx, p->dhdt, DHDT, 1, 1, n);
+    rc |= upload_aos(ctx, p->force, F0, 3, 3, n);
+    rc |= upload_aos(ctx, p->dBevoldt, DB0, 3, 3, n);
+    rc |= upload_aos(ctx, p->dendt, DENDT, 1, 1, n);
+    rc |= upload_aos(ctx, p->daldt, DAL0, 3, 3, n);
+    if (rc) return rc;
+    if (const int* v = (const int*)host_view(ctx, p->itype))
+        launch_int_shift(ctx->S.itype, v, n, 0, ctx->st);
+    else
+        CK(cudaMemcpyAsync(ctx->S.itype, p->itype, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+    launch_iota(ctx->S.id, n, ctx->st);
+    launch_iota(ctx->S.pos_of_id, n, ctx->st);
+    CK(cudaMemsetAsync(ctx->S.ireal, 0xff, sizeof(int) * (size_t)n, ctx->st));   // no fixed particles
+    ctx->linked = false;
+    return 0;
+}
+
 extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts)
 {
     GUARD_CTX(); GUARD_N();
     // the predictor is per particle, so the state need not be cell-sorted
     // before the step: derivs links after the predictor
     const long long l0 = ndsph_launch_counter().load();
-    int rc = dev_upload_impl(ctx, p, npart, false);
+    int rc = step_upload(ctx, p, npart);
     if (rc) return rc;
     if (dts) { ctx->dt = dts->dt; ctx->time = dts->time; ctx->nsteps = dts->nsteps; }
+    // without fixed particles the density outputs and the primitives are
+    // final before the rates sweep: copy them back while it runs
+    const bool early = !ctx->o.has_fixed && !ctx->opts.learned_h;
+    ctx->dl_early = early ? p : nullptr;
+    ctx->dl_density_done = ctx->dl_prim_done = false;
+    ctx->arena_used = 0;
     rc = dev_step_once(ctx);
-    if (rc) return rc;
+    if (rc) {
+        cudaStreamSynchronize(ctx->st_cp);
+        ctx->dl_early = nullptr;
+        ctx->dl_density_done = ctx->dl_prim_done = false;
+        return rc;
+    }
+    ctx->dl_early = p;   // also: pmass is not copied back (the step never writes it)
     rc = download_all(ctx, p);
+    ctx->dl_early = nullptr;
+    ctx->dl_density_done = ctx->dl_prim_done = false;
     ctx->timing.launches = (int32_t)(ndsph_launch_counter().load() - l0);
     fill_dt(ctx, dts);
     return rc;
@@ -1801,6 +1982,15 @@ extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, 
         if (dt_out) dt_out[s2] = ctx->h_sim_out[s2 * 4 + 2];
         if (time_out) time_out[s2] = ctx->h_sim_out[s2 * 4 + 3];
     }
+    return 0;
+}
+
+extern "C" int ndsph_set_host_access(ndsph_ctx* ctx, int32_t mode)
+{
+    GUARD_CTX();
+    if (mode != 0 && mode != 1) { ctx->err = "host access mode must be 0 or 1"; return NDSPH_E_ARG; }
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->host_access = mode;
     return 0;
 }
 

@@ -346,6 +346,15 @@ __global__ void k_slab_to_int(int* dst, const int* src, const int* id, int n)
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) dst[id ? id[k] : k] = src[k];
 }
+__global__ void k_int_shift(int* dst, const int* src, int n, int add)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i] + add;
+}
+void launch_int_shift(int* dst, const int* src, int n, int add, cudaStream_t st)
+{
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_int_shift<<<nblk(n, 256), 256, 0, st>>>(dst, src, n, add);
+}
 void launch_slab_to_int(int* dst, const int* src, const int* id, int n, cudaStream_t st)
 {
     if (n > 0) NDSPH_COUNT_LAUNCH, k_slab_to_int<<<nblk(n, 256), 256, 0, st>>>(dst, src, id, n);

@@ -94,6 +94,7 @@ void launch_slab_to_aos(double* aos, int stride, FieldPtrs F, int f0, int ncomp,
 void launch_int_to_slab(int* dst, const int* src, const int* id, int n, cudaStream_t st);
 void launch_slab_to_int(int* dst, const int* src, const int* id, int n, cudaStream_t st);
 void launch_iota(int* a, int n, cudaStream_t st);
+void launch_int_shift(int* dst, const int* src, int n, int add, cudaStream_t st);   // dst = src + add
 void launch_fill(double* a, double v, int n, cudaStream_t st);
 void launch_copy(double* dst, const double* src, int n, cudaStream_t st);
 

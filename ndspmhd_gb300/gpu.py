@@ -185,6 +185,9 @@ class GpuSPH:
                                            t.ctypes.data_as(C.POINTER(C.c_double))))
         return dt, t
 
+    def set_host_access(self, mode: int):
+        self._check(lib().ndsph_set_host_access(self._h, int(mode)))
+
     def batch_set_graph(self, mode: int):
         self._check(lib().ndsph_batch_set_graph(self._h, int(mode)))
 
