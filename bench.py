@@ -138,11 +138,14 @@ def run_device(o, st, steps: int, warmup: int, dist=None):
         dist.barrier()
     torch.cuda.synchronize()
     clk = ClockSampler(torch.cuda.current_device())
+    kept0, builds0 = g.timing()["nl_reused"], g.timing()["nl_builds"]
     clk.start()
     g.dev_step(steps)              # bracketed by CUDA events on the library's stream
     torch.cuda.synchronize()
     clocks = clk.stop()
     t_timed = g.timing()
+    t_timed["kept_link_steps"] = t_timed["nl_reused"] - kept0
+    t_timed["row_builds"] = t_timed["nl_builds"] - builds0
     total_ms = t_timed["total_ms"]
     launches = t_timed["launches"]
     # kernel breakdown on one extra profiled step (not part of the timed loop)
@@ -150,6 +153,8 @@ def run_device(o, st, steps: int, warmup: int, dist=None):
     g.dev_step(1)
     tim = g.timing()
     tim["launches_timed"] = launches
+    tim["kept_link_steps"] = t_timed["kept_link_steps"]
+    tim["row_builds"] = t_timed["row_builds"]
     dts = g.dts()
     g.close()
     return total_ms / steps, tim, dts, clocks
@@ -427,7 +432,8 @@ def main():
         "config": {"workload": f"3D MHD box {N1D}^3 = {n} particles, periodic, full leapfrog step",
                    "form": "FP32 pair sums (compensated), FP64 state/integration",
                    "l2": "inputs larger than L2 (state slab ~1.3 GB)", "parallelism": f"replicas x{world}",
-                   "nr_passes_per_step": tim32["density_passes"]},
+                   "nr_passes_per_step": tim32["density_passes"],
+                   "steps_keeping_the_link": tim32["kept_link_steps"], "row_builds": tim32["row_builds"]},
         "gpu_launches": None,
         "kernels_ms_per_step": {"rates": round(tim32["rates_ms"], 3), "density_all_passes": round(tim32["density_ms"], 3),
                                 "link": round(tim32["link_ms"], 3), "step_total": round(tim32["step_ms"], 3)},

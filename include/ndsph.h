@@ -291,8 +291,34 @@ typedef struct ndsph_timing {
     int32_t nl_builds;       /* neighbour-list builds so far (link + rebuilds)  */
     int32_t graph_steps;     /* batched steps run as a captured CUDA graph      */
     int32_t graph_redos;     /* of those, steps redone on the eager path        */
+    int32_t nl_reused;       /* steps that kept the previous link and rows      */
 } ndsph_timing;
 NDSPH_API int ndsph_get_timing(ndsph_ctx* ctx, ndsph_timing* t);
+
+/* ---- search tuning ----------------------------------------------------------
+ * Knobs of the neighbour search; none changes which pairs are summed.  No
+ * reference counterpart: the reference rebuilds its cell link list every step
+ * (derivs.f90:82-92 calling set_linklist, linkND.f90:45-161) with cells of
+ * 2 hmax and no neighbour rows.  ndspmhd_gb300/autotune.py times candidate
+ * settings on a workload and picks one.
+ *   nl_skin   rows hold every pair within 2 max(h_i, h_j) nl_skin     (1.1)
+ *   nl_reuse  FP32 form, one simulation: a step keeps the slot order, cells
+ *             (sized 2 hmax nl_skin) and rows of the previous link while
+ *             h + dmax <= nl_skin h_build holds for every particle, dmax
+ *             being the largest displacement since the rows were built  (1)
+ *   nl_grow   room for Newton-Raphson growth of h in that check      (1.005)
+ *   graph_cell_margin  batched captured steps: cells of 2 hmax margin, so
+ *             h may grow by the margin before a step leaves the graph (1.05)
+ * ndsph_set_tuning rejects values outside nl_skin in [1, 2], nl_grow in
+ * [1, 1.5], graph_cell_margin in [1, 2]; the next step links afresh.        */
+typedef struct ndsph_tuning {
+    float   nl_skin;
+    int32_t nl_reuse;
+    float   nl_grow;
+    float   graph_cell_margin;
+} ndsph_tuning;
+NDSPH_API int ndsph_set_tuning(ndsph_ctx* ctx, const ndsph_tuning* t);
+NDSPH_API int ndsph_get_tuning(ndsph_ctx* ctx, ndsph_tuning* t);
 
 /* ---- learned-h predictor: standalone forward / gradient (tests) ------------
  * params: the 1313 FP32 master weights (W1[32][6], b1[32], W2[32][32], b2[32],

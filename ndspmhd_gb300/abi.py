@@ -65,8 +65,17 @@ class NdsphTiming(C.Structure):
         ("step_ms", C.c_float), ("total_ms", C.c_float), ("density_passes", C.c_int32),
         ("launches", C.c_int32), ("pairs_density", C.c_int64), ("pairs_rates", C.c_int64),
         ("mlp_loss", C.c_float), ("mlp_ms", C.c_float), ("mlp_updates", C.c_int32), ("nl_builds", C.c_int32),
-        ("graph_steps", C.c_int32), ("graph_redos", C.c_int32),
+        ("graph_steps", C.c_int32), ("graph_redos", C.c_int32), ("nl_reused", C.c_int32),
     ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class NdsphTuning(C.Structure):
+    """ndsph_tuning: neighbour-search knobs (include/ndsph.h)."""
+    _fields_ = [("nl_skin", C.c_float), ("nl_reuse", C.c_int32), ("nl_grow", C.c_float),
+                ("graph_cell_margin", C.c_float)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

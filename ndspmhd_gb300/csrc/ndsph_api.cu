@@ -46,6 +46,7 @@ struct ndsph_ctx {
     // grid
     Grid g;
     double cell_hmax = 0.0;      // hmax the grid was built for
+    double grid_cf = 1.0;        // cell size / (2 hmax) of the grid
     bool linked = false;
     // reductions
     Reduce* red = nullptr;
@@ -74,6 +75,17 @@ struct ndsph_ctx {
     // neighbour lists
     int nl_stride = 0;
     float nl_skin = 1.1f;
+    // reuse of the rows across steps (FP32 form, one simulation): a step
+    // keeps the slot order, the cells and the rows of the last link while
+    // every particle has h + dmax <= skin * h_build (dmax: the largest
+    // displacement since the rows were built) and hmax + dmax <= cell / 2;
+    // the cells are then sized 2 hmax * skin so the stencil covers the rows'
+    // radius.  The pair sums see the same pairs either way.
+    int nl_reuse = 1;            // tuning switch
+    bool nl_valid = false;       // order, cells and rows match the device state
+    float nl_dmax = 0.f;         // displacement bound of this step (0 after a build)
+    float nl_grow = 1.005f;      // room left for Newton-Raphson growth of h
+    int nl_reused = 0;           // steps that kept the last link
     // learned-h predictor
     float* mlp_p = nullptr;      // FP32 master weights
     float* mlp_m = nullptr;      // Adam moments
@@ -298,7 +310,7 @@ static void free_particles(ndsph_ctx* ctx)
                     ctx->S.numneigh, ctx->S.cell, ctx->S.xs, ctx->S.h1, ctx->S.active, ctx->S.active_next,
                     ctx->S.flag, ctx->itype2, ctx->id2, ctx->ireal2, ctx->srt.key, ctx->srt.slot, ctx->srt.perm,
                     ctx->d_stage, ctx->d_istage, ctx->S.pk_v, ctx->S.pk_t, ctx->S.pk_b, ctx->S.pk_a,
-                    ctx->S.nl, ctx->S.nl_cnt, ctx->S.hb, ctx->S.sim, ctx->sim2};
+                    ctx->S.nl, ctx->S.nl_cnt, ctx->S.hb, ctx->S.xsb, ctx->S.sim, ctx->sim2};
     for (void* p : ptrs) if (p) cudaFree(p);
     ctx->slab[0] = ctx->slab[1] = nullptr;
     memset(&ctx->S, 0, sizeof(ctx->S));
@@ -341,7 +353,9 @@ static int ensure_capacity(ndsph_ctx* ctx, int n)
     CK(cudaMalloc(&ctx->sim2, ib));
     CK(cudaMemsetAsync(ctx->S.sim, 0, ib, ctx->st));
     CK(cudaMalloc(&ctx->S.hb, sizeof(float) * (size_t)cap));
+    CK(cudaMalloc(&ctx->S.xsb, sizeof(float4) * (size_t)cap));
     ctx->S.nl = nullptr;
+    ctx->nl_valid = false;
     ctx->nl_stride = 0;
     CK(cudaMalloc(&ctx->d_istage, ib));
     CK(cudaMemsetAsync(ctx->S.numneigh, 0, ib, ctx->st));
@@ -525,12 +539,15 @@ static const void* host_view(ndsph_ctx* ctx, const void* host)
     return ctx->pageable_access ? host : nullptr;
 }
 
-static int upload_aos(ndsph_ctx* ctx, const double* host, int f0, int ncomp, int stride, int n)
+// host array (AoS, `stride` doubles per particle) -> slab fields; slot k
+// takes particle id[k] (id = nullptr: particle k)
+static int upload_aos(ndsph_ctx* ctx, const double* host, int f0, int ncomp, int stride, int n,
+                      const int* id = nullptr)
 {
     if (!host) return 0;
     const double* src = (const double*)host_view(ctx, host);
     if (src) {
-        launch_aos_to_slab(ctx->F, f0, ncomp, src, stride, nullptr, n, ctx->st);
+        launch_aos_to_slab(ctx->F, f0, ncomp, src, stride, id, n, ctx->st);
         return 0;
     }
     // copy into one staging buffer on the copy stream while the layout kernel
@@ -541,7 +558,7 @@ static int upload_aos(ndsph_ctx* ctx, const double* host, int f0, int ncomp, int
     CK(cudaMemcpyAsync(buf, host, sizeof(double) * (size_t)stride * n, cudaMemcpyHostToDevice, ctx->st_cp));
     CK(cudaEventRecord(ctx->ev_cp[b], ctx->st_cp));
     CK(cudaStreamWaitEvent(ctx->st, ctx->ev_cp[b], 0));
-    launch_aos_to_slab(ctx->F, f0, ncomp, buf, stride, nullptr, n, ctx->st);
+    launch_aos_to_slab(ctx->F, f0, ncomp, buf, stride, id, n, ctx->st);
     CK(cudaEventRecord(ctx->ev_used[b], ctx->st));
     return 0;
 }
@@ -621,6 +638,7 @@ static int upload_inputs(ndsph_ctx* ctx, const ndsph_particles* p, int n, bool w
     int rc = ensure_capacity(ctx, n);
     if (rc) return rc;
     ctx->n = n;
+    ctx->nl_valid = false;   // slot order reset below
     rc |= upload_aos(ctx, p->x, X0, nd, nd, n);
     rc |= upload_aos(ctx, p->vel, V0, 3, 3, n);
     rc |= upload_aos(ctx, p->Bevol, BE0, 3, 3, n);
@@ -669,10 +687,22 @@ static int upload_inputs(ndsph_ctx* ctx, const ndsph_particles* p, int n, bool w
 // cell grid for the current hmax: periodic dims tile [xmin,xmax] with
 // nc = floor(L/(2 hmax (1+1e-9))) >= 3 cells, open dims pad the bounding box
 // by one cell each side (like linkND.f90:80-89)
+static bool reuse_on(const ndsph_ctx* ctx)
+{
+    return ctx->nl_reuse && ctx->o.precision == NDSPH_PREC_FP32 && !ctx->o.batched;
+}
+
 static int build_grid(ndsph_ctx* ctx, double hmax, const double* lo, const double* hi)
 {
     Grid& g = ctx->g;
-    const double cmin = 2.0 * hmax * (1.0 + 1.e-9);
+    // cells of 2 hmax skin when the rows may be kept across steps (their
+    // radius is 2 h skin), 2 hmax otherwise; a periodic box too small for
+    // three of the larger cells takes the plain size
+    double cf = reuse_on(ctx) ? (double)ctx->nl_skin : 1.0;
+    for (int d = 0; d < ctx->o.ndim; d++)
+        if (ctx->o.periodic[d] && (long)floor(ctx->o.L[d] / (2.0 * hmax * (1.0 + 1.e-9) * cf)) < 3) cf = 1.0;
+    ctx->grid_cf = cf;
+    const double cmin = 2.0 * hmax * (1.0 + 1.e-9) * cf;
     long ncells = 1;
     for (int d = 0; d < 3; d++) {
         if (d >= ctx->o.ndim) {
@@ -706,11 +736,84 @@ static int build_grid(ndsph_ctx* ctx, double hmax, const double* lo, const doubl
     return ensure_cells(ctx, g.ncells);
 }
 
-// link: hmax + bbox, grid, counting sort by cell, permutation of `fields`
-static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hmax_ghost)
+static float unord_bitsf(unsigned u)
+{
+    u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float f;
+    memcpy(&f, &u, sizeof f);
+    return f;
+}
+
+// A step may keep the last link when the check of k_reuse_check passes:
+// h + dmax <= skin h_build for every particle (the rows hold every pair
+// within 2 max(h_i, h_j)) and hmax + dmax <= cell/2 (the Newton-Raphson
+// relink cap).  Returns true and sets the step's dmax if so; the positions
+// in xs are refreshed either way.
+static bool try_keep_link(ndsph_ctx* ctx, bool keep_hmax_ghost, int* rc)
+{
+    *rc = 0;
+    if (!reuse_on(ctx) || !ctx->nl_valid || !ctx->linked || ctx->grid_cf <= 1.0 || !ctx->S.nl) return false;
+    cudaStream_t st = ctx->st;
+    Reduce* r = ctx->red;
+    const unsigned init[2] = {0u, 0xffffffffu};
+    if (cudaMemsetAsync(&r->hmax, 0, sizeof(unsigned long long), st) != cudaSuccess ||
+        cudaMemcpyAsync(&r->reuse_d2, init, sizeof init, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        *rc = NDSPH_E_CUDA;
+        return false;
+    }
+    launch_reuse_check(ctx->F, ctx->S, ctx->g, ctx->o, ctx->n, ctx->nl_skin, ctx->nl_grow, r, st);
+    if (cudaMemcpyAsync(ctx->h_red, r, sizeof(Reduce), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        *rc = NDSPH_E_CUDA;
+        return false;
+    }
+    const double hmax = bitsd(ctx->h_red->hmax);
+    float d2;
+    memcpy(&d2, &ctx->h_red->reuse_d2, sizeof d2);
+    const float slack = unord_bitsf(ctx->h_red->reuse_slack);
+    float csmax = 0.f;
+    double csmin = 1e300;
+    for (int d = 0; d < ctx->o.ndim; d++) {
+        csmax = std::max(csmax, ctx->g.csf[d]);
+        csmin = std::min(csmin, ctx->g.cs[d]);
+    }
+    // rounding of the FP32 coordinates: a relative and an absolute margin
+    const float dmax = sqrtf(d2) * 1.001f + 2e-6f * csmax;
+    if (!(hmax > 0.0) || !std::isfinite(hmax) || !(dmax <= slack) ||
+        !(hmax * ctx->nl_grow + dmax <= 0.5 * csmin / (1.0 + 1.e-9)))
+        return false;
+    if (!keep_hmax_ghost) {
+        ctx->h_red->hmax_ghost = dbits(hmax);
+        if (cudaMemcpyAsync(&r->hmax_ghost, &ctx->h_red->hmax_ghost, sizeof(unsigned long long),
+                            cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            *rc = NDSPH_E_CUDA;
+            return false;
+        }
+    }
+    // the check covers every particle's current h: no row is stale
+    if (cudaMemsetAsync(&r->nl_stale, 0, sizeof(int), st) != cudaSuccess) {
+        *rc = NDSPH_E_CUDA;
+        return false;
+    }
+    ctx->cell_hmax = hmax;
+    ctx->nl_dmax = dmax;
+    ctx->nl_reused++;
+    return true;
+}
+
+// link: hmax + bbox, grid, counting sort by cell, permutation of `fields`;
+// with may_keep, a step whose rows still hold every pair keeps the last link
+static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hmax_ghost, bool may_keep = false)
 {
     const int n = ctx->n;
     cudaStream_t st = ctx->st;
+    if (may_keep) {
+        int rc = 0;
+        if (try_keep_link(ctx, keep_hmax_ghost, &rc)) return 0;
+        if (rc) return rc;
+    }
+    ctx->nl_valid = false;
+    ctx->nl_dmax = 0.f;
     launch_link_reset(ctx->red, st);
     launch_hmax_bbox(ctx->F, ctx->o.ndim, n, ctx->red, &ctx->red->hmax, st);
     CK(cudaMemcpyAsync(ctx->h_red, ctx->red, sizeof(Reduce), cudaMemcpyDeviceToHost, st));
@@ -798,6 +901,7 @@ static SweepArgs sweep_args(ndsph_ctx* ctx)
     a.nl_ld = ctx->cap;
     a.nl_stride = ctx->nl_stride;
     a.nl_skin = ctx->nl_skin;
+    a.nl_dmax = ctx->nl_dmax;
     a.d_its = nullptr;
     a.d_nlist = nullptr;
     a.gate = nullptr;
@@ -810,6 +914,7 @@ static SweepArgs sweep_args(ndsph_ctx* ctx)
 static int build_nlist(ndsph_ctx* ctx)
 {
     cudaStream_t st = ctx->st;
+    ctx->nl_valid = false;
     if (ctx->nl_stride == 0) {
         int s0 = ctx->o.ndim == 1 ? 32 : (ctx->o.ndim == 2 ? 64 : 160);
         CK(cudaMalloc(&ctx->S.nl, sizeof(unsigned) * (size_t)s0 * ctx->cap));
@@ -825,7 +930,10 @@ static int build_nlist(ndsph_ctx* ctx)
         int h[3];
         CK(cudaMemcpyAsync(h, &ctx->red->nl_stale, sizeof(int) * 3, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        if (!h[1]) return 0;
+        if (!h[1]) {
+            ctx->nl_valid = reuse_on(ctx) && ctx->grid_cf > 1.0 && ctx->nl_dmax == 0.f;
+            return 0;
+        }
         // overflow: grow to the largest count seen (+25%) and rebuild
         int ns = (h[2] + h[2] / 4 + 8 + 3) & ~3;   // rows of whole 16-byte groups
         CK(cudaFree(ctx->S.nl));
@@ -847,7 +955,7 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
     int zero = 0;
     CK(cudaMemcpyAsync(&ctx->red->redolink, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
     int its = 0, ncalc = n, ncalctotal = 0, nrelink = 0;
-    bool redolink = false, h1_stale = true;
+    bool redolink = false, h1_stale = true, rows_stale = false;
     if (ctx->o.precision == NDSPH_PREC_FP32) {
         SweepArgs pa = sweep_args(ctx);
         launch_pack_v(pa, st);
@@ -856,7 +964,11 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
     float dens_ms = 0.f, pass1_ms = 0.f;
     while (ncalc > 0 && its <= itsmax) {
         its++;
-        if (redolink) {
+        // rows outgrown on a step that kept the last link: the cells no longer
+        // bound the displacements, so the rows are rebuilt by a full relink
+        const bool rows_relink = rows_stale && ctx->nl_dmax > 0.f;
+        bool relinked = false;
+        if (redolink || rows_relink) {
             // relink (iterate_density.f90:122-126): the ghosts' hhmax becomes the
             // current max h.  The cells and the neighbour lists only have to be
             // rebuilt if h outgrew them; otherwise refreshing hhmax is enough.
@@ -867,8 +979,9 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
             CK(cudaStreamSynchronize(st));
             const double hmax_now = bitsd(hb);
             double cap = 1e300;
-            for (int d = 0; d < ctx->o.ndim; d++) cap = std::min(cap, 0.5 * ctx->g.cs[d] / (1.0 + 1.e-9));
-            if (hmax_now <= cap) {
+            for (int d = 0; d < ctx->o.ndim; d++)
+                cap = std::min(cap, 0.5 * ctx->g.cs[d] / (1.0 + 1.e-9) - (double)ctx->nl_dmax);
+            if (hmax_now <= cap && !rows_relink) {
                 CK(cudaMemcpyAsync(&ctx->red->hmax_ghost, &hb, sizeof(hb), cudaMemcpyHostToDevice, st));
             } else {
                 // active list -> ids
@@ -876,8 +989,10 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
                 CK(cudaMemcpy(act.data(), ctx->S.active, sizeof(int) * (size_t)ncalc, cudaMemcpyDeviceToHost));
                 CK(cudaMemcpy(ids.data(), ctx->S.id, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
                 for (int k = 0; k < ncalc; k++) act[k] = ids[act[k]];
-                int rc = link_all(ctx, false);
+                // a relink asked for by the rows alone keeps the ghosts' hhmax
+                int rc = link_all(ctx, !redolink);
                 if (rc) return rc;
+                relinked = true;
                 std::vector<int> pos(n);
                 CK(cudaMemcpy(pos.data(), ctx->S.pos_of_id, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
                 for (int k = 0; k < ncalc; k++) act[k] = pos[act[k]];
@@ -888,8 +1003,15 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
                 }
                 h1_stale = true;
             }
-            nrelink++;
+            if (redolink) nrelink++;
         }
+        if (rows_stale && !relinked) {
+            if (h1_stale) launch_h1(ctx->F, ctx->S, n, st);   // list radius from the current h
+            h1_stale = false;
+            int rc = build_nlist(ctx);
+            if (rc) return rc;
+        }
+        rows_stale = false;
         const bool full = (ncalc == n);
         // 1/h: after the start, a full pass (every h changed) or a relink; a
         // partial pass keeps it current for the particles it updates
@@ -920,12 +1042,9 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
         redolink = ctx->h_red->redolink != 0;
         ncalc = h_ncalc;
         std::swap(ctx->S.active, ctx->S.active_next);
-        if (ctx->h_red->nl_stale && !redolink) {
-            if (h1_stale) launch_h1(ctx->F, ctx->S, n, st);   // list radius from the current h
-            h1_stale = false;
-            rc = build_nlist(ctx);
-            if (rc) return rc;
-        }
+        // rows outgrown by some h: rebuilt before the next pass (a particle
+        // that flags them is unconverged, so there is one)
+        rows_stale = ctx->h_red->nl_stale != 0;
     }
     ctx->timing.density_ms = dens_ms;
     ctx->timing.density_pass1_ms = pass1_ms;
@@ -986,7 +1105,7 @@ static int do_derivs(ndsph_ctx* ctx, const int* fields, int nfields)
     bool anyb = false;
     for (int d = 0; d < ctx->o.ndim; d++) if (ctx->o.ibound[d] != 0) anyb = true;
     if (anyb) launch_boundary_wrap(ctx->F, ctx->o, ctx->n, st);
-    int rc = do_link(ctx, fields, nfields, false);
+    int rc = do_link(ctx, fields, nfields, false, true);
     if (rc) return rc;
     tmark(ctx, 1);
     launch_reduce_reset(ctx->red, st);
@@ -1526,32 +1645,51 @@ extern "C" int ndsph_dev_derivs(ndsph_ctx* ctx, ndsph_dt* dts)
 static int step_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
 {
     if (ctx->o.has_fixed || ctx->o.maxdensits < 1) return dev_upload_impl(ctx, p, npart, false);
-    int rc = ensure_capacity(ctx, npart);
-    if (rc) return rc;
-    ctx->n = npart;
+    // when the last step's link may be kept, the caller's arrays go straight
+    // into that step's slot order (slot k <- particle id[k]); the link's
+    // check then decides from the uploaded positions and h whether the rows
+    // still hold every pair, so arrays the caller changed are safe
+    const bool keep = ctx->nl_valid && ctx->linked && npart == ctx->n && reuse_on(ctx);
+    int rc = 0;
+    if (!keep) {
+        rc = ensure_capacity(ctx, npart);
+        if (rc) return rc;
+        ctx->n = npart;
+        ctx->nl_valid = false;
+    }
     const int n = npart, nd = ctx->o.ndim;
-    rc |= upload_aos(ctx, p->x, X0, nd, nd, n);
-    rc |= upload_aos(ctx, p->vel, V0, 3, 3, n);
-    rc |= upload_aos(ctx, p->Bevol, BE0, 3, 3, n);
-    rc |= upload_aos(ctx, p->en, EN, 1, 1, n);
-    rc |= upload_aos(ctx, p->hh, HH, 1, 1, n);
-    rc |= upload_aos(ctx, p->pmass, PM, 1, 1, n);
-    rc |= upload_aos(ctx, p->alpha, AL0, 3, 3, n);
-    rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n);
-    rc |= upload_aos(ctx, p->dhdt, DHDT, 1, 1, n);
-    rc |= upload_aos(ctx, p->force, F0, 3, 3, n);
-    rc |= upload_aos(ctx, p->dBevoldt, DB0, 3, 3, n);
-    rc |= upload_aos(ctx, p->dendt, DENDT, 1, 1, n);
-    rc |= upload_aos(ctx, p->daldt, DAL0, 3, 3, n);
+    const int* idm = keep ? ctx->S.id : nullptr;
+    rc |= upload_aos(ctx, p->x, X0, nd, nd, n, idm);
+    rc |= upload_aos(ctx, p->vel, V0, 3, 3, n, idm);
+    rc |= upload_aos(ctx, p->Bevol, BE0, 3, 3, n, idm);
+    rc |= upload_aos(ctx, p->en, EN, 1, 1, n, idm);
+    rc |= upload_aos(ctx, p->hh, HH, 1, 1, n, idm);
+    rc |= upload_aos(ctx, p->pmass, PM, 1, 1, n, idm);
+    rc |= upload_aos(ctx, p->alpha, AL0, 3, 3, n, idm);
+    rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n, idm);
+    rc |= upload_aos(ctx, p->dhdt, DHDT, 1, 1, n, idm);
+    rc |= upload_aos(ctx, p->force, F0, 3, 3, n, idm);
+    rc |= upload_aos(ctx, p->dBevoldt, DB0, 3, 3, n, idm);
+    rc |= upload_aos(ctx, p->dendt, DENDT, 1, 1, n, idm);
+    rc |= upload_aos(ctx, p->daldt, DAL0, 3, 3, n, idm);
     if (rc) return rc;
-    if (const int* v = (const int*)host_view(ctx, p->itype))
-        launch_int_shift(ctx->S.itype, v, n, 0, ctx->st);
-    else
-        CK(cudaMemcpyAsync(ctx->S.itype, p->itype, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
-    launch_iota(ctx->S.id, n, ctx->st);
-    launch_iota(ctx->S.pos_of_id, n, ctx->st);
+    if (keep) {
+        const int* v = (const int*)host_view(ctx, p->itype);
+        if (!v) {
+            CK(cudaMemcpyAsync(ctx->d_istage, p->itype, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+            v = ctx->d_istage;
+        }
+        launch_int_to_slab(ctx->S.itype, v, ctx->S.id, n, ctx->st);
+    } else {
+        if (const int* v = (const int*)host_view(ctx, p->itype))
+            launch_int_shift(ctx->S.itype, v, n, 0, ctx->st);
+        else
+            CK(cudaMemcpyAsync(ctx->S.itype, p->itype, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+        launch_iota(ctx->S.id, n, ctx->st);
+        launch_iota(ctx->S.pos_of_id, n, ctx->st);
+        ctx->linked = false;
+    }
     CK(cudaMemsetAsync(ctx->S.ireal, 0xff, sizeof(int) * (size_t)n, ctx->st));   // no fixed particles
-    ctx->linked = false;
     return 0;
 }
 
@@ -2044,9 +2182,39 @@ extern "C" int ndsph_neighbour_csr(ndsph_ctx* ctx, int32_t mode, int64_t* offset
     return 0;
 }
 
+extern "C" int ndsph_set_tuning(ndsph_ctx* ctx, const ndsph_tuning* t)
+{
+    GUARD_CTX();
+    if (!t || !(t->nl_skin >= 1.0f && t->nl_skin <= 2.0f) || !(t->nl_grow >= 1.0f && t->nl_grow <= 1.5f) ||
+        !(t->graph_cell_margin >= 1.0f && t->graph_cell_margin <= 2.0f) || (t->nl_reuse != 0 && t->nl_reuse != 1)) {
+        ctx->err = "tuning out of range (nl_skin in [1,2], nl_grow in [1,1.5], graph_cell_margin in [1,2])";
+        return NDSPH_E_ARG;
+    }
+    ctx->nl_skin = t->nl_skin;
+    ctx->nl_reuse = t->nl_reuse;
+    ctx->nl_grow = t->nl_grow;
+    if ((double)t->graph_cell_margin != ctx->gmargin) graph_drop(ctx);
+    ctx->gmargin = t->graph_cell_margin;
+    // rows built with the old radius: the next step links afresh
+    ctx->nl_valid = false;
+    return 0;
+}
+
+extern "C" int ndsph_get_tuning(ndsph_ctx* ctx, ndsph_tuning* t)
+{
+    GUARD_CTX();
+    if (!t) return NDSPH_E_ARG;
+    t->nl_skin = ctx->nl_skin;
+    t->nl_reuse = ctx->nl_reuse;
+    t->nl_grow = ctx->nl_grow;
+    t->graph_cell_margin = (float)ctx->gmargin;
+    return 0;
+}
+
 extern "C" int ndsph_get_timing(ndsph_ctx* ctx, ndsph_timing* t)
 {
     GUARD_CTX();
+    ctx->timing.nl_reused = ctx->nl_reused;
     if (t) *t = ctx->timing;
     return 0;
 }

@@ -124,6 +124,9 @@ struct Reduce {
     int g_gate;                     // relink check of this pass (redolink of the previous pass)
     int g_rebuild;                  // rebuild the neighbour rows after this pass
     int g_pad;
+    // neighbour-row reuse check of a step that skips the link
+    unsigned reuse_d2;              // max squared displacement since the build (float bits)
+    unsigned reuse_slack;           // min of skin*h_build - grow*h (order-preserving float bits)
 };
 
 __host__ __device__ inline unsigned long long dbits(double v)
@@ -163,6 +166,16 @@ __device__ inline unsigned long long ord_bits(double v)
 {
     unsigned long long u = dbits(v);
     return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+// order-preserving map of a float to uint32 (signed min/max atomics)
+__host__ __device__ inline unsigned ord_bitsf(float v)
+{
+#ifdef __CUDA_ARCH__
+    unsigned u = __float_as_uint(v);
+#else
+    union { float f; unsigned u; } c; c.f = v; unsigned u = c.u;
+#endif
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 __device__ inline void raise_err(Reduce* r, int code, int idx)
 {

@@ -301,6 +301,71 @@ void launch_xs(FieldPtrs F, Side S, Grid g, DevOpts o, int n, cudaStream_t st)
     if (n > 0) NDSPH_COUNT_LAUNCH, k_xs<<<nblk(n, 256), 256, 0, st>>>(F, S, g, o.ndim, n);
 }
 
+// A step that keeps the previous link (same slot order, cells and rows).
+// Each slot's position is taken relative to the lower corner of the cell it
+// was sorted into, with a periodic jump of the boundary wrap undone, so the
+// stencil offsets stored in the rows stay the cell offsets between the two
+// slots.  Reduced: the largest displacement since the rows were built, the
+// smallest row slack skin*h_build - grow*h, and the largest h.  A pair with
+// r < 2 max(h_i, h_j) now was within 2 max(h) + 2 dmax when the rows were
+// built, so every such pair is in the rows while h + dmax <= skin*h_build
+// holds for every particle (the host checks it with dmax and the slack).
+__global__ void k_reuse_check(FieldPtrs F, Side S, Grid g, DevOpts o, int n, float skin, float grow, Reduce* red)
+{
+    __shared__ float sd[8], ss[8];
+    __shared__ double sh[8];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    float d2 = 0.f, slack = 3.0e38f;
+    double h = 0.0;
+    if (k < n) {
+        const int c = S.cell[k];
+        int cc[3];
+        cc[0] = c % g.nc[0];
+        cc[1] = (c / g.nc[0]) % g.nc[1];
+        cc[2] = c / (g.nc[0] * g.nc[1]);
+        float r[3] = {0.f, 0.f, 0.f};
+        for (int d = 0; d < o.ndim; d++) {
+            double v = F.f[X0 + d][k] - (g.origin[d] + cc[d] * g.cs[d]);
+            if (o.periodic[d]) {
+                if (v > 0.5 * o.L[d]) v -= o.L[d];
+                else if (v < -0.5 * o.L[d]) v += o.L[d];
+            }
+            r[d] = (float)v;
+        }
+        h = F.f[HH][k];
+        S.xs[k] = make_float4(r[0], r[1], r[2], (float)h);
+        const float4 b = S.xsb[k];
+        const float e0 = r[0] - b.x, e1 = r[1] - b.y, e2 = r[2] - b.z;
+        d2 = e0 * e0 + e1 * e1 + e2 * e2;
+        slack = skin * S.hb[k] - grow * (float)h;
+        if (!(d2 <= 3.0e38f)) d2 = 3.0e38f;          // non-finite position: fails the check
+        if (!(slack >= -3.0e38f)) slack = -3.0e38f;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, off));
+        slack = fminf(slack, __shfl_down_sync(0xffffffffu, slack, off));
+        h = fmax(h, __shfl_down_sync(0xffffffffu, h, off));
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { sd[warp] = d2; ss[warp] = slack; sh[warp] = h; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+            d2 = fmaxf(d2, sd[w]);
+            slack = fminf(slack, ss[w]);
+            h = fmax(h, sh[w]);
+        }
+        atomicMax(&red->reuse_d2, __float_as_uint(d2));
+        atomicMin(&red->reuse_slack, ord_bitsf(slack));
+        atomicMax(&red->hmax, dbits(h));
+    }
+}
+void launch_reuse_check(FieldPtrs F, Side S, Grid g, DevOpts o, int n, float skin, float grow, Reduce* red,
+                        cudaStream_t st)
+{
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_reuse_check<<<nblk(n, 256), 256, 0, st>>>(F, S, g, o, n, skin, grow, red);
+}
+
 // ---------------------------------------------------------------------------
 // host layout <-> slab
 // ---------------------------------------------------------------------------

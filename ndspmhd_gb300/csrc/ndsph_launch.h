@@ -32,6 +32,7 @@ struct Side {
     unsigned* nl;
     int* nl_cnt;
     float* hb;        // h of each slot when its list was built
+    float4* xsb;      // xs of each slot when its list was built (reuse check)
     int* sim;         // simulation of the slot (batched form)
 };
 
@@ -61,6 +62,7 @@ struct SweepArgs {
     long long nl_ld;         // leading dimension of the list (>= n)
     int nl_stride;           // entries per particle
     float nl_skin;           // list radius = 2 max(h_i,h_j) skin (h may grow by skin before a rebuild)
+    float nl_dmax;           // largest displacement since the rows were built (0 right after a build)
     // device-side control (captured step): when set, the pass number, the
     // active count and the row-build gate are read from device memory
     const int* d_its;
@@ -84,6 +86,11 @@ void launch_gather_int(int* dst, const int* src, const int* perm, int n, cudaStr
 void launch_post_sort(Side S, SortScratch s, int n, int ncells, Grid g, FieldPtrs F, DevOpts o,
                       cudaStream_t st);
 void launch_xs(FieldPtrs F, Side S, Grid g, DevOpts o, int n, cudaStream_t st);
+// step that keeps the last link: xs relative to each slot's cell of that link
+// (periodic jumps undone), max displacement since the row build, min row
+// slack skin*h_build - grow*h, max h (red->hmax, red->reuse_d2, red->reuse_slack)
+void launch_reuse_check(FieldPtrs F, Side S, Grid g, DevOpts o, int n, float skin, float grow, Reduce* red,
+                        cudaStream_t st);
 
 // ---- host layout <-> device slab ------------------------------------------
 // AoS host-layout staging buffer (one field: stride comps) -> sorted slab fields

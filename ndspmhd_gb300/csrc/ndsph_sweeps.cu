@@ -494,7 +494,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
             }
         }
         if (hnew > bitsd(a.red->hmax_ghost)) relink = true;
-        if ((float)hnew > a.S.hb[i] * a.nl_skin) a.red->nl_stale = 1;
+        if ((float)hnew + a.nl_dmax > a.S.hb[i] * a.nl_skin) a.red->nl_stale = 1;
     } else {
         drhodt = drhodt * gradh;
         F.f[DHDT][i] = dhdrhoi * drhodt;
@@ -1136,6 +1136,7 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
     }
     a.S.nl_cnt[i] = cnt < a.nl_stride ? cnt : a.nl_stride;
     a.S.hb[i] = hi;
+    if (a.S.xsb) a.S.xsb[i] = xsi;
     if (cnt > a.nl_stride) { a.red->nl_overflow = 1; if (a.graph) a.red->gfail |= 2; }
     atomicMax(&a.red->nl_maxcnt, cnt);
 }

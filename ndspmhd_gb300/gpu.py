@@ -26,7 +26,7 @@ import os
 
 import numpy as np
 
-from .abi import (NdsphDt, NdsphOpts, NdsphParticles, NdsphTiming, alloc_state, make_opts,
+from .abi import (NdsphDt, NdsphOpts, NdsphParticles, NdsphTiming, NdsphTuning, alloc_state, make_opts,
                   make_particles)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -79,6 +79,8 @@ def lib() -> C.CDLL:
     L.ndsph_batch_upload.argtypes = [P, parts, C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.c_int32]
     L.ndsph_batch_step.argtypes = [P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.ndsph_batch_download.argtypes = [P, parts]
+    L.ndsph_set_tuning.argtypes = [P, C.POINTER(NdsphTuning)]
+    L.ndsph_get_tuning.argtypes = [P, C.POINTER(NdsphTuning)]
     _lib = L
     return L
 
@@ -213,6 +215,22 @@ class GpuSPH:
 
     def set_learning(self, lr: float = 2e-3, iters_per_step: int = 4, batch: int = 16384):
         self._check(lib().ndsph_set_learning(self._h, lr, iters_per_step, batch))
+
+    def get_tuning(self) -> dict:
+        t = NdsphTuning()
+        self._check(lib().ndsph_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        """Change neighbour-search knobs (nl_skin, nl_reuse, nl_grow,
+        graph_cell_margin); the others keep their values."""
+        t = NdsphTuning()
+        self._check(lib().ndsph_get_tuning(self._h, C.byref(t)))
+        for k, v in kw.items():
+            if k not in dict(NdsphTuning._fields_):
+                raise KeyError(k)
+            setattr(t, k, v)
+        self._check(lib().ndsph_set_tuning(self._h, C.byref(t)))
 
     def set_profiling(self, on: bool = True):
         self._check(lib().ndsph_set_profiling(self._h, 1 if on else 0))

@@ -1,0 +1,127 @@
+"""Neighbour-row reuse across steps (FP32 form, one simulation).
+
+A step may keep the slot order, cells and rows of the previous link when
+every particle satisfies h + dmax <= skin * h_build (dmax: the largest
+displacement since the rows were built).  The pairs summed are then the same
+as after a fresh link, so results agree with the relink-every-step run within
+the FP32 form's rounding: |d| / max(|ref|, rms(ref), physical scale) <= 1e-5
+after a few steps, and the union-criterion neighbour counts of the first
+density pass agree except for pairs within FP32 rounding of the cut-off
+(cell-relative coordinates are taken from different cell corners), which
+may go either way and stay rare -- a row missing real neighbours would show
+up as a one-sided excess of lower counts.
+"""
+import numpy as np
+import pytest
+
+from ndspmhd_gb300 import configs
+from tests.helpers import compare_fields
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["x", "vel", "hh", "rho", "en", "Bevol", "force"]
+
+
+def _initial(case):
+    from ndspmhd_gb300.gpu import GpuSPH
+    o, p = case()
+    o = dict(o)
+    o["precision"] = 1
+    g = GpuSPH(o, configs.full_state(p, o["ndim"]))
+    g.primitive2conservative()
+    st = {k: v.copy() for k, v in g.state.items()}
+    g.close()
+    return o, st
+
+
+def _device_run(o, st, nsteps, **tuning):
+    from ndspmhd_gb300.gpu import GpuSPH
+    g = GpuSPH(o, {k: v.copy() for k, v in st.items()})
+    g.set_tuning(**tuning)
+    g.dev_upload()
+    g.set_dt(0.0)
+    for _ in range(nsteps):
+        g.dev_step(1)
+    g.dev_download()
+    out = {k: v.copy() for k, v in g.state.items()}
+    tim, dts = g.timing(), g.dts()
+    g.close()
+    return out, tim, dts
+
+
+@pytest.mark.parametrize("skin", [1.1, 1.2])
+def test_device_steps_with_reuse_match_relinking(skin, gpulib):
+    o, st = _initial(lambda: configs.mhd_box_3d(24, seed=4))
+    nsteps = 12
+    a, ta, da = _device_run(o, st, nsteps, nl_reuse=1, nl_skin=skin)
+    b, tb, db = _device_run(o, st, nsteps, nl_reuse=0, nl_skin=skin)
+    assert ta["nl_reused"] >= nsteps // 2, ta
+    assert tb["nl_reused"] == 0
+    assert ta["nl_builds"] < tb["nl_builds"], (ta["nl_builds"], tb["nl_builds"])
+    errs, bad = compare_fields(a, b, FIELDS, 1e-5)
+    assert not bad, errs
+    assert abs(da["time"] - db["time"]) <= 1e-6 * db["time"]
+
+
+def test_host_steps_with_reuse_same_pairs(gpulib):
+    """ndsph_step with host arrays: a context that keeps its link across calls
+    and one that relinks on every call take the same inputs at every step."""
+    from ndspmhd_gb300.gpu import GpuSPH
+    o, st = _initial(lambda: configs.mhd_box_3d(20, seed=9))
+    n = st["x"].shape[0]
+    ga = GpuSPH(o, {k: v.copy() for k, v in st.items()})
+    ga.set_tuning(nl_reuse=1)
+    ga.set_dt(0.0)
+    cur = {k: v.copy() for k, v in st.items()}
+    dt, t = 0.0, 0.0
+    lower = higher = 0
+    for step in range(8):
+        ga.rebind({k: v.copy() for k, v in cur.items()})
+        ga.dt.dt, ga.dt.time, ga.dt.nsteps = dt, t, step
+        ga.step()
+        gb = GpuSPH(o, {k: v.copy() for k, v in cur.items()})
+        gb.set_tuning(nl_reuse=0)
+        gb.dt.dt, gb.dt.time, gb.dt.nsteps = dt, t, step
+        gb.step()
+        na, nb = ga.state["numneigh"], gb.state["numneigh"]
+        assert np.max(np.abs(na.astype(np.int64) - nb)) <= 1, step
+        lower += int(np.sum(na < nb))
+        higher += int(np.sum(na > nb))
+        errs, bad = compare_fields(ga.state, gb.state, ["rho", "hh", "force", "dudt", "dBevoldt"], 1e-5)
+        assert not bad, (step, errs)
+        cur = {k: v.copy() for k, v in gb.state.items()}
+        dt, t = gb.dt.dt, gb.dt.time
+        gb.close()
+    reused = ga.timing()["nl_reused"]
+    ga.close()
+    assert reused >= 4, reused
+    # near-cut rounding only: rare, and not one-sided
+    assert lower <= max(4, 1e-4 * n * 8), (lower, higher)
+
+
+def test_reuse_check_falls_back_to_relink(gpulib):
+    """Supersonic flow, thin skin and no room left for Newton-Raphson growth
+    of h: the check fails on some steps (a fresh link), and rows can go stale
+    during the iteration of a step that kept the link (a relink there);
+    results still match the relinking run."""
+    o, st = _initial(lambda: configs.turbulent_box_3d(24))
+    nsteps = 10
+    a, ta, _ = _device_run(o, st, nsteps, nl_reuse=1, nl_skin=1.05, nl_grow=1.0)
+    b, tb, _ = _device_run(o, st, nsteps, nl_reuse=0, nl_skin=1.05, nl_grow=1.0)
+    assert ta["nl_reused"] < nsteps
+    errs, bad = compare_fields(a, b, ["x", "vel", "hh", "rho", "force"], 1e-5)
+    assert not bad, errs
+
+
+def test_tuning_rejects_out_of_range(gpulib):
+    from ndspmhd_gb300.gpu import GpuSPH, NdsphError
+    o, p = configs.mhd_box_3d(10, seed=1)
+    g = GpuSPH(o, configs.full_state(p, 3))
+    t0 = g.get_tuning()
+    assert t0["nl_reuse"] == 1 and abs(t0["nl_skin"] - 1.1) < 1e-6
+    for bad in ({"nl_skin": 0.9}, {"nl_skin": 2.5}, {"nl_grow": 0.99}, {"graph_cell_margin": 0.5},
+                {"nl_reuse": 2}):
+        with pytest.raises(NdsphError):
+            g.set_tuning(**bad)
+    assert g.get_tuning() == t0
+    g.close()
