@@ -126,10 +126,22 @@ def init_state(o, st):
     return g
 
 
-def run_device(o, st, steps: int, warmup: int, dist=None):
+def tune(o, st):
+    """Search settings for this workload from the project autotuner (timed
+    trials on copies of the initial state; the timed run starts afresh)."""
+    from ndspmhd_gb300 import autotune
+    g = init_state(o, st)
+    st0 = {k: v.copy() for k, v in g.state.items()}
+    g.close()
+    return autotune.tune_device(o, st0, steps=8, warmup=3)
+
+
+def run_device(o, st, steps: int, warmup: int, dist=None, tuning=None):
     """Device-resident timing: returns (ms_per_step, timing dict, dts, clocks)."""
     import torch
     g = init_state(o, st)
+    if tuning:
+        g.set_tuning(**tuning)
     g.dev_upload()
     g.set_dt(0.0)
     g.dev_step(warmup)
@@ -160,7 +172,7 @@ def run_device(o, st, steps: int, warmup: int, dist=None):
     return total_ms / steps, tim, dts, clocks
 
 
-def run_e2e(o, steps: int, warmup: int):
+def run_e2e(o, steps: int, warmup: int, tuning=None):
     """Reference-facing C-ABI call with pinned host buffers: ndsph_step."""
     import numpy as np
     import torch
@@ -189,6 +201,8 @@ def run_e2e(o, steps: int, warmup: int):
         for k, (t, a) in pinned.items():
             a[...] = st[k]
         g = GpuSPH(o2, host)
+        if tuning:
+            g.set_tuning(**tuning)
         g.set_host_access(mode)
         g.set_dt(0.0)
         g.dt.dt, g.dt.time, g.dt.nsteps = 0.0, 0.0, 0
@@ -217,14 +231,18 @@ def run_batched(steps: int, warmup: int, ntubes: int = 4096):
     each (seeded), one device state, per-tube dt; FP32 pair sums.  `steps`
     timed steps as captured CUDA graphs (one launch per step), then the same
     problem on the eager host loop for comparison."""
-    from ndspmhd_gb300 import configs
+    from ndspmhd_gb300 import autotune, configs
     from ndspmhd_gb300.gpu import GpuSPH
     o, p, sim, counts = configs.brio_wu_batch(ntubes)
     o["precision"] = 1
     n = int(counts.sum())
+    cands = [{"graph_cell_margin": m, "nl_skin": sk} for m in (1.02, 1.05, 1.1) for sk in (1.05, 1.1)]
+    tuned = autotune.tune_batched(o, configs.full_state(p, 1), sim, len(counts), candidates=cands,
+                                  steps=20, warmup=3)
     out = {}
     for mode, nst in ((1, steps), (0, max(steps // 4, 5))):
         g = GpuSPH(o, configs.full_state(p, 1))
+        g.set_tuning(**tuned["tuning"])
         g.batch_upload(sim, len(counts), initialise=True)
         g.batch_set_graph(mode)
         g.batch_step(warmup)
@@ -238,7 +256,8 @@ def run_batched(steps: int, warmup: int, ntubes: int = 4096):
     res = dict(out[1])
     res.update({"unit": UNIT, "config": f"{ntubes} Brio-Wu tubes, {n} particles, FP32 pairs, per-tube dt, "
                                         f"one captured graph launch per step",
-                "eager": out[0]})
+                "eager": out[0], "search_tuning": tuned["tuning"],
+                "autotune_trials": [[t["tuning"], t["ms_per_step"]] for t in tuned["trials"]]})
     return res
 
 
@@ -365,7 +384,7 @@ def reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form measurement")
@@ -397,7 +416,9 @@ def main():
 
     o32, st32 = make_problem(N1D, 1)
     n = st32["x"].shape[0]
-    ms32, tim32, dts32, clocks = run_device(o32, st32, args.steps, warmup, dist)
+    tuned = tune(o32, st32)
+    tuning = tuned["tuning"]
+    ms32, tim32, dts32, clocks = run_device(o32, st32, args.steps, warmup, dist, tuning)
     ms64 = tim64 = None
     if not args.no_fp64:
         o64, st64 = make_problem(N1D, 0)
@@ -410,7 +431,7 @@ def main():
         ms32 = float(t.item())
     value = world * n / (ms32 * 1e-3)
 
-    e2e_val, h2d, d2h, e2e_staged = run_e2e(o32, max(3, args.steps), 3)
+    e2e_val, h2d, d2h, e2e_staged = run_e2e(o32, max(3, args.steps), 3, tuning)
 
     peak, peak_kind = _load_peaks()
     rates_ms = tim32["rates_ms"]
@@ -433,7 +454,9 @@ def main():
                    "form": "FP32 pair sums (compensated), FP64 state/integration",
                    "l2": "inputs larger than L2 (state slab ~1.3 GB)", "parallelism": f"replicas x{world}",
                    "nr_passes_per_step": tim32["density_passes"],
-                   "steps_keeping_the_link": tim32["kept_link_steps"], "row_builds": tim32["row_builds"]},
+                   "steps_keeping_the_link": tim32["kept_link_steps"], "row_builds": tim32["row_builds"],
+                   "search_tuning": tuning,
+                   "autotune_trials": [[t["tuning"], t["ms_per_step"]] for t in tuned["trials"]]},
         "gpu_launches": None,
         "kernels_ms_per_step": {"rates": round(tim32["rates_ms"], 3), "density_all_passes": round(tim32["density_ms"], 3),
                                 "link": round(tim32["link_ms"], 3), "step_total": round(tim32["step_ms"], 3)},

@@ -542,7 +542,13 @@ __global__ void k_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
         int it = S.itype[k];
         if (o.iener == 0) {
             if (rho > 0.0 && it == NDSPH_ITYPE_GAS) {
-                pr = o.polyk * pow(rho, o.gamma);
+                // rho^gamma: FP64 pow in the parity form; in the FP32 form the
+                // pressure only enters FP32 pair terms, and FP64 pow costs
+                // ~100 FP64 instructions on this part, so powf (~1e-7 relative)
+                if (o.precision == NDSPH_PREC_FP32)
+                    pr = o.polyk * (double)powf((float)rho, (float)o.gamma);
+                else
+                    pr = o.polyk * pow(rho, o.gamma);
                 cs = sqrt(o.gamma * pr / rho);
             } else if (it != NDSPH_ITYPE_BND) {
                 pr = 0.0;

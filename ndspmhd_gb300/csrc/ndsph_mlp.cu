@@ -31,6 +31,14 @@ __device__ __forceinline__ unsigned pack_bf16(float lo, float hi)
     return *reinterpret_cast<unsigned*>(&v);
 }
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+// hardware tanh (special-function unit, max abs error ~5e-4): inference only,
+// where every activation is rounded to BF16 (relative step 4e-3) anyway
+__device__ __forceinline__ float tanh_fast(float x)
+{
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
 __device__ __forceinline__ void mma_bf16(float (&d)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
                                          unsigned b0, unsigned b1)
@@ -92,10 +100,10 @@ __device__ __forceinline__ void mlp_tile(const MlpFrag& fr, unsigned xa0, unsign
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         const int col = 8 * j + 2 * t;
-        const float h0 = tanhf(c1[j][0] + fr.b1[col]);
-        const float h1 = tanhf(c1[j][1] + fr.b1[col + 1]);
-        const float h2 = tanhf(c1[j][2] + fr.b1[col]);
-        const float h3 = tanhf(c1[j][3] + fr.b1[col + 1]);
+        const float h0 = tanh_fast(c1[j][0] + fr.b1[col]);
+        const float h1 = tanh_fast(c1[j][1] + fr.b1[col + 1]);
+        const float h2 = tanh_fast(c1[j][2] + fr.b1[col]);
+        const float h3 = tanh_fast(c1[j][3] + fr.b1[col + 1]);
         const int s = j >> 1, hiHalf = j & 1;
         a2[s][hiHalf * 2 + 0] = pack_bf16(h0, h1);   // row g
         a2[s][hiHalf * 2 + 1] = pack_bf16(h2, h3);   // row g+8
@@ -116,8 +124,8 @@ __device__ __forceinline__ void mlp_tile(const MlpFrag& fr, unsigned xa0, unsign
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         const int col = 8 * j + 2 * t;
-        pg += fr.w3[col] * bf16r(tanhf(c2[j][0] + fr.b2[col])) + fr.w3[col + 1] * bf16r(tanhf(c2[j][1] + fr.b2[col + 1]));
-        pg8 += fr.w3[col] * bf16r(tanhf(c2[j][2] + fr.b2[col])) + fr.w3[col + 1] * bf16r(tanhf(c2[j][3] + fr.b2[col + 1]));
+        pg += fr.w3[col] * bf16r(tanh_fast(c2[j][0] + fr.b2[col])) + fr.w3[col + 1] * bf16r(tanh_fast(c2[j][1] + fr.b2[col + 1]));
+        pg8 += fr.w3[col] * bf16r(tanh_fast(c2[j][2] + fr.b2[col])) + fr.w3[col + 1] * bf16r(tanh_fast(c2[j][3] + fr.b2[col + 1]));
     }
     pg += __shfl_xor_sync(0xffffffffu, pg, 1);
     pg += __shfl_xor_sync(0xffffffffu, pg, 2);
@@ -220,10 +228,15 @@ __global__ void k_mlp_infer(const MlpFrag* __restrict__ frp, MlpInferArgs a)
     }
 }
 
-// training: each thread one sample; forward/backward in FP32 with the
-// BF16-rounded weights; block gradients summed in shared memory, one atomic
-// per parameter per block
+// training: each thread one sample of a 64-sample tile; forward/backward in
+// FP32 with the BF16-rounded weights.  A block walks several tiles and keeps
+// its share of the parameter gradient in registers (thread q owns parameters
+// q, q+64, ...), so each block adds to a parameter once per launch: the
+// same-address atomics of the gradient, not the arithmetic, bounded a
+// one-tile-per-block launch.
 constexpr int TRAIN_BS = 64;
+constexpr int TRAIN_PPT = (MLP_NPARAM + TRAIN_BS - 1) / TRAIN_BS;   // parameters per thread
+constexpr int TRAIN_MAXBLOCKS = 1024;
 __global__ void __launch_bounds__(TRAIN_BS) k_mlp_grad(const float* __restrict__ p, MlpTrainArgs a,
                                                        float* __restrict__ grad, float* __restrict__ loss)
 {
@@ -240,75 +253,93 @@ __global__ void __launch_bounds__(TRAIN_BS) k_mlp_grad(const float* __restrict__
     }
     const float b3 = p[MLP_OFF_B3];
     __syncthreads();
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const int tid = threadIdx.x;
-    const bool valid = s < a.nbatch;
-    float x[MLP_NIN], y = 0.f;
-    if (valid) {
-        if (a.feats) {      // explicit arrays (tests)
-            for (int k = 0; k < MLP_NIN; k++) x[k] = a.feats[(size_t)s * MLP_NIN + k];
-            y = a.targets[s];
-        } else {            // strided sample of the slots
-            const long long i = ((long long)s * a.stride + a.offset) % a.n;
-            for (int k = 0; k < MLP_NIN; k++) x[k] = (float)a.feat[k][i];
-            y = 100.f * logf((float)a.hconv[i] / (float)a.hpred[i]);
-        }
-        for (int k = 0; k < MLP_NIN; k++) x[k] = bf16r(x[k]);
-    } else {
-        for (int k = 0; k < MLP_NIN; k++) x[k] = 0.f;
-    }
-    float h1[32], h2[32];
-    for (int n = 0; n < 32; n++) {
-        float z = B1[n];
-        for (int k = 0; k < MLP_NIN; k++) z += W1[n * MLP_NIN + k] * x[k];
-        h1[n] = tanhf(z);
-    }
-    for (int n = 0; n < 32; n++) {
-        float z = B2[n];
-        for (int k = 0; k < 32; k++) z += W2[n * 32 + k] * h1[k];
-        h2[n] = tanhf(z);
-    }
-    float out = b3;
-    for (int k = 0; k < 32; k++) out += W3[k] * h2[k];
     const float inv = 1.0f / (float)a.nbatch;
-    const float r = valid ? (out - y) : 0.f;
-    const float dz3 = 2.f * r * inv;
-    if (valid) atomicAdd(loss, r * r * inv);
-    float dz2[32];
-    for (int n = 0; n < 32; n++) dz2[n] = dz3 * W3[n] * (1.f - h2[n] * h2[n]);
-    float dz1[32];
-    for (int k = 0; k < 32; k++) {
-        float acc = 0.f;
-        for (int n = 0; n < 32; n++) acc += dz2[n] * W2[n * 32 + k];
-        dz1[k] = acc * (1.f - h1[k] * h1[k]);
-    }
-    for (int k = 0; k < MLP_NIN; k++) sx[tid][k] = x[k];
-    for (int k = 0; k < 32; k++) { sh1[tid][k] = h1[k]; sh2[tid][k] = h2[k]; sd1[tid][k] = dz1[k]; sd2[tid][k] = dz2[k]; }
-    sdz3[tid] = dz3;
-    __syncthreads();
-    // reduce over the block's samples: thread q owns parameters q, q+128, ...
-    for (int q = tid; q < MLP_NPARAM; q += blockDim.x) {
-        float acc = 0.f;
-        if (q < MLP_OFF_B1) {                              // W1[n][k]
-            const int n = q / MLP_NIN, k = q % MLP_NIN;
-            for (int m = 0; m < TRAIN_BS; m++) acc += sd1[m][n] * sx[m][k];
-        } else if (q < MLP_OFF_W2) {                       // b1[n]
-            const int n = q - MLP_OFF_B1;
-            for (int m = 0; m < TRAIN_BS; m++) acc += sd1[m][n];
-        } else if (q < MLP_OFF_B2) {                       // W2[n][k]
-            const int n = (q - MLP_OFF_W2) / 32, k = (q - MLP_OFF_W2) % 32;
-            for (int m = 0; m < TRAIN_BS; m++) acc += sd2[m][n] * sh1[m][k];
-        } else if (q < MLP_OFF_W3) {                       // b2[n]
-            const int n = q - MLP_OFF_B2;
-            for (int m = 0; m < TRAIN_BS; m++) acc += sd2[m][n];
-        } else if (q < MLP_OFF_B3) {                       // W3[k]
-            const int k = q - MLP_OFF_W3;
-            for (int m = 0; m < TRAIN_BS; m++) acc += sdz3[m] * sh2[m][k];
-        } else {                                           // b3
-            for (int m = 0; m < TRAIN_BS; m++) acc += sdz3[m];
+    float gacc[TRAIN_PPT];
+#pragma unroll
+    for (int u = 0; u < TRAIN_PPT; u++) gacc[u] = 0.f;
+    float lacc = 0.f;
+    const int ntiles = (a.nbatch + TRAIN_BS - 1) / TRAIN_BS;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int s = tile * TRAIN_BS + tid;
+        const bool valid = s < a.nbatch;
+        float x[MLP_NIN], y = 0.f;
+        if (valid) {
+            if (a.feats) {      // explicit arrays (tests)
+                for (int k = 0; k < MLP_NIN; k++) x[k] = a.feats[(size_t)s * MLP_NIN + k];
+                y = a.targets[s];
+            } else {            // strided sample of the slots
+                const long long i = ((long long)s * a.stride + a.offset) % a.n;
+                for (int k = 0; k < MLP_NIN; k++) x[k] = (float)a.feat[k][i];
+                y = 100.f * logf((float)a.hconv[i] / (float)a.hpred[i]);
+            }
+            for (int k = 0; k < MLP_NIN; k++) x[k] = bf16r(x[k]);
+        } else {
+            for (int k = 0; k < MLP_NIN; k++) x[k] = 0.f;
         }
-        atomicAdd(&grad[q], acc);
+        float h1[32], h2[32];
+        for (int n = 0; n < 32; n++) {
+            float z = B1[n];
+            for (int k = 0; k < MLP_NIN; k++) z += W1[n * MLP_NIN + k] * x[k];
+            h1[n] = tanhf(z);
+        }
+        for (int n = 0; n < 32; n++) {
+            float z = B2[n];
+            for (int k = 0; k < 32; k++) z += W2[n * 32 + k] * h1[k];
+            h2[n] = tanhf(z);
+        }
+        float out = b3;
+        for (int k = 0; k < 32; k++) out += W3[k] * h2[k];
+        const float r = valid ? (out - y) : 0.f;
+        const float dz3 = 2.f * r * inv;
+        lacc += r * r * inv;
+        float dz2[32];
+        for (int n = 0; n < 32; n++) dz2[n] = dz3 * W3[n] * (1.f - h2[n] * h2[n]);
+        float dz1[32];
+        for (int k = 0; k < 32; k++) {
+            float acc = 0.f;
+            for (int n = 0; n < 32; n++) acc += dz2[n] * W2[n * 32 + k];
+            dz1[k] = acc * (1.f - h1[k] * h1[k]);
+        }
+        for (int k = 0; k < MLP_NIN; k++) sx[tid][k] = x[k];
+        for (int k = 0; k < 32; k++) { sh1[tid][k] = h1[k]; sh2[tid][k] = h2[k]; sd1[tid][k] = dz1[k]; sd2[tid][k] = dz2[k]; }
+        sdz3[tid] = dz3;
+        __syncthreads();
+        // this tile's contribution to the parameters the thread owns
+#pragma unroll
+        for (int u = 0; u < TRAIN_PPT; u++) {
+            const int q = tid + u * TRAIN_BS;
+            if (q >= MLP_NPARAM) break;
+            float acc = 0.f;
+            if (q < MLP_OFF_B1) {                              // W1[n][k]
+                const int n = q / MLP_NIN, k = q % MLP_NIN;
+                for (int m = 0; m < TRAIN_BS; m++) acc += sd1[m][n] * sx[m][k];
+            } else if (q < MLP_OFF_W2) {                       // b1[n]
+                const int n = q - MLP_OFF_B1;
+                for (int m = 0; m < TRAIN_BS; m++) acc += sd1[m][n];
+            } else if (q < MLP_OFF_B2) {                       // W2[n][k]
+                const int n = (q - MLP_OFF_W2) / 32, k = (q - MLP_OFF_W2) % 32;
+                for (int m = 0; m < TRAIN_BS; m++) acc += sd2[m][n] * sh1[m][k];
+            } else if (q < MLP_OFF_W3) {                       // b2[n]
+                const int n = q - MLP_OFF_B2;
+                for (int m = 0; m < TRAIN_BS; m++) acc += sd2[m][n];
+            } else if (q < MLP_OFF_B3) {                       // W3[k]
+                const int k = q - MLP_OFF_W3;
+                for (int m = 0; m < TRAIN_BS; m++) acc += sdz3[m] * sh2[m][k];
+            } else {                                           // b3
+                for (int m = 0; m < TRAIN_BS; m++) acc += sdz3[m];
+            }
+            gacc[u] += acc;
+        }
+        __syncthreads();   // the next tile overwrites the shared arrays
     }
+#pragma unroll
+    for (int u = 0; u < TRAIN_PPT; u++) {
+        const int q = tid + u * TRAIN_BS;
+        if (q < MLP_NPARAM) atomicAdd(&grad[q], gacc[u]);
+    }
+    for (int off = 16; off > 0; off >>= 1) lacc += __shfl_down_sync(0xffffffffu, lacc, off);
+    if ((tid & 31) == 0) atomicAdd(loss, lacc);
 }
 
 // Adam (Kingma & Ba 2015) on the FP32 master weights
@@ -371,7 +402,9 @@ void launch_mlp_infer(const MlpFrag* fr, const MlpInferArgs& a, cudaStream_t st)
 void launch_mlp_grad(const float* p, const MlpTrainArgs& a, float* grad, float* loss, cudaStream_t st)
 {
     // grad must be zero on entry (the Adam kernel leaves it so); loss accumulates
-    const int blocks = (a.nbatch + TRAIN_BS - 1) / TRAIN_BS;
+    int blocks = (a.nbatch + TRAIN_BS - 1) / TRAIN_BS;
+    if (blocks > TRAIN_MAXBLOCKS) blocks = TRAIN_MAXBLOCKS;
+    if (blocks < 1) blocks = 1;
     NDSPH_COUNT_LAUNCH, k_mlp_grad<<<blocks, TRAIN_BS, 0, st>>>(p, a, grad, loss);
 }
 void launch_mlp_adam(float* p, float* m, float* v, float* g, int step, float lr, cudaStream_t st)

@@ -481,8 +481,17 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
         o.maxdensits == 0;
     double* hdst = FULL ? F.f[HNEXT] : F.f[HH];
     if (!converged) {
-        const int k = atomicAdd(a.ncalc_next, 1);
-        a.S.active_next[k] = i;
+        // warp-aggregated append: the lanes running here together take
+        // consecutive entries in lane order, so the next pass's warps read
+        // runs of neighbouring slots (spatially close particles) instead of
+        // one slot per atomic in arbitrary order
+        const unsigned am = __activemask();
+        const int lane = (int)(threadIdx.x & 31u);
+        const int leader = __ffs(am) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(a.ncalc_next, __popc(am));
+        base = __shfl_sync(am, base, leader);
+        a.S.active_next[base + __popc(am & ((1u << lane) - 1u))] = i;
         if (its <= o.maxdensits) {
             hdst[i] = hnew;
             if (!FULL) {
@@ -573,8 +582,13 @@ __device__ __forceinline__ void load_p(const SweepArgs& a, int j,
 #ifndef NDSPH_RATES_FP32_MINB
 #define NDSPH_RATES_FP32_MINB 4
 #endif
+constexpr int RATES_BS = 128;      // threads per block of the rates sweep
+#ifndef NDSPH_RATES_CHUNK
+#define NDSPH_RATES_CHUNK 32
+#endif
+constexpr int RATES_CHUNK = NDSPH_RATES_CHUNK;   // accepted entries per thread per chunk (FP32 form)
 template <int NDIM, int PREC>
-__global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_rates(SweepArgs a)
+__global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_rates(SweepArgs a)
 {
     typedef typename std::conditional<PREC == NDSPH_PREC_FP64, double, float>::type R;
     // no early return: every lane of the warp takes part in the final
@@ -638,11 +652,13 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
 
     Stencil<NDIM> stn(a.S.cell[i], g);
     const int ncand = live ? a.S.nl_cnt[i] : 0;
-    {
-        for (int k = 0; k < ncand; k++) {
-            const unsigned pk = a.S.nl[(size_t)i * a.nl_stride + k];
+    const unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
+    // the terms of one candidate pair (rates_core, artificial_dissipation,
+    // mhd_terms, drag_forces for the pair (i, j)); returns early when the
+    // pair is out of range
+    auto pair_terms = [&](const unsigned pk) {
             const int j = (int)(pk >> 5);
-            if (j == i) continue;
+            if (j == i) return;
             int d[3], w[3];
             stn.offset((int)(pk & 31u), g, d, w);
             const float4 xsj = a.S.xs[j];
@@ -652,13 +668,13 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
             R dr[3], rij, q2i, q2j, hj1;
             if constexpr (PREC == NDSPH_PREC_FP64) {
                 const float rc = 2.0f * hm * 1.0002f + abs_tol;
-                if (r2f > rc * rc) continue;
+                if (r2f > rc * rc) return;
                 double dx[3], rij2;
-                if (!exact_dx<NDIM>(F, j, xi, w, o, dxbound, dx, rij2)) continue;
+                if (!exact_dx<NDIM>(F, j, xi, w, o, dxbound, dx, rij2)) return;
                 const double hj1d = a.S.h1[j];
                 const double q2id = __dmul_rn(rij2, hi21_d);
                 const double q2jd = __dmul_rn(rij2, __dmul_rn(hj1d, hj1d));
-                if (!(q2id < 4.0 || q2jd < 4.0)) continue;
+                if (!(q2id < 4.0 || q2jd < 4.0)) return;
                 const double rijd = sqrt(rij2);
                 if (rijd <= 2.220446049250313e-16) {
                     if (a.S.itype[j] == typei && rijd < 2.2250738585072014e-308 && typei != 2)
@@ -670,7 +686,7 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
                 }
                 rij = rijd; q2i = q2id; q2j = q2jd; hj1 = hj1d;
             } else {
-                if (!(r2f < 4.0f * hm * hm)) continue;
+                if (!(r2f < 4.0f * hm * hm)) return;
                 const float ir = rsqrtf(fmaxf(r2f, 1e-37f));
                 const float rr = r2f * ir;
                 if (rr <= 1e-30f) {
@@ -843,7 +859,7 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
                 const R dv2 = dvel[0] * dvel[0] + dvel[1] * dvel[1] + dvel[2] * dvel[2];
                 R drd[3];
                 if (rij <= (R)2.220446049250313e-16) {
-                    if (dv2 <= (R)2.220446049250313e-16) continue;
+                    if (dv2 <= (R)2.220446049250313e-16) return;
                     const R ivij = rcp(sqrt(dv2));
                     drd[0] = dvel[0] * ivij; drd[1] = dvel[1] * ivij; drd[2] = dvel[2] * ivij;
                 } else {
@@ -863,7 +879,7 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
                     csg = csi;
                     hcsts = fmax(hcsts, hi / (csg * ts));
                 } else {
-                    if (typej != NDSPH_ITYPE_GAS && typej != NDSPH_ITYPE_BND) continue;
+                    if (typej != NDSPH_ITYPE_GAS && typej != NDSPH_ITYPE_BND) return;
                     R wdj;
                     if constexpr (PREC == 0) wdj = tab_val(a.t.wdrag, tab_index(a.t, q2j));
                     else wdj = tab_valf(a.t.wdragf, tab_indexf(a.t, q2j));
@@ -883,6 +899,50 @@ __global__ void __launch_bounds__(128, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_
                 fz.add(-dragterm * mj * drd[2]);
                 if (typei == NDSPH_ITYPE_GAS) du.add(mj * dragterm_en);
             }
+    };
+    if constexpr (PREC == NDSPH_PREC_FP64) {
+        for (int k = 0; k < ncand; k++) pair_terms(row[k]);
+    } else {
+        // Two phases per chunk of the row: screen the candidates (four row
+        // entries and positions in flight at a time) and keep the accepted
+        // entries in shared memory, then run the pair terms over those only,
+        // so the lanes of a warp do not idle on rejected candidates in the
+        // long part.  The accepted pairs, their order and the screen
+        // arithmetic are those of a single pass over the row.
+        __shared__ unsigned acc_buf[RATES_CHUNK * RATES_BS];
+        unsigned* mine = acc_buf + threadIdx.x;
+        int k = 0;   // a multiple of 4 whenever a vector row load is issued
+        while (k < ncand) {
+            int na = 0;
+            while (na + 4 <= RATES_CHUNK && k < ncand) {
+                unsigned pq[4];
+                int m = 4;
+                if (k + 4 <= ncand) {
+                    const uint4 r4 = *reinterpret_cast<const uint4*>(row + k);
+                    pq[0] = r4.x; pq[1] = r4.y; pq[2] = r4.z; pq[3] = r4.w;
+                } else {
+                    m = ncand - k;
+#pragma unroll
+                    for (int u = 0; u < 4; u++) pq[u] = (u < m) ? row[k + u] : ((unsigned)i << 5);
+                }
+                float4 xq[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) xq[u] = a.S.xs[pq[u] >> 5];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    int d[3], w[3];
+                    stn.offset((int)(pq[u] & 31u), g, d, w);
+                    float dxf[3];
+                    const float r2f = screen_r2<NDIM>(xsi, xq[u], d, g, dxf);
+                    const float hm = fmaxf(hif, xq[u].w);
+                    if ((int)(pq[u] >> 5) != i && r2f < 4.0f * hm * hm) {
+                        mine[na * RATES_BS] = pq[u];
+                        na++;
+                    }
+                }
+                k += m;
+            }
+            for (int q = 0; q < na; q++) pair_terms(mine[q * RATES_BS]);
         }
     }
 
@@ -1041,7 +1101,7 @@ void launch_pack_rates(const SweepArgs& a, cudaStream_t st)
 
 void launch_rates(const SweepArgs& a, cudaStream_t st)
 {
-    const int bs = 128;
+    const int bs = RATES_BS;
     if (a.n <= 0) return;
     const int nb = nblk(a.n, bs);
     if (a.o.precision == NDSPH_PREC_FP64) {
