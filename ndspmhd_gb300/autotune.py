@@ -8,6 +8,8 @@ candidates in every sweep:
   2 max(h_i, h_j) * skin.  A thicker skin lengthens every row (each sweep
   screens more candidates) but lets the rows be kept for more steps.
 * ``nl_reuse`` -- whether a step may keep the previous link (FP32 form).
+* ``stencil`` -- 5: search 5^ndim stencils of half-size cells (FP32 form of
+  one simulation), fewer candidates per row build; 3: 3^ndim stencils.
 * ``graph_cell_margin`` -- batched captured steps size their cells
   2 hmax * margin; a step whose h outgrows the margin leaves the graph and is
   redone on the eager path, a larger margin puts more candidates in each
@@ -29,12 +31,13 @@ import math
 import os
 
 DEVICE_CANDIDATES = [
-    {"nl_reuse": 0, "nl_skin": 1.1},
-    {"nl_reuse": 1, "nl_skin": 1.05},
-    {"nl_reuse": 1, "nl_skin": 1.1},
-    {"nl_reuse": 1, "nl_skin": 1.15},
-    {"nl_reuse": 1, "nl_skin": 1.2},
-    {"nl_reuse": 1, "nl_skin": 1.3},
+    {"nl_reuse": 0, "nl_skin": 1.1, "stencil": 5},
+    {"nl_reuse": 1, "nl_skin": 1.1, "stencil": 3},
+    {"nl_reuse": 1, "nl_skin": 1.05, "stencil": 5},
+    {"nl_reuse": 1, "nl_skin": 1.1, "stencil": 5},
+    {"nl_reuse": 1, "nl_skin": 1.15, "stencil": 5},
+    {"nl_reuse": 1, "nl_skin": 1.2, "stencil": 5},
+    {"nl_reuse": 1, "nl_skin": 1.3, "stencil": 5},
 ]
 BATCHED_CANDIDATES = [
     {"graph_cell_margin": m, "nl_skin": s} for m in (1.02, 1.05, 1.1) for s in (1.05, 1.1, 1.2)

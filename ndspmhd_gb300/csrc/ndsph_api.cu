@@ -82,6 +82,7 @@ struct ndsph_ctx {
     // the cells are then sized 2 hmax * skin so the stencil covers the rows'
     // radius.  The pair sums see the same pairs either way.
     int nl_reuse = 1;            // tuning switch
+    int nl_sw5 = 1;              // tuning switch: FP32 form searches 5-wide stencils of half cells
     bool nl_valid = false;       // order, cells and rows match the device state
     float nl_dmax = 0.f;         // displacement bound of this step (0 after a build)
     float nl_grow = 1.005f;      // room left for Newton-Raphson growth of h
@@ -696,13 +697,32 @@ static int build_grid(ndsph_ctx* ctx, double hmax, const double* lo, const doubl
 {
     Grid& g = ctx->g;
     // cells of 2 hmax skin when the rows may be kept across steps (their
-    // radius is 2 h skin), 2 hmax otherwise; a periodic box too small for
-    // three of the larger cells takes the plain size
-    double cf = reuse_on(ctx) ? (double)ctx->nl_skin : 1.0;
-    for (int d = 0; d < ctx->o.ndim; d++)
-        if (ctx->o.periodic[d] && (long)floor(ctx->o.L[d] / (2.0 * hmax * (1.0 + 1.e-9) * cf)) < 3) cf = 1.0;
+    // radius is 2 h skin), 2 hmax otherwise.  The FP32 form of one simulation
+    // searches a 5^ndim stencil of half-size cells (the candidates screened
+    // per particle roughly halve); the FP64 form keeps the reference's 3^ndim
+    // cells of 2 hmax.  A periodic box needs at least `sw` cells per dim (no
+    // particle may meet two images of another): smaller boxes fall back to
+    // the 3-wide stencil, then to the plain cell size.
+    const double base = 2.0 * hmax * (1.0 + 1.e-9);
+    const double skin_cf = reuse_on(ctx) ? (double)ctx->nl_skin : 1.0;
+    const bool sw5_ok = ctx->nl_sw5 && ctx->o.precision == NDSPH_PREC_FP32 && !ctx->o.batched &&
+                        ctx->n < (1 << 25);
+    const int tries_sw[3] = {5, 3, 3};
+    const double tries_cf[3] = {skin_cf, skin_cf, 1.0};
+    int sw = 3;
+    double cf = 1.0;
+    for (int t = sw5_ok ? 0 : 1; t < 3; t++) {
+        const int reach = (tries_sw[t] - 1) / 2;
+        bool fits = true;
+        for (int d = 0; d < ctx->o.ndim; d++)
+            if (ctx->o.periodic[d] && (long)floor(ctx->o.L[d] / (base * tries_cf[t] / reach)) < tries_sw[t])
+                fits = false;
+        if (fits || t == 2) { sw = tries_sw[t]; cf = tries_cf[t]; break; }
+    }
     ctx->grid_cf = cf;
-    const double cmin = 2.0 * hmax * (1.0 + 1.e-9) * cf;
+    g.sw = sw;
+    g.nlshift = (sw == 5) ? 7 : 5;
+    const double cmin = base * cf / (double)((sw - 1) / 2);
     long ncells = 1;
     for (int d = 0; d < 3; d++) {
         if (d >= ctx->o.ndim) {
@@ -710,7 +730,7 @@ static int build_grid(ndsph_ctx* ctx, double hmax, const double* lo, const doubl
         } else if (ctx->o.periodic[d]) {
             double L = ctx->o.L[d];
             long nc = (long)floor(L / cmin);
-            if (nc < 3) {
+            if (nc < sw) {
                 ctx->err = "periodic box smaller than 3 cells of 2*hmax";
                 return NDSPH_E_CELLS;
             }
@@ -734,6 +754,15 @@ static int build_grid(ndsph_ctx* ctx, double hmax, const double* lo, const doubl
     g.ncells = (int)ncells;
     ctx->cell_hmax = hmax;
     return ensure_cells(ctx, g.ncells);
+}
+
+// distance the search stencil covers around any point of a cell in every
+// dimension: reach cells (every pair within it is found by a build)
+static double stencil_cover(const ndsph_ctx* ctx)
+{
+    double c = 1e300;
+    for (int d = 0; d < ctx->o.ndim; d++) c = std::min(c, ctx->g.cs[d]);
+    return c * (double)((ctx->g.sw - 1) / 2);
 }
 
 static float unord_bitsf(unsigned u)
@@ -772,15 +801,11 @@ static bool try_keep_link(ndsph_ctx* ctx, bool keep_hmax_ghost, int* rc)
     memcpy(&d2, &ctx->h_red->reuse_d2, sizeof d2);
     const float slack = unord_bitsf(ctx->h_red->reuse_slack);
     float csmax = 0.f;
-    double csmin = 1e300;
-    for (int d = 0; d < ctx->o.ndim; d++) {
-        csmax = std::max(csmax, ctx->g.csf[d]);
-        csmin = std::min(csmin, ctx->g.cs[d]);
-    }
+    for (int d = 0; d < ctx->o.ndim; d++) csmax = std::max(csmax, ctx->g.csf[d]);
     // rounding of the FP32 coordinates: a relative and an absolute margin
     const float dmax = sqrtf(d2) * 1.001f + 2e-6f * csmax;
     if (!(hmax > 0.0) || !std::isfinite(hmax) || !(dmax <= slack) ||
-        !(hmax * ctx->nl_grow + dmax <= 0.5 * csmin / (1.0 + 1.e-9)))
+        !(hmax * ctx->nl_grow + dmax <= 0.5 * stencil_cover(ctx) / (1.0 + 1.e-9)))
         return false;
     if (!keep_hmax_ghost) {
         ctx->h_red->hmax_ghost = dbits(hmax);
@@ -934,8 +959,9 @@ static int build_nlist(ndsph_ctx* ctx)
             ctx->nl_valid = reuse_on(ctx) && ctx->grid_cf > 1.0 && ctx->nl_dmax == 0.f;
             return 0;
         }
-        // overflow: grow to the largest count seen (+25%) and rebuild
-        int ns = (h[2] + h[2] / 4 + 8 + 3) & ~3;   // rows of whole 16-byte groups
+        // overflow: grow to the largest count seen (+50%, so a slowly
+        // growing maximum does not reallocate every few steps) and rebuild
+        int ns = (h[2] + h[2] / 2 + 8 + 3) & ~3;   // rows of whole 16-byte groups
         CK(cudaFree(ctx->S.nl));
         ctx->S.nl = nullptr;
         CK(cudaMalloc(&ctx->S.nl, sizeof(unsigned) * (size_t)ns * ctx->cap));
@@ -978,9 +1004,7 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
             CK(cudaMemcpyAsync(&hb, &ctx->red->hmax, sizeof(hb), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
             const double hmax_now = bitsd(hb);
-            double cap = 1e300;
-            for (int d = 0; d < ctx->o.ndim; d++)
-                cap = std::min(cap, 0.5 * ctx->g.cs[d] / (1.0 + 1.e-9) - (double)ctx->nl_dmax);
+            const double cap = 0.5 * stencil_cover(ctx) / (1.0 + 1.e-9) - (double)ctx->nl_dmax;
             if (hmax_now <= cap && !rows_relink) {
                 CK(cudaMemcpyAsync(&ctx->red->hmax_ghost, &hb, sizeof(hb), cudaMemcpyHostToDevice, st));
             } else {
@@ -2186,13 +2210,16 @@ extern "C" int ndsph_set_tuning(ndsph_ctx* ctx, const ndsph_tuning* t)
 {
     GUARD_CTX();
     if (!t || !(t->nl_skin >= 1.0f && t->nl_skin <= 2.0f) || !(t->nl_grow >= 1.0f && t->nl_grow <= 1.5f) ||
-        !(t->graph_cell_margin >= 1.0f && t->graph_cell_margin <= 2.0f) || (t->nl_reuse != 0 && t->nl_reuse != 1)) {
-        ctx->err = "tuning out of range (nl_skin in [1,2], nl_grow in [1,1.5], graph_cell_margin in [1,2])";
+        !(t->graph_cell_margin >= 1.0f && t->graph_cell_margin <= 2.0f) || (t->nl_reuse != 0 && t->nl_reuse != 1) ||
+        (t->stencil != 3 && t->stencil != 5)) {
+        ctx->err = "tuning out of range (nl_skin in [1,2], nl_grow in [1,1.5], graph_cell_margin in [1,2], "
+                   "stencil 3 or 5)";
         return NDSPH_E_ARG;
     }
     ctx->nl_skin = t->nl_skin;
     ctx->nl_reuse = t->nl_reuse;
     ctx->nl_grow = t->nl_grow;
+    ctx->nl_sw5 = (t->stencil == 5) ? 1 : 0;
     if ((double)t->graph_cell_margin != ctx->gmargin) graph_drop(ctx);
     ctx->gmargin = t->graph_cell_margin;
     // rows built with the old radius: the next step links afresh
@@ -2208,6 +2235,7 @@ extern "C" int ndsph_get_tuning(ndsph_ctx* ctx, ndsph_tuning* t)
     t->nl_reuse = ctx->nl_reuse;
     t->nl_grow = ctx->nl_grow;
     t->graph_cell_margin = (float)ctx->gmargin;
+    t->stencil = ctx->nl_sw5 ? 5 : 3;
     return 0;
 }
 

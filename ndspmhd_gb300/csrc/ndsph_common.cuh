@@ -70,9 +70,14 @@ struct Grid {
     int nc[3];          // cells per dim (1 for unused dims)
     int ncells;
     double origin[3];   // lower corner
-    double cs[3];       // cell size per dim (>= 2 hmax)
+    double cs[3];       // cell size per dim (>= 2 hmax / reach)
     double inv_cs[3];
     float csf[3];
+    // search stencil: sw = 3 (cells of >= 2 hmax, reach 1) or 5 (cells of
+    // >= hmax, reach 2); a neighbour-row entry packs (j << nlshift) | offset,
+    // offset = (dx+r) + sw (dy+r) + sw^2 (dz+r), r = (sw-1)/2
+    int sw = 3;
+    int nlshift = 5;
 };
 
 // kernel tables: value and slope per entry, slope(i) = (t(i+1)-t(i))*ddq2table

@@ -418,6 +418,8 @@ extern "C" int ndsph_density_noalloc(const ndsph_opts* opts, const double* d_x, 
     o.ndim = nd;
     Grid g;
     memset(&g, 0, sizeof g);
+    g.sw = 3;
+    g.nlshift = 5;
     const double cmin = 2.0 * hmax * (1.0 + 1.e-9);
     long ncells = 1;
     for (int d = 0; d < 3; d++) {

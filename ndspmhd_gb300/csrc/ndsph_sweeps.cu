@@ -102,6 +102,33 @@ __device__ __forceinline__ KerF kern_cubic(float q, float c)
     return k;
 }
 
+// cell offsets (dx, dy, dz) of a stencil index o = (dx+r) + sw (dy+r) +
+// sw^2 (dz+r), r = (sw-1)/2, sw = 3 or 5; the divisions by 3, 9, 5, 25 are
+// exact multiply-shifts for o < sw^3 (checked for every o)
+template <int NDIM>
+__device__ __forceinline__ void stencil_d(unsigned o, int sw, int d[3])
+{
+    unsigned q, q2;
+    int r;
+    if (sw == 5) {
+        q = (o * 205u) >> 10;    // o / 5
+        q2 = (o * 41u) >> 10;    // o / 25
+        d[0] = (int)(o - 5u * q);
+        d[1] = (int)(q - 5u * q2);
+        r = 2;
+    } else {
+        q = (o * 11u) >> 5;      // o / 3
+        q2 = (o * 57u) >> 9;     // o / 9
+        d[0] = (int)(o - 3u * q);
+        d[1] = (int)(q - 3u * q2);
+        r = 1;
+    }
+    d[2] = (int)q2;
+    d[0] -= r;
+    d[1] = (NDIM >= 2) ? d[1] - r : 0;
+    d[2] = (NDIM >= 3) ? d[2] - r : 0;
+}
+
 // stencil cell with periodic wrap; returns false if outside (open dims)
 template <int NDIM>
 struct Stencil {
@@ -112,14 +139,12 @@ struct Stencil {
         cc[1] = (cell / g.nc[0]) % g.nc[1];
         cc[2] = cell / (g.nc[0] * g.nc[1]);
     }
-    // offset index o in [0, 3^NDIM): d = (o%3-1, (o/3)%3-1, o/9-1)
-    __device__ __forceinline__ bool cell_at(int o, const Grid& g, const DevOpts& op, int& cid, int d[3],
-                                            int w[3]) const
+    // cell at offset d (a stencil of any width) with periodic wrap flags;
+    // false if outside an open dimension
+    __device__ __forceinline__ bool cell_at_d(const int d[3], const Grid& g, const DevOpts& op, int& cid,
+                                              int w[3]) const
     {
         int c[3];
-        d[0] = o % 3 - 1;
-        d[1] = (NDIM >= 2) ? (o / 3) % 3 - 1 : 0;
-        d[2] = (NDIM >= 3) ? o / 9 - 1 : 0;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             w[k] = 0;
@@ -139,12 +164,11 @@ struct Stencil {
         cid = (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
         return true;
     }
-    // offsets and wrap flags of a stored stencil index (the cell exists)
-    __device__ __forceinline__ void offset(int o, const Grid& g, int d[3], int w[3]) const
+    // offsets and wrap flags of a stored row entry's stencil index
+    // o = (dx+r) + sw (dy+r) + sw^2 (dz+r) (the cell exists)
+    __device__ __forceinline__ void offset(unsigned o, const Grid& g, int d[3], int w[3]) const
     {
-        d[0] = o % 3 - 1;
-        d[1] = (NDIM >= 2) ? (o / 3) % 3 - 1 : 0;
-        d[2] = (NDIM >= 3) ? o / 9 - 1 : 0;
+        stencil_d<NDIM>(o, g.sw, d);
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const int c = cc[k] + d[k];
@@ -288,10 +312,11 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
     const unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
     // one candidate: its list entry, position and type, and (FP32 form) its
     // velocity/mass pack, loaded by the caller
+    const unsigned shift = (unsigned)g.nlshift, omask = (1u << shift) - 1u;
     auto pair = [&](unsigned pk, const float4& xsj, int typej, const float4& pvj) {
-        const int j = (int)(pk >> 5);
+        const int j = (int)(pk >> shift);
         int d[3], w[3];
-        stn.offset((int)(pk & 31u), g, d, w);
+        stn.offset(pk & omask, g, d, w);
         float dxf[3];
         const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
         const float hm = FULL ? fmaxf(hif, xsj.w) : hif;
@@ -372,7 +397,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int k = 0; k < ncand; k++) {
             const unsigned pk = row[k];
-            const int j = (int)(pk >> 5);
+            const int j = (int)(pk >> shift);
             pair(pk, a.S.xs[j], a.S.itype[j], z4);
         }
     } else {
@@ -386,10 +411,10 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
             float4 xj[4], vj[4];
             int tj[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) if (k0 + u >= ncand) pk[u] = (unsigned)i << 5;
+            for (int u = 0; u < 4; u++) if (k0 + u >= ncand) pk[u] = (unsigned)i << shift;
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const int j = (int)(pk[u] >> 5);
+                const int j = (int)(pk[u] >> shift);
                 xj[u] = a.S.xs[j];
                 tj[u] = typed ? a.S.itype[j] : typei;
                 vj[u] = a.S.pk_v[j];
@@ -584,7 +609,7 @@ __device__ __forceinline__ void load_p(const SweepArgs& a, int j,
 #endif
 constexpr int RATES_BS = 128;      // threads per block of the rates sweep
 #ifndef NDSPH_RATES_CHUNK
-#define NDSPH_RATES_CHUNK 32
+#define NDSPH_RATES_CHUNK 64
 #endif
 constexpr int RATES_CHUNK = NDSPH_RATES_CHUNK;   // accepted entries per thread per chunk (FP32 form)
 template <int NDIM, int PREC>
@@ -656,11 +681,12 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
     // the terms of one candidate pair (rates_core, artificial_dissipation,
     // mhd_terms, drag_forces for the pair (i, j)); returns early when the
     // pair is out of range
+    const unsigned shift = (unsigned)g.nlshift, omask = (1u << shift) - 1u;
     auto pair_terms = [&](const unsigned pk) {
-            const int j = (int)(pk >> 5);
+            const int j = (int)(pk >> shift);
             if (j == i) return;
             int d[3], w[3];
-            stn.offset((int)(pk & 31u), g, d, w);
+            stn.offset(pk & omask, g, d, w);
             const float4 xsj = a.S.xs[j];
             float dxf[3];
             const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
@@ -923,19 +949,19 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
                 } else {
                     m = ncand - k;
 #pragma unroll
-                    for (int u = 0; u < 4; u++) pq[u] = (u < m) ? row[k + u] : ((unsigned)i << 5);
+                    for (int u = 0; u < 4; u++) pq[u] = (u < m) ? row[k + u] : ((unsigned)i << shift);
                 }
                 float4 xq[4];
 #pragma unroll
-                for (int u = 0; u < 4; u++) xq[u] = a.S.xs[pq[u] >> 5];
+                for (int u = 0; u < 4; u++) xq[u] = a.S.xs[pq[u] >> shift];
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
                     int d[3], w[3];
-                    stn.offset((int)(pq[u] & 31u), g, d, w);
+                    stn.offset(pq[u] & omask, g, d, w);
                     float dxf[3];
                     const float r2f = screen_r2<NDIM>(xsi, xq[u], d, g, dxf);
                     const float hm = fmaxf(hif, xq[u].w);
-                    if ((int)(pq[u] >> 5) != i && r2f < 4.0f * hm * hm) {
+                    if ((int)(pq[u] >> shift) != i && r2f < 4.0f * hm * hm) {
                         mine[na * RATES_BS] = pq[u];
                         na++;
                     }
@@ -1118,20 +1144,32 @@ void launch_rates(const SweepArgs& a, cudaStream_t st)
 
 // ===========================================================================
 // neighbour lists: every candidate j (self included) of slot i with
-// |x_i - x_j| < 2 max(h_i, h_j) skin (+ FP32 margin), from the 3^NDIM stencil.
-// The sweeps then test only these; a list is rebuilt when some h grows by
-// more than `skin` (NR epilogue flag) and after every link.
+// |x_i - x_j| < 2 max(h_i, h_j) skin (+ FP32 margin) inside the search
+// stencil (sw^NDIM cells around i's cell).  The sweeps then test only these;
+// a list is rebuilt when some h grows past its slack (NR epilogue flag) and
+// on every link.
 // ===========================================================================
-// candidates of slot i in the slot range [jb, je); the x offset of the cell
-// of j steps at b1 and b2 (a merged run of three x-adjacent cells) or stays
-// at d0 (b1 = b2 = je); stencil index so0 + 0/1/2 accordingly.  Loads are
-// issued four at a time so that their latencies overlap.
+// distance from a cell-relative coordinate x to the slab of cells at offset
+// dc, [dc cs, (dc+1) cs)
+__device__ __forceinline__ float slab_dist(float x, int dc, float cs)
+{
+    const float lo = (float)dc * cs;
+    return fmaxf(fmaxf(lo - x, x - (lo + cs)), 0.0f);
+}
+
+// candidates of slot i in the slot range [jb, je) of a run of x-adjacent
+// cells starting at x offset dx0: the x offset of j's cell steps up at each
+// of the run's inner cell starts b[0..3] (je where the run is shorter); the
+// stencil index is obase + dx + r.  Loads are issued four at a time so that
+// their latencies overlap.
 template <int NDIM>
-__device__ __forceinline__ void nl_scan_range(const SweepArgs& a, const float4& xsi, float hi, float sk,
-                                              float abs_tol, int jb, int je, int b1, int b2, int d0,
-                                              float oy, float oz, int so0, unsigned* row, int& cnt)
+__device__ __forceinline__ void nl_scan_run(const SweepArgs& a, const float4& xsi, float hi, float sk,
+                                            float abs_tol, int jb, int je, const int b[4], int dx0, float oy,
+                                            float oz, unsigned obase, unsigned* row, int& cnt)
 {
     const Grid& g = a.g;
+    const unsigned shift = (unsigned)g.nlshift;
+    const int r = (g.sw - 1) >> 1;
     for (int j0 = jb; j0 < je; j0 += 4) {
         float4 q[4];
 #pragma unroll
@@ -1140,19 +1178,24 @@ __device__ __forceinline__ void nl_scan_range(const SweepArgs& a, const float4& 
         for (int u = 0; u < 4; u++) {
             const int j = j0 + u;
             if (j >= je) break;
-            const int dx = (j < b1) ? d0 : ((j < b2) ? d0 + 1 : d0 + 2);
+            const int dx = dx0 + (j >= b[0]) + (j >= b[1]) + (j >= b[2]) + (j >= b[3]);
             float r2 = (xsi.x - q[u].x) - (float)dx * g.csf[0];
             r2 = r2 * r2;
             if (NDIM >= 2) { const float t = (xsi.y - q[u].y) - oy; r2 += t * t; }
             if (NDIM >= 3) { const float t = (xsi.z - q[u].z) - oz; r2 += t * t; }
             const float rc = sk * fmaxf(hi, q[u].w) + abs_tol;
             if (r2 > rc * rc) continue;
-            if (cnt < a.nl_stride) row[cnt] = ((unsigned)j << 5) | (unsigned)(so0 + dx - d0);
+            if (cnt < a.nl_stride) row[cnt] = ((unsigned)j << shift) | (obase + (unsigned)(dx + r));
             cnt++;
         }
     }
 }
 
+// One thread per particle.  For each (dy, dz) row of the stencil, the cells
+// whose box lies within the stencil's reach of the particle (r cells: every
+// pair a sweep may need is within it) form a run of x-adjacent cells, one
+// slot range unless it wraps or leaves an open box; rows and cells beyond
+// the reach are skipped.
 template <int NDIM>
 __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
 {
@@ -1162,35 +1205,53 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
     const Grid& g = a.g;
     const float4 xsi = a.S.xs[i];
     const float hi = xsi.w;
+    const float csmin = fminf(g.csf[0], fminf(NDIM >= 2 ? g.csf[1] : g.csf[0], NDIM >= 3 ? g.csf[2] : g.csf[0]));
     const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
     const float sk = 2.0f * a.nl_skin * 1.0002f;
+    const int sw = g.sw, r = (sw - 1) >> 1;
+    const float reach = (float)r * csmin * 1.001f + abs_tol;
+    const float reach2 = reach * reach;
     Stencil<NDIM> stn(a.S.cell[i], g);
-    constexpr int NYZ = (NDIM == 1) ? 1 : (NDIM == 2 ? 3 : 9);
     unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
     int cnt = 0;
-    for (int yz = 0; yz < NYZ; yz++) {
-        // the three x-neighbours at this (dy, dz): one slot range when they are
-        // consecutive cells (no x wrap), else cell by cell
-        int cid[3], dd[3][3], ww[3][3];
-        bool ok[3];
+    const int zlo = (NDIM >= 3) ? -r : 0, ylo = (NDIM >= 2) ? -r : 0;
+    for (int dz = zlo; dz <= -zlo; dz++) {
+        const float ez = (NDIM >= 3) ? slab_dist(xsi.z, dz, g.csf[2]) : 0.f;
+        for (int dy = ylo; dy <= -ylo; dy++) {
+            const float ey = (NDIM >= 2) ? slab_dist(xsi.y, dy, g.csf[1]) : 0.f;
+            const float e2 = ey * ey + ez * ez;
+            if (e2 > reach2) continue;
+            // x cells whose box is within the reach
+            const float ax = sqrtf(reach2 - e2) + abs_tol;
+            const int dx0 = max(-r, (int)floorf((xsi.x - ax) / g.csf[0]));
+            const int dx1 = min(r, (int)floorf((xsi.x + ax) / g.csf[0]));
+            if (dx0 > dx1) continue;
+            unsigned obase = 0;
+            if (NDIM >= 2) obase += (unsigned)((dy + r) * sw);
+            if (NDIM >= 3) obase += (unsigned)((dz + r) * sw * sw);
+            const float oy = (NDIM >= 2) ? (float)dy * g.csf[1] : 0.f;
+            const float oz = (NDIM >= 3) ? (float)dz * g.csf[2] : 0.f;
+            int d[3] = {dx0, dy, dz}, w[3];
+            int c0, c1;
+            const bool ok0 = stn.cell_at_d(d, g, a.o, c0, w);
+            d[0] = dx1;
+            const bool ok1 = stn.cell_at_d(d, g, a.o, c1, w);
+            if (ok0 && ok1 && c1 - c0 == dx1 - dx0) {
+                // consecutive cells: one slot range
+                int b[4];
 #pragma unroll
-        for (int ox = 0; ox < 3; ox++) ok[ox] = stn.cell_at(3 * yz + ox, g, a.o, cid[ox], dd[ox], ww[ox]);
-        const int so0 = 3 * yz;
-        const float oy = (NDIM >= 2) ? (float)(yz % 3 - 1) * g.csf[1] : 0.f;
-        const float oz = (NDIM >= 3) ? (float)(yz / 3 - 1) * g.csf[2] : 0.f;
-        if (ok[0] && ok[1] && ok[2] && cid[1] == cid[0] + 1 && cid[2] == cid[0] + 2) {
-            const int jb = a.cell_start[cid[0]];
-            const int b1 = a.cell_start[cid[1]];
-            const int b2 = a.cell_start[cid[2]];
-            const int je = a.cell_start[cid[2] + 1];
-            nl_scan_range<NDIM>(a, xsi, hi, sk, abs_tol, jb, je, b1, b2, -1, oy, oz, so0, row, cnt);
-        } else {
-#pragma unroll
-            for (int ox = 0; ox < 3; ox++) {
-                if (!ok[ox]) continue;
-                const int jb = a.cell_start[cid[ox]], je = a.cell_start[cid[ox] + 1];
-                nl_scan_range<NDIM>(a, xsi, hi, sk, abs_tol, jb, je, je, je, ox - 1, oy, oz, so0 + ox, row,
-                                    cnt);
+                for (int k = 0; k < 4; k++) b[k] = (k < dx1 - dx0) ? a.cell_start[c0 + k + 1] : 0x7fffffff;
+                nl_scan_run<NDIM>(a, xsi, hi, sk, abs_tol, a.cell_start[c0], a.cell_start[c1 + 1], b, dx0, oy, oz,
+                                  obase, row, cnt);
+            } else {
+                const int bnone[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+                for (int dx = dx0; dx <= dx1; dx++) {
+                    d[0] = dx;
+                    int cid;
+                    if (!stn.cell_at_d(d, g, a.o, cid, w)) continue;
+                    nl_scan_run<NDIM>(a, xsi, hi, sk, abs_tol, a.cell_start[cid], a.cell_start[cid + 1], bnone, dx,
+                                      oy, oz, obase, row, cnt);
+                }
             }
         }
     }
@@ -1201,74 +1262,9 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
     atomicMax(&a.red->nl_maxcnt, cnt);
 }
 
-// Warp-cooperative build: one warp per cell.  The cell's particles (up to 32
-// at a time, one per lane) share their 3^NDIM candidate cells, so each chunk
-// of 32 candidates is loaded once, coalesced, and broadcast by shuffle; the
-// per-particle build above walks the same cells divergently.  Same screen,
-// same order of entries (stencil cell, then slot), so the lists are equal.
-template <int NDIM>
-__global__ void __launch_bounds__(256) k_build_nlist_cell(SweepArgs a)
-{
-    const int c = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (c >= a.g.ncells) return;                 // uniform per warp
-    const Grid& g = a.g;
-    const int hb0 = a.cell_start[c], he = a.cell_start[c + 1];
-    if (hb0 == he) return;
-    const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
-    const float sk = 2.0f * a.nl_skin * 1.0002f;
-    Stencil<NDIM> stn(c, g);
-    constexpr int NST = (NDIM == 1) ? 3 : (NDIM == 2 ? 9 : 27);
-    for (int h0 = hb0; h0 < he; h0 += 32) {
-        const int i = h0 + lane;
-        const bool home = i < he;
-        const float4 xsi = home ? a.S.xs[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        int cnt = 0;
-        for (int so = 0; so < NST; so++) {
-            int cid, d[3], w[3];
-            if (!stn.cell_at(so, g, a.o, cid, d, w)) continue;
-            const int jb = a.cell_start[cid], je = a.cell_start[cid + 1];
-            const float ox = (float)d[0] * g.csf[0];
-            const float oy = (NDIM >= 2) ? (float)d[1] * g.csf[1] : 0.f;
-            const float oz = (NDIM >= 3) ? (float)d[2] * g.csf[2] : 0.f;
-            for (int j0 = jb; j0 < je; j0 += 32) {
-                const int jj = j0 + lane;
-                const float4 xc = (jj < je) ? a.S.xs[jj] : make_float4(0.f, 0.f, 0.f, 0.f);
-                const int m = min(32, je - j0);
-                for (int k = 0; k < m; k++) {
-                    const float cx = __shfl_sync(0xffffffffu, xc.x, k);
-                    const float cy = (NDIM >= 2) ? __shfl_sync(0xffffffffu, xc.y, k) : 0.f;
-                    const float cz = (NDIM >= 3) ? __shfl_sync(0xffffffffu, xc.z, k) : 0.f;
-                    const float cw = __shfl_sync(0xffffffffu, xc.w, k);
-                    const float dx0 = (xsi.x - cx) - ox;
-                    const float dx1 = (NDIM >= 2) ? (xsi.y - cy) - oy : 0.f;
-                    const float dx2 = (NDIM >= 3) ? (xsi.z - cz) - oz : 0.f;
-                    const float r2f = dx0 * dx0 + dx1 * dx1 + dx2 * dx2;
-                    const float rc = sk * fmaxf(xsi.w, cw) + abs_tol;
-                    if (home && !(r2f > rc * rc)) {
-                        if (cnt < a.nl_stride) a.S.nl[(size_t)i * a.nl_stride + cnt] = ((unsigned)(j0 + k) << 5) | (unsigned)so;
-                        cnt++;
-                    }
-                }
-            }
-        }
-        if (home) {
-            a.S.nl_cnt[i] = cnt < a.nl_stride ? cnt : a.nl_stride;
-            a.S.hb[i] = xsi.w;
-            if (cnt > a.nl_stride) a.red->nl_overflow = 1;
-            atomicMax(&a.red->nl_maxcnt, cnt);
-        }
-    }
-}
-
 void launch_build_nlist(const SweepArgs& a, cudaStream_t st)
 {
     if (a.n <= 0) return;
-    const long long threads = (long long)a.g.ncells * 32;
-    const int nb = (int)((threads + 255) / 256);
-    (void)nb;
-    // per-particle build (rows are contiguous per particle, so its appends
-    // merge in L2); the warp-per-cell variant above is kept for comparison
     const int nbp = nblk(a.n, 128);
     if (a.o.ndim == 1) NDSPH_COUNT_LAUNCH, k_build_nlist<1><<<nbp, 128, 0, st>>>(a);
     else if (a.o.ndim == 2) NDSPH_COUNT_LAUNCH, k_build_nlist<2><<<nbp, 128, 0, st>>>(a);
@@ -1293,12 +1289,16 @@ __global__ void k_neigh(SweepArgs a, int mode, const long long* offsets, long lo
     const int typei = a.S.itype[i];
     const double dxbound = 2.0 * bitsd(a.red->hmax_ghost);
     Stencil<NDIM> stn(a.S.cell[i], a.g);
-    constexpr int NST = (NDIM == 1) ? 3 : (NDIM == 2 ? 9 : 27);
+    const int sw = a.g.sw, r = (sw - 1) >> 1;
+    const int nst = (NDIM == 1) ? sw : (NDIM == 2 ? sw * sw : sw * sw * sw);
     long long k = offsets ? offsets[a.S.id[i]] : 0;
     long long cnt = 0;
-    for (int so = 0; so < NST; so++) {
+    for (int so = 0; so < nst; so++) {
         int cid, d[3], w[3];
-        if (!stn.cell_at(so, a.g, a.o, cid, d, w)) continue;
+        d[0] = so % sw - r;
+        d[1] = (NDIM >= 2) ? (so / sw) % sw - r : 0;
+        d[2] = (NDIM >= 3) ? so / (sw * sw) - r : 0;
+        if (!stn.cell_at_d(d, a.g, a.o, cid, w)) continue;
         for (int j = a.cell_start[cid]; j < a.cell_start[cid + 1]; j++) {
             if (j == i) continue;
             if (!type_match(typei, a.S.itype[j])) continue;

@@ -42,6 +42,14 @@ module gpu_sph
     integer(c_int32_t) :: its, ncalctotal, nsteps, nrelink
  end type
 
+ ! neighbour-search settings (ndsph_tuning); optional, see ndsph_set_tuning
+ type, bind(C) :: ndsph_tuning_t
+    real(c_float)      :: nl_skin
+    integer(c_int32_t) :: nl_reuse
+    real(c_float)      :: nl_grow, graph_cell_margin
+    integer(c_int32_t) :: stencil
+ end type
+
  interface
     integer(c_int) function ndsph_init(ctx, opts, nmax) bind(C, name="ndsph_init")
       import :: c_ptr, c_int, c_int32_t, ndsph_opts_t
@@ -80,6 +88,16 @@ module gpu_sph
       type(ndsph_particles_t), intent(inout) :: p
       integer(c_int32_t), value              :: npart
       type(ndsph_dt_t), intent(inout)        :: dts
+    end function
+    integer(c_int) function ndsph_set_tuning(ctx, t) bind(C, name="ndsph_set_tuning")
+      import :: c_ptr, c_int, ndsph_tuning_t
+      type(c_ptr), value                :: ctx
+      type(ndsph_tuning_t), intent(in)  :: t
+    end function
+    integer(c_int) function ndsph_get_tuning(ctx, t) bind(C, name="ndsph_get_tuning")
+      import :: c_ptr, c_int, ndsph_tuning_t
+      type(c_ptr), value                :: ctx
+      type(ndsph_tuning_t), intent(out) :: t
     end function
  end interface
 

@@ -65,6 +65,24 @@ def test_neighbour_sets_bit_exact(initialised):
     g.close()
 
 
+def test_neighbour_sets_fp32_contexts(initialised):
+    """An FP32-form context links on its own cells (5^ndim stencils of cells
+    of hmax x skin where the box allows it); ndsph_neighbour_csr decides in
+    exact FP64 over that stencil, so the sets must still equal the
+    oracle's."""
+    from ndspmhd_gb300.gpu import GpuSPH
+    name, o, orc = initialised
+    g = GpuSPH(dict(o, precision=1), orc.snapshot())
+    g.set_linklist()
+    for mode in (0, 1):
+        go, gn = g.neighbours(mode)
+        oo, on = orc.neighbours(mode)
+        gs, os_ = csr_sets(go, gn), csr_sets(oo, on)
+        bad = [i for i in range(len(gs)) if not np.array_equal(gs[i], os_[i])]
+        assert not bad, f"{name} mode {mode}: {len(bad)} particles differ, first {bad[:5]}"
+    g.close()
+
+
 def test_iterate_density(initialised):
     from ndspmhd_gb300.gpu import GpuSPH
     name, o, orc = initialised

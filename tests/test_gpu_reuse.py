@@ -5,13 +5,20 @@ every particle satisfies h + dmax <= skin * h_build (dmax: the largest
 displacement since the rows were built).  The pairs summed are then the same
 as after a fresh link, so results agree with the relink-every-step run within
 the FP32 form's rounding: |d| / max(|ref|, rms(ref), physical scale) <= 1e-5
-after a few steps, and the union-criterion neighbour counts of the first
-density pass agree except for pairs within FP32 rounding of the cut-off
-(cell-relative coordinates are taken from different cell corners), which
-may go either way and stay rare -- a row missing real neighbours would show
-up as a one-sided excess of lower counts.
+after a few steps.  A row missing a neighbour inside the kernel support
+would move that particle's density by ~1/60 and its force by far more than
+that bound.  (numneigh is not compared: the reference defines it by the
+union criterion in the first Newton-Raphson pass and by q_i < 2 in later
+ones, so a particle converging one pass earlier in one run reports the other
+count.)
+
+The runs use tolh = 1e-6.  At the default 1e-3 a particle whose
+Newton-Raphson residual sits at the threshold converges one pass earlier in
+one run than in the other (the two differ by rounding), which legitimately
+moves its h by up to ~tolh and its neighbours' forces by ~1e-4 -- the same
+happens between the FP32 and FP64 forms; a tight tolerance puts every h at
+the root, so the comparison sees the pair sums alone.
 """
-import numpy as np
 import pytest
 
 from ndspmhd_gb300 import configs
@@ -27,6 +34,7 @@ def _initial(case):
     o, p = case()
     o = dict(o)
     o["precision"] = 1
+    o["tolh"] = 1e-6
     g = GpuSPH(o, configs.full_state(p, o["ndim"]))
     g.primitive2conservative()
     st = {k: v.copy() for k, v in g.state.items()}
@@ -68,13 +76,11 @@ def test_host_steps_with_reuse_same_pairs(gpulib):
     and one that relinks on every call take the same inputs at every step."""
     from ndspmhd_gb300.gpu import GpuSPH
     o, st = _initial(lambda: configs.mhd_box_3d(20, seed=9))
-    n = st["x"].shape[0]
     ga = GpuSPH(o, {k: v.copy() for k, v in st.items()})
     ga.set_tuning(nl_reuse=1)
     ga.set_dt(0.0)
     cur = {k: v.copy() for k, v in st.items()}
     dt, t = 0.0, 0.0
-    lower = higher = 0
     for step in range(8):
         ga.rebind({k: v.copy() for k, v in cur.items()})
         ga.dt.dt, ga.dt.time, ga.dt.nsteps = dt, t, step
@@ -83,10 +89,6 @@ def test_host_steps_with_reuse_same_pairs(gpulib):
         gb.set_tuning(nl_reuse=0)
         gb.dt.dt, gb.dt.time, gb.dt.nsteps = dt, t, step
         gb.step()
-        na, nb = ga.state["numneigh"], gb.state["numneigh"]
-        assert np.max(np.abs(na.astype(np.int64) - nb)) <= 1, step
-        lower += int(np.sum(na < nb))
-        higher += int(np.sum(na > nb))
         errs, bad = compare_fields(ga.state, gb.state, ["rho", "hh", "force", "dudt", "dBevoldt"], 1e-5)
         assert not bad, (step, errs)
         cur = {k: v.copy() for k, v in gb.state.items()}
@@ -95,8 +97,6 @@ def test_host_steps_with_reuse_same_pairs(gpulib):
     reused = ga.timing()["nl_reused"]
     ga.close()
     assert reused >= 4, reused
-    # near-cut rounding only: rare, and not one-sided
-    assert lower <= max(4, 1e-4 * n * 8), (lower, higher)
 
 
 def test_reuse_check_falls_back_to_relink(gpulib):
@@ -113,14 +113,26 @@ def test_reuse_check_falls_back_to_relink(gpulib):
     assert not bad, errs
 
 
+def test_stencils_agree(gpulib):
+    """5-wide stencils of half-size cells (the FP32 default) and 3-wide
+    stencils of full cells find the same pairs: device runs agree within the
+    FP32 form's rounding."""
+    o, st = _initial(lambda: configs.mhd_box_3d(24, seed=6))
+    a, ta, _ = _device_run(o, st, 6, stencil=5)
+    b, tb, _ = _device_run(o, st, 6, stencil=3)
+    errs, bad = compare_fields(a, b, FIELDS, 1e-5)
+    assert not bad, errs
+
+
 def test_tuning_rejects_out_of_range(gpulib):
     from ndspmhd_gb300.gpu import GpuSPH, NdsphError
     o, p = configs.mhd_box_3d(10, seed=1)
     g = GpuSPH(o, configs.full_state(p, 3))
     t0 = g.get_tuning()
     assert t0["nl_reuse"] == 1 and abs(t0["nl_skin"] - 1.1) < 1e-6
+    assert t0["stencil"] == 5
     for bad in ({"nl_skin": 0.9}, {"nl_skin": 2.5}, {"nl_grow": 0.99}, {"graph_cell_margin": 0.5},
-                {"nl_reuse": 2}):
+                {"nl_reuse": 2}, {"stencil": 4}):
         with pytest.raises(NdsphError):
             g.set_tuning(**bad)
     assert g.get_tuning() == t0
