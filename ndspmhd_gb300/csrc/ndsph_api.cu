@@ -87,6 +87,8 @@ struct ndsph_ctx {
     float nl_dmax = 0.f;         // displacement bound of this step (0 after a build)
     float nl_grow = 1.005f;      // room left for Newton-Raphson growth of h
     int nl_reused = 0;           // steps that kept the last link
+    int keep_fails = 0;          // consecutive failed checks
+    int keep_skip = 0;           // steps left before the check is tried again
     // learned-h predictor
     float* mlp_p = nullptr;      // FP32 master weights
     float* mlp_m = nullptr;      // Adam moments
@@ -782,6 +784,13 @@ static bool try_keep_link(ndsph_ctx* ctx, bool keep_hmax_ghost, int* rc)
 {
     *rc = 0;
     if (!reuse_on(ctx) || !ctx->nl_valid || !ctx->linked || ctx->grid_cf <= 1.0 || !ctx->S.nl) return false;
+    // where particles outrun the skin every step (a supersonic flow), the
+    // check fails each time: after two failures in a row it is tried again
+    // only every eighth step
+    if (ctx->keep_skip > 0) {
+        ctx->keep_skip--;
+        return false;
+    }
     cudaStream_t st = ctx->st;
     Reduce* r = ctx->red;
     const unsigned init[2] = {0u, 0xffffffffu};
@@ -805,8 +814,14 @@ static bool try_keep_link(ndsph_ctx* ctx, bool keep_hmax_ghost, int* rc)
     // rounding of the FP32 coordinates: a relative and an absolute margin
     const float dmax = sqrtf(d2) * 1.001f + 2e-6f * csmax;
     if (!(hmax > 0.0) || !std::isfinite(hmax) || !(dmax <= slack) ||
-        !(hmax * ctx->nl_grow + dmax <= 0.5 * stencil_cover(ctx) / (1.0 + 1.e-9)))
+        !(hmax * ctx->nl_grow + dmax <= 0.5 * stencil_cover(ctx) / (1.0 + 1.e-9))) {
+        if (++ctx->keep_fails >= 2) {
+            ctx->keep_skip = 7;
+            ctx->keep_fails = 0;
+        }
         return false;
+    }
+    ctx->keep_fails = 0;
     if (!keep_hmax_ghost) {
         ctx->h_red->hmax_ghost = dbits(hmax);
         if (cudaMemcpyAsync(&r->hmax_ghost, &ctx->h_red->hmax_ghost, sizeof(unsigned long long),
@@ -2224,6 +2239,7 @@ extern "C" int ndsph_set_tuning(ndsph_ctx* ctx, const ndsph_tuning* t)
     ctx->gmargin = t->graph_cell_margin;
     // rows built with the old radius: the next step links afresh
     ctx->nl_valid = false;
+    ctx->keep_fails = ctx->keep_skip = 0;
     return 0;
 }
 
