@@ -265,15 +265,23 @@ def run_learned(n1d: int, steps: int, warmup: int):
     """Learned-h workload: isothermal log-normal turbulent box, tolh = 1e-4,
     FP32 pairs; NR density work and step rate with the reference's predictor
     vs the learned predictor (trained online from step 0)."""
-    from ndspmhd_gb300 import configs
+    from ndspmhd_gb300 import autotune, configs
     from ndspmhd_gb300.gpu import GpuSPH
     out = {}
     o, p = configs.turbulent_box_3d(n1d)
+    # search settings from the autotuner on this workload (reference predictor),
+    # the same for both runs
+    g = GpuSPH(dict(o, precision=1, learned_h=0), configs.full_state(p, 3))
+    g.primitive2conservative()
+    st0 = {k: v.copy() for k, v in g.state.items()}
+    g.close()
+    tuned = autotune.tune_device(dict(o, precision=1, learned_h=0), st0, steps=6, warmup=3)
     for learned in (0, 1):
         o2 = dict(o)
         o2["precision"] = 1
         o2["learned_h"] = learned
         g = GpuSPH(o2, configs.full_state(p, 3))
+        g.set_tuning(**tuned["tuning"])
         g.primitive2conservative()
         g.dev_upload()
         g.set_dt(0.0)
@@ -292,6 +300,7 @@ def run_learned(n1d: int, steps: int, warmup: int):
                     "value": round(g.n * steps / (tot * 1e-3), 1), "ms_per_step": round(tot / steps, 3)}
         g.close()
     out["config"] = f"isothermal turbulent box {n1d}^3, tolh 1e-4, FP32 pairs, {warmup} warm-up steps then {steps} timed"
+    out["search_tuning"] = tuned["tuning"]
     out["work_reduction"] = round(1 - out["learned"]["particle_passes_per_step"] /
                                   out["predictor"]["particle_passes_per_step"], 4)
     return out
@@ -307,11 +316,21 @@ def run_dust(n1d: int, steps: int, warmup: int, nset: int = 8):
     rng = np.random.default_rng(99)
     eps = np.exp(rng.uniform(np.log(0.01), np.log(1.0), nset))
     ts = np.exp(rng.uniform(np.log(1e-3), np.log(1.0), nset))
+    from ndspmhd_gb300 import autotune
     tot_ms, tot_upd, dtdrag = 0.0, 0, []
+    tuning = None
     for k in range(nset):
         o, p = configs.dust_gas_box_3d(n1d, eps=float(eps[k]), tstop=float(ts[k]), seed=77 + k)
         o["precision"] = 1
+        if tuning is None:
+            # search settings tuned on the first setting, kept for the batch
+            g = GpuSPH(o, configs.full_state(p, 3))
+            g.primitive2conservative()
+            st0 = {kk: v.copy() for kk, v in g.state.items()}
+            g.close()
+            tuning = autotune.tune_device(o, st0, steps=6, warmup=3)["tuning"]
         g = GpuSPH(o, configs.full_state(p, 3))
+        g.set_tuning(**tuning)
         g.primitive2conservative()
         g.dev_upload()
         g.set_dt(0.0)
@@ -323,6 +342,7 @@ def run_dust(n1d: int, steps: int, warmup: int, nset: int = 8):
         g.close()
     return {"value": round(tot_upd / (tot_ms * 1e-3), 1), "unit": UNIT, "ms_per_step_per_setting": round(tot_ms / (steps * nset), 3),
             "config": f"gas+dust box 2x{n1d}^3, {nset} (eps, t_s) settings, eps in [0.01,1], t_s in [1e-3,1], FP32 pairs",
+            "search_tuning": tuning,
             "dtdrag_range": [min(dtdrag), max(dtdrag)]}
 
 

@@ -182,6 +182,39 @@ __host__ __device__ inline unsigned ord_bitsf(float v)
 #endif
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
+// block-wide max of non-negative doubles through their bit patterns (the
+// integer pipe orders them; the FP64 pipe is narrow on this part); every
+// thread of the block must call it; the result is valid in thread 0
+__device__ inline unsigned long long block_max_bits(unsigned long long b)
+{
+    __shared__ unsigned long long sm_bits[32];
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_down_sync(0xffffffffu, b, off);
+        b = o > b ? o : b;
+    }
+    const int warp = threadIdx.x >> 5;
+    __syncthreads();   // a previous call's readers are done with sm_bits
+    if ((threadIdx.x & 31) == 0) sm_bits[warp] = b;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = sm_bits[w] > b ? sm_bits[w] : b;
+    return b;
+}
+__device__ inline unsigned long long block_min_bits(unsigned long long b)
+{
+    __shared__ unsigned long long sm_bits_min[32];
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_down_sync(0xffffffffu, b, off);
+        b = o < b ? o : b;
+    }
+    const int warp = threadIdx.x >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sm_bits_min[warp] = b;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = sm_bits_min[w] < b ? sm_bits_min[w] : b;
+    return b;
+}
 __device__ inline void raise_err(Reduce* r, int code, int idx)
 {
     if (atomicCAS(&r->err, 0, code) == 0) r->err_index = idx;

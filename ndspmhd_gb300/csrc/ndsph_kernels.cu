@@ -313,7 +313,7 @@ void launch_xs(FieldPtrs F, Side S, Grid g, DevOpts o, int n, cudaStream_t st)
 __global__ void k_reuse_check(FieldPtrs F, Side S, Grid g, DevOpts o, int n, float skin, float grow, Reduce* red)
 {
     __shared__ float sd[8], ss[8];
-    __shared__ double sh[8];
+    __shared__ unsigned long long sh[8];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     float d2 = 0.f, slack = 3.0e38f;
     double h = 0.0;
@@ -341,23 +341,26 @@ __global__ void k_reuse_check(FieldPtrs F, Side S, Grid g, DevOpts o, int n, flo
         if (!(d2 <= 3.0e38f)) d2 = 3.0e38f;          // non-finite position: fails the check
         if (!(slack >= -3.0e38f)) slack = -3.0e38f;
     }
+    // h as its bit pattern: h >= 0 orders like its bits (integer pipe)
+    unsigned long long hb = dbits(h);
     for (int off = 16; off > 0; off >>= 1) {
         d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, off));
         slack = fminf(slack, __shfl_down_sync(0xffffffffu, slack, off));
-        h = fmax(h, __shfl_down_sync(0xffffffffu, h, off));
+        const unsigned long long o = __shfl_down_sync(0xffffffffu, hb, off);
+        hb = o > hb ? o : hb;
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) { sd[warp] = d2; ss[warp] = slack; sh[warp] = h; }
+    if (lane == 0) { sd[warp] = d2; ss[warp] = slack; sh[warp] = hb; }
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
             d2 = fmaxf(d2, sd[w]);
             slack = fminf(slack, ss[w]);
-            h = fmax(h, sh[w]);
+            hb = sh[w] > hb ? sh[w] : hb;
         }
         atomicMax(&red->reuse_d2, __float_as_uint(d2));
         atomicMin(&red->reuse_slack, ord_bitsf(slack));
-        atomicMax(&red->hmax, dbits(h));
+        atomicMax(&red->hmax, hb);
     }
 }
 void launch_reuse_check(FieldPtrs F, Side S, Grid g, DevOpts o, int n, float skin, float grow, Reduce* red,
@@ -572,8 +575,10 @@ __global__ void k_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
         if (k < n && st > 0.0) atomic_max_pos(&o.sim_red[(size_t)S.sim[k] * SIMRED + SR_STRESS], st);
         return;
     }
-    for (int off = 16; off > 0; off >>= 1) st = fmax(st, __shfl_down_sync(0xffffffffu, st, off));
-    if ((threadIdx.x & 31) == 0 && st > 0.0) atomic_max_pos(&red->stressmax, st);
+    // one atomic per block (one per warp serialised ~65k same-address
+    // atomics at the 128^3 box)
+    const unsigned long long sb = block_max_bits(dbits(st));   // st >= 0
+    if (threadIdx.x == 0 && sb != 0ull) atomicMax(&red->stressmax, sb);
 }
 void launch_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st)
 {
@@ -651,9 +656,51 @@ __global__ void k_predictor2(FieldPtrs F, Side S, DevOpts o, int n, const Reduce
             if (o.iavlim[d] != 0) F.f[AL0 + d][i] = fmin(F.f[ALIN0 + d][i] + dt * F.f[DALIN0 + d][i], 1.0);
     }
 }
+// save and predictor in one pass, for states without fixed particles (no
+// particle reads another's saved velocity and force, so no grid-wide order
+// is needed between the two); same arithmetic as k_predictor + k_predictor2
+__global__ void k_predictor_fused(FieldPtrs F, Side S, DevOpts o, int n, const Reduce* red)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double dt = o.batched ? o.sim_dt[S.sim[i]] : red->dt;
+    double x[3], v[3], f[3], be[3], db[3], al[3], dal[3];
+    for (int d = 0; d < o.ndim; d++) x[d] = F.f[X0 + d][i];
+    for (int d = 0; d < 3; d++) {
+        v[d] = F.f[V0 + d][i]; f[d] = F.f[F0 + d][i]; be[d] = F.f[BE0 + d][i]; db[d] = F.f[DB0 + d][i];
+        al[d] = F.f[AL0 + d][i]; dal[d] = F.f[DAL0 + d][i];
+    }
+    const double h = F.f[HH][i], en = F.f[EN][i], rho = F.f[RHO][i], dh = F.f[DHDT][i], den = F.f[DENDT][i];
+    // save (stepND_leapfrog_mhd.f90:70-101)
+    for (int d = 0; d < o.ndim; d++) F.f[XIN0 + d][i] = x[d];
+    for (int d = 0; d < 3; d++) {
+        F.f[VIN0 + d][i] = v[d]; F.f[BIN0 + d][i] = be[d]; F.f[ALIN0 + d][i] = al[d];
+        F.f[FIN0 + d][i] = f[d]; F.f[DBIN0 + d][i] = db[d]; F.f[DALIN0 + d][i] = dal[d];
+    }
+    F.f[HIN][i] = h; F.f[ENIN][i] = en; F.f[RHOIN][i] = rho; F.f[DHIN][i] = dh; F.f[DENIN][i] = den;
+    const int t = S.itype[i];
+    if (t == NDSPH_ITYPE_BND || t == NDSPH_ITYPE_BNDDUST) {
+        // moved by its own saved velocity and force; everything else held
+        for (int d = 0; d < o.ndim; d++) F.f[X0 + d][i] = x[d] + dt * v[d] + 0.5 * dt * dt * f[d];
+        return;
+    }
+    for (int d = 0; d < o.ndim; d++) F.f[X0 + d][i] = x[d] + dt * v[d] + 0.5 * dt * dt * f[d];
+    for (int d = 0; d < 3; d++) F.f[V0 + d][i] = (v[d] + dt * f[d]) / (1.0 + 0.0);
+    if (o.imhd != 0)
+        for (int d = 0; d < 3; d++) F.f[BE0 + d][i] = be[d] + dt * db[d];
+    F.f[HH][i] = h + dt * dh;
+    if (o.iener != 0) F.f[EN][i] = en + dt * den;
+    for (int d = 0; d < 3; d++)
+        if (o.iavlim[d] != 0) F.f[AL0 + d][i] = fmin(al[d] + dt * dal[d], 1.0);
+}
+
 void launch_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st)
 {
     if (n <= 0) return;
+    if (!o.has_fixed) {
+        NDSPH_COUNT_LAUNCH, k_predictor_fused<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+        return;
+    }
     NDSPH_COUNT_LAUNCH, k_predictor<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
     NDSPH_COUNT_LAUNCH, k_predictor2<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
 }

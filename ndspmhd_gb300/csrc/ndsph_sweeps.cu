@@ -1080,20 +1080,20 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
         }
         return;
     }
-    for (int off = 16; off > 0; off >>= 1) {
-        rdtc = fmin(rdtc, __shfl_down_sync(0xffffffffu, rdtc, off));
-        rdtav = fmin(rdtav, __shfl_down_sync(0xffffffffu, rdtav, off));
-        rvs = fmax(rvs, __shfl_down_sync(0xffffffffu, rvs, off));
-        rts = fmin(rts, __shfl_down_sync(0xffffffffu, rts, off));
-        fonh = fmax(fonh, __shfl_down_sync(0xffffffffu, fonh, off));
-    }
+    // block-wide reductions on the bit patterns of the non-negative values,
+    // one atomic per block and quantity
     (void)hcsts;
-    if ((threadIdx.x & 31) == 0) {
-        atomic_min_pos(&a.red->dtcourant, rdtc);
-        atomic_min_pos(&a.red->dtav, rdtav);
-        atomic_max_pos(&a.red->vsigmax, rvs);
-        atomic_min_pos(&a.red->ts_min, rts);
-        atomic_max_pos(&a.red->fhmax, fonh);
+    const unsigned long long b_dtc = block_min_bits(dbits(fmax(rdtc, 0.0)));
+    const unsigned long long b_dtav = block_min_bits(dbits(fmax(rdtav, 0.0)));
+    const unsigned long long b_vs = block_max_bits(dbits(fmax(rvs, 0.0)));
+    const unsigned long long b_ts = block_min_bits(dbits(fmax(rts, 0.0)));
+    const unsigned long long b_fh = block_max_bits(dbits(fmax(fonh, 0.0)));
+    if (threadIdx.x == 0) {
+        atomicMin(&a.red->dtcourant, b_dtc);
+        atomicMin(&a.red->dtav, b_dtav);
+        atomicMax(&a.red->vsigmax, b_vs);
+        atomicMin(&a.red->ts_min, b_ts);
+        atomicMax(&a.red->fhmax, b_fh);
     }
 }
 
