@@ -571,7 +571,7 @@ static int download_aos(ndsph_ctx* ctx, double* host, int f0, int ncomp, int str
 {
     if (!host) return 0;
     if (double* direct = (double*)host_view(ctx, host)) {
-        launch_slab_to_aos(direct, stride, ctx->F, f0, ncomp, ctx->S.id, n, ctx->st);
+        launch_slab_to_aos(direct, stride, ctx->F, f0, ncomp, ctx->S.pos_of_id, n, ctx->st);
         return 0;
     }
     const size_t need = (size_t)stride * n;
@@ -587,7 +587,7 @@ static int download_aos(ndsph_ctx* ctx, double* host, int f0, int ncomp, int str
     }
     double* dst = ctx->d_arena + ctx->arena_used;
     ctx->arena_used += need;
-    launch_slab_to_aos(dst, stride, ctx->F, f0, ncomp, ctx->S.id, n, ctx->st);
+    launch_slab_to_aos(dst, stride, ctx->F, f0, ncomp, ctx->S.pos_of_id, n, ctx->st);
     CK(cudaEventRecord(ctx->ev_dl, ctx->st));
     CK(cudaStreamWaitEvent(ctx->st_cp, ctx->ev_dl, 0));
     CK(cudaMemcpyAsync(host, dst, sizeof(double) * need, cudaMemcpyDeviceToHost, ctx->st_cp));
@@ -604,9 +604,9 @@ static int download_int(ndsph_ctx* ctx, int* host, const int* dsrc, int n, bool 
 {
     if (!host) return download_end(ctx);
     if (int* direct = (int*)host_view(ctx, host)) {
-        launch_slab_to_int(direct, dsrc, ctx->S.id, n, ctx->st);
+        launch_slab_to_int(direct, dsrc, ctx->S.pos_of_id, n, ctx->st);
     } else {
-        launch_slab_to_int(ctx->d_istage, dsrc, ctx->S.id, n, ctx->st);
+        launch_slab_to_int(ctx->d_istage, dsrc, ctx->S.pos_of_id, n, ctx->st);
         CK(cudaMemcpyAsync(host, ctx->d_istage, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, ctx->st));
     }
     CK(cudaStreamSynchronize(ctx->st));
@@ -1194,7 +1194,7 @@ static int download_density_group(ndsph_ctx* ctx, ndsph_particles* p)
         const size_t need = ((size_t)n * sizeof(int) + sizeof(double) - 1) / sizeof(double);
         if (ctx->arena_used + need <= ctx->arena_cap) {
             ctx->arena_used += need;
-            launch_slab_to_int(dst, ctx->S.numneigh, ctx->S.id, n, ctx->st);
+            launch_slab_to_int(dst, ctx->S.numneigh, ctx->S.pos_of_id, n, ctx->st);
             CK(cudaEventRecord(ctx->ev_dl, ctx->st));
             CK(cudaStreamWaitEvent(ctx->st_cp, ctx->ev_dl, 0));
             CK(cudaMemcpyAsync(p->numneigh, dst, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, ctx->st_cp));

@@ -386,18 +386,22 @@ void launch_aos_to_slab(FieldPtrs F, int f0, int ncomp, const double* aos, int s
     if (n > 0) NDSPH_COUNT_LAUNCH, k_aos_to_slab<<<nblk(n, 256), 256, 0, st>>>(F, f0, ncomp, aos, stride, id, n);
 }
 
+// gather in host order: particle p comes from slot pos[p] (pos = inverse of
+// the slot -> particle map), so the stores -- to a staging buffer or straight
+// to the caller's array over the CPU-GPU link -- are coalesced and the
+// scattered reads hit the slab's L2-resident field
 __global__ void k_slab_to_aos(double* __restrict__ aos, int stride, FieldPtrs F, int f0, int ncomp,
-                              const int* __restrict__ id, int n)
+                              const int* __restrict__ pos, int n)
 {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    int dst = id ? id[k] : k;
-    for (int c = 0; c < ncomp; c++) aos[(size_t)dst * stride + c] = F.f[f0 + c][k];
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int src = pos ? pos[p] : p;
+    for (int c = 0; c < ncomp; c++) aos[(size_t)p * stride + c] = F.f[f0 + c][src];
 }
-void launch_slab_to_aos(double* aos, int stride, FieldPtrs F, int f0, int ncomp, const int* id, int n,
+void launch_slab_to_aos(double* aos, int stride, FieldPtrs F, int f0, int ncomp, const int* pos, int n,
                         cudaStream_t st)
 {
-    if (n > 0) NDSPH_COUNT_LAUNCH, k_slab_to_aos<<<nblk(n, 256), 256, 0, st>>>(aos, stride, F, f0, ncomp, id, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_slab_to_aos<<<nblk(n, 256), 256, 0, st>>>(aos, stride, F, f0, ncomp, pos, n);
 }
 
 __global__ void k_int_to_slab(int* dst, const int* src, const int* id, int n)
@@ -409,10 +413,10 @@ void launch_int_to_slab(int* dst, const int* src, const int* id, int n, cudaStre
 {
     if (n > 0) NDSPH_COUNT_LAUNCH, k_int_to_slab<<<nblk(n, 256), 256, 0, st>>>(dst, src, id, n);
 }
-__global__ void k_slab_to_int(int* dst, const int* src, const int* id, int n)
+__global__ void k_slab_to_int(int* dst, const int* src, const int* pos, int n)
 {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) dst[id ? id[k] : k] = src[k];
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) dst[p] = src[pos ? pos[p] : p];
 }
 __global__ void k_int_shift(int* dst, const int* src, int n, int add)
 {
@@ -423,9 +427,9 @@ void launch_int_shift(int* dst, const int* src, int n, int add, cudaStream_t st)
 {
     if (n > 0) NDSPH_COUNT_LAUNCH, k_int_shift<<<nblk(n, 256), 256, 0, st>>>(dst, src, n, add);
 }
-void launch_slab_to_int(int* dst, const int* src, const int* id, int n, cudaStream_t st)
+void launch_slab_to_int(int* dst, const int* src, const int* pos, int n, cudaStream_t st)
 {
-    if (n > 0) NDSPH_COUNT_LAUNCH, k_slab_to_int<<<nblk(n, 256), 256, 0, st>>>(dst, src, id, n);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_slab_to_int<<<nblk(n, 256), 256, 0, st>>>(dst, src, pos, n);
 }
 __global__ void k_iota(int* a, int n)
 {

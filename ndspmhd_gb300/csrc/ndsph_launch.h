@@ -96,10 +96,11 @@ void launch_reuse_check(FieldPtrs F, Side S, Grid g, DevOpts o, int n, float ski
 // AoS host-layout staging buffer (one field: stride comps) -> sorted slab fields
 void launch_aos_to_slab(FieldPtrs F, int f0, int ncomp, const double* aos, int stride, const int* id, int n,
                         cudaStream_t st);
-void launch_slab_to_aos(double* aos, int stride, FieldPtrs F, int f0, int ncomp, const int* id, int n,
+// slab fields -> host layout; particle p from slot pos[p] (pos_of_id)
+void launch_slab_to_aos(double* aos, int stride, FieldPtrs F, int f0, int ncomp, const int* pos, int n,
                         cudaStream_t st);
 void launch_int_to_slab(int* dst, const int* src, const int* id, int n, cudaStream_t st);
-void launch_slab_to_int(int* dst, const int* src, const int* id, int n, cudaStream_t st);
+void launch_slab_to_int(int* dst, const int* src, const int* pos, int n, cudaStream_t st);
 void launch_iota(int* a, int n, cudaStream_t st);
 void launch_int_shift(int* dst, const int* src, int n, int add, cudaStream_t st);   // dst = src + add
 void launch_fill(double* a, double v, int n, cudaStream_t st);

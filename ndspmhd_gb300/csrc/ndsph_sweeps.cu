@@ -578,6 +578,15 @@ struct Acc<float> {
     __device__ __forceinline__ void add(float x) { k.add(x); }
     __device__ __forceinline__ double val() const { return k.val(); }
 };
+// plain sum in the pair precision: the sources of the dissipation switches
+// (del2u, graddivv), which only enter dalpha/dt and carry no cancellation
+// the switches are sensitive to
+template <typename R>
+struct AccPlain {
+    R v = 0;
+    __device__ __forceinline__ void add(R x) { v += x; }
+    __device__ __forceinline__ double val() const { return (double)v; }
+};
 
 // per-particle quantities the rates sweep reads for either side of a pair
 template <typename R>
@@ -609,9 +618,13 @@ __device__ __forceinline__ void load_p(const SweepArgs& a, int j,
 #endif
 constexpr int RATES_BS = 128;      // threads per block of the rates sweep
 #ifndef NDSPH_RATES_CHUNK
-#define NDSPH_RATES_CHUNK 64
+#define NDSPH_RATES_CHUNK 80
 #endif
-constexpr int RATES_CHUNK = NDSPH_RATES_CHUNK;   // accepted entries per thread per chunk (FP32 form)
+// accepted entries per thread per chunk (FP32 form): rows hold ~90 candidates
+// in 3D, ~25 in 2D, ~8 in 1D; the shared buffer sets how many blocks fit
+// on an SM, so short rows take short chunks
+template <int NDIM>
+constexpr int rates_chunk() { return NDIM == 3 ? NDSPH_RATES_CHUNK : (NDIM == 2 ? 32 : 16); }
 template <int NDIM, int PREC>
 __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_rates(SweepArgs a)
 {
@@ -672,7 +685,8 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
     const R Kdrag = (R)o.Kdrag;
     const bool i_dust = (typei == NDSPH_ITYPE_DUST);
 
-    Acc<R> fx, fy, fz, dbx, dby, dbz, du, dvb, cbx, cby, cbz, d2u, gx, gy, gz;
+    Acc<R> fx, fy, fz, dbx, dby, dbz, du, dvb, cbx, cby, cbz;
+    AccPlain<R> d2u, gx, gy, gz;
     R dtc = (R)1.e6, dtav = (R)3.0e38, vsmax = 0, tsmin = (R)3.0e38, hcsts = 0;
 
     Stencil<NDIM> stn(a.S.cell[i], g);
@@ -935,6 +949,7 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
         // so the lanes of a warp do not idle on rejected candidates in the
         // long part.  The accepted pairs, their order and the screen
         // arithmetic are those of a single pass over the row.
+        constexpr int RATES_CHUNK = rates_chunk<NDIM>();
         __shared__ unsigned acc_buf[RATES_CHUNK * RATES_BS];
         unsigned* mine = acc_buf + threadIdx.x;
         int k = 0;   // a multiple of 4 whenever a vector row load is issued
