@@ -68,6 +68,13 @@ struct ndsph_ctx {
     cudaEvent_t ev_cp[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr}, ev_dl = nullptr;
     int stage_k = 0;
     ndsph_particles* dl_early = nullptr;   // ndsph_step: where the early outputs go
+    // ndsph_step: the inputs only the EOS and the Bevol/energy/alpha predictor
+    // read are uploaded on their own stream while the link and density run
+    cudaStream_t st_up = nullptr;
+    cudaEvent_t ev_late = nullptr, ev_up0 = nullptr;
+    double* d_stage_late = nullptr;   // two staging buffers of 3 doubles per particle
+    int late_k = 0;
+    bool late_pending = false;
     bool dl_density_done = false, dl_prim_done = false;
     double* d_arena = nullptr;   // download staging: every output field side by side
     size_t arena_cap = 0;        // doubles
@@ -312,7 +319,7 @@ static void free_particles(ndsph_ctx* ctx)
     void* ptrs[] = {ctx->slab[0], ctx->slab[1], ctx->S.itype, ctx->S.id, ctx->S.ireal, ctx->S.pos_of_id,
                     ctx->S.numneigh, ctx->S.cell, ctx->S.xs, ctx->S.h1, ctx->S.active, ctx->S.active_next,
                     ctx->S.flag, ctx->itype2, ctx->id2, ctx->ireal2, ctx->srt.key, ctx->srt.slot, ctx->srt.perm,
-                    ctx->d_stage, ctx->d_istage, ctx->S.pk_v, ctx->S.pk_t, ctx->S.pk_b, ctx->S.pk_a,
+                    ctx->d_stage, ctx->d_stage_late, ctx->d_istage, ctx->S.pk_v, ctx->S.pk_t, ctx->S.pk_b, ctx->S.pk_a,
                     ctx->S.nl, ctx->S.nl_cnt, ctx->S.hb, ctx->S.xsb, ctx->S.sim, ctx->sim2};
     for (void* p : ptrs) if (p) cudaFree(p);
     ctx->slab[0] = ctx->slab[1] = nullptr;
@@ -320,7 +327,7 @@ static void free_particles(ndsph_ctx* ctx)
     ctx->itype2 = ctx->id2 = ctx->ireal2 = nullptr;
     ctx->sim2 = nullptr;
     ctx->srt.key = ctx->srt.slot = ctx->srt.perm = nullptr;
-    ctx->d_stage = nullptr; ctx->d_istage = nullptr;
+    ctx->d_stage = nullptr; ctx->d_istage = nullptr; ctx->d_stage_late = nullptr;
     ctx->cap = 0;
 }
 
@@ -347,6 +354,7 @@ static int ensure_capacity(ndsph_ctx* ctx, int n)
     CK(cudaMalloc(&ctx->itype2, ib)); CK(cudaMalloc(&ctx->id2, ib)); CK(cudaMalloc(&ctx->ireal2, ib));
     CK(cudaMalloc(&ctx->srt.key, ib)); CK(cudaMalloc(&ctx->srt.slot, ib)); CK(cudaMalloc(&ctx->srt.perm, ib));
     CK(cudaMalloc(&ctx->d_stage, sizeof(double) * 6 * (size_t)cap));   // two staging buffers
+    CK(cudaMalloc(&ctx->d_stage_late, sizeof(double) * 6 * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_v, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_t, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_b, sizeof(float4) * (size_t)cap));
@@ -412,7 +420,10 @@ extern "C" int ndsph_init(ndsph_ctx** out, const ndsph_opts* opts, int32_t nmax)
         cudaEventCreateWithFlags(&ctx->ev_cp[1], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_used[0], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_used[1], cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_dl, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&ctx->ev_dl, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->st_up, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_late, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_up0, cudaEventDisableTiming) != cudaSuccess) {
         g_err = "stream/event creation failed";
         delete ctx;
         return NDSPH_E_CUDA;
@@ -497,6 +508,9 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
     for (int k = 0; k < 16; k++) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     for (int k = 0; k < 2; k++) if (ctx->gexec[k]) cudaGraphExecDestroy(ctx->gexec[k]);
     if (ctx->st_cp) { cudaStreamSynchronize(ctx->st_cp); cudaStreamDestroy(ctx->st_cp); }
+    if (ctx->st_up) { cudaStreamSynchronize(ctx->st_up); cudaStreamDestroy(ctx->st_up); }
+    if (ctx->ev_late) cudaEventDestroy(ctx->ev_late);
+    if (ctx->ev_up0) cudaEventDestroy(ctx->ev_up0);
     for (cudaEvent_t ev : {ctx->ev_cp[0], ctx->ev_cp[1], ctx->ev_used[0], ctx->ev_used[1], ctx->ev_dl})
         if (ev) cudaEventDestroy(ev);
     if (ctx->d_live) cudaFree(ctx->d_live);
@@ -565,6 +579,37 @@ static int upload_aos(ndsph_ctx* ctx, const double* host, int f0, int ncomp, int
     CK(cudaEventRecord(ctx->ev_used[b], ctx->st));
     return 0;
 }
+// an input of the host-buffer step that the link and the density passes do
+// not read: copied and laid out on the upload stream, behind the early ones
+static int upload_aos_late(ndsph_ctx* ctx, const double* host, int f0, int ncomp, int stride, int n,
+                           const int* id)
+{
+    if (!host) return 0;
+    if (const double* src = (const double*)host_view(ctx, host)) {
+        launch_aos_to_slab(ctx->F, f0, ncomp, src, stride, id, n, ctx->st_up);
+        return 0;
+    }
+    // two staging buffers used in turn on one stream: a copy into a buffer
+    // follows the layout kernel that read it two fields earlier
+    double* buf = ctx->d_stage_late + (size_t)((ctx->late_k++) & 1) * 3 * ctx->cap;
+    CK(cudaMemcpyAsync(buf, host, sizeof(double) * (size_t)stride * n, cudaMemcpyHostToDevice, ctx->st_up));
+    launch_aos_to_slab(ctx->F, f0, ncomp, buf, stride, id, n, ctx->st_up);
+    return 0;
+}
+
+// the late inputs of a host-buffer step have arrived: the main stream waits
+// for them and runs their part of the predictor (before the EOS, or before a
+// link permutes the fields)
+static int wait_late(ndsph_ctx* ctx)
+{
+    if (!ctx->late_pending) return 0;
+    ctx->late_pending = false;
+    CK(cudaStreamWaitEvent(ctx->st, ctx->ev_late, 0));
+    launch_predictor_part(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, 2, ctx->st);
+    CK(cudaGetLastError());
+    return 0;
+}
+
 // downloads are staged in an arena and copied out asynchronously; the
 // caller synchronises once (download_end)
 static int download_aos(ndsph_ctx* ctx, double* host, int f0, int ncomp, int stride, int n)
@@ -850,6 +895,10 @@ static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hma
     if (may_keep) {
         int rc = 0;
         if (try_keep_link(ctx, keep_hmax_ghost, &rc)) return 0;
+        if (rc) return rc;
+    }
+    {
+        int rc = wait_late(ctx);   // the gather permutes every live field
         if (rc) return rc;
     }
     ctx->nl_valid = false;
@@ -1158,6 +1207,8 @@ static int do_derivs(ndsph_ctx* ctx, const int* fields, int nfields)
         ctx->dl_density_done = true;
     }
     tmark(ctx, 6);
+    rc = wait_late(ctx);
+    if (rc) return rc;
     rc = do_cons2prim(ctx);
     if (rc) return rc;
     if (ctx->dl_early) {
@@ -1480,7 +1531,10 @@ static int dev_step_once(ndsph_ctx* ctx)
     cudaStream_t st = ctx->st;
     // dt lives in the Reduce block
     CK(cudaMemcpyAsync(&ctx->red->dt, &ctx->dt, sizeof(double), cudaMemcpyHostToDevice, st));
-    launch_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+    if (ctx->late_pending)
+        launch_predictor_part(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, 1, st);   // the rest in wait_late
+    else
+        launch_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
     const bool learned = ctx->opts.learned_h && ctx->mlp_p;
     if (learned) {
         tmark(ctx, 12);
@@ -1698,20 +1752,41 @@ static int step_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
     }
     const int n = npart, nd = ctx->o.ndim;
     const int* idm = keep ? ctx->S.id : nullptr;
+    // early inputs (the predictor of x, v, h; the link; the density passes)
     rc |= upload_aos(ctx, p->x, X0, nd, nd, n, idm);
     rc |= upload_aos(ctx, p->vel, V0, 3, 3, n, idm);
-    rc |= upload_aos(ctx, p->Bevol, BE0, 3, 3, n, idm);
-    rc |= upload_aos(ctx, p->en, EN, 1, 1, n, idm);
     rc |= upload_aos(ctx, p->hh, HH, 1, 1, n, idm);
     rc |= upload_aos(ctx, p->pmass, PM, 1, 1, n, idm);
-    rc |= upload_aos(ctx, p->alpha, AL0, 3, 3, n, idm);
     rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n, idm);
     rc |= upload_aos(ctx, p->dhdt, DHDT, 1, 1, n, idm);
     rc |= upload_aos(ctx, p->force, F0, 3, 3, n, idm);
-    rc |= upload_aos(ctx, p->dBevoldt, DB0, 3, 3, n, idm);
-    rc |= upload_aos(ctx, p->dendt, DENDT, 1, 1, n, idm);
-    rc |= upload_aos(ctx, p->daldt, DAL0, 3, 3, n, idm);
     if (rc) return rc;
+    // late inputs (Bevol, energy, alpha and their rates: the EOS and their
+    // part of the predictor) on the upload stream, overlapping the link and
+    // the density passes; the learned-h form reads them before the link
+    const bool split = !ctx->opts.learned_h;
+    if (split) {
+        // behind the early copies, so they do not share the link's bandwidth
+        CK(cudaEventRecord(ctx->ev_up0, ctx->st_cp));
+        CK(cudaStreamWaitEvent(ctx->st_up, ctx->ev_up0, 0));
+        rc |= upload_aos_late(ctx, p->Bevol, BE0, 3, 3, n, idm);
+        rc |= upload_aos_late(ctx, p->en, EN, 1, 1, n, idm);
+        rc |= upload_aos_late(ctx, p->alpha, AL0, 3, 3, n, idm);
+        rc |= upload_aos_late(ctx, p->dBevoldt, DB0, 3, 3, n, idm);
+        rc |= upload_aos_late(ctx, p->dendt, DENDT, 1, 1, n, idm);
+        rc |= upload_aos_late(ctx, p->daldt, DAL0, 3, 3, n, idm);
+        if (rc) return rc;
+        CK(cudaEventRecord(ctx->ev_late, ctx->st_up));
+        ctx->late_pending = true;
+    } else {
+        rc |= upload_aos(ctx, p->Bevol, BE0, 3, 3, n, idm);
+        rc |= upload_aos(ctx, p->en, EN, 1, 1, n, idm);
+        rc |= upload_aos(ctx, p->alpha, AL0, 3, 3, n, idm);
+        rc |= upload_aos(ctx, p->dBevoldt, DB0, 3, 3, n, idm);
+        rc |= upload_aos(ctx, p->dendt, DENDT, 1, 1, n, idm);
+        rc |= upload_aos(ctx, p->daldt, DAL0, 3, 3, n, idm);
+        if (rc) return rc;
+    }
     if (keep) {
         const int* v = (const int*)host_view(ctx, p->itype);
         if (!v) {
@@ -1750,6 +1825,8 @@ extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, nds
     rc = dev_step_once(ctx);
     if (rc) {
         cudaStreamSynchronize(ctx->st_cp);
+        cudaStreamSynchronize(ctx->st_up);
+        ctx->late_pending = false;
         ctx->dl_early = nullptr;
         ctx->dl_density_done = ctx->dl_prim_done = false;
         return rc;

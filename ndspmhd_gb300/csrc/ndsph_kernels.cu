@@ -662,47 +662,63 @@ __global__ void k_predictor2(FieldPtrs F, Side S, DevOpts o, int n, const Reduce
 }
 // save and predictor in one pass, for states without fixed particles (no
 // particle reads another's saved velocity and force, so no grid-wide order
-// is needed between the two); same arithmetic as k_predictor + k_predictor2
-__global__ void k_predictor_fused(FieldPtrs F, Side S, DevOpts o, int n, const Reduce* red)
+// is needed between the two); same arithmetic as k_predictor + k_predictor2.
+// part 0: every field; 1: position, velocity and h (with the saves of x, v,
+// force, h, dh/dt, rho); 2: Bevol, energy and alpha (with their saves and the
+// saves of their rates) -- a host-buffer step uploads the latter while the
+// link and the density passes run
+__global__ void k_predictor_fused(FieldPtrs F, Side S, DevOpts o, int n, const Reduce* red, int part)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double dt = o.batched ? o.sim_dt[S.sim[i]] : red->dt;
-    double x[3], v[3], f[3], be[3], db[3], al[3], dal[3];
-    for (int d = 0; d < o.ndim; d++) x[d] = F.f[X0 + d][i];
-    for (int d = 0; d < 3; d++) {
-        v[d] = F.f[V0 + d][i]; f[d] = F.f[F0 + d][i]; be[d] = F.f[BE0 + d][i]; db[d] = F.f[DB0 + d][i];
-        al[d] = F.f[AL0 + d][i]; dal[d] = F.f[DAL0 + d][i];
-    }
-    const double h = F.f[HH][i], en = F.f[EN][i], rho = F.f[RHO][i], dh = F.f[DHDT][i], den = F.f[DENDT][i];
-    // save (stepND_leapfrog_mhd.f90:70-101)
-    for (int d = 0; d < o.ndim; d++) F.f[XIN0 + d][i] = x[d];
-    for (int d = 0; d < 3; d++) {
-        F.f[VIN0 + d][i] = v[d]; F.f[BIN0 + d][i] = be[d]; F.f[ALIN0 + d][i] = al[d];
-        F.f[FIN0 + d][i] = f[d]; F.f[DBIN0 + d][i] = db[d]; F.f[DALIN0 + d][i] = dal[d];
-    }
-    F.f[HIN][i] = h; F.f[ENIN][i] = en; F.f[RHOIN][i] = rho; F.f[DHIN][i] = dh; F.f[DENIN][i] = den;
     const int t = S.itype[i];
-    if (t == NDSPH_ITYPE_BND || t == NDSPH_ITYPE_BNDDUST) {
-        // moved by its own saved velocity and force; everything else held
+    const bool fixed = (t == NDSPH_ITYPE_BND || t == NDSPH_ITYPE_BNDDUST);
+    if (part != 2) {
+        double x[3], v[3], f[3];
+        for (int d = 0; d < o.ndim; d++) x[d] = F.f[X0 + d][i];
+        for (int d = 0; d < 3; d++) { v[d] = F.f[V0 + d][i]; f[d] = F.f[F0 + d][i]; }
+        const double h = F.f[HH][i], rho = F.f[RHO][i], dh = F.f[DHDT][i];
+        // save (stepND_leapfrog_mhd.f90:70-101)
+        for (int d = 0; d < o.ndim; d++) F.f[XIN0 + d][i] = x[d];
+        for (int d = 0; d < 3; d++) { F.f[VIN0 + d][i] = v[d]; F.f[FIN0 + d][i] = f[d]; }
+        F.f[HIN][i] = h; F.f[RHOIN][i] = rho; F.f[DHIN][i] = dh;
+        // a fixed particle moves by its own saved velocity and force; the rest is held
         for (int d = 0; d < o.ndim; d++) F.f[X0 + d][i] = x[d] + dt * v[d] + 0.5 * dt * dt * f[d];
-        return;
+        if (!fixed) {
+            for (int d = 0; d < 3; d++) F.f[V0 + d][i] = (v[d] + dt * f[d]) / (1.0 + 0.0);
+            F.f[HH][i] = h + dt * dh;
+        }
     }
-    for (int d = 0; d < o.ndim; d++) F.f[X0 + d][i] = x[d] + dt * v[d] + 0.5 * dt * dt * f[d];
-    for (int d = 0; d < 3; d++) F.f[V0 + d][i] = (v[d] + dt * f[d]) / (1.0 + 0.0);
-    if (o.imhd != 0)
-        for (int d = 0; d < 3; d++) F.f[BE0 + d][i] = be[d] + dt * db[d];
-    F.f[HH][i] = h + dt * dh;
-    if (o.iener != 0) F.f[EN][i] = en + dt * den;
-    for (int d = 0; d < 3; d++)
-        if (o.iavlim[d] != 0) F.f[AL0 + d][i] = fmin(al[d] + dt * dal[d], 1.0);
+    if (part != 1) {
+        double be[3], db[3], al[3], dal[3];
+        for (int d = 0; d < 3; d++) {
+            be[d] = F.f[BE0 + d][i]; db[d] = F.f[DB0 + d][i]; al[d] = F.f[AL0 + d][i]; dal[d] = F.f[DAL0 + d][i];
+        }
+        const double en = F.f[EN][i], den = F.f[DENDT][i];
+        for (int d = 0; d < 3; d++) {
+            F.f[BIN0 + d][i] = be[d]; F.f[ALIN0 + d][i] = al[d]; F.f[DBIN0 + d][i] = db[d]; F.f[DALIN0 + d][i] = dal[d];
+        }
+        F.f[ENIN][i] = en; F.f[DENIN][i] = den;
+        if (fixed) return;
+        if (o.imhd != 0)
+            for (int d = 0; d < 3; d++) F.f[BE0 + d][i] = be[d] + dt * db[d];
+        if (o.iener != 0) F.f[EN][i] = en + dt * den;
+        for (int d = 0; d < 3; d++)
+            if (o.iavlim[d] != 0) F.f[AL0 + d][i] = fmin(al[d] + dt * dal[d], 1.0);
+    }
+}
+
+void launch_predictor_part(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, int part, cudaStream_t st)
+{
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_predictor_fused<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red, part);
 }
 
 void launch_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st)
 {
     if (n <= 0) return;
     if (!o.has_fixed) {
-        NDSPH_COUNT_LAUNCH, k_predictor_fused<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+        NDSPH_COUNT_LAUNCH, k_predictor_fused<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red, 0);
         return;
     }
     NDSPH_COUNT_LAUNCH, k_predictor<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);

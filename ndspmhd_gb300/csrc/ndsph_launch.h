@@ -113,6 +113,8 @@ void launch_fixed_density_copy(FieldPtrs F, Side S, int n, cudaStream_t st);
 void launch_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st);
 void launch_fixed_copy(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
 void launch_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st);
+// states without fixed particles: part 1 = x, v, h; part 2 = Bevol, energy, alpha
+void launch_predictor_part(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, int part, cudaStream_t st);
 void launch_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st);
 void launch_finalize_dt(Reduce* red, DevOpts o, double* out, cudaStream_t st);
 void launch_reduce_reset(Reduce* red, cudaStream_t st);

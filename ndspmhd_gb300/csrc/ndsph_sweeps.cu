@@ -620,11 +620,9 @@ constexpr int RATES_BS = 128;      // threads per block of the rates sweep
 #ifndef NDSPH_RATES_CHUNK
 #define NDSPH_RATES_CHUNK 80
 #endif
-// accepted entries per thread per chunk (FP32 form): rows hold ~90 candidates
-// in 3D, ~25 in 2D, ~8 in 1D; the shared buffer sets how many blocks fit
-// on an SM, so short rows take short chunks
+// accepted entries per thread per chunk of the 3D FP32 rows (~90 candidates)
 template <int NDIM>
-constexpr int rates_chunk() { return NDIM == 3 ? NDSPH_RATES_CHUNK : (NDIM == 2 ? 32 : 16); }
+constexpr int rates_chunk() { return NDSPH_RATES_CHUNK; }
 template <int NDIM, int PREC>
 __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_rates(SweepArgs a)
 {
@@ -940,7 +938,9 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
                 if (typei == NDSPH_ITYPE_GAS) du.add(mj * dragterm_en);
             }
     };
-    if constexpr (PREC == NDSPH_PREC_FP64) {
+    if constexpr (PREC == NDSPH_PREC_FP64 || NDIM < 3) {
+        // the FP64 form, and short 1D/2D rows (~8 / ~25 entries, most of them
+        // accepted), take one pass over the row
         for (int k = 0; k < ncand; k++) pair_terms(row[k]);
     } else {
         // Two phases per chunk of the row: screen the candidates (four row
