@@ -15,12 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUTDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUTDIR, "libndsph_gpu.so")
 SOURCES = ["ndsph_api.cu", "ndsph_kernels.cu", "ndsph_sweeps.cu", "ndsph_noalloc.cu", "ndsph_mlp.cu"]
-# The pair sweeps: FP32 division and square root approximate, FP32 denormals
-# flushed to zero (the FP32 form's pair terms; without -ftz every hardware
-# reciprocal and rsqrt carries a denormal fix-up).  FP64 arithmetic -- the
-# parity form, positions, the Newton-Raphson residual -- is not affected by
-# these flags.  Measured: the 128^3 rates sweep 10 % faster.
-EXTRA = {"ndsph_sweeps.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]}
+# per-source extra nvcc flags (none at present)
+EXTRA: dict = {}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr"]

@@ -753,7 +753,7 @@ static int build_grid(ndsph_ctx* ctx, double hmax, const double* lo, const doubl
     const double base = 2.0 * hmax * (1.0 + 1.e-9);
     const double skin_cf = reuse_on(ctx) ? (double)ctx->nl_skin : 1.0;
     const bool sw5_ok = ctx->nl_sw5 && ctx->o.precision == NDSPH_PREC_FP32 && !ctx->o.batched &&
-                        ctx->n < (1 << 25);
+                        ctx->o.ndim == 3 && ctx->n < (1 << 25);
     const int tries_sw[3] = {5, 3, 3};
     const double tries_cf[3] = {skin_cf, skin_cf, 1.0};
     int sw = 3;

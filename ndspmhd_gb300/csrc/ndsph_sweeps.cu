@@ -168,7 +168,7 @@ struct Stencil {
     // o = (dx+r) + sw (dy+r) + sw^2 (dz+r) (the cell exists)
     __device__ __forceinline__ void offset(unsigned o, const Grid& g, int d[3], int w[3]) const
     {
-        stencil_d<NDIM>(o, g.sw, d);
+        stencil_d<NDIM>(o, NDIM == 3 ? g.sw : 3, d);   // 1D and 2D always search 3 wide
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const int c = cc[k] + d[k];
@@ -228,22 +228,44 @@ __device__ __forceinline__ float screen_r2(const float4& xsi, const float4& xsj,
 
 // reciprocal and square root in the pair precision: exact (IEEE) in FP64,
 // the hardware approximations (MUFU, ~1 ulp) in the FP32 form
+// The FP32 forms are the PTX approximate instructions with denormals flushed
+// (.ftz): without .ftz each one carries a scaling fix-up for denormal inputs,
+// which no physical quantity of the pair sums is; that fix-up was ~10 % of
+// the 128^3 rates sweep's instructions.
+__device__ __forceinline__ float rsqrt_ftz(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float div_ftz(float a, float b)
+{
+    float y;
+    asm("div.approx.ftz.f32 %0, %1, %2;" : "=f"(y) : "f"(a), "f"(b));
+    return y;
+}
+__device__ __forceinline__ float rcp_ftz(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 template <typename R>
 __device__ __forceinline__ R rcp(R x)
 {
-    if constexpr (std::is_same<R, float>::value) return __fdividef(1.0f, x);
+    if constexpr (std::is_same<R, float>::value) return rcp_ftz(x);
     else return 1.0 / x;
 }
 template <typename R>
 __device__ __forceinline__ R sqrtp(R x)
 {
-    if constexpr (std::is_same<R, float>::value) return x * rsqrtf(fmaxf(x, 1e-37f));
+    if constexpr (std::is_same<R, float>::value) return x * rsqrt_ftz(fmaxf(x, 1e-37f));
     else return sqrt(x);
 }
 template <typename R>
 __device__ __forceinline__ R divp(R a, R b)
 {
-    if constexpr (std::is_same<R, float>::value) return __fdividef(a, b);
+    if constexpr (std::is_same<R, float>::value) return div_ftz(a, b);
     else return a / b;
 }
 
@@ -312,7 +334,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
     const unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
     // one candidate: its list entry, position and type, and (FP32 form) its
     // velocity/mass pack, loaded by the caller
-    const unsigned shift = (unsigned)g.nlshift, omask = (1u << shift) - 1u;
+    const unsigned shift = (NDIM == 3) ? (unsigned)g.nlshift : 5u, omask = (1u << shift) - 1u;
     auto pair = [&](unsigned pk, const float4& xsj, int typej, const float4& pvj) {
         const int j = (int)(pk >> shift);
         int d[3], w[3];
@@ -389,7 +411,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
                 float dvr = (vif[0] - pvj.x) * dxf[0];
                 if (NDIM >= 2) dvr += (vif[1] - pvj.y) * dxf[1];
                 if (NDIM >= 3) dvr += (vif[2] - pvj.z) * dxf[2];
-                fd.add(mj * dvr * gw * __fdividef(1.0f, rij + 1e-30f));
+                fd.add(mj * dvr * gw * rcp_ftz(rij + 1e-30f));
             }
         }
     };
@@ -693,7 +715,7 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
     // the terms of one candidate pair (rates_core, artificial_dissipation,
     // mhd_terms, drag_forces for the pair (i, j)); returns early when the
     // pair is out of range
-    const unsigned shift = (unsigned)g.nlshift, omask = (1u << shift) - 1u;
+    const unsigned shift = (NDIM == 3) ? (unsigned)g.nlshift : 5u, omask = (1u << shift) - 1u;
     auto pair_terms = [&](const unsigned pk) {
             const int j = (int)(pk >> shift);
             if (j == i) return;
@@ -725,7 +747,7 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
                 rij = rijd; q2i = q2id; q2j = q2jd; hj1 = hj1d;
             } else {
                 if (!(r2f < 4.0f * hm * hm)) return;
-                const float ir = rsqrtf(fmaxf(r2f, 1e-37f));
+                const float ir = rsqrt_ftz(fmaxf(r2f, 1e-37f));
                 const float rr = r2f * ir;
                 if (rr <= 1e-30f) {
                     if (a.S.itype[j] == typei && typei != 2) raise_err(a.red, NDSPH_E_CLUMP, a.S.id[i]);
@@ -898,13 +920,13 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
                 R drd[3];
                 if (rij <= (R)2.220446049250313e-16) {
                     if (dv2 <= (R)2.220446049250313e-16) return;
-                    const R ivij = rcp(sqrt(dv2));
+                    const R ivij = rcp(sqrtp(dv2));
                     drd[0] = dvel[0] * ivij; drd[1] = dvel[1] * ivij; drd[2] = dvel[2] * ivij;
                 } else {
                     drd[0] = dr[0]; drd[1] = dr[1]; drd[2] = dr[2];
                 }
                 const R rsum = rhoi + rhoj;
-                const R ts = rhoj * rhoi / (Kdrag * rsum);
+                const R ts = divp(rhoj * rhoi, Kdrag * rsum);
                 R wgas, csg;
                 if (typei == NDSPH_ITYPE_GAS || typei == NDSPH_ITYPE_BND) {
                     R wdi;
@@ -915,7 +937,7 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
                     if (NDIM >= 3) hfw *= hi1;
                     wgas = wdi * hfw;
                     csg = csi;
-                    hcsts = fmax(hcsts, hi / (csg * ts));
+                    hcsts = fmax(hcsts, divp(hi, csg * ts));
                 } else {
                     if (typej != NDSPH_ITYPE_GAS && typej != NDSPH_ITYPE_BND) return;
                     R wdj;
@@ -926,11 +948,11 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
                     if (NDIM >= 3) hfw *= hj1;
                     wgas = wdj * hfw;
                     csg = pj.cs;
-                    hcsts = fmax(hcsts, pj.h / (csg * ts));
+                    hcsts = fmax(hcsts, divp(pj.h, csg * ts));
                 }
                 tsmin = fmin(tsmin, ts);
                 const R projv = dvel[0] * drd[0] + dvel[1] * drd[1] + dvel[2] * drd[2];
-                const R dragterm = (R)NDIM * wgas / (rsum * ts) * projv;
+                const R dragterm = divp((R)NDIM * wgas, rsum * ts) * projv;
                 const R dragterm_en = dragterm * projv;
                 fx.add(-dragterm * mj * drd[0]);
                 fy.add(-dragterm * mj * drd[1]);
@@ -1003,12 +1025,12 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
             for (int c = 0; c < 3; c++) curlB[c] *= rho1;
         divB *= rho1;
     }
-    const R fmag = sqrt(force[0] * force[0] + force[1] * force[1] + force[2] * force[2]);
-    R fonh_r = fmag / hi_p;
+    const R fmag = sqrtp(force[0] * force[0] + force[1] * force[1] + force[2] * force[2]);
+    R fonh_r = divp(fmag, hi_p);
     if (typei == 1) fonh_r = 0;
     R va2 = 0;
     if (mhd) va2 = B2i * rho1i;   // B^2/dens with dens = rho
-    const R vsig = sqrt(csi * csi + va2);
+    const R vsig = sqrtp(csi * csi + va2);
     const R drhodt = (R)F.f[DRHODT][i];
     if (o.imhd >= 11 && o.imhd <= 19) {
         for (int c = 0; c < 3; c++) dBe[c] = dBe[c] + (R)F.f[BE0 + c][i] * rho1 * drhodt;
@@ -1027,7 +1049,7 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
     if (typei == NDSPH_ITYPE_DUST) dendt = 0;
     R daldt[3] = {0, 0, 0};
     if (o.iavlim[0] != 0 || o.iavlim[1] != 0 || o.iavlim[2] != 0) {
-        const R tdecay1 = ((R)o.avdecayconst * vsig) / hi_p;
+        const R tdecay1 = divp((R)o.avdecayconst * vsig, hi_p);
         if (o.iavlim[0] == 1 || o.iavlim[0] == 2) {
             R source = fmax(drhodt * rho1, (R)0);
             if (o.iavlim[0] == 2) source = source * ((R)2 - alphai);
@@ -1035,7 +1057,7 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
         }
         if (o.iener > 0 && o.iavlim[1] > 0) {
             R sourceu = 0;
-            if (ui > (R)2.220446049250313e-16) sourceu = hi_p * fabs(del2u) / sqrt(ui);
+            if (ui > (R)2.220446049250313e-16) sourceu = divp(hi_p * fabs(del2u), sqrtp(ui));
             daldt[1] = ((R)o.alphaumin - alphaui) * tdecay1 + sourceu;
         }
     }
@@ -1183,8 +1205,8 @@ __device__ __forceinline__ void nl_scan_run(const SweepArgs& a, const float4& xs
                                             float oz, unsigned obase, unsigned* row, int& cnt)
 {
     const Grid& g = a.g;
-    const unsigned shift = (unsigned)g.nlshift;
-    const int r = (g.sw - 1) >> 1;
+    const unsigned shift = (NDIM == 3) ? (unsigned)g.nlshift : 5u;
+    const int r = (NDIM == 3) ? (g.sw - 1) >> 1 : 1;
     for (int j0 = jb; j0 < je; j0 += 4) {
         float4 q[4];
 #pragma unroll
@@ -1223,7 +1245,7 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
     const float csmin = fminf(g.csf[0], fminf(NDIM >= 2 ? g.csf[1] : g.csf[0], NDIM >= 3 ? g.csf[2] : g.csf[0]));
     const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
     const float sk = 2.0f * a.nl_skin * 1.0002f;
-    const int sw = g.sw, r = (sw - 1) >> 1;
+    const int sw = (NDIM == 3) ? g.sw : 3, r = (sw - 1) >> 1;
     const float reach = (float)r * csmin * 1.001f + abs_tol;
     const float reach2 = reach * reach;
     Stencil<NDIM> stn(a.S.cell[i], g);
