@@ -57,6 +57,23 @@ def _load_peaks():
     return 6800.0, "fallback"
 
 
+def max_over_ranks(x: float, dist, device: str) -> float:
+    """Largest value over the ranks (the slowest replica's time); the value
+    itself without a process group."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(n_per_rank: int, world: int, ms_max: float) -> float:
+    """Whole-job particle-updates/s of `world` independent replicas of an
+    n-particle box, timed by the slowest (weak scaling)."""
+    return world * n_per_rank / (ms_max * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling during the timed region."""
 
@@ -64,6 +81,7 @@ class ClockSampler:
         self.gpu = gpu_index
         self.samples = []
         self._stop = threading.Event()
+        self._first = threading.Event()
         self._proc = None
 
     def start(self):
@@ -73,7 +91,7 @@ class ClockSampler:
         try:
             self._proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self._proc = None
             return
@@ -84,9 +102,15 @@ class ClockSampler:
         for line in self._proc.stdout:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) >= 7:
+                if self._stop.is_set():
+                    break
                 self.samples.append(parts)
-            if self._stop.is_set():
-                break
+                self._first.set()
+
+    def wait_first(self, timeout: float = 3.0):
+        """Block until nvidia-smi delivered its first sample (its start-up
+        takes longer than a short timed region)."""
+        self._first.wait(timeout)
 
     def stop(self) -> dict:
         self._stop.set()
@@ -152,6 +176,7 @@ def run_device(o, st, steps: int, warmup: int, dist=None, tuning=None):
     clk = ClockSampler(torch.cuda.current_device())
     kept0, builds0 = g.timing()["nl_reused"], g.timing()["nl_builds"]
     clk.start()
+    clk.wait_first()
     g.dev_step(steps)              # bracketed by CUDA events on the library's stream
     torch.cuda.synchronize()
     clocks = clk.stop()
@@ -445,11 +470,8 @@ def main():
         ms64, tim64, _, _ = run_device(o64, st64, max(2, args.steps // 2), 3, dist)
 
     # max over ranks
-    if dist is not None:
-        t = torch.tensor([ms32], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms32 = float(t.item())
-    value = world * n / (ms32 * 1e-3)
+    ms32 = max_over_ranks(ms32, dist, "cuda")
+    value = replica_value(n, world, ms32)
 
     e2e_val, h2d, d2h, e2e_staged = run_e2e(o32, max(3, args.steps), 3, tuning)
 

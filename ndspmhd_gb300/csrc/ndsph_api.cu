@@ -15,10 +15,6 @@
 #include "ndsph_launch.h"
 #include "ndsph_mlp.h"
 
-namespace ndsph {
-void launch_density_init2(FieldPtrs F, Side S, int n, Reduce* red, cudaStream_t st);
-}
-
 using namespace ndsph;
 
 struct ndsph_ctx {
@@ -1041,7 +1037,7 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
     const int n = ctx->n;
     cudaStream_t st = ctx->st;
     const int itsmax = ctx->o.maxdensits;
-    launch_density_init2(ctx->F, ctx->S, n, ctx->red, st);
+    launch_density_init(ctx->F, ctx->S, n, ctx->red, st);
     int zero = 0;
     CK(cudaMemcpyAsync(&ctx->red->redolink, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
     int its = 0, ncalc = n, ncalctotal = 0, nrelink = 0;
@@ -2048,7 +2044,7 @@ static int capture_one(ndsph_ctx* ctx, cudaGraphExec_t* out, long long* nmain, l
     launch_reduce_reset(ctx->red, st);
     launch_sim_reset(ctx->o, st);
     // iterate_density
-    launch_density_init2(ctx->F, ctx->S, n, ctx->red, st);
+    launch_density_init(ctx->F, ctx->S, n, ctx->red, st);
     GCK(cudaMemsetAsync(&ctx->red->redolink, 0, sizeof(int), st));
     launch_h1(ctx->F, ctx->S, n, st);
     if (ctx->o.precision == NDSPH_PREC_FP32) {

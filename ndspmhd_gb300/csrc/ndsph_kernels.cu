@@ -84,10 +84,6 @@ __global__ void k_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned 
         }
     }
 }
-void launch_hmax(const double* h, int n, Reduce* red, unsigned long long* dst, cudaStream_t st)
-{
-    (void)h; (void)n; (void)red; (void)dst; (void)st;
-}
 void launch_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, cudaStream_t st,
                       const int* gate)
 {
@@ -492,11 +488,7 @@ __global__ void k_density_init(FieldPtrs F, Side S, int n, Reduce* red)
     F.f[HDEN0][k] = h;
     if (!(h > 2.2250738585072014e-308)) raise_err(red, NDSPH_E_H_NONPOS, S.id[k]);
 }
-void launch_density_init(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st)
-{
-    (void)o; (void)F; (void)S; (void)n; (void)st;
-}
-void launch_density_init2(FieldPtrs F, Side S, int n, Reduce* red, cudaStream_t st)
+void launch_density_init(FieldPtrs F, Side S, int n, Reduce* red, cudaStream_t st)
 {
     if (n > 0) NDSPH_COUNT_LAUNCH, k_density_init<<<nblk(n, 256), 256, 0, st>>>(F, S, n, red);
 }

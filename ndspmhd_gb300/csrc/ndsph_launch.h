@@ -73,7 +73,6 @@ struct SweepArgs {
 
 // ---- link / sort (ndsph_kernels.cu) ------------------------------------------
 void launch_boundary_wrap(FieldPtrs F, DevOpts o, int n, cudaStream_t st);
-void launch_hmax(const double* h, int n, Reduce* red, unsigned long long* dst, cudaStream_t st);
 // max h and bounding box; skipped when `gate` is set and points to 0
 void launch_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, cudaStream_t st,
                       const int* gate = nullptr);
@@ -108,7 +107,8 @@ void launch_copy(double* dst, const double* src, int n, cudaStream_t st);
 
 // ---- per-particle physics (ndsph_kernels.cu) --------------------------------
 void launch_h1(FieldPtrs F, Side S, int n, cudaStream_t st);
-void launch_density_init(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
+// zero the hterms of non-fixed particles, save h at entry (hhin), check h > 0
+void launch_density_init(FieldPtrs F, Side S, int n, Reduce* red, cudaStream_t st);
 void launch_fixed_density_copy(FieldPtrs F, Side S, int n, cudaStream_t st);
 void launch_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st);
 void launch_fixed_copy(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);

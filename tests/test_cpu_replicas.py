@@ -1,0 +1,48 @@
+"""The multi-GPU form is replicas: bench.py under torchrun runs one
+independent box per rank and reports the whole job's updates/s timed by the
+slowest rank.  The rank aggregation runs here as two gloo processes on CPU."""
+import os
+import socket
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+import bench  # noqa: E402
+
+
+def _free_port() -> int:
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _rank(rank: int, world: int, port: int, out):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    ms = [7.5, 9.25][rank]                     # the second replica is slower
+    got = bench.max_over_ranks(ms, dist, "cpu")
+    out[rank] = (got, bench.replica_value(1000, world, got))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_replicas_time_by_slowest_rank():
+    world = 2
+    mgr = mp.get_context("spawn").Manager()
+    out = mgr.dict()
+    mp.start_processes(_rank, args=(world, _free_port(), out), nprocs=world, start_method="spawn")
+    for r in range(world):
+        got, value = out[r]
+        assert got == 9.25
+        assert value == pytest.approx(world * 1000 / 9.25e-3)
+
+
+def test_single_process_passes_through():
+    assert bench.max_over_ranks(3.0, None, "cpu") == 3.0
+    assert bench.replica_value(2_097_152, 1, 6.0) == pytest.approx(2_097_152 / 6e-3)
