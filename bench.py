@@ -331,6 +331,39 @@ def run_learned(n1d: int, steps: int, warmup: int):
     return out
 
 
+def run_ot2d(steps: int = 50, cpu_steps: int = 10):
+    """The reference's own CPU case: the 2D Orszag-Tang vortex, 256 x 296
+    particles on the close-packed lattice, FP64, 50 leapfrog steps from the
+    initial conditions (plus the FP32 form), and the 1-core oracle on the
+    first `cpu_steps` steps of the same run."""
+    from ndspmhd_gb300 import configs
+    from ndspmhd_gb300.gpu import GpuSPH
+    from oracle.oracle import Oracle
+    o, p = configs.orszag_tang_2d(256)
+    n = p["x"].shape[0]
+    out = {"config": f"2D Orszag-Tang, {n} particles (256 x 296 hcp), periodic, {steps} leapfrog steps"}
+    for prec, key in ((0, "fp64"), (1, "fp32")):
+        o2 = dict(o, precision=prec)
+        g = GpuSPH(o2, configs.full_state(p, 2))
+        g.primitive2conservative()
+        g.dev_upload()
+        g.set_dt(0.0)
+        g.dev_step(steps)
+        ms = g.timing()["total_ms"]
+        d = g.dts()
+        g.close()
+        out[key] = {"value": round(n * steps / (ms * 1e-3), 1), "ms_per_step": round(ms / steps, 3),
+                    "time_reached": d["time"]}
+    orc = Oracle(o, configs.full_state(p, 2))
+    orc.primitive2conservative()
+    orc.set_dt(0.0, 0.0)
+    t0 = time.perf_counter()
+    orc.step(cpu_steps)
+    el = time.perf_counter() - t0
+    out["cpu_oracle_1core"] = {"value": round(n * cpu_steps / el, 1), "sample": f"first {cpu_steps} steps, {el:.1f} s"}
+    return out
+
+
 def run_dust(n1d: int, steps: int, warmup: int, nset: int = 8):
     """Two-fluid dust + gas MHD box (2 x n1d^3, periodic), a batch of `nset`
     (dust-to-gas ratio, stopping time) settings run one after another;
@@ -518,6 +551,7 @@ def main():
         line["batched"] = run_batched(200, 3)
         line["learned_h"] = run_learned(min(N1D, 128), 20, 40)
         line["dust"] = run_dust(96 if N1D >= 128 else 32, 3, 2)
+        line["orszag_tang_2d"] = run_ot2d()
     # kernel launches the library issued inside the timed step loop (counted
     # at every launch site)
     line["gpu_launches"] = tim32["launches_timed"]
