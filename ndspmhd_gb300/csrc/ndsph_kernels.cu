@@ -548,7 +548,8 @@ __global__ void k_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
                     pr = o.polyk * (double)powf((float)rho, (float)o.gamma);
                 else
                     pr = o.polyk * pow(rho, o.gamma);
-                cs = sqrt(o.gamma * pr / rho);
+                cs = (o.precision == NDSPH_PREC_FP32) ? (double)sqrtf((float)o.gamma * (float)pr / (float)rho)
+                                                      : sqrt(o.gamma * pr / rho);
             } else if (it != NDSPH_ITYPE_BND) {
                 pr = 0.0;
             }
@@ -556,7 +557,12 @@ __global__ void k_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
         } else {
             if (rho > 0.0) {
                 pr = (o.gamma - 1.0) * uu * rho;
-                cs = sqrt(o.gamma * pr / rho);
+                // FP32 form: c_s only enters FP32 pair terms and timestep bounds;
+                // gamma P / rho = gamma (gamma - 1) u without the FP64 divide and
+                // square root (~40 FP64 pipe slots per particle on this part)
+                cs = (o.precision == NDSPH_PREC_FP32)
+                         ? (double)sqrtf((float)(o.gamma * (o.gamma - 1.0)) * (float)uu)
+                         : sqrt(o.gamma * pr / rho);
             }
         }
         F.f[UU][k] = uu;

@@ -335,6 +335,34 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
     // one candidate: its list entry, position and type, and (FP32 form) its
     // velocity/mass pack, loaded by the caller
     const unsigned shift = (NDIM == 3) ? (unsigned)g.nlshift : 5u, omask = (1u << shift) - 1u;
+    // FP32 form: the kernel sums of one accepted pair (q_i < 2)
+    auto sums32 = [&](int j, float q2i, const float dxf[3], const float4& pvj) {
+        const float mj = pvj.w;
+        const float q = sqrtp(q2i);
+        float wv, gw, ggw;
+        if (q2i >= KERN_Q2_DIRECT) {
+            const KerF kf = kern_cubic(q, a.t.cnormf);
+            wv = kf.w; gw = kf.gw; ggw = kf.ggw;
+        } else {
+            const TabIdxF ix = tab_indexf(a.t, q2i);
+            wv = tab_valf(a.t.wf, ix);
+            gw = tab_valf(a.t.gwf, ix);
+            ggw = tab_valf(a.t.ggwf, ix);
+        }
+        fw.add(mj * wv);
+        fn.add(wv);
+        const float tg = q * gw + (float)NDIM * wv;
+        fg.add(mj * tg);
+        fgn.add(tg);
+        fgg.add(mj * ((float)(NDIM * (NDIM + 1)) * wv + (float)(2 * (NDIM + 1)) * q * gw + q2i * ggw));
+        if (j != i) {
+            const float rij = q * hif;
+            float dvr = (vif[0] - pvj.x) * dxf[0];
+            if (NDIM >= 2) dvr += (vif[1] - pvj.y) * dxf[1];
+            if (NDIM >= 3) dvr += (vif[2] - pvj.z) * dxf[2];
+            fd.add(mj * dvr * gw * rcp_ftz(rij + 1e-30f));
+        }
+    };
     auto pair = [&](unsigned pk, const float4& xsj, int typej, const float4& pvj) {
         const int j = (int)(pk >> shift);
         int d[3], w[3];
@@ -388,31 +416,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
             const float q2i = r2f * hi21f;
             nn++;
             if (fixed_i || !(q2i < 4.0f)) return;
-            const float mj = pvj.w;
-            const float q = sqrtp(q2i);
-            float wv, gw, ggw;
-            if (q2i >= KERN_Q2_DIRECT) {
-                const KerF kf = kern_cubic(q, a.t.cnormf);
-                wv = kf.w; gw = kf.gw; ggw = kf.ggw;
-            } else {
-                const TabIdxF ix = tab_indexf(a.t, q2i);
-                wv = tab_valf(a.t.wf, ix);
-                gw = tab_valf(a.t.gwf, ix);
-                ggw = tab_valf(a.t.ggwf, ix);
-            }
-            fw.add(mj * wv);
-            fn.add(wv);
-            const float tg = q * gw + (float)NDIM * wv;
-            fg.add(mj * tg);
-            fgn.add(tg);
-            fgg.add(mj * ((float)(NDIM * (NDIM + 1)) * wv + (float)(2 * (NDIM + 1)) * q * gw + q2i * ggw));
-            if (j != i) {
-                const float rij = q * hif;
-                float dvr = (vif[0] - pvj.x) * dxf[0];
-                if (NDIM >= 2) dvr += (vif[1] - pvj.y) * dxf[1];
-                if (NDIM >= 3) dvr += (vif[2] - pvj.z) * dxf[2];
-                fd.add(mj * dvr * gw * rcp_ftz(rij + 1e-30f));
-            }
+            sums32(j, q2i, dxf, pvj);
         }
     };
     if (PREC == NDSPH_PREC_FP64) {
