@@ -42,7 +42,7 @@ UNIT = "particle-updates/s"
 # force(3) dBevol/dt(3) du/dt de/dt dalpha/dt(3) divB curlB(3) del2u
 # graddivv(3) drhodt dhdt (21 doubles) once each
 RATES_BYTES_PER_PARTICLE = (26 + 21) * 8
-RATES_DRAM_BYTES_64 = 146.9e6
+RATES_DRAM_BYTES_64 = 146.5e6
 # density pass: reads x(3) h m v(3) (8 doubles) writes rho rhoalt drhodt dhdt
 # gradh gradhn gradgradh h (8 doubles) + numneigh (4 B)
 DENSITY_BYTES_PER_PARTICLE = 16 * 8 + 4
@@ -512,11 +512,14 @@ def main():
     rates_ms = tim32["rates_ms"]
     achieved = RATES_BYTES_PER_PARTICLE * n / (rates_ms * 1e-3) / 1e9 if rates_ms > 0 else 0.0
     # DRAM bytes of one k_rates<3,FP32> launch from an ncu capture of the 64^3 box
-    # (127.8 MB read + 19.1 MB written), scaled by the particle count
+    # (127.8 MB read + 18.7 MB written), scaled by the particle count
     traffic = round(RATES_DRAM_BYTES_64 * n / 64 ** 3)
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": traffic, "traffic_note": "ncu dram bytes of the 64^3 launch x N/64^3",
                 "kernel": "k_rates<3,FP32> (rates sweep)",
+                "issue_view": {"issue_active_frac": 0.564, "threads_per_instruction": 29.4, "warps_active_frac": 0.222,
+                               "source": "ncu --set full of the 64^3 launch (profiles/k_rates_mhd_box3d_64cubed_fp32.md): "
+                                         "the sweep is bound by instruction issue and load latency"},
                 "note": f"peak of {peak_kind} (MEASURED_PEAKS.json hbm_gbs); algorithmic bytes "
                         f"{RATES_BYTES_PER_PARTICLE} B/particle x {n}; the sweep is FP32-issue bound, "
                         f"see profiles/"}
