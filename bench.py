@@ -404,14 +404,18 @@ def run_dust(n1d: int, steps: int, warmup: int, nset: int = 8):
             "dtdrag_range": [min(dtdrag), max(dtdrag)]}
 
 
-def cpu_baseline(n1d: int = CPU_SAMPLE_N1D, steps: int = CPU_SAMPLE_STEPS) -> dict:
+def cpu_baseline(n1d: int = CPU_SAMPLE_N1D, steps: int = CPU_SAMPLE_STEPS, warmup: int = 0) -> dict:
     """The oracle (single-threaded C restatement of the reference) on a
-    bounded sample of the same workload: a n1d^3 box, `steps` leapfrog steps."""
+    bounded sample of the same workload: a n1d^3 box, `warmup` untimed then
+    `steps` timed leapfrog steps."""
     from ndspmhd_gb300 import configs
     from oracle.oracle import Oracle
     o, p = configs.mhd_box_3d(n1d, seed=1234)
     orc = Oracle(o, configs.full_state(p, 3))
     orc.primitive2conservative()
+    orc.set_dt(0.0, 0.0)
+    if warmup > 0:
+        orc.step(warmup)
     t0 = time.perf_counter()
     orc.step(steps)
     el = time.perf_counter() - t0
@@ -422,8 +426,8 @@ def cpu_baseline(n1d: int = CPU_SAMPLE_N1D, steps: int = CPU_SAMPLE_STEPS) -> di
 
 
 def _cpu_worker(args):
-    n1d, steps = args
-    return cpu_baseline(n1d, steps)["value"]
+    n1d, steps, warmup = args
+    return cpu_baseline(n1d, steps, warmup)["value"]
 
 
 def reference_arm(args):
@@ -437,23 +441,25 @@ def reference_arm(args):
     import multiprocessing as mp
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
-    for _ in range(max(args.warmup, 0) and 0):
-        pass
+    # every core runs its own replica of the sample: `warmup` untimed steps,
+    # then `steps` timed ones (the reference is serial)
+    steps = max(1, args.steps)
+    warmup = max(0, args.warmup)
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
-        vals = pool.map(_cpu_worker, [(CPU_SAMPLE_N1D, CPU_SAMPLE_STEPS)] * cores)
+        vals = pool.map(_cpu_worker, [(CPU_SAMPLE_N1D, steps, warmup)] * cores)
     el = time.perf_counter() - t0
     value = float(sum(vals))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
-        "n_gpus": args.gpus, "steps": CPU_SAMPLE_STEPS, "warmup": 0,
+        "n_gpus": args.gpus, "steps": steps, "warmup": warmup,
         "ms_per_step": 1e3 * (CPU_SAMPLE_N1D ** 3) / (value / cores) if value > 0 else None,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded 3D MHD box)",
         "config": {"workload": f"3D MHD box, sample {CPU_SAMPLE_N1D}^3 per core", "n1d": CPU_SAMPLE_N1D,
                    "parallelism": f"{cores} independent serial replicas"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} x ({CPU_SAMPLE_N1D}^3 box, {CPU_SAMPLE_STEPS} steps), wall {el:.1f} s"},
+                         "sample": f"{cores} x ({CPU_SAMPLE_N1D}^3 box, {warmup} + {steps} steps), wall {el:.1f} s"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -2308,7 +2308,8 @@ extern "C" int ndsph_set_tuning(ndsph_ctx* ctx, const ndsph_tuning* t)
     ctx->nl_reuse = t->nl_reuse;
     ctx->nl_grow = t->nl_grow;
     ctx->nl_sw5 = (t->stencil == 5) ? 1 : 0;
-    if ((double)t->graph_cell_margin != ctx->gmargin) graph_drop(ctx);
+    // captured batched steps hold the old settings: capture afresh
+    graph_drop(ctx);
     ctx->gmargin = t->graph_cell_margin;
     // rows built with the old radius: the next step links afresh
     ctx->nl_valid = false;
