@@ -309,12 +309,14 @@ NDSPH_API int ndsph_get_timing(ndsph_ctx* ctx, ndsph_timing* t);
  *   nl_grow   room for Newton-Raphson growth of h in that check      (1.005)
  *   graph_cell_margin  batched captured steps: cells of 2 hmax margin, so
  *             h may grow by the margin before a step leaves the graph (1.05)
- *   stencil   5: the FP32 form of one 3D simulation searches 5^3 stencils
- *             of cells of hmax (x skin), about half the candidates of 3^3
- *             stencils of 2 hmax cells; 3: always the latter.  The FP64 form,
- *             1D and 2D, and the batched form use 3^ndim.  With 5 the neighbour rows
- *             pack 25-bit particle indices (npart < 2^25; larger runs fall
- *             back to 3).                                                  (5)
+ *   stencil   5 (wide): the FP32 form of one 3D simulation searches 5^3
+ *             stencils of cells of hmax (x skin), about half the candidates
+ *             of 3^3 stencils of 2 hmax cells, its rows packing 25-bit
+ *             particle indices (npart < 2^25, else 3^3); 1D contexts (every
+ *             form, batches included) search runs of 17 cells of hmax/4 and
+ *             skip each cell farther than 2 skin max(h_i, the cell's largest
+ *             h).  3 (narrow): 3^ndim stencils of 2 hmax cells everywhere.
+ *             2D, the 3D FP64 form and 3D batches always use 3^ndim.     (5)
  * ndsph_set_tuning rejects values outside nl_skin in [1, 2], nl_grow in
  * [1, 1.5], graph_cell_margin in [1, 2], stencil in {3, 5}; the next step
  * links afresh.                                                              */

@@ -379,10 +379,12 @@ static int ensure_cells(ndsph_ctx* ctx, int ncells)
     if (ctx->srt.count) cudaFree(ctx->srt.count);
     if (ctx->srt.start) cudaFree(ctx->srt.start);
     if (ctx->srt.blocksums) cudaFree(ctx->srt.blocksums);
+    if (ctx->srt.cell_h) cudaFree(ctx->srt.cell_h);
     int cap = std::max(ncells + 1, 4096);
     cap = cap + cap / 4;
     CK(cudaMalloc(&ctx->srt.count, sizeof(int) * (size_t)cap));
     CK(cudaMalloc(&ctx->srt.start, sizeof(int) * (size_t)(cap + 1)));
+    CK(cudaMalloc(&ctx->srt.cell_h, sizeof(float) * (size_t)cap));
     int nb = (cap + 4095) / 4096 + 1;
     CK(cudaMalloc(&ctx->srt.blocksums, sizeof(int) * (size_t)nb));
     ctx->srt.cap_cells = cap;
@@ -493,7 +495,7 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     free_particles(ctx);
     void* ptrs[] = {ctx->tab64, ctx->tab32, ctx->red, ctx->d_dtout, ctx->d_ncalc, ctx->d_fields,
-                    ctx->srt.count, ctx->srt.start, ctx->srt.blocksums, ctx->mlp_p, ctx->mlp_m, ctx->mlp_v,
+                    ctx->srt.count, ctx->srt.start, ctx->srt.blocksums, ctx->srt.cell_h, ctx->mlp_p, ctx->mlp_m, ctx->mlp_v,
                     ctx->mlp_g, ctx->mlp_loss, ctx->mlp_frag, ctx->d_sim_red, ctx->d_sim_dt, ctx->d_sim_dtnext,
                     ctx->d_sim_out, ctx->d_sim_off};
     for (void* p : ptrs) if (p) cudaFree(p);
@@ -748,13 +750,20 @@ static int build_grid(ndsph_ctx* ctx, double hmax, const double* lo, const doubl
     // the 3-wide stencil, then to the plain cell size.
     const double base = 2.0 * hmax * (1.0 + 1.e-9);
     const double skin_cf = reuse_on(ctx) ? (double)ctx->nl_skin : 1.0;
-    const bool sw5_ok = ctx->nl_sw5 && ctx->o.precision == NDSPH_PREC_FP32 && !ctx->o.batched &&
-                        ctx->o.ndim == 3 && ctx->n < (1 << 25);
-    const int tries_sw[3] = {5, 3, 3};
+    // the wide stencil: 5^3 cells of hmax in 3D (FP32 form, one simulation);
+    // in 1D (every form, batches included) a run of 17 cells of hmax/4, which
+    // keeps cells small in the dense tubes of a batch whose cell size the
+    // sparsest tube sets
+    int wide = 3;
+    if (ctx->nl_sw5 && ctx->o.ndim == 1) wide = 17;
+    else if (ctx->nl_sw5 && ctx->o.ndim == 3 && ctx->o.precision == NDSPH_PREC_FP32 && !ctx->o.batched &&
+             ctx->n < (1 << 25))
+        wide = 5;
+    const int tries_sw[3] = {wide, 3, 3};
     const double tries_cf[3] = {skin_cf, skin_cf, 1.0};
     int sw = 3;
     double cf = 1.0;
-    for (int t = sw5_ok ? 0 : 1; t < 3; t++) {
+    for (int t = (wide > 3) ? 0 : 1; t < 3; t++) {
         const int reach = (tries_sw[t] - 1) / 2;
         bool fits = true;
         for (int d = 0; d < ctx->o.ndim; d++)
@@ -764,7 +773,7 @@ static int build_grid(ndsph_ctx* ctx, double hmax, const double* lo, const doubl
     }
     ctx->grid_cf = cf;
     g.sw = sw;
-    g.nlshift = (sw == 5) ? 7 : 5;
+    g.nlshift = (ctx->o.ndim == 3 && sw == 5) ? 7 : 5;   // offsets < 32 otherwise
     const double cmin = base * cf / (double)((sw - 1) / 2);
     long ncells = 1;
     for (int d = 0; d < 3; d++) {
@@ -975,6 +984,7 @@ static SweepArgs sweep_args(ndsph_ctx* ctx)
     a.F = ctx->F;
     a.S = ctx->S;
     a.cell_start = ctx->srt.start;
+    a.cell_h = ctx->srt.cell_h;
     a.g = ctx->g;
     a.o = ctx->o;
     a.t = ctx->t;
@@ -1974,7 +1984,8 @@ static bool graph_usable(const ndsph_ctx* ctx)
 static double cell_cap(const ndsph_ctx* ctx)
 {
     double cap = 1e300;
-    for (int d = 0; d < ctx->o.ndim; d++) cap = std::min(cap, 0.5 * ctx->g.cs[d] / (1.0 + 1.e-9));
+    const double reach = (double)((ctx->g.sw - 1) / 2);
+    for (int d = 0; d < ctx->o.ndim; d++) cap = std::min(cap, 0.5 * reach * ctx->g.cs[d] / (1.0 + 1.e-9));
     return cap;
 }
 

@@ -926,7 +926,8 @@ __global__ void k_grid_check(Reduce* red, Grid g, DevOpts o)
 {
     const double hmax = bitsd(red->hmax);
     double cap = 1e300;
-    for (int d = 0; d < o.ndim; d++) cap = fmin(cap, 0.5 * g.cs[d] / (1.0 + 1.e-9));
+    const double reach = (double)((g.sw - 1) / 2);
+    for (int d = 0; d < o.ndim; d++) cap = fmin(cap, 0.5 * reach * g.cs[d] / (1.0 + 1.e-9));
     bool ok = (hmax > 0.0) && (hmax <= cap);
     for (int d = 0; d < o.ndim; d++) {
         if (o.periodic[d]) continue;

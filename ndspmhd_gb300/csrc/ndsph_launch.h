@@ -43,6 +43,7 @@ struct SortScratch {
     int* start;       // exclusive scan (ncells + 1)
     int* perm;        // sorted slot -> unsorted index
     int* blocksums;   // scan scratch
+    float* cell_h;    // largest h of each cell's particles (1D row-build pruning)
     int cap_cells;
     int cap_blocks;
 };
@@ -51,6 +52,7 @@ struct SweepArgs {
     FieldPtrs F;
     Side S;
     const int* cell_start;   // ncells + 1
+    float* cell_h;           // ncells: largest h per cell (filled by the 1D row build)
     Grid g;
     DevOpts o;
     Tables t;

@@ -108,6 +108,11 @@ __device__ __forceinline__ KerF kern_cubic(float q, float c)
 template <int NDIM>
 __device__ __forceinline__ void stencil_d(unsigned o, int sw, int d[3])
 {
+    if (NDIM == 1) {   // any odd width
+        d[0] = (int)o - ((sw - 1) >> 1);
+        d[1] = d[2] = 0;
+        return;
+    }
     unsigned q, q2;
     int r;
     if (sw == 5) {
@@ -168,7 +173,7 @@ struct Stencil {
     // o = (dx+r) + sw (dy+r) + sw^2 (dz+r) (the cell exists)
     __device__ __forceinline__ void offset(unsigned o, const Grid& g, int d[3], int w[3]) const
     {
-        stencil_d<NDIM>(o, NDIM == 3 ? g.sw : 3, d);   // 1D and 2D always search 3 wide
+        stencil_d<NDIM>(o, NDIM == 2 ? 3 : g.sw, d);   // 2D always searches 3 wide
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             const int c = cc[k] + d[k];
@@ -1210,7 +1215,7 @@ __device__ __forceinline__ void nl_scan_run(const SweepArgs& a, const float4& xs
 {
     const Grid& g = a.g;
     const unsigned shift = (NDIM == 3) ? (unsigned)g.nlshift : 5u;
-    const int r = (NDIM == 3) ? (g.sw - 1) >> 1 : 1;
+    const int r = (NDIM == 2) ? 1 : (g.sw - 1) >> 1;
     for (int j0 = jb; j0 < je; j0 += 4) {
         float4 q[4];
 #pragma unroll
@@ -1249,14 +1254,30 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
     const float csmin = fminf(g.csf[0], fminf(NDIM >= 2 ? g.csf[1] : g.csf[0], NDIM >= 3 ? g.csf[2] : g.csf[0]));
     const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
     const float sk = 2.0f * a.nl_skin * 1.0002f;
-    const int sw = (NDIM == 3) ? g.sw : 3, r = (sw - 1) >> 1;
+    const int sw = (NDIM == 2) ? 3 : g.sw, r = (sw - 1) >> 1;
     const float reach = (float)r * csmin * 1.001f + abs_tol;
     const float reach2 = reach * reach;
     Stencil<NDIM> stn(a.S.cell[i], g);
     unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
     int cnt = 0;
+    if (NDIM == 1) {
+        // 1D: cells of 2 hmax / r in a run of 2r + 1; a cell is searched only
+        // within 2 skin max(h_i, largest h of the cell) of the particle, so a
+        // particle of small h in a dense region (a dense tube of a batch,
+        // whose cells are sized by the sparsest) scans only the cells next to it
+        const int bnone[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+        for (int dx = -r; dx <= r; dx++) {
+            const float ex = slab_dist(xsi.x, dx, g.csf[0]);
+            if (ex > reach) continue;
+            int d[3] = {dx, 0, 0}, w[3], cid;
+            if (!stn.cell_at_d(d, g, a.o, cid, w)) continue;
+            if (ex > sk * fmaxf(hi, a.cell_h[cid]) + abs_tol) continue;
+            nl_scan_run<NDIM>(a, xsi, hi, sk, abs_tol, a.cell_start[cid], a.cell_start[cid + 1], bnone, dx, 0.f, 0.f,
+                              0u, row, cnt);
+        }
+    }
     const int zlo = (NDIM >= 3) ? -r : 0, ylo = (NDIM >= 2) ? -r : 0;
-    for (int dz = zlo; dz <= -zlo; dz++) {
+    for (int dz = zlo; dz <= -zlo && NDIM >= 2; dz++) {
         const float ez = (NDIM >= 3) ? slab_dist(xsi.z, dz, g.csf[2]) : 0.f;
         for (int dy = ylo; dy <= -ylo; dy++) {
             const float ey = (NDIM >= 2) ? slab_dist(xsi.y, dy, g.csf[1]) : 0.f;
@@ -1303,9 +1324,23 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
     atomicMax(&a.red->nl_maxcnt, cnt);
 }
 
+// largest h (the xs.w the build uses) of each cell's particles (1D pruning)
+__global__ void k_cell_hmax(const int* __restrict__ start, const float4* __restrict__ xs, float* cell_h,
+                            int ncells)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    float m = 0.f;
+    for (int k = start[c]; k < start[c + 1]; k++) m = fmaxf(m, xs[k].w);
+    cell_h[c] = m;
+}
+
 void launch_build_nlist(const SweepArgs& a, cudaStream_t st)
 {
     if (a.n <= 0) return;
+    if (a.o.ndim == 1)
+        NDSPH_COUNT_LAUNCH, k_cell_hmax<<<nblk(a.g.ncells, 256), 256, 0, st>>>(a.cell_start, a.S.xs, a.cell_h,
+                                                                            a.g.ncells);
     const int nbp = nblk(a.n, 128);
     if (a.o.ndim == 1) NDSPH_COUNT_LAUNCH, k_build_nlist<1><<<nbp, 128, 0, st>>>(a);
     else if (a.o.ndim == 2) NDSPH_COUNT_LAUNCH, k_build_nlist<2><<<nbp, 128, 0, st>>>(a);
