@@ -89,6 +89,13 @@ module gpu_sph
       integer(c_int32_t), value              :: npart
       type(ndsph_dt_t), intent(inout)        :: dts
     end function
+    integer(c_int) function ndsph_step(ctx, p, npart, dts) bind(C, name="ndsph_step")
+      import :: c_ptr, c_int, c_int32_t, ndsph_particles_t, ndsph_dt_t
+      type(c_ptr), value                     :: ctx
+      type(ndsph_particles_t), intent(inout) :: p
+      integer(c_int32_t), value              :: npart
+      type(ndsph_dt_t), intent(inout)        :: dts
+    end function
     integer(c_int) function ndsph_set_tuning(ctx, t) bind(C, name="ndsph_set_tuning")
       import :: c_ptr, c_int, ndsph_tuning_t
       type(c_ptr), value                :: ctx
@@ -102,6 +109,8 @@ module gpu_sph
  end interface
 
  type(c_ptr), save :: ctx = c_null_ptr
+ ! pair-sum form of the context: 0 plain FP64 (the parity form), 1 FP32 pairs
+ integer, save :: gpu_precision = 0
 
 contains
 
@@ -125,7 +134,7 @@ contains
   o%beta = beta;  o%avdecayconst = avdecayconst;  o%gamma = gamma;  o%polyk = polyk
   o%idust = idust;  o%idrag_nature = idrag_nature;  o%Kdrag = Kdrag
   o%C_cour = C_cour;  o%C_force = C_force
-  o%precision = 0;  o%learned_h = 0
+  o%precision = gpu_precision;  o%learned_h = 0
  end subroutine gpu_opts
 
  subroutine gpu_particles(p)
@@ -205,5 +214,24 @@ contains
   dtcourant = d%dtcourant;  dtforce = d%dtforce;  dtav = d%dtav
   dtdrag = d%dtdrag;  dtvisc = d%dtvisc
  end subroutine gpu_derivs
+
+ ! replacement body of step (stepND_leapfrog_mhd.f90:31): predictor, derivs,
+ ! corrector and the next dt on the device in one call; evolve.f90:93-96
+ ! advances time and nsteps itself before calling step, so only dt and the
+ ! timestep bounds come back
+ subroutine gpu_step()
+  use part,     only:npart,ntotal
+  use timestep, only:dt,time,nsteps,dtcourant,dtforce,dtav,dtdrag,dtvisc
+  type(ndsph_particles_t) :: p
+  type(ndsph_dt_t) :: d
+  call gpu_ensure()
+  call gpu_particles(p)
+  d%dt = dt;  d%time = time;  d%nsteps = int(nsteps,c_int32_t)
+  call gpu_check(ndsph_step(ctx, p, int(npart,c_int32_t), d), 'step')
+  ntotal = npart
+  dtcourant = d%dtcourant;  dtforce = d%dtforce;  dtav = d%dtav
+  dtdrag = d%dtdrag;  dtvisc = d%dtvisc
+  dt = d%dt
+ end subroutine gpu_step
 
 end module gpu_sph
