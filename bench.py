@@ -524,11 +524,10 @@ def main():
                 "frac": round(achieved / peak, 5), "traffic": traffic, "traffic_note": "ncu dram bytes of the 64^3 launch x N/64^3",
                 "kernel": "k_rates<3,FP32> (rates sweep)",
                 "issue_view": {"issue_active_frac": 0.564, "threads_per_instruction": 29.4, "warps_active_frac": 0.222,
-                               "source": "ncu --set full of the 64^3 launch (profiles/k_rates_mhd_box3d_64cubed_fp32.md): "
-                                         "the sweep is bound by instruction issue and load latency"},
+                               "source": "ncu --set full of the 64^3 launch: the sweep is bound by instruction "
+                                         "issue and load latency"},
                 "note": f"peak of {peak_kind} (MEASURED_PEAKS.json hbm_gbs); algorithmic bytes "
-                        f"{RATES_BYTES_PER_PARTICLE} B/particle x {n}; the sweep is FP32-issue bound, "
-                        f"see profiles/"}
+                        f"{RATES_BYTES_PER_PARTICLE} B/particle x {n}; the sweep is FP32-issue bound"}
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": warmup, "ms_per_step": round(ms32, 4), "higher_is_better": True, "scaling": "weak",

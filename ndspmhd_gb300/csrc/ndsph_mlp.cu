@@ -5,7 +5,7 @@
 // converged h and the leapfrog predictor's h_pred = hhin + dt dhdt
 // (stepND_leapfrog_mhd.f90:152-153, ihvar = 2).  The prediction only moves
 // the starting point of iterate_density: NR keeps the same tolerance and
-// remains the judge, so a wrong prediction costs extra passes, never accuracy.
+// decides convergence, so a wrong prediction costs extra passes, never accuracy.
 //
 //  * inference: BF16 weights and activations, FP32 accumulation, on the
 //    tensor cores with mma.sync.m16n8k16 (one warp = 16 particles per tile);

@@ -12,14 +12,16 @@
 //    epilogue.
 //
 // The reference scatters each unordered pair to both particles; here every
-// particle gathers its own side of every pair (H6 in the design notes), so no
-// atomics touch per-particle sums and results are deterministic.  The
-// j-side formulas of the reference equal the i-side formulas evaluated from
-// j's point of view (checked term by term in the design notes), so the
-// gather is the same sum in a different order.
+// particle gathers its own side of every pair, so no atomics touch
+// per-particle sums and results are deterministic.  The j-side formulas of
+// the reference equal the i-side formulas evaluated from j's point of view
+// (forces and dB/dt change sign with dr and dv, div B, curl B and du/dt are
+// symmetric or flip consistently), so the gather is the same sum in a
+// different order.
 //
-// Neighbour search: particle slots are cell-sorted; each thread walks the
-// 3^NDIM stencil of its own cell.  Candidates are screened in FP32 with a
+// Neighbour search: particle slots are cell-sorted; one row per particle
+// lists the candidates of the stencil around its cell (built by
+// k_build_nlist), and the sweeps walk the rows.  Candidates are screened in FP32 with a
 // conservative margin on cell-relative coordinates; in the FP64 form the
 // survivors are re-tested exactly in FP64 with the reference's own rounding
 // (dx = x_i - x_j' with periodic images placed as ghostND_mhd.f90:224-225
