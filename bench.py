@@ -430,6 +430,49 @@ def _cpu_worker(args):
     return cpu_baseline(n1d, steps, warmup)["value"]
 
 
+def _cpu_tube_worker(args):
+    """One host process: the oracle on each of its Brio-Wu tubes in turn,
+    `warmup` untimed then `steps` timed steps from the initial conditions;
+    returns (particle-updates, seconds in the timed steps)."""
+    counts, steps, warmup = args
+    from ndspmhd_gb300 import configs
+    from oracle.oracle import Oracle
+    upd, el = 0, 0.0
+    for c in counts:
+        o, p = configs.brio_wu_tube(int(c))
+        orc = Oracle(o, configs.full_state(p, 1))
+        orc.primitive2conservative()
+        orc.set_dt(0.0, 0.0)
+        if warmup > 0:
+            orc.step(warmup)
+        t0 = time.perf_counter()
+        orc.step(steps)
+        el += time.perf_counter() - t0
+        upd += p["x"].shape[0] * steps
+    return upd, el
+
+
+def cpu_batched_baseline(counts, steps: int, warmup: int, ntubes: int = 1024) -> dict:
+    """The batched workload on the host: the reference is serial, so the
+    tubes are spread over all host cores as independent processes (spawned:
+    the parent already holds a CUDA context).  Bounded sample: the first
+    `ntubes` tubes of the same seeded batch, the same steps as the GPU run."""
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    sample = [int(c) for c in counts[:ntubes]]
+    work = [(sample[w::cores], steps, warmup) for w in range(cores)]
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_cpu_tube_worker, work)
+    wall = time.perf_counter() - t0
+    upd = sum(r[0] for r in res)
+    el = max(r[1] for r in res)
+    return {"value": round(upd / el, 1), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"first {len(sample)} tubes ({upd // steps} particles), {warmup} + {steps} steps each, "
+                      f"FP64 oracle, {cores} processes, slowest process {el:.1f} s in the timed steps, "
+                      f"wall {wall:.1f} s"}
+
+
 def reference_arm(args):
     """--impl reference: the reference's CPU implementation of the path (the
     oracle port; the Fortran reference cannot be built here) on all host
@@ -557,6 +600,9 @@ def main():
         line["cpu_baseline"] = cpu
     if not args.no_extra and world == 1:
         line["batched"] = run_batched(200, 3)
+        if not args.no_cpu:
+            from ndspmhd_gb300 import configs
+            line["batched"]["cpu_baseline"] = cpu_batched_baseline(configs.brio_wu_batch(4096)[3], 200, 3)
         line["learned_h"] = run_learned(min(N1D, 128), 20, 40)
         line["dust"] = run_dust(96 if N1D >= 128 else 32, 3, 2)
         line["orszag_tang_2d"] = run_ot2d()

@@ -46,3 +46,16 @@ def test_replicas_time_by_slowest_rank():
 def test_single_process_passes_through():
     assert bench.max_over_ranks(3.0, None, "cpu") == 3.0
     assert bench.replica_value(2_097_152, 1, 6.0) == pytest.approx(2_097_152 / 6e-3)
+
+
+def test_batched_cpu_baseline_spreads_tubes_over_processes():
+    """The batched workload's host baseline: every sampled tube is stepped
+    once by one process, and the rate counts each tube's particles x steps."""
+    from ndspmhd_gb300 import configs
+    counts = [200, 300, 450]
+    res = bench.cpu_batched_baseline(counts, 4, 1, ntubes=3)
+    n = sum(configs.brio_wu_tube(c)[1]["x"].shape[0] for c in counts)
+    assert res["kind"] == "port" and res["cores"] >= 1 and res["value"] > 0
+    assert f"({n} particles)" in res["sample"]
+    upd, el = bench._cpu_tube_worker(([counts[0]], 4, 1))
+    assert upd == configs.brio_wu_tube(counts[0])[1]["x"].shape[0] * 4 and el > 0
