@@ -187,7 +187,10 @@ NDSPH_API const char* ndsph_last_error(ndsph_ctx* ctx);
  *                     in one H2D + one D2H.
  * ndsph_step          replaces step               stepND_leapfrog_mhd.f90:31-275
  *                     (predictor, derivs, corrector, boundary, dt) with the
- *                     leapfrog on the device; state in host arrays.            */
+ *                     leapfrog on the device; state in host arrays.  Outputs
+ *                     are copied back while the step runs, so after a
+ *                     non-zero status the arrays hold a mix of old and new
+ *                     values (the reference stops there too).                  */
 NDSPH_API int ndsph_set_linklist(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts);
 NDSPH_API int ndsph_iterate_density(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, ndsph_dt* dts);
 NDSPH_API int ndsph_conservative2primitive(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart);
@@ -317,15 +320,22 @@ NDSPH_API int ndsph_get_timing(ndsph_ctx* ctx, ndsph_timing* t);
  *             skip each cell farther than 2 skin max(h_i, the cell's largest
  *             h).  3 (narrow): 3^ndim stencils of 2 hmax cells everywhere.
  *             2D, the 3D FP64 form and 3D batches always use 3^ndim.     (5)
+ *   step_pieces  ndsph_step on staged host arrays of >= 65536 particles and
+ *             no fixed particles: the rates sweep runs in this many pieces,
+ *             piece c over the particles of the c-th chunk of the host
+ *             arrays, and each chunk's rates and corrected state go back
+ *             while the later pieces run; 1: all after the corrector.  The
+ *             values returned are the same either way.                   (4)
  * ndsph_set_tuning rejects values outside nl_skin in [1, 2], nl_grow in
- * [1, 1.5], graph_cell_margin in [1, 2], stencil in {3, 5}; the next step
- * links afresh.                                                              */
+ * [1, 1.5], graph_cell_margin in [1, 2], stencil in {3, 5}, step_pieces in
+ * [1, 8]; the next step links afresh.                                        */
 typedef struct ndsph_tuning {
     float   nl_skin;
     int32_t nl_reuse;
     float   nl_grow;
     float   graph_cell_margin;
     int32_t stencil;
+    int32_t step_pieces;
 } ndsph_tuning;
 NDSPH_API int ndsph_set_tuning(ndsph_ctx* ctx, const ndsph_tuning* t);
 NDSPH_API int ndsph_get_tuning(ndsph_ctx* ctx, ndsph_tuning* t);

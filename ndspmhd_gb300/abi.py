@@ -75,7 +75,7 @@ class NdsphTiming(C.Structure):
 class NdsphTuning(C.Structure):
     """ndsph_tuning: neighbour-search knobs (include/ndsph.h)."""
     _fields_ = [("nl_skin", C.c_float), ("nl_reuse", C.c_int32), ("nl_grow", C.c_float),
-                ("graph_cell_margin", C.c_float), ("stencil", C.c_int32)]
+                ("graph_cell_margin", C.c_float), ("stencil", C.c_int32), ("step_pieces", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

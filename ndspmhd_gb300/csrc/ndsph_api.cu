@@ -49,6 +49,8 @@ struct ndsph_ctx {
     Reduce* h_red = nullptr;     // pinned mirror
     double* d_dtout = nullptr;
     double* h_dtout = nullptr;
+    Reduce* hd_red = nullptr;    // device addresses of the pinned mirrors (null: not mapped)
+    double* hd_dtout = nullptr;
     int* d_ncalc = nullptr;
     // host staging
     double* d_stage = nullptr;   // n*3 doubles
@@ -62,6 +64,7 @@ struct ndsph_ctx {
     // buffers), and outputs final before the rates sweep go back under it
     cudaStream_t st_cp = nullptr;
     cudaEvent_t ev_cp[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr}, ev_dl = nullptr;
+    cudaEvent_t ev_pfork = nullptr, ev_pjoin = nullptr;   // rates pieces on two streams
     int stage_k = 0;
     ndsph_particles* dl_early = nullptr;   // ndsph_step: where the early outputs go
     // ndsph_step: the inputs only the EOS and the Bevol/energy/alpha predictor
@@ -72,6 +75,14 @@ struct ndsph_ctx {
     int late_k = 0;
     bool late_pending = false;
     bool dl_density_done = false, dl_prim_done = false;
+    // ndsph_step: the rates sweep runs in dl_pieces pieces, one per chunk of
+    // the host arrays, and each chunk's last outputs go back while the later
+    // pieces run (dl_tail: where they go; null: all after the corrector)
+    ndsph_particles* dl_tail = nullptr;
+    bool dl_tail_done = false;
+    int dl_pieces = 4;
+    int* d_plist = nullptr;      // slots grouped by host chunk
+    int* d_pcnt = nullptr;       // its scratch: dl_pieces counts per 1024 slots
     double* d_arena = nullptr;   // download staging: every output field side by side
     size_t arena_cap = 0;        // doubles
     size_t arena_used = 0;
@@ -316,7 +327,8 @@ static void free_particles(ndsph_ctx* ctx)
                     ctx->S.numneigh, ctx->S.cell, ctx->S.xs, ctx->S.h1, ctx->S.active, ctx->S.active_next,
                     ctx->S.flag, ctx->itype2, ctx->id2, ctx->ireal2, ctx->srt.key, ctx->srt.slot, ctx->srt.perm,
                     ctx->d_stage, ctx->d_stage_late, ctx->d_istage, ctx->S.pk_v, ctx->S.pk_t, ctx->S.pk_b, ctx->S.pk_a,
-                    ctx->S.nl, ctx->S.nl_cnt, ctx->S.hb, ctx->S.xsb, ctx->S.sim, ctx->sim2};
+                    ctx->S.nl, ctx->S.nl_cnt, ctx->S.hb, ctx->S.xsb, ctx->S.sim, ctx->sim2, ctx->d_plist,
+                    ctx->d_pcnt};
     for (void* p : ptrs) if (p) cudaFree(p);
     ctx->slab[0] = ctx->slab[1] = nullptr;
     memset(&ctx->S, 0, sizeof(ctx->S));
@@ -324,6 +336,7 @@ static void free_particles(ndsph_ctx* ctx)
     ctx->sim2 = nullptr;
     ctx->srt.key = ctx->srt.slot = ctx->srt.perm = nullptr;
     ctx->d_stage = nullptr; ctx->d_istage = nullptr; ctx->d_stage_late = nullptr;
+    ctx->d_plist = ctx->d_pcnt = nullptr;
     ctx->cap = 0;
 }
 
@@ -358,6 +371,8 @@ static int ensure_capacity(ndsph_ctx* ctx, int n)
     CK(cudaMalloc(&ctx->S.nl_cnt, ib));
     CK(cudaMalloc(&ctx->S.sim, ib));
     CK(cudaMalloc(&ctx->sim2, ib));
+    CK(cudaMalloc(&ctx->d_plist, ib));
+    CK(cudaMalloc(&ctx->d_pcnt, sizeof(int) * 8 * ((size_t)cap / 1024 + 1)));
     CK(cudaMemsetAsync(ctx->S.sim, 0, ib, ctx->st));
     CK(cudaMalloc(&ctx->S.hb, sizeof(float) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.xsb, sizeof(float4) * (size_t)cap));
@@ -419,6 +434,8 @@ extern "C" int ndsph_init(ndsph_ctx** out, const ndsph_opts* opts, int32_t nmax)
         cudaEventCreateWithFlags(&ctx->ev_used[0], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_used[1], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_dl, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_pfork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_pjoin, cudaEventDisableTiming) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->st_up, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_late, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_up0, cudaEventDisableTiming) != cudaSuccess) {
@@ -450,6 +467,12 @@ extern "C" int ndsph_init(ndsph_ctx** out, const ndsph_opts* opts, int32_t nmax)
         g_err = "cudaMalloc failed in ndsph_init";
         ndsph_finalize(ctx);
         return NDSPH_E_CUDA;
+    }
+    if (cudaHostGetDevicePointer((void**)&ctx->hd_red, ctx->h_red, 0) != cudaSuccess ||
+        cudaHostGetDevicePointer((void**)&ctx->hd_dtout, ctx->h_dtout, 0) != cudaSuccess) {
+        cudaGetLastError();
+        ctx->hd_red = nullptr;
+        ctx->hd_dtout = nullptr;
     }
     cudaMemcpy(ctx->tab64, h64.data(), sizeof(double2) * 4 * NTAB, cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->tab32, h32.data(), sizeof(float2) * 4 * NTAB, cudaMemcpyHostToDevice);
@@ -509,7 +532,8 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
     if (ctx->st_up) { cudaStreamSynchronize(ctx->st_up); cudaStreamDestroy(ctx->st_up); }
     if (ctx->ev_late) cudaEventDestroy(ctx->ev_late);
     if (ctx->ev_up0) cudaEventDestroy(ctx->ev_up0);
-    for (cudaEvent_t ev : {ctx->ev_cp[0], ctx->ev_cp[1], ctx->ev_used[0], ctx->ev_used[1], ctx->ev_dl})
+    for (cudaEvent_t ev : {ctx->ev_cp[0], ctx->ev_cp[1], ctx->ev_used[0], ctx->ev_used[1], ctx->ev_dl,
+                            ctx->ev_pfork, ctx->ev_pjoin})
         if (ev) cudaEventDestroy(ev);
     if (ctx->d_live) cudaFree(ctx->d_live);
     if (ctx->st2) cudaStreamDestroy(ctx->st2);
@@ -521,9 +545,30 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
 // ---------------------------------------------------------------------------
 // helpers
 // ---------------------------------------------------------------------------
+// the reductions (and dt results) the host reads between kernels: a
+// one-block kernel writes them into the mapped pinned mirror, so the read is
+// not queued behind the bulk output copies on the copy engines
+static_assert(sizeof(Reduce) % 4 == 0, "Reduce is read back in 4-byte words");
+static cudaError_t read_red(ndsph_ctx* ctx, const Reduce* src, cudaStream_t st)
+{
+    if (ctx->hd_red) {
+        launch_read_words(ctx->hd_red, src, sizeof(Reduce), st);
+        return cudaGetLastError();
+    }
+    return cudaMemcpyAsync(ctx->h_red, src, sizeof(Reduce), cudaMemcpyDeviceToHost, st);
+}
+static cudaError_t read_dtout(ndsph_ctx* ctx, cudaStream_t st)
+{
+    if (ctx->hd_dtout) {
+        launch_read_words(ctx->hd_dtout, ctx->d_dtout, sizeof(double) * 8, st);
+        return cudaGetLastError();
+    }
+    return cudaMemcpyAsync(ctx->h_dtout, ctx->d_dtout, sizeof(double) * 8, cudaMemcpyDeviceToHost, st);
+}
+
 static int sync_red(ndsph_ctx* ctx)
 {
-    CK(cudaMemcpyAsync(ctx->h_red, ctx->red, sizeof(Reduce), cudaMemcpyDeviceToHost, ctx->st));
+    CK(read_red(ctx, ctx->red, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     if (ctx->h_red->err) {
         int code = ctx->h_red->err;
@@ -610,6 +655,21 @@ static int wait_late(ndsph_ctx* ctx)
 
 // downloads are staged in an arena and copied out asynchronously; the
 // caller synchronises once (download_end)
+// room for `need` more doubles in the arena; growing it first finishes the
+// pending copies out of it (the staging handed out before is then free)
+static int arena_reserve(ndsph_ctx* ctx, size_t need)
+{
+    if (ctx->arena_used + need <= ctx->arena_cap) return 0;
+    CK(cudaStreamSynchronize(ctx->st));
+    CK(cudaStreamSynchronize(ctx->st_cp));
+    if (ctx->d_arena) CK(cudaFree(ctx->d_arena));
+    ctx->d_arena = nullptr;
+    size_t cap = std::max(std::max(ctx->arena_cap * 2, (size_t)ctx->cap * 80), need);
+    CK(cudaMalloc(&ctx->d_arena, sizeof(double) * cap));
+    ctx->arena_cap = cap;
+    ctx->arena_used = 0;
+    return 0;
+}
 static int download_aos(ndsph_ctx* ctx, double* host, int f0, int ncomp, int stride, int n)
 {
     if (!host) return 0;
@@ -618,16 +678,8 @@ static int download_aos(ndsph_ctx* ctx, double* host, int f0, int ncomp, int str
         return 0;
     }
     const size_t need = (size_t)stride * n;
-    if (ctx->arena_used + need > ctx->arena_cap) {
-        // grow: finish pending copies first, then reallocate
-        CK(cudaStreamSynchronize(ctx->st));
-        CK(cudaStreamSynchronize(ctx->st_cp));
-        if (ctx->d_arena) CK(cudaFree(ctx->d_arena));
-        size_t cap = std::max(ctx->arena_cap * 2, (size_t)ctx->cap * 80);
-        CK(cudaMalloc(&ctx->d_arena, sizeof(double) * cap));
-        ctx->arena_cap = cap;
-        ctx->arena_used = 0;
-    }
+    int rc = arena_reserve(ctx, need);
+    if (rc) return rc;
     double* dst = ctx->d_arena + ctx->arena_used;
     ctx->arena_used += need;
     launch_slab_to_aos(dst, stride, ctx->F, f0, ncomp, ctx->S.pos_of_id, n, ctx->st);
@@ -850,8 +902,7 @@ static bool try_keep_link(ndsph_ctx* ctx, bool keep_hmax_ghost, int* rc)
         return false;
     }
     launch_reuse_check(ctx->F, ctx->S, ctx->g, ctx->o, ctx->n, ctx->nl_skin, ctx->nl_grow, r, st);
-    if (cudaMemcpyAsync(ctx->h_red, r, sizeof(Reduce), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess) {
+    if (read_red(ctx, r, st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
         *rc = NDSPH_E_CUDA;
         return false;
     }
@@ -910,7 +961,7 @@ static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hma
     ctx->nl_dmax = 0.f;
     launch_link_reset(ctx->red, st);
     launch_hmax_bbox(ctx->F, ctx->o.ndim, n, ctx->red, &ctx->red->hmax, st);
-    CK(cudaMemcpyAsync(ctx->h_red, ctx->red, sizeof(Reduce), cudaMemcpyDeviceToHost, st));
+    CK(read_red(ctx, ctx->red, st));
     CK(cudaStreamSynchronize(st));
     double hmax = bitsd(ctx->h_red->hmax);
     if (!(hmax > 0.0) || !std::isfinite(hmax)) {
@@ -1001,6 +1052,10 @@ static SweepArgs sweep_args(ndsph_ctx* ctx)
     a.d_nlist = nullptr;
     a.gate = nullptr;
     a.graph = 0;
+    a.plist = nullptr;
+    a.pi0 = a.pn = 0;
+    a.tail_on = 0;
+    memset(&a.tail, 0, sizeof a.tail);
     return a;
 }
 
@@ -1163,6 +1218,68 @@ static int do_cons2prim(ndsph_ctx* ctx)
     return 0;
 }
 
+// ndsph_step without fixed particles: the rates sweep in pieces, piece c
+// over the slots of host particles c*len .. (c+1)*len (in slot order, so a
+// piece keeps the cells' locality).  Each particle's rates and corrected
+// state (the corrector's arithmetic, read-only) go into the host-order
+// staging from the sweep itself, and each chunk goes back to the host on the
+// copy stream while the later pieces run; the corrector follows the whole
+// sweep as before.
+static int rates_streamed(ndsph_ctx* ctx, SweepArgs a)
+{
+    cudaStream_t st = ctx->st;
+    ndsph_particles* p = ctx->dl_tail;
+    const int n = ctx->n, nd = ctx->o.ndim, K = ctx->dl_pieces;
+    const int len = (n + K - 1) / K;
+    StepTail t;
+    struct Out { double* host; double** stage; int stride; };
+    Out outs[] = {{p->x, &t.x, nd}, {p->vel, &t.v, 3}, {p->Bevol, &t.be, 3}, {p->en, &t.en, 1},
+                  {p->hh, &t.hh, 1}, {p->alpha, &t.al, 3}, {p->drhodt, &t.drhodt, 1}, {p->dhdt, &t.dhdt, 1},
+                  {p->force, &t.force, 3}, {p->dBevoldt, &t.db, 3}, {p->dudt, &t.dudt, 1},
+                  {p->dendt, &t.dendt, 1}, {p->daldt, &t.dal, 3}, {p->divB, &t.divb, 1},
+                  {p->curlB, &t.curlb, 3}, {p->del2u, &t.del2u, 1}, {p->graddivv, &t.gdv, 3}};
+    size_t need = 0;
+    for (const Out& o : outs) if (o.host) need += (size_t)o.stride * n;
+    int rc = arena_reserve(ctx, need);
+    if (rc) return rc;
+    for (Out& o : outs) {
+        *o.stage = nullptr;
+        if (!o.host) continue;
+        *o.stage = ctx->d_arena + ctx->arena_used;
+        ctx->arena_used += (size_t)o.stride * n;
+    }
+    launch_piece_list(ctx->S.id, n, K, len, ctx->d_pcnt, ctx->d_plist, st);
+    a.plist = ctx->d_plist;
+    a.tail_on = 1;
+    a.tail = t;
+    // pieces alternate between the main and the upload stream (idle since
+    // the late inputs arrived), so the next piece's blocks fill the SMs
+    // while a piece drains; the pieces touch disjoint slots
+    cudaStream_t ps[2] = {st, ctx->st_up};
+    CK(cudaEventRecord(ctx->ev_pfork, st));
+    CK(cudaStreamWaitEvent(ctx->st_up, ctx->ev_pfork, 0));
+    for (int c = 0; c < K; c++) {
+        const int h0 = c * len, cnt = std::min(len, n - h0);
+        if (cnt <= 0) break;
+        a.pi0 = h0;
+        a.pn = cnt;
+        // the sweep writes each particle's outputs and corrected state into
+        // the staging; the chunk's copies follow the piece
+        launch_rates(a, ps[c & 1]);
+        CK(cudaEventRecord(ctx->ev_dl, ps[c & 1]));
+        CK(cudaStreamWaitEvent(ctx->st_cp, ctx->ev_dl, 0));
+        for (const Out& o : outs)
+            if (o.host)
+                CK(cudaMemcpyAsync(o.host + (size_t)h0 * o.stride, *o.stage + (size_t)h0 * o.stride,
+                                   sizeof(double) * (size_t)cnt * o.stride, cudaMemcpyDeviceToHost, ctx->st_cp));
+    }
+    CK(cudaEventRecord(ctx->ev_pjoin, ctx->st_up));
+    CK(cudaStreamWaitEvent(st, ctx->ev_pjoin, 0));
+    CK(cudaGetLastError());
+    ctx->dl_tail_done = true;
+    return 0;
+}
+
 static int do_rates(ndsph_ctx* ctx)
 {
     cudaStream_t st = ctx->st;
@@ -1170,12 +1287,17 @@ static int do_rates(ndsph_ctx* ctx)
     SweepArgs a = sweep_args(ctx);
     if (ctx->o.precision == NDSPH_PREC_FP32) launch_pack_rates(a, st);
     tmark(ctx, 4);
-    launch_rates(a, st);
+    if (ctx->dl_tail) {
+        int rc = rates_streamed(ctx, a);
+        if (rc) return rc;
+    } else {
+        launch_rates(a, st);
+    }
     tmark(ctx, 5);
     launch_finalize_dt(ctx->red, ctx->o, ctx->d_dtout, st);
     if (ctx->o.batched) launch_sim_finalize(ctx->o, ctx->d_sim_dtnext, ctx->d_sim_out, st);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(ctx->h_dtout, ctx->d_dtout, sizeof(double) * 8, cudaMemcpyDeviceToHost, st));
+    CK(read_dtout(ctx, st));
     int rc = sync_red(ctx);
     if (rc) return rc;
     ctx->timing.rates_ms = tdiff(ctx, 4, 5);
@@ -1277,6 +1399,8 @@ static int download_all(ndsph_ctx* ctx, ndsph_particles* p)
 {
     const int n = ctx->n, nd = ctx->o.ndim;
     int rc = 0;
+    // streamed with the rates pieces; the density and EOS groups went before
+    if (ctx->dl_tail_done) return download_end(ctx);
     rc |= download_aos(ctx, p->x, X0, nd, nd, n);
     rc |= download_aos(ctx, p->vel, V0, 3, 3, n);
     rc |= download_aos(ctx, p->Bevol, BE0, 3, 3, n);
@@ -1826,7 +1950,11 @@ extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, nds
     // final before the rates sweep: copy them back while it runs
     const bool early = !ctx->o.has_fixed && !ctx->opts.learned_h;
     ctx->dl_early = early ? p : nullptr;
-    ctx->dl_density_done = ctx->dl_prim_done = false;
+    // the rest streams with the rates pieces when the copies are staged and
+    // the arrays are large enough for the pieces to pay
+    const bool streamed = early && !ctx->host_access && ctx->dl_pieces > 1 && npart >= (1 << 16);
+    ctx->dl_tail = streamed ? p : nullptr;
+    ctx->dl_density_done = ctx->dl_prim_done = ctx->dl_tail_done = false;
     ctx->arena_used = 0;
     rc = dev_step_once(ctx);
     if (rc) {
@@ -1834,13 +1962,15 @@ extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, nds
         cudaStreamSynchronize(ctx->st_up);
         ctx->late_pending = false;
         ctx->dl_early = nullptr;
-        ctx->dl_density_done = ctx->dl_prim_done = false;
+        ctx->dl_tail = nullptr;
+        ctx->dl_density_done = ctx->dl_prim_done = ctx->dl_tail_done = false;
         return rc;
     }
     ctx->dl_early = p;   // also: pmass is not copied back (the step never writes it)
     rc = download_all(ctx, p);
     ctx->dl_early = nullptr;
-    ctx->dl_density_done = ctx->dl_prim_done = false;
+    ctx->dl_tail = nullptr;
+    ctx->dl_density_done = ctx->dl_prim_done = ctx->dl_tail_done = false;
     ctx->timing.launches = (int32_t)(ndsph_launch_counter().load() - l0);
     fill_dt(ctx, dts);
     return rc;
@@ -2310,15 +2440,16 @@ extern "C" int ndsph_set_tuning(ndsph_ctx* ctx, const ndsph_tuning* t)
     GUARD_CTX();
     if (!t || !(t->nl_skin >= 1.0f && t->nl_skin <= 2.0f) || !(t->nl_grow >= 1.0f && t->nl_grow <= 1.5f) ||
         !(t->graph_cell_margin >= 1.0f && t->graph_cell_margin <= 2.0f) || (t->nl_reuse != 0 && t->nl_reuse != 1) ||
-        (t->stencil != 3 && t->stencil != 5)) {
+        (t->stencil != 3 && t->stencil != 5) || t->step_pieces < 1 || t->step_pieces > 8) {
         ctx->err = "tuning out of range (nl_skin in [1,2], nl_grow in [1,1.5], graph_cell_margin in [1,2], "
-                   "stencil 3 or 5)";
+                   "stencil 3 or 5, step_pieces in [1,8])";
         return NDSPH_E_ARG;
     }
     ctx->nl_skin = t->nl_skin;
     ctx->nl_reuse = t->nl_reuse;
     ctx->nl_grow = t->nl_grow;
     ctx->nl_sw5 = (t->stencil == 5) ? 1 : 0;
+    ctx->dl_pieces = t->step_pieces;
     // captured batched steps hold the old settings: capture afresh
     graph_drop(ctx);
     ctx->gmargin = t->graph_cell_margin;
@@ -2337,6 +2468,7 @@ extern "C" int ndsph_get_tuning(ndsph_ctx* ctx, ndsph_tuning* t)
     t->nl_grow = ctx->nl_grow;
     t->graph_cell_margin = (float)ctx->gmargin;
     t->stencil = ctx->nl_sw5 ? 5 : 3;
+    t->step_pieces = ctx->dl_pieces;
     return 0;
 }
 

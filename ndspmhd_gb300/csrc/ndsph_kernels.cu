@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cmath>
 #include "ndsph_launch.h"
+#include "ndsph_step.cuh"
 
 namespace ndsph {
 
@@ -729,41 +730,119 @@ __global__ void k_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
     if (i >= n) return;
     if (red->gfail) return;   // a captured step that failed is redone from the predicted state
     const double dt = o.batched ? o.sim_dt[S.sim[i]] : red->dt;
-    const double hdt = 0.5 * dt;
-    int t = S.itype[i];
-    if (t == NDSPH_ITYPE_BND || t == NDSPH_ITYPE_BNDDUST) {
-        for (int d = 0; d < 3; d++) F.f[V0 + d][i] = F.f[VIN0 + d][i];
-        for (int d = 0; d < 3; d++) F.f[BE0 + d][i] = F.f[BIN0 + d][i];
-        F.f[RHO][i] = F.f[RHOIN][i];
-        F.f[HH][i] = F.f[HIN][i];
-        F.f[EN][i] = F.f[ENIN][i];
-        for (int d = 0; d < 3; d++) F.f[AL0 + d][i] = F.f[ALIN0 + d][i];
-    } else {
-        for (int d = 0; d < 3; d++)
-            F.f[V0 + d][i] = (F.f[VIN0 + d][i] + hdt * (F.f[F0 + d][i] + F.f[FIN0 + d][i])) / (1.0 + 0.0);
-        if (o.imhd != 0)
-            for (int d = 0; d < 3; d++)
-                F.f[BE0 + d][i] = F.f[BIN0 + d][i] + hdt * (F.f[DB0 + d][i] + F.f[DBIN0 + d][i]);
-        double h = F.f[HIN][i] + hdt * (F.f[DHDT][i] + F.f[DHIN][i]);
-        F.f[HH][i] = h;
-        if (!(h > 0.0)) raise_err(red, NDSPH_E_H_NONPOS, S.id[i]);
-        if (o.iener != 0) F.f[EN][i] = F.f[ENIN][i] + hdt * (F.f[DENDT][i] + F.f[DENIN][i]);
-        for (int d = 0; d < 3; d++)
-            if (o.iavlim[d] != 0)
-                F.f[AL0 + d][i] = fmin(F.f[ALIN0 + d][i] + hdt * (F.f[DAL0 + d][i] + F.f[DALIN0 + d][i]), 1.0);
-    }
-    // boundary after the corrector (:221)
-    for (int d = 0; d < o.ndim; d++) {
-        if (o.ibound[d] != 3) continue;
-        double x = F.f[X0 + d][i];
-        if (x > o.xmax[d]) x = __dsub_rn(__dadd_rn(o.xmin[d], x), o.xmax[d]);
-        else if (x < o.xmin[d]) x = __dsub_rn(o.xmax[d], __dsub_rn(o.xmin[d], x));
-        F.f[X0 + d][i] = x;
-    }
+    Corrected c;
+    corrector_values(F, S, o, dt, i, c);
+    const int t = S.itype[i];
+    const bool fixed = (t == NDSPH_ITYPE_BND || t == NDSPH_ITYPE_BNDDUST);
+    if (!fixed && !(c.h > 0.0)) raise_err(red, NDSPH_E_H_NONPOS, S.id[i]);
+    // write back what the step changes
+    for (int d = 0; d < 3; d++) F.f[V0 + d][i] = c.v[d];
+    if (fixed || o.imhd != 0)
+        for (int d = 0; d < 3; d++) F.f[BE0 + d][i] = c.be[d];
+    for (int d = 0; d < 3; d++)
+        if (fixed || o.iavlim[d] != 0) F.f[AL0 + d][i] = c.al[d];
+    if (fixed) F.f[RHO][i] = c.rho;
+    F.f[HH][i] = c.h;
+    if (fixed || o.iener != 0) F.f[EN][i] = c.en;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+        if (d < o.ndim && o.ibound[d] == 3) F.f[X0 + d][i] = c.x[d];
 }
 void launch_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st)
 {
     if (n > 0) NDSPH_COUNT_LAUNCH, k_corrector<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+}
+
+__global__ void k_read_words(const unsigned* __restrict__ src, unsigned* __restrict__ dst, int nw)
+{
+    for (int k = threadIdx.x; k < nw; k += blockDim.x) dst[k] = src[k];
+}
+void launch_read_words(void* dst, const void* src, size_t bytes, cudaStream_t st)
+{
+    NDSPH_COUNT_LAUNCH, k_read_words<<<1, 128, 0, st>>>((const unsigned*)src, (unsigned*)dst, (int)(bytes / 4));
+}
+
+// stable partition of the slots by host chunk, in three passes: counts per
+// block and chunk, a scan over the blocks of each chunk, then each block
+// places its slots (warp ballots give the rank among the block's slots of
+// the same chunk)
+constexpr int PL_BS = 1024;
+constexpr int PL_MAXCHUNK = 8;
+__global__ void __launch_bounds__(PL_BS) k_piece_count(const int* __restrict__ id, int n, int nchunk, int len,
+                                                       int* __restrict__ cnt)
+{
+    __shared__ int c[PL_MAXCHUNK];
+    if (threadIdx.x < PL_MAXCHUNK) c[threadIdx.x] = 0;
+    __syncthreads();
+    const int s = blockIdx.x * PL_BS + threadIdx.x;
+    if (s < n) atomicAdd(&c[id[s] / len], 1);
+    __syncthreads();
+    if (threadIdx.x < nchunk) cnt[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = c[threadIdx.x];
+}
+// one block: exclusive scan of each chunk's counts over the blocks, offset by
+// the chunk's start c*len
+__global__ void __launch_bounds__(PL_BS) k_piece_scan(int* cnt, int nblocks, int nchunk, int len)
+{
+    __shared__ int wsum[PL_BS / 32];
+    __shared__ int carry;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int c = 0; c < nchunk; c++) {
+        if (threadIdx.x == 0) carry = c * len;
+        __syncthreads();
+        for (int b0 = 0; b0 < nblocks; b0 += PL_BS) {
+            const int b = b0 + threadIdx.x;
+            const int v = (b < nblocks) ? cnt[(size_t)c * nblocks + b] : 0;
+            int x = v;   // inclusive warp scan
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) wsum[w] = x;
+            __syncthreads();
+            if (w == 0) {
+                int z = wsum[lane];
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, z, o);
+                    if (lane >= o) z += y;
+                }
+                wsum[lane] = z;   // inclusive over warps
+            }
+            __syncthreads();
+            const int before = carry + (w > 0 ? wsum[w - 1] : 0) + x - v;
+            if (b < nblocks) cnt[(size_t)c * nblocks + b] = before;
+            __syncthreads();
+            if (threadIdx.x == PL_BS - 1) carry += wsum[31];
+            __syncthreads();
+        }
+    }
+}
+__global__ void __launch_bounds__(PL_BS) k_piece_place(const int* __restrict__ id, int n, int nchunk, int len,
+                                                       const int* __restrict__ off, int* __restrict__ plist)
+{
+    __shared__ int wc[PL_BS / 32][PL_MAXCHUNK];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int s = blockIdx.x * PL_BS + threadIdx.x;
+    const int c = (s < n) ? id[s] / len : -1;
+    int rank = 0;
+    for (int k = 0; k < nchunk; k++) {
+        const unsigned m = __ballot_sync(0xffffffffu, c == k);
+        if (c == k) rank = __popc(m & ((1u << lane) - 1u));
+        if (lane == 0) wc[w][k] = __popc(m);
+    }
+    __syncthreads();
+    if (c >= 0) {
+        int before = 0;
+        for (int v = 0; v < w; v++) before += wc[v][c];
+        plist[off[(size_t)c * gridDim.x + blockIdx.x] + before + rank] = s;
+    }
+}
+void launch_piece_list(const int* id, int n, int nchunk, int len, int* cnt, int* plist, cudaStream_t st)
+{
+    if (n <= 0 || nchunk < 1 || nchunk > PL_MAXCHUNK) return;
+    const int nb = (n + PL_BS - 1) / PL_BS;
+    NDSPH_COUNT_LAUNCH, k_piece_count<<<nb, PL_BS, 0, st>>>(id, n, nchunk, len, cnt);
+    NDSPH_COUNT_LAUNCH, k_piece_scan<<<1, PL_BS, 0, st>>>(cnt, nb, nchunk, len);
+    NDSPH_COUNT_LAUNCH, k_piece_place<<<nb, PL_BS, 0, st>>>(id, n, nchunk, len, cnt, plist);
 }
 
 // dt = min(C_force*dtforce, C_cour*dtcourant, 0.9*dtdrag, C_force*dtvisc)

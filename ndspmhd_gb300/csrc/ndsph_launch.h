@@ -48,6 +48,13 @@ struct SortScratch {
     int cap_blocks;
 };
 
+// host-layout staging of the outputs a host-buffer step returns last: the
+// corrected state and the rates (nullptr: not returned)
+struct StepTail {
+    double *x, *v, *be, *en, *hh, *al, *drhodt, *dhdt;
+    double *force, *db, *dudt, *dendt, *dal, *divb, *curlb, *del2u, *gdv;
+};
+
 struct SweepArgs {
     FieldPtrs F;
     Side S;
@@ -71,6 +78,14 @@ struct SweepArgs {
     const int* d_nlist;
     const int* gate;
     int graph;               // captured step: a row overflow sets gfail
+    // rates sweep in pieces: when set, the sweep covers slots
+    // plist[pi0 .. pi0 + pn) instead of 0 .. n, and with tail_on each
+    // particle's outputs and corrected state also go to the host-order
+    // staging `tail` at its host index
+    const int* plist;
+    int pi0, pn;
+    int tail_on;
+    StepTail tail;
 };
 
 // ---- link / sort (ndsph_kernels.cu) ------------------------------------------
@@ -118,6 +133,13 @@ void launch_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaSt
 // states without fixed particles: part 1 = x, v, h; part 2 = Bevol, energy, alpha
 void launch_predictor_part(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, int part, cudaStream_t st);
 void launch_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st);
+// slots grouped by the host chunk of their particle (chunk c = particles
+// c*len .. (c+1)*len), ascending within a chunk: plist[c*len + r] is the
+// r-th slot of chunk c.  cnt: scratch of nchunk * ceil(n / 1024) ints
+void launch_piece_list(const int* id, int n, int nchunk, int len, int* cnt, int* plist, cudaStream_t st);
+// small device -> host read into mapped pinned memory (dst: its device
+// address) by a one-block kernel; bytes a multiple of 4
+void launch_read_words(void* dst, const void* src, size_t bytes, cudaStream_t st);
 void launch_finalize_dt(Reduce* red, DevOpts o, double* out, cudaStream_t st);
 void launch_reduce_reset(Reduce* red, cudaStream_t st);
 void launch_p2c_init(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);

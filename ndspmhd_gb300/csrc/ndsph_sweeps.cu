@@ -30,6 +30,7 @@
 #include <cstdio>
 #include <type_traits>
 #include "ndsph_launch.h"
+#include "ndsph_step.cuh"
 
 namespace ndsph {
 
@@ -663,8 +664,8 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
     // no early return: every lane of the warp takes part in the final
     // shuffle reductions; lanes past n run an empty stencil on slot 0
     const int ithread = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = ithread < a.n;
-    const int i = live ? ithread : 0;
+    const bool live = ithread < (a.plist ? a.pn : a.n);
+    const int i = live ? (a.plist ? a.plist[a.pi0 + ithread] : ithread) : 0;
     const FieldPtrs& F = a.F;
     const DevOpts& o = a.o;
     const Grid& g = a.g;
@@ -1095,6 +1096,7 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
         F.f[DENDT][i] = dendt;
         F.f[DIVB][i] = divB;
         F.f[DEL2U][i] = del2u;
+        if (a.tail_on) step_tail_one(F, o, a.red->dt, i, (size_t)a.S.id[i], a.S, a.tail);
     }
 
     // ---- global reductions (warp first, then one atomic per warp) ----
@@ -1176,8 +1178,9 @@ void launch_pack_rates(const SweepArgs& a, cudaStream_t st)
 void launch_rates(const SweepArgs& a, cudaStream_t st)
 {
     const int bs = RATES_BS;
-    if (a.n <= 0) return;
-    const int nb = nblk(a.n, bs);
+    const int np = a.plist ? a.pn : a.n;
+    if (np <= 0) return;
+    const int nb = nblk(np, bs);
     if (a.o.precision == NDSPH_PREC_FP64) {
         if (a.o.ndim == 1) NDSPH_COUNT_LAUNCH, k_rates<1, 0><<<nb, bs, 0, st>>>(a);
         else if (a.o.ndim == 2) NDSPH_COUNT_LAUNCH, k_rates<2, 0><<<nb, bs, 0, st>>>(a);

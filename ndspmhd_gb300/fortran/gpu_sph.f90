@@ -48,6 +48,7 @@ module gpu_sph
     integer(c_int32_t) :: nl_reuse
     real(c_float)      :: nl_grow, graph_cell_margin
     integer(c_int32_t) :: stencil
+    integer(c_int32_t) :: step_pieces
  end type
 
  interface

@@ -222,8 +222,9 @@ class GpuSPH:
         return t.as_dict()
 
     def set_tuning(self, **kw):
-        """Change neighbour-search knobs (nl_skin, nl_reuse, nl_grow,
-        graph_cell_margin, stencil); the others keep their values."""
+        """Change tuning knobs (nl_skin, nl_reuse, nl_grow,
+        graph_cell_margin, stencil, step_pieces); the others keep their
+        values."""
         t = NdsphTuning()
         self._check(lib().ndsph_get_tuning(self._h, C.byref(t)))
         for k, v in kw.items():

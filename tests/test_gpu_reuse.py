@@ -130,10 +130,39 @@ def test_tuning_rejects_out_of_range(gpulib):
     g = GpuSPH(o, configs.full_state(p, 3))
     t0 = g.get_tuning()
     assert t0["nl_reuse"] == 1 and abs(t0["nl_skin"] - 1.1) < 1e-6
-    assert t0["stencil"] == 5
+    assert t0["stencil"] == 5 and t0["step_pieces"] == 4
     for bad in ({"nl_skin": 0.9}, {"nl_skin": 2.5}, {"nl_grow": 0.99}, {"graph_cell_margin": 0.5},
-                {"nl_reuse": 2}, {"stencil": 4}):
+                {"nl_reuse": 2}, {"stencil": 4}, {"step_pieces": 0}, {"step_pieces": 9}):
         with pytest.raises(NdsphError):
             g.set_tuning(**bad)
     assert g.get_tuning() == t0
     g.close()
+
+
+@pytest.mark.parametrize("precision,pieces", [(1, 3), (1, 8), (0, 3)])
+def test_host_step_streamed_outputs_identical(precision, pieces, gpulib):
+    """ndsph_step on 110,592 particles: with the rates sweep in pieces (each
+    chunk of the host arrays copied back while the later pieces run) every
+    array the step returns is bit-identical to the single-sweep step."""
+    import numpy as np
+    from ndspmhd_gb300.gpu import GpuSPH
+    o, p = configs.mhd_box_3d(48, seed=6)
+    o = dict(o)
+    o["precision"] = precision
+    g0 = GpuSPH(o, configs.full_state(p, 3))
+    g0.primitive2conservative()
+    st = {k: v.copy() for k, v in g0.state.items()}
+    g0.close()
+    runs = []
+    for k in (1, pieces):
+        g = GpuSPH(o, {key: v.copy() for key, v in st.items()})
+        g.set_tuning(step_pieces=k)
+        g.dt.dt, g.dt.time, g.dt.nsteps = 0.0, 0.0, 0
+        for _ in range(4):
+            g.step()
+        runs.append(({key: v.copy() for key, v in g.state.items()}, g.dt.dt, g.dt.time))
+        g.close()
+    (a, dta, ta), (b, dtb, tb) = runs
+    assert dta == dtb and ta == tb
+    differ = [key for key in a if not np.array_equal(a[key], b[key])]
+    assert not differ, differ
