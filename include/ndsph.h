@@ -325,7 +325,7 @@ NDSPH_API int ndsph_get_timing(ndsph_ctx* ctx, ndsph_timing* t);
  *             piece c over the particles of the c-th chunk of the host
  *             arrays, and each chunk's rates and corrected state go back
  *             while the later pieces run; 1: all after the corrector.  The
- *             values returned are the same either way.                   (4)
+ *             values returned are the same either way.                   (8)
  * ndsph_set_tuning rejects values outside nl_skin in [1, 2], nl_grow in
  * [1, 1.5], graph_cell_margin in [1, 2], stencil in {3, 5}, step_pieces in
  * [1, 8]; the next step links afresh.                                        */

@@ -71,8 +71,14 @@ struct ndsph_ctx {
     // read are uploaded on their own stream while the link and density run
     cudaStream_t st_up = nullptr;
     cudaEvent_t ev_late = nullptr, ev_up0 = nullptr;
-    double* d_stage_late = nullptr;   // two staging buffers of 3 doubles per particle
-    int late_k = 0;
+    // late inputs staged whole, in host order (16 doubles per particle), so
+    // a relink before they are used lays them out again in the new order
+    double* d_stage_late = nullptr;
+    struct LateField { int f0, ncomp, stride; const double* buf; };
+    LateField late_f[8];
+    int late_nf = 0;
+    size_t late_used = 0;
+    bool late_relayout = false;
     bool late_pending = false;
     bool dl_density_done = false, dl_prim_done = false;
     // ndsph_step: the rates sweep runs in dl_pieces pieces, one per chunk of
@@ -80,7 +86,7 @@ struct ndsph_ctx {
     // pieces run (dl_tail: where they go; null: all after the corrector)
     ndsph_particles* dl_tail = nullptr;
     bool dl_tail_done = false;
-    int dl_pieces = 4;
+    int dl_pieces = 8;
     int* d_plist = nullptr;      // slots grouped by host chunk
     int* d_pcnt = nullptr;       // its scratch: dl_pieces counts per 1024 slots
     double* d_arena = nullptr;   // download staging: every output field side by side
@@ -363,7 +369,7 @@ static int ensure_capacity(ndsph_ctx* ctx, int n)
     CK(cudaMalloc(&ctx->itype2, ib)); CK(cudaMalloc(&ctx->id2, ib)); CK(cudaMalloc(&ctx->ireal2, ib));
     CK(cudaMalloc(&ctx->srt.key, ib)); CK(cudaMalloc(&ctx->srt.slot, ib)); CK(cudaMalloc(&ctx->srt.perm, ib));
     CK(cudaMalloc(&ctx->d_stage, sizeof(double) * 6 * (size_t)cap));   // two staging buffers
-    CK(cudaMalloc(&ctx->d_stage_late, sizeof(double) * 6 * (size_t)cap));
+    CK(cudaMalloc(&ctx->d_stage_late, sizeof(double) * 16 * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_v, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_t, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_b, sizeof(float4) * (size_t)cap));
@@ -623,31 +629,46 @@ static int upload_aos(ndsph_ctx* ctx, const double* host, int f0, int ncomp, int
     return 0;
 }
 // an input of the host-buffer step that the link and the density passes do
-// not read: copied and laid out on the upload stream, behind the early ones
+// not read: copied whole into the late staging (host order) and laid out on
+// the upload stream, behind the early ones.  A relink before the main stream
+// uses them lays them out again from the staging in the new order.
 static int upload_aos_late(ndsph_ctx* ctx, const double* host, int f0, int ncomp, int stride, int n,
                            const int* id)
 {
     if (!host) return 0;
     if (const double* src = (const double*)host_view(ctx, host)) {
         launch_aos_to_slab(ctx->F, f0, ncomp, src, stride, id, n, ctx->st_up);
+        if (ctx->late_nf < 8) ctx->late_f[ctx->late_nf++] = {f0, ncomp, stride, src};
         return 0;
     }
-    // two staging buffers used in turn on one stream: a copy into a buffer
-    // follows the layout kernel that read it two fields earlier
-    double* buf = ctx->d_stage_late + (size_t)((ctx->late_k++) & 1) * 3 * ctx->cap;
-    CK(cudaMemcpyAsync(buf, host, sizeof(double) * (size_t)stride * n, cudaMemcpyHostToDevice, ctx->st_up));
+    const size_t need = (size_t)stride * n;
+    if (ctx->late_used + need > (size_t)16 * ctx->cap || ctx->late_nf >= 8) {
+        ctx->err = "late staging overflow";
+        return NDSPH_E_ARG;
+    }
+    double* buf = ctx->d_stage_late + ctx->late_used;
+    ctx->late_used += need;
+    CK(cudaMemcpyAsync(buf, host, sizeof(double) * need, cudaMemcpyHostToDevice, ctx->st_up));
     launch_aos_to_slab(ctx->F, f0, ncomp, buf, stride, id, n, ctx->st_up);
+    ctx->late_f[ctx->late_nf++] = {f0, ncomp, stride, buf};
     return 0;
 }
 
 // the late inputs of a host-buffer step have arrived: the main stream waits
-// for them and runs their part of the predictor (before the EOS, or before a
-// link permutes the fields)
+// for them (laying them out again in the current slot order when a relink
+// came in between) and runs their part of the predictor (before the EOS)
 static int wait_late(ndsph_ctx* ctx)
 {
     if (!ctx->late_pending) return 0;
     ctx->late_pending = false;
     CK(cudaStreamWaitEvent(ctx->st, ctx->ev_late, 0));
+    if (ctx->late_relayout) {
+        for (int k = 0; k < ctx->late_nf; k++) {
+            const auto& L = ctx->late_f[k];
+            launch_aos_to_slab(ctx->F, L.f0, L.ncomp, L.buf, L.stride, ctx->S.id, ctx->n, ctx->st);
+        }
+        ctx->late_relayout = false;
+    }
     launch_predictor_part(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, 2, ctx->st);
     CK(cudaGetLastError());
     return 0;
@@ -953,10 +974,9 @@ static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hma
         if (try_keep_link(ctx, keep_hmax_ghost, &rc)) return 0;
         if (rc) return rc;
     }
-    {
-        int rc = wait_late(ctx);   // the gather permutes every live field
-        if (rc) return rc;
-    }
+    // late inputs still on their way are laid out again after this link
+    // (what the gather moves of them now is overwritten then)
+    if (ctx->late_pending) ctx->late_relayout = true;
     ctx->nl_valid = false;
     ctx->nl_dmax = 0.f;
     launch_link_reset(ctx->red, st);
@@ -1899,6 +1919,9 @@ static int step_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
         // behind the early copies, so they do not share the link's bandwidth
         CK(cudaEventRecord(ctx->ev_up0, ctx->st_cp));
         CK(cudaStreamWaitEvent(ctx->st_up, ctx->ev_up0, 0));
+        ctx->late_nf = 0;
+        ctx->late_used = 0;
+        ctx->late_relayout = false;
         rc |= upload_aos_late(ctx, p->Bevol, BE0, 3, 3, n, idm);
         rc |= upload_aos_late(ctx, p->en, EN, 1, 1, n, idm);
         rc |= upload_aos_late(ctx, p->alpha, AL0, 3, 3, n, idm);

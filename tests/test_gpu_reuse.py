@@ -130,7 +130,7 @@ def test_tuning_rejects_out_of_range(gpulib):
     g = GpuSPH(o, configs.full_state(p, 3))
     t0 = g.get_tuning()
     assert t0["nl_reuse"] == 1 and abs(t0["nl_skin"] - 1.1) < 1e-6
-    assert t0["stencil"] == 5 and t0["step_pieces"] == 4
+    assert t0["stencil"] == 5 and t0["step_pieces"] == 8
     for bad in ({"nl_skin": 0.9}, {"nl_skin": 2.5}, {"nl_grow": 0.99}, {"graph_cell_margin": 0.5},
                 {"nl_reuse": 2}, {"stencil": 4}, {"step_pieces": 0}, {"step_pieces": 9}):
         with pytest.raises(NdsphError):
