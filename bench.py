@@ -241,11 +241,11 @@ def run_e2e(o, steps: int, warmup: int, tuning=None):
         rates[mode] = n * steps / (time.perf_counter() - t0)
         g.close()
     # bytes per particle: ndsph_step uploads the step's inputs x(3) v(3) Bevol(3)
-    # en hh pmass alpha(3) rho dhdt force(3) dBevoldt(3) dendt daldt(3) + itype,
+    # en hh pmass alpha(3) dhdt force(3) dBevoldt(3) dendt daldt(3) + itype,
     # and downloads every array the step writes: x v Bevol en hh alpha, rho
     # rhoalt drhodt dhdt gradh gradhn gradgradh, dens uu pr spsound Bfield(3),
     # force dBevoldt dudt dendt daldt divB curlB(3) del2u graddivv(3) + numneigh
-    d_up = (3 + 3 + 3 + 1 + 1 + 1 + 3 + 1 + 1 + 3 + 3 + 1 + 3) * 8 + 4
+    d_up = (3 + 3 + 3 + 1 + 1 + 1 + 3 + 1 + 3 + 3 + 1 + 3) * 8 + 4
     d_dn = (3 + 3 + 3 + 1 + 1 + 3 + 7 + 4 + 3 + 3 + 3 + 1 + 1 + 3 + 1 + 3 + 1 + 3) * 8 + 4
     del dt0
     return rates[0], d_up * n, d_dn * n, rates[1]

@@ -1880,8 +1880,9 @@ extern "C" int ndsph_dev_derivs(ndsph_ctx* ctx, ndsph_dt* dts)
     return rc;
 }
 
-// inputs of one leapfrog step: the state, the previous rates the predictor
-// reads (force, dBevol/dt, de/dt, dalpha/dt, dh/dt) and rho.  Every other
+// inputs of one leapfrog step: the state and the previous rates the
+// predictor reads (force, dBevol/dt, de/dt, dalpha/dt, dh/dt); rho only for
+// the learned-h predictor, whose features include it.  Every other
 // array the step returns is recomputed for every particle -- except with
 // fixed particles (whose gradgradh and rates the reference carries through)
 // or maxdensits = 0 (no density pass), where everything is uploaded.
@@ -1902,19 +1903,22 @@ static int step_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
     }
     const int n = npart, nd = ctx->o.ndim;
     const int* idm = keep ? ctx->S.id : nullptr;
-    // early inputs (the predictor of x, v, h; the link; the density passes)
-    rc |= upload_aos(ctx, p->x, X0, nd, nd, n, idm);
-    rc |= upload_aos(ctx, p->vel, V0, 3, 3, n, idm);
-    rc |= upload_aos(ctx, p->hh, HH, 1, 1, n, idm);
-    rc |= upload_aos(ctx, p->pmass, PM, 1, 1, n, idm);
-    rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n, idm);
-    rc |= upload_aos(ctx, p->dhdt, DHDT, 1, 1, n, idm);
-    rc |= upload_aos(ctx, p->force, F0, 3, 3, n, idm);
-    if (rc) return rc;
     // late inputs (Bevol, energy, alpha and their rates: the EOS and their
     // part of the predictor) on the upload stream, overlapping the link and
     // the density passes; the learned-h form reads them before the link
     const bool split = !ctx->opts.learned_h;
+    // early inputs (the predictor of x, v, h; the link; the density passes).
+    // rho is recomputed for every particle by the first density pass and
+    // read before it only as the save of fixed particles (none here) and as
+    // a feature of the learned-h predictor
+    rc |= upload_aos(ctx, p->x, X0, nd, nd, n, idm);
+    rc |= upload_aos(ctx, p->vel, V0, 3, 3, n, idm);
+    rc |= upload_aos(ctx, p->hh, HH, 1, 1, n, idm);
+    rc |= upload_aos(ctx, p->pmass, PM, 1, 1, n, idm);
+    if (!split) rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n, idm);
+    rc |= upload_aos(ctx, p->dhdt, DHDT, 1, 1, n, idm);
+    rc |= upload_aos(ctx, p->force, F0, 3, 3, n, idm);
+    if (rc) return rc;
     if (split) {
         // behind the early copies, so they do not share the link's bandwidth
         CK(cudaEventRecord(ctx->ev_up0, ctx->st_cp));
