@@ -65,6 +65,8 @@ struct ndsph_ctx {
     cudaStream_t st_cp = nullptr;
     cudaEvent_t ev_cp[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr}, ev_dl = nullptr;
     cudaEvent_t ev_pfork = nullptr, ev_pjoin = nullptr;   // rates pieces on two streams
+    cudaStream_t st_g = nullptr;   // gathers of the staged downloads
+    cudaEvent_t ev_g = nullptr;
     int stage_k = 0;
     ndsph_particles* dl_early = nullptr;   // ndsph_step: where the early outputs go
     // ndsph_step: the inputs only the EOS and the Bevol/energy/alpha predictor
@@ -434,7 +436,14 @@ extern "C" int ndsph_init(ndsph_ctx** out, const ndsph_opts* opts, int32_t nmax)
             ctx->pageable_access = pa != 0;
         cudaGetLastError();
     }
+    // the gathers of the downloads run on their own stream at the highest
+    // priority (their blocks go in as the sweeps' blocks retire), ahead of
+    // the copies that wait for them one by one on the copy stream
+    int prio_lo = 0, prio_hi = 0;
+    if (cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess) prio_hi = 0;
     if (cudaStreamCreateWithFlags(&ctx->st_cp, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&ctx->st_g, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_g, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_cp[0], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_cp[1], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_used[0], cudaEventDisableTiming) != cudaSuccess ||
@@ -536,10 +545,11 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
     for (int k = 0; k < 2; k++) if (ctx->gexec[k]) cudaGraphExecDestroy(ctx->gexec[k]);
     if (ctx->st_cp) { cudaStreamSynchronize(ctx->st_cp); cudaStreamDestroy(ctx->st_cp); }
     if (ctx->st_up) { cudaStreamSynchronize(ctx->st_up); cudaStreamDestroy(ctx->st_up); }
+    if (ctx->st_g) { cudaStreamSynchronize(ctx->st_g); cudaStreamDestroy(ctx->st_g); }
     if (ctx->ev_late) cudaEventDestroy(ctx->ev_late);
     if (ctx->ev_up0) cudaEventDestroy(ctx->ev_up0);
     for (cudaEvent_t ev : {ctx->ev_cp[0], ctx->ev_cp[1], ctx->ev_used[0], ctx->ev_used[1], ctx->ev_dl,
-                            ctx->ev_pfork, ctx->ev_pjoin})
+                            ctx->ev_pfork, ctx->ev_pjoin, ctx->ev_g})
         if (ev) cudaEventDestroy(ev);
     if (ctx->d_live) cudaFree(ctx->d_live);
     if (ctx->st2) cudaStreamDestroy(ctx->st2);
@@ -703,9 +713,14 @@ static int download_aos(ndsph_ctx* ctx, double* host, int f0, int ncomp, int str
     if (rc) return rc;
     double* dst = ctx->d_arena + ctx->arena_used;
     ctx->arena_used += need;
-    launch_slab_to_aos(dst, stride, ctx->F, f0, ncomp, ctx->S.pos_of_id, n, ctx->st);
+    // the gather runs on the gather stream beside whatever the main stream
+    // does next (a field is downloaded once it is final for the call), its
+    // copy on the copy stream behind it
     CK(cudaEventRecord(ctx->ev_dl, ctx->st));
-    CK(cudaStreamWaitEvent(ctx->st_cp, ctx->ev_dl, 0));
+    CK(cudaStreamWaitEvent(ctx->st_g, ctx->ev_dl, 0));
+    launch_slab_to_aos(dst, stride, ctx->F, f0, ncomp, ctx->S.pos_of_id, n, ctx->st_g);
+    CK(cudaEventRecord(ctx->ev_g, ctx->st_g));
+    CK(cudaStreamWaitEvent(ctx->st_cp, ctx->ev_g, 0));
     CK(cudaMemcpyAsync(host, dst, sizeof(double) * need, cudaMemcpyDeviceToHost, ctx->st_cp));
     return 0;
 }
@@ -1393,9 +1408,11 @@ static int download_density_group(ndsph_ctx* ctx, ndsph_particles* p)
         const size_t need = ((size_t)n * sizeof(int) + sizeof(double) - 1) / sizeof(double);
         if (ctx->arena_used + need <= ctx->arena_cap) {
             ctx->arena_used += need;
-            launch_slab_to_int(dst, ctx->S.numneigh, ctx->S.pos_of_id, n, ctx->st);
             CK(cudaEventRecord(ctx->ev_dl, ctx->st));
-            CK(cudaStreamWaitEvent(ctx->st_cp, ctx->ev_dl, 0));
+            CK(cudaStreamWaitEvent(ctx->st_g, ctx->ev_dl, 0));
+            launch_slab_to_int(dst, ctx->S.numneigh, ctx->S.pos_of_id, n, ctx->st_g);
+            CK(cudaEventRecord(ctx->ev_g, ctx->st_g));
+            CK(cudaStreamWaitEvent(ctx->st_cp, ctx->ev_g, 0));
             CK(cudaMemcpyAsync(p->numneigh, dst, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, ctx->st_cp));
         } else {
             rc |= download_int(ctx, p->numneigh, ctx->S.numneigh, n, false);
@@ -1985,6 +2002,7 @@ extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, nds
     ctx->arena_used = 0;
     rc = dev_step_once(ctx);
     if (rc) {
+        cudaStreamSynchronize(ctx->st_g);
         cudaStreamSynchronize(ctx->st_cp);
         cudaStreamSynchronize(ctx->st_up);
         ctx->late_pending = false;

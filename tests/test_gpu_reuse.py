@@ -166,3 +166,38 @@ def test_host_step_streamed_outputs_identical(precision, pieces, gpulib):
     assert dta == dtb and ta == tb
     differ = [key for key in a if not np.array_equal(a[key], b[key])]
     assert not differ, differ
+
+
+def test_host_step_streamed_skips_null_outputs(gpulib):
+    """Outputs the caller passes as null are not written (the rest streams as
+    usual and matches a step that returns everything)."""
+    import numpy as np
+    from ndspmhd_gb300.gpu import GpuSPH
+    o, p = configs.mhd_box_3d(48, seed=7)
+    o = dict(o)
+    o["precision"] = 1
+    g0 = GpuSPH(o, configs.full_state(p, 3))
+    g0.primitive2conservative()
+    st = {k: v.copy() for k, v in g0.state.items()}
+    g0.close()
+    dropped = ("del2u", "graddivv", "curlB", "divB")
+    runs = []
+    for drop in (False, True):
+        s = {k: v.copy() for k, v in st.items()}
+        if drop:
+            for k in dropped:
+                s[k][...] = -7.0
+        g = GpuSPH(o, s)
+        if drop:
+            for k in dropped:
+                setattr(g._p, k, None)
+        g.dt.dt, g.dt.time, g.dt.nsteps = 0.0, 0.0, 0
+        for _ in range(3):
+            g.step()
+        runs.append({k: v.copy() for k, v in g.state.items()})
+        g.close()
+    full, part = runs
+    for k in dropped:
+        assert np.all(part[k] == -7.0), k
+    differ = [k for k in full if k not in dropped and not np.array_equal(full[k], part[k])]
+    assert not differ, differ
