@@ -1996,7 +1996,8 @@ extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, nds
     ctx->dl_early = early ? p : nullptr;
     // the rest streams with the rates pieces when the copies are staged and
     // the arrays are large enough for the pieces to pay
-    const bool streamed = early && !ctx->host_access && ctx->dl_pieces > 1 && npart >= (1 << 16);
+    const bool streamed = early && !ctx->host_access && !ctx->o.batched && ctx->dl_pieces > 1 &&
+                          npart >= (1 << 16);
     ctx->dl_tail = streamed ? p : nullptr;
     ctx->dl_density_done = ctx->dl_prim_done = ctx->dl_tail_done = false;
     ctx->arena_used = 0;

@@ -139,11 +139,12 @@ def test_tuning_rejects_out_of_range(gpulib):
     g.close()
 
 
-@pytest.mark.parametrize("precision,pieces", [(1, 3), (1, 8), (0, 3)])
+@pytest.mark.parametrize("precision,pieces", [(1, 3), (1, 7), (1, 8), (0, 3)])
 def test_host_step_streamed_outputs_identical(precision, pieces, gpulib):
     """ndsph_step on 110,592 particles: with the rates sweep in pieces (each
     chunk of the host arrays copied back while the later pieces run) every
-    array the step returns is bit-identical to the single-sweep step."""
+    array the step returns is bit-identical to the single-sweep step (7
+    pieces: chunks of 15,799 and a last one of 15,798)."""
     import numpy as np
     from ndspmhd_gb300.gpu import GpuSPH
     o, p = configs.mhd_box_3d(48, seed=6)
