@@ -289,6 +289,7 @@ struct KSum {
         s = t;
     }
     __device__ __forceinline__ double val() const { return (double)s - (double)c; }
+    __device__ __forceinline__ float valf() const { return s - c; }
 };
 
 // ===========================================================================
@@ -458,24 +459,38 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
                 if (k0 + u < ncand) pair(pk[u], xj[u], tj[u], vj[u]);
         }
     }
-    if (PREC == NDSPH_PREC_FP32) {
-        sw = fw.val(); sn = fn.val(); sg = fg.val(); sgn = fgn.val(); sgg = fgg.val(); sd = fd.val();
-    }
     a.S.numneigh[i] = nn;
     if (fixed_i) return;
 
-    // ---- sums in reference units ----
+    // ---- sums in reference units and the Newton-Raphson update
+    // (iterate_density.f90:163-278).  FP64 for the parity form.  The FP32
+    // form keeps FP64 for rho (its compensated sum carries ~48 bits), the
+    // residual f = m (hfact/h)^ndim - rho (a difference ~1e-3 of its terms)
+    // and h, and runs omega, dh/drho, the other sums and the second
+    // derivative in FP32: an FP64 division costs ~30 FP32 issue slots on
+    // this part, and an FP32 residual would move the convergence decision of
+    // particles near the tolerance ----
+    typedef typename std::conditional<PREC == NDSPH_PREC_FP64, double, float>::type E;
     double hfac = hi1;
     if (NDIM >= 2) hfac *= hi1;
     if (NDIM >= 3) hfac *= hi1;
-    const double rho = hfac * sw;
-    const double rhoalt = hfac * sn;
-    double gradh = -hfac * hi1 * sg;
-    const double gradhn = -hfac * hi1 * sgn;
-    double gradgradh = hfac * hi1 * hi1 * sgg;
-    double drhodt = hfac * hi1 * sd;
+    double rho;
+    E hfacE, h1E, Esn, Esg, Esgn, Esgg, Esd;
+    if constexpr (PREC == NDSPH_PREC_FP64) {
+        rho = hfac * sw;
+        hfacE = hfac; h1E = hi1;
+        Esn = sn; Esg = sg; Esgn = sgn; Esgg = sgg; Esd = sd;
+    } else {
+        rho = hfac * fw.val();
+        hfacE = (float)hfac; h1E = (float)hi1;
+        Esn = fn.valf(); Esg = fg.valf(); Esgn = fgn.valf(); Esgg = fgg.valf(); Esd = fd.valf();
+    }
+    const E rhoalt = hfacE * Esn;
+    E gradh = -hfacE * h1E * Esg;
+    const E gradhn = -hfacE * h1E * Esgn;
+    E gradgradh = hfacE * h1E * h1E * Esgg;
+    E drhodt = hfacE * h1E * Esd;
 
-    // ---- Newton-Raphson update, iterate_density.f90:163-278 ----
     const double pm = F.f[PM][i];
     const double hfact = o.hfact;
     const int its = a.d_its ? *a.d_its : a.its;
@@ -483,15 +498,16 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
         raise_err(a.red, NDSPH_E_RHO_NONPOS, a.S.id[i]);
         return;
     }
-    const double dwdhsumi = gradh;
-    double rhoi, dhdrhoi, omegai, d2hdrho2i, hnew;
-    if (PREC == NDSPH_PREC_FP64) {
+    const E dwdhsumi = gradh;
+    E dhdrhoi, omegai, d2hdrho2i;
+    double hnew;
+    if constexpr (PREC == NDSPH_PREC_FP64) {
         // the reference's expressions and association (parity form)
         double hb = hi / hfact;
         double hpow = hb;
         if (NDIM >= 2) hpow = hpow * hb;
         if (NDIM >= 3) hpow = hpow * hb;
-        rhoi = pm / hpow;
+        const double rhoi = pm / hpow;
         dhdrhoi = -hi / ((double)NDIM * rho);
         omegai = 1.0 - dhdrhoi * gradh;
         if (omegai < 1.e-5 && fabs(omegai) == 0.0) omegai = 1.0;
@@ -502,28 +518,25 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
         d2hdrho2i = hi * (double)(NDIM + 1) / (rn * rn);
         hnew = hi - func / dfdh;
     } else {
-        // FP32 form: the same FP64 residual and Newton step with two FP64
-        // divisions instead of six (an FP64 division costs ~16 FP32 issue
-        // slots per operation on this part): 1/h comes from h1, 1/rho once,
         // f/f' = f dh/drho / omega
-        const double rho1 = 1.0 / rho;
         const double hb1 = hfact * hi1;
         double hpow1 = hb1;
         if (NDIM >= 2) hpow1 = hpow1 * hb1;
         if (NDIM >= 3) hpow1 = hpow1 * hb1;
-        rhoi = pm * hpow1;
-        dhdrhoi = -hi * rho1 * (1.0 / (double)NDIM);
-        omegai = 1.0 - dhdrhoi * gradh;
-        if (omegai < 1.e-5 && fabs(omegai) == 0.0) omegai = 1.0;
-        gradh = 1.0 / omegai;
-        const double func = rhoi - rho;
-        d2hdrho2i = hi * (double)(NDIM + 1) * (rho1 * rho1) * (1.0 / (double)(NDIM * NDIM));
-        hnew = hi - func * dhdrhoi * gradh;
+        const float func = (float)(pm * hpow1 - rho);
+        const float rhof = (float)rho;
+        const float rho1 = __frcp_rn(rhof);
+        dhdrhoi = -hif * rho1 * (1.0f / (float)NDIM);
+        omegai = 1.0f - dhdrhoi * gradh;
+        if (omegai < 1.e-5f && fabsf(omegai) == 0.0f) omegai = 1.0f;
+        gradh = __frcp_rn(omegai);
+        d2hdrho2i = hif * (float)(NDIM + 1) * (rho1 * rho1) * (1.0f / (float)(NDIM * NDIM));
+        hnew = hi - (double)(func * dhdrhoi * gradh);
     }
-    gradgradh = rho * (d2hdrho2i * dwdhsumi + dhdrhoi * dhdrhoi * gradgradh);
+    gradgradh = (E)rho * (d2hdrho2i * dwdhsumi + dhdrhoi * dhdrhoi * gradgradh);
     if (hnew > 1.2 * hi) hnew = 1.2 * hi;
     else if (hnew < 0.8 * hi) hnew = 0.8 * hi;
-    if (hnew <= 0.0 || gradh <= 2.2250738585072014e-308) {
+    if (hnew <= 0.0 || (double)gradh <= 2.2250738585072014e-308) {
         hnew = hfact * pow(pm / rho, 1.0 / (double)NDIM);
     } else if (its > 100) {
         hnew = hfact * pow(pm / rho, 1.0 / (double)NDIM);
@@ -536,7 +549,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
     const double hin = F.f[HDEN0][i];
     const bool converged =
         ((PREC == NDSPH_PREC_FP64 ? fabs((hnew - hi) / hin) < o.tolh : fabs(hnew - hi) < o.tolh * hin) &&
-         omegai > 0.0) ||
+         omegai > (E)0) ||
         o.maxdensits == 0;
     double* hdst = FULL ? F.f[HNEXT] : F.f[HH];
     if (!converged) {
@@ -565,15 +578,15 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
         if ((float)hnew + a.nl_dmax > a.S.hb[i] * a.nl_skin) a.red->nl_stale = 1;
     } else {
         drhodt = drhodt * gradh;
-        F.f[DHDT][i] = dhdrhoi * drhodt;
+        F.f[DHDT][i] = (double)(dhdrhoi * drhodt);
     }
     if (relink) a.red->redolink = 1;
-    F.f[RHO][i] = rho;
-    F.f[RHOALT][i] = rhoalt;
-    F.f[DRHODT][i] = drhodt;
-    F.f[GRADH][i] = gradh;
-    F.f[GRADHN][i] = gradhn;
-    F.f[GRADGRADH][i] = gradgradh;
+    F.f[RHO][i] = (double)rho;
+    F.f[RHOALT][i] = (double)rhoalt;
+    F.f[DRHODT][i] = (double)drhodt;
+    F.f[GRADH][i] = (double)gradh;
+    F.f[GRADHN][i] = (double)gradhn;
+    F.f[GRADGRADH][i] = (double)gradgradh;
 }
 
 void launch_density(const SweepArgs& a, bool full, cudaStream_t st)
