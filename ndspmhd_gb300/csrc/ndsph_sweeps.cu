@@ -624,6 +624,7 @@ struct Acc<float> {
     KSum k;
     __device__ __forceinline__ void add(float x) { k.add(x); }
     __device__ __forceinline__ double val() const { return k.val(); }
+    __device__ __forceinline__ float valf() const { return k.valf(); }
 };
 // plain sum in the pair precision: the sources of the dissipation switches
 // (del2u, graddivv), which only enter dalpha/dt and carry no cancellation
@@ -633,7 +634,17 @@ struct AccPlain {
     R v = 0;
     __device__ __forceinline__ void add(R x) { v += x; }
     __device__ __forceinline__ double val() const { return (double)v; }
+    __device__ __forceinline__ R valf() const { return v; }
 };
+// an accumulator's value in the pair precision R: for FP32, the compensated
+// pair's difference rounded once in FP32 (the same float as rounding its
+// exact FP64 difference), with no FP64 conversion on the way
+template <typename R, typename A>
+__device__ __forceinline__ R accv(const A& x)
+{
+    if constexpr (std::is_same<R, float>::value) return x.valf();
+    else return x.val();
+}
 
 // per-particle quantities the rates sweep reads for either side of a pair
 template <typename R>
@@ -1038,13 +1049,13 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
     // precision R: FP64 for the parity form, FP32 for the FP32 form) ----
     const R hi_p = (PREC == 0) ? (R)F.f[HH][i] : hi;
     const R rho1 = (PREC == 0) ? (R)(1.0 / F.f[RHO][i]) : rho1i;
-    R force[3] = {(R)fx.val(), (R)fy.val(), (R)fz.val()};
-    R dBe[3] = {(R)dbx.val(), (R)dby.val(), (R)dbz.val()};
-    R dudt = (R)du.val();
-    R divB = (R)dvb.val();
-    R curlB[3] = {(R)cbx.val(), (R)cby.val(), (R)cbz.val()};
-    const R del2u = (R)d2u.val();
-    const R gdv[3] = {(R)gx.val(), (R)gy.val(), (R)gz.val()};
+    R force[3] = {accv<R>(fx), accv<R>(fy), accv<R>(fz)};
+    R dBe[3] = {accv<R>(dbx), accv<R>(dby), accv<R>(dbz)};
+    R dudt = accv<R>(du);
+    R divB = accv<R>(dvb);
+    R curlB[3] = {accv<R>(cbx), accv<R>(cby), accv<R>(cbz)};
+    const R del2u = accv<R>(d2u);
+    const R gdv[3] = {accv<R>(gx), accv<R>(gy), accv<R>(gz)};
     if (mhd) {
         if (o.imhd > 0)
             for (int c = 0; c < 3; c++) curlB[c] *= rho1;
@@ -1112,7 +1123,35 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
         if (a.tail_on) step_tail_one(F, o, a.red->dt, i, (size_t)a.S.id[i], a.S, a.tail);
     }
 
-    // ---- global reductions (warp first, then one atomic per warp) ----
+    // ---- global reductions ----
+    if (PREC != 0 && !o.batched) {
+        // FP32 form, one simulation: block reductions on the FP32 bit
+        // patterns of the non-negative values (ordered as integers), then one
+        // conversion to FP64 per block and quantity -- the same doubles as
+        // converting every value first
+        (void)hcsts;
+        const float fh = live ? (float)fonh_r : 0.f;
+        const unsigned long long b_dtc = block_min_bits(__float_as_uint(fmaxf((float)dtc, 0.f)));
+        const unsigned long long b_dtav = block_min_bits(__float_as_uint(fmaxf((float)dtav, 0.f)));
+        const unsigned long long b_vs = block_max_bits(__float_as_uint(fmaxf((float)vsmax, 0.f)));
+        const unsigned long long b_ts = block_min_bits(__float_as_uint(fmaxf((float)tsmin, 0.f)));
+        const unsigned long long b_fh = block_max_bits(__float_as_uint(fmaxf(fh, 0.f)));
+        if (threadIdx.x == 0) {
+            // FP32 "no limit" (above 1e37) is the FP64 largest value
+            auto up = [](unsigned long long b, bool nolimit) {
+                double v = (double)__uint_as_float((unsigned)b);
+                if (nolimit && v > 1e37) v = 1.7976931348623157e308;
+                return dbits(v);
+            };
+            atomicMin(&a.red->dtcourant, up(b_dtc, false));
+            atomicMin(&a.red->dtav, up(b_dtav, true));
+            atomicMax(&a.red->vsigmax, up(b_vs, false));
+            atomicMin(&a.red->ts_min, up(b_ts, true));
+            atomicMax(&a.red->fhmax, up(b_fh, false));
+        }
+        return;
+    }
+    // (warp first, then one atomic per warp or block)
     double rdtc = (double)dtc, rdtav = (double)dtav, rvs = (double)vsmax, rts = (double)tsmin;
     if (PREC != 0) {
         if (rdtav > 1e37) rdtav = 1.7976931348623157e308;
