@@ -335,7 +335,7 @@ static void free_particles(ndsph_ctx* ctx)
                     ctx->S.numneigh, ctx->S.cell, ctx->S.xs, ctx->S.h1, ctx->S.active, ctx->S.active_next,
                     ctx->S.flag, ctx->itype2, ctx->id2, ctx->ireal2, ctx->srt.key, ctx->srt.slot, ctx->srt.perm,
                     ctx->d_stage, ctx->d_stage_late, ctx->d_istage, ctx->S.pk_v, ctx->S.pk_t, ctx->S.pk_b, ctx->S.pk_a,
-                    ctx->S.nl, ctx->S.nl_cnt, ctx->S.hb, ctx->S.xsb, ctx->S.sim, ctx->sim2, ctx->d_plist,
+                    ctx->S.nl, ctx->S.nl_cnt, ctx->S.hb, ctx->S.xsb, ctx->S.xg, ctx->S.sim, ctx->sim2, ctx->d_plist,
                     ctx->d_pcnt};
     for (void* p : ptrs) if (p) cudaFree(p);
     ctx->slab[0] = ctx->slab[1] = nullptr;
@@ -384,6 +384,7 @@ static int ensure_capacity(ndsph_ctx* ctx, int n)
     CK(cudaMemsetAsync(ctx->S.sim, 0, ib, ctx->st));
     CK(cudaMalloc(&ctx->S.hb, sizeof(float) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.xsb, sizeof(float4) * (size_t)cap));
+    CK(cudaMalloc(&ctx->S.xg, sizeof(float4) * (size_t)cap));
     ctx->S.nl = nullptr;
     ctx->nl_valid = false;
     ctx->nl_stride = 0;

@@ -33,6 +33,7 @@ struct Side {
     int* nl_cnt;
     float* hb;        // h of each slot when its list was built
     float4* xsb;      // xs of each slot when its list was built (reuse check)
+    float4* xg;       // FP32 position relative to the grid origin + h (3D row build)
     int* sim;         // simulation of the slot (batched form)
 };
 

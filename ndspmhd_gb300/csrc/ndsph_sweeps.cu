@@ -1294,12 +1294,57 @@ __device__ __forceinline__ void nl_scan_run(const SweepArgs& a, const float4& xs
     }
 }
 
+// the same scan on positions relative to the grid origin (3D, one
+// simulation): the separation is a plain difference (ox: the periodic image
+// shift of the run's cells), and the x cell offset is counted only for the
+// entries written
+__device__ __forceinline__ void nl_scan_run_g(const SweepArgs& a, const float4& xgi, float hi, float sk,
+                                              float abs_tol, int jb, int je, const int b[4], int dx0, float ox,
+                                              float oy, float oz, unsigned obase, unsigned* row, int& cnt)
+{
+    const unsigned shift = (unsigned)a.g.nlshift;
+    const int r = (a.g.sw - 1) >> 1;
+    const float xi = xgi.x - ox, yi = xgi.y - oy, zi = xgi.z - oz;
+    for (int j0 = jb; j0 < je; j0 += 4) {
+        float4 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) q[u] = (j0 + u < je) ? a.S.xg[j0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int j = j0 + u;
+            if (j >= je) break;
+            const float tx = xi - q[u].x, ty = yi - q[u].y, tz = zi - q[u].z;
+            const float r2 = tx * tx + ty * ty + tz * tz;
+            const float rc = sk * fmaxf(hi, q[u].w) + abs_tol;
+            if (r2 > rc * rc) continue;
+            if (cnt < a.nl_stride) {
+                const int dx = dx0 + (j >= b[0]) + (j >= b[1]) + (j >= b[2]) + (j >= b[3]);
+                row[cnt] = ((unsigned)j << shift) | (obase + (unsigned)(dx + r));
+            }
+            cnt++;
+        }
+    }
+}
+
+// origin-relative FP32 positions for the 3D row build: the slot's cell
+// corner plus its cell-relative position (after a kept link the slot may
+// have left that cell; the sum is still its position, unwrapped)
+__global__ void k_xg(Side S, Grid g, int n)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int c = S.cell[k];
+    const int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+    const float4 x = S.xs[k];
+    S.xg[k] = make_float4((float)cx * g.csf[0] + x.x, (float)cy * g.csf[1] + x.y, (float)cz * g.csf[2] + x.z, x.w);
+}
+
 // One thread per particle.  For each (dy, dz) row of the stencil, the cells
 // whose box lies within the stencil's reach of the particle (r cells: every
 // pair a sweep may need is within it) form a run of x-adjacent cells, one
 // slot range unless it wraps or leaves an open box; rows and cells beyond
 // the reach are skipped.
-template <int NDIM>
+template <int NDIM, bool XG = false>
 __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1307,6 +1352,7 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
     if (a.gate && *a.gate == 0) return;
     const Grid& g = a.g;
     const float4 xsi = a.S.xs[i];
+    const float4 xgi = XG ? a.S.xg[i] : xsi;
     const float hi = xsi.w;
     const float csmin = fminf(g.csf[0], fminf(NDIM >= 2 ? g.csf[1] : g.csf[0], NDIM >= 3 ? g.csf[2] : g.csf[0]));
     const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
@@ -1355,21 +1401,33 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
             const bool ok0 = stn.cell_at_d(d, g, a.o, c0, w);
             d[0] = dx1;
             const bool ok1 = stn.cell_at_d(d, g, a.o, c1, w);
+            // origin-relative positions: the periodic image shifts of the
+            // row (the same for every cell of it in y and z)
+            const float gy = XG ? (float)w[1] * (float)a.o.L[1] : 0.f;
+            const float gz = XG ? (float)w[2] * (float)a.o.L[2] : 0.f;
             if (ok0 && ok1 && c1 - c0 == dx1 - dx0) {
                 // consecutive cells: one slot range
                 int b[4];
 #pragma unroll
                 for (int k = 0; k < 4; k++) b[k] = (k < dx1 - dx0) ? a.cell_start[c0 + k + 1] : 0x7fffffff;
-                nl_scan_run<NDIM>(a, xsi, hi, sk, abs_tol, a.cell_start[c0], a.cell_start[c1 + 1], b, dx0, oy, oz,
-                                  obase, row, cnt);
+                if (XG)
+                    nl_scan_run_g(a, xgi, hi, sk, abs_tol, a.cell_start[c0], a.cell_start[c1 + 1], b, dx0,
+                                  (float)w[0] * (float)a.o.L[0], gy, gz, obase, row, cnt);
+                else
+                    nl_scan_run<NDIM>(a, xsi, hi, sk, abs_tol, a.cell_start[c0], a.cell_start[c1 + 1], b, dx0, oy,
+                                      oz, obase, row, cnt);
             } else {
                 const int bnone[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
                 for (int dx = dx0; dx <= dx1; dx++) {
                     d[0] = dx;
                     int cid;
                     if (!stn.cell_at_d(d, g, a.o, cid, w)) continue;
-                    nl_scan_run<NDIM>(a, xsi, hi, sk, abs_tol, a.cell_start[cid], a.cell_start[cid + 1], bnone, dx,
-                                      oy, oz, obase, row, cnt);
+                    if (XG)
+                        nl_scan_run_g(a, xgi, hi, sk, abs_tol, a.cell_start[cid], a.cell_start[cid + 1], bnone, dx,
+                                      (float)w[0] * (float)a.o.L[0], gy, gz, obase, row, cnt);
+                    else
+                        nl_scan_run<NDIM>(a, xsi, hi, sk, abs_tol, a.cell_start[cid], a.cell_start[cid + 1], bnone,
+                                          dx, oy, oz, obase, row, cnt);
                 }
             }
         }
@@ -1401,7 +1459,13 @@ void launch_build_nlist(const SweepArgs& a, cudaStream_t st)
     const int nbp = nblk(a.n, 128);
     if (a.o.ndim == 1) NDSPH_COUNT_LAUNCH, k_build_nlist<1><<<nbp, 128, 0, st>>>(a);
     else if (a.o.ndim == 2) NDSPH_COUNT_LAUNCH, k_build_nlist<2><<<nbp, 128, 0, st>>>(a);
-    else NDSPH_COUNT_LAUNCH, k_build_nlist<3><<<nbp, 128, 0, st>>>(a);
+    else if (!a.o.batched && a.g.nc[0] <= 1024 && a.g.nc[1] <= 1024 && a.g.nc[2] <= 1024) {
+        // one 3D simulation of at most 1024 cells a side: the scan runs on
+        // FP32 positions relative to the grid origin, which carry an error of
+        // at most ~6e-8 x 1024 cells, well inside the rows' 2e-4 radius margin
+        NDSPH_COUNT_LAUNCH, k_xg<<<nbp, 128, 0, st>>>(a.S, a.g, a.n);
+        NDSPH_COUNT_LAUNCH, k_build_nlist<3, true><<<nbp, 128, 0, st>>>(a);
+    } else NDSPH_COUNT_LAUNCH, k_build_nlist<3><<<nbp, 128, 0, st>>>(a);
 }
 
 // ===========================================================================
