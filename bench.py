@@ -42,7 +42,7 @@ UNIT = "particle-updates/s"
 # force(3) dBevol/dt(3) du/dt de/dt dalpha/dt(3) divB curlB(3) del2u
 # graddivv(3) drhodt dhdt (21 doubles) once each
 RATES_BYTES_PER_PARTICLE = (26 + 21) * 8
-RATES_DRAM_BYTES_64 = 146.5e6
+RATES_DRAM_BYTES_64 = 146.7e6
 # density pass: reads x(3) h m v(3) (8 doubles) writes rho rhoalt drhodt dhdt
 # gradh gradhn gradgradh h (8 doubles) + numneigh (4 B)
 DENSITY_BYTES_PER_PARTICLE = 16 * 8 + 4
