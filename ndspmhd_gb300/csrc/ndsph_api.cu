@@ -51,6 +51,8 @@ struct ndsph_ctx {
     double* h_dtout = nullptr;
     Reduce* hd_red = nullptr;    // device addresses of the pinned mirrors (null: not mapped)
     double* hd_dtout = nullptr;
+    int* h_ncalc = nullptr;      // pinned: the next pass's active count
+    int* hd_ncalc = nullptr;
     int* d_ncalc = nullptr;
     // host staging
     double* d_stage = nullptr;   // n*3 doubles
@@ -478,6 +480,7 @@ extern "C" int ndsph_init(ndsph_ctx** out, const ndsph_opts* opts, int32_t nmax)
         cudaMallocHost(&ctx->h_red, sizeof(Reduce)) != cudaSuccess ||
         cudaMalloc(&ctx->d_dtout, sizeof(double) * 8) != cudaSuccess ||
         cudaMallocHost(&ctx->h_dtout, sizeof(double) * 8) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_ncalc, sizeof(int) * 4) != cudaSuccess ||
         cudaMalloc(&ctx->d_ncalc, sizeof(int) * 4) != cudaSuccess ||
         cudaMalloc(&ctx->d_fields, sizeof(int) * NF) != cudaSuccess) {
         g_err = "cudaMalloc failed in ndsph_init";
@@ -485,10 +488,12 @@ extern "C" int ndsph_init(ndsph_ctx** out, const ndsph_opts* opts, int32_t nmax)
         return NDSPH_E_CUDA;
     }
     if (cudaHostGetDevicePointer((void**)&ctx->hd_red, ctx->h_red, 0) != cudaSuccess ||
-        cudaHostGetDevicePointer((void**)&ctx->hd_dtout, ctx->h_dtout, 0) != cudaSuccess) {
+        cudaHostGetDevicePointer((void**)&ctx->hd_dtout, ctx->h_dtout, 0) != cudaSuccess ||
+        cudaHostGetDevicePointer((void**)&ctx->hd_ncalc, ctx->h_ncalc, 0) != cudaSuccess) {
         cudaGetLastError();
         ctx->hd_red = nullptr;
         ctx->hd_dtout = nullptr;
+        ctx->hd_ncalc = nullptr;
     }
     cudaMemcpy(ctx->tab64, h64.data(), sizeof(double2) * 4 * NTAB, cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->tab32, h32.data(), sizeof(float2) * 4 * NTAB, cudaMemcpyHostToDevice);
@@ -541,6 +546,7 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
     if (ctx->h_red) cudaFreeHost(ctx->h_red);
     if (ctx->d_arena) cudaFree(ctx->d_arena);
     if (ctx->h_dtout) cudaFreeHost(ctx->h_dtout);
+    if (ctx->h_ncalc) cudaFreeHost(ctx->h_ncalc);
     if (ctx->h_sim_out) cudaFreeHost(ctx->h_sim_out);
     for (int k = 0; k < 16; k++) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     for (int k = 0; k < 2; k++) if (ctx->gexec[k]) cudaGraphExecDestroy(ctx->gexec[k]);
@@ -1215,10 +1221,12 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
         if (full) std::swap(ctx->F.f[HH], ctx->F.f[HNEXT]);
         if (ctx->o.has_fixed) launch_fixed_density_copy(ctx->F, ctx->S, n, st);
         ncalctotal += ncalc;
-        int h_ncalc = 0;
-        CK(cudaMemcpyAsync(&h_ncalc, ctx->d_ncalc, sizeof(int), cudaMemcpyDeviceToHost, st));
+        // the next pass's count comes back with the reductions, one wait
+        if (ctx->hd_ncalc) launch_read_words(ctx->hd_ncalc, ctx->d_ncalc, sizeof(int), st);
+        else CK(cudaMemcpyAsync(ctx->h_ncalc, ctx->d_ncalc, sizeof(int), cudaMemcpyDeviceToHost, st));
         int rc = sync_red(ctx);
         if (rc) return rc;
+        const int h_ncalc = *ctx->h_ncalc;
         if (ctx->profiling) {
             float ms = tdiff(ctx, 2, 3);
             dens_ms += ms;
