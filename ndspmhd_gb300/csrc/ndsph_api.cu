@@ -335,7 +335,7 @@ static void free_particles(ndsph_ctx* ctx)
 {
     void* ptrs[] = {ctx->slab[0], ctx->slab[1], ctx->S.itype, ctx->S.id, ctx->S.ireal, ctx->S.pos_of_id,
                     ctx->S.numneigh, ctx->S.cell, ctx->S.xs, ctx->S.h1, ctx->S.active, ctx->S.active_next,
-                    ctx->S.flag, ctx->itype2, ctx->id2, ctx->ireal2, ctx->srt.key, ctx->srt.slot, ctx->srt.perm,
+                    ctx->S.flag, ctx->itype2, ctx->id2, ctx->ireal2, ctx->srt.key, ctx->srt.slot, ctx->srt.perm, ctx->srt.perm2,
                     ctx->d_stage, ctx->d_stage_late, ctx->d_istage, ctx->S.pk_v, ctx->S.pk_t, ctx->S.pk_b, ctx->S.pk_a,
                     ctx->S.nl, ctx->S.nl_cnt, ctx->S.hb, ctx->S.xsb, ctx->S.xg, ctx->S.sim, ctx->sim2, ctx->d_plist,
                     ctx->d_pcnt};
@@ -344,7 +344,7 @@ static void free_particles(ndsph_ctx* ctx)
     memset(&ctx->S, 0, sizeof(ctx->S));
     ctx->itype2 = ctx->id2 = ctx->ireal2 = nullptr;
     ctx->sim2 = nullptr;
-    ctx->srt.key = ctx->srt.slot = ctx->srt.perm = nullptr;
+    ctx->srt.key = ctx->srt.slot = ctx->srt.perm = ctx->srt.perm2 = nullptr;
     ctx->d_stage = nullptr; ctx->d_istage = nullptr; ctx->d_stage_late = nullptr;
     ctx->d_plist = ctx->d_pcnt = nullptr;
     ctx->cap = 0;
@@ -372,6 +372,7 @@ static int ensure_capacity(ndsph_ctx* ctx, int n)
     CK(cudaMalloc(&ctx->S.active, ib)); CK(cudaMalloc(&ctx->S.active_next, ib)); CK(cudaMalloc(&ctx->S.flag, ib));
     CK(cudaMalloc(&ctx->itype2, ib)); CK(cudaMalloc(&ctx->id2, ib)); CK(cudaMalloc(&ctx->ireal2, ib));
     CK(cudaMalloc(&ctx->srt.key, ib)); CK(cudaMalloc(&ctx->srt.slot, ib)); CK(cudaMalloc(&ctx->srt.perm, ib));
+    CK(cudaMalloc(&ctx->srt.perm2, ib));
     CK(cudaMalloc(&ctx->d_stage, sizeof(double) * 6 * (size_t)cap));   // two staging buffers
     CK(cudaMalloc(&ctx->d_stage_late, sizeof(double) * 16 * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_v, sizeof(float4) * (size_t)cap));

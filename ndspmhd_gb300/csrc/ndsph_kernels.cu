@@ -212,27 +212,30 @@ __global__ void k_scatter(SortScratch s, int n)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    s.perm[s.start[s.key[i]] + s.slot[i]] = i;
+    s.perm2[s.start[s.key[i]] + s.slot[i]] = i;
 }
 
-// per-cell insertion sort of the (previous-order) indices: deterministic order
-__global__ void k_cell_sort(SortScratch s, int ncells)
+// deterministic order inside each cell: every slot takes its rank by index
+// among the cell's slots (the indices are distinct, so the ranks fill the
+// cell; one thread per slot, the cell's indices read by all its threads)
+__global__ void k_cell_rank(SortScratch s, int n)
 {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncells) return;
-    int a = s.start[c], b = s.start[c + 1];
-    for (int k = a + 1; k < b; k++) {
-        int v = s.perm[k];
-        int m = k - 1;
-        while (m >= a && s.perm[m] > v) { s.perm[m + 1] = s.perm[m]; m--; }
-        s.perm[m + 1] = v;
-    }
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int v = s.perm2[k];
+    const int c = s.key[v];
+    const int a = s.start[c], b = s.start[c + 1];
+    int r = 0;
+    for (int j = a; j < b; j++) r += (s.perm2[j] < v);
+    s.perm[a + r] = v;
 }
 
 void launch_scatter_sort(SortScratch s, int n, int ncells, cudaStream_t st)
 {
-    if (n > 0) NDSPH_COUNT_LAUNCH, k_scatter<<<nblk(n, 256), 256, 0, st>>>(s, n);
-    NDSPH_COUNT_LAUNCH, k_cell_sort<<<nblk(ncells, 128), 128, 0, st>>>(s, ncells);
+    (void)ncells;
+    if (n <= 0) return;
+    NDSPH_COUNT_LAUNCH, k_scatter<<<nblk(n, 256), 256, 0, st>>>(s, n);
+    NDSPH_COUNT_LAUNCH, k_cell_rank<<<nblk(n, 256), 256, 0, st>>>(s, n);
 }
 
 // permutation gather of the live fields: dst[f][k] = src[f][perm[k]]

@@ -43,6 +43,7 @@ struct SortScratch {
     int* count;       // per-cell counts (ncells)
     int* start;       // exclusive scan (ncells + 1)
     int* perm;        // sorted slot -> unsorted index
+    int* perm2;       // the scatter's order inside each cell (atomic, varies run to run)
     int* blocksums;   // scan scratch
     float* cell_h;    // largest h of each cell's particles (1D row-build pruning)
     int cap_cells;
