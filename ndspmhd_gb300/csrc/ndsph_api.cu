@@ -1640,6 +1640,33 @@ extern "C" int ndsph_primitive2conservative(ndsph_ctx* ctx, ndsph_particles* p, 
 
 static const int MLP_FIELDS[] = {HPRED, YPREV, FT0, FT1, FT2, FT3, FT4, FT5};
 
+// fields the link at the start of a step's derivs carries into the new slot
+// order: the state and the step's saves, without position components beyond
+// ndim, and without the density outputs when a density pass follows and no
+// particle is fixed (the first pass then rewrites them for every particle;
+// fixed particles carry some of theirs through; dh/dt stays, a particle left
+// unconverged keeps it).  A relink inside the Newton-Raphson loop carries
+// every field.
+static std::vector<int> step_live_fields(const ndsph_ctx* ctx, bool learned)
+{
+    const int nd = ctx->o.ndim;
+    const bool dens = ctx->o.maxdensits >= 1 && !ctx->o.has_fixed;
+    std::vector<int> live;
+    for (int f : STATE_FIELDS) {
+        if ((f == X1 && nd < 2) || (f == X2 && nd < 3)) continue;
+        if (dens && (f == RHO || f == RHOALT || f == DRHODT || f == GRADH || f == GRADHN || f == GRADGRADH))
+            continue;
+        live.push_back(f);
+    }
+    for (int f : INCOPY_FIELDS) {
+        if ((f == XIN1 && nd < 2) || (f == XIN2 && nd < 3)) continue;
+        live.push_back(f);
+    }
+    if (learned)
+        for (int f : MLP_FIELDS) live.push_back(f);
+    return live;
+}
+
 // learned h, before the link: features of the previous step, h_pred -> h_init
 static void mlp_infer(ndsph_ctx* ctx)
 {
@@ -1718,11 +1745,7 @@ static int dev_step_once(ndsph_ctx* ctx)
         mlp_infer(ctx);
         tmark(ctx, 13);
     }
-    std::vector<int> live;
-    for (int f : STATE_FIELDS) live.push_back(f);
-    for (int f : INCOPY_FIELDS) live.push_back(f);
-    if (learned)
-        for (int f : MLP_FIELDS) live.push_back(f);
+    const std::vector<int> live = step_live_fields(ctx, learned);
     int rc = do_derivs(ctx, live.data(), (int)live.size());
     if (rc) return rc;
     if (learned) {
@@ -2110,9 +2133,7 @@ static int batch_step_eager(ndsph_ctx* ctx)
 {
     cudaStream_t st = ctx->st;
     launch_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
-    std::vector<int> live;
-    for (int f : STATE_FIELDS) live.push_back(f);
-    for (int f : INCOPY_FIELDS) live.push_back(f);
+    const std::vector<int> live = step_live_fields(ctx, false);
     int rc = do_derivs(ctx, live.data(), (int)live.size());
     if (rc) return rc;
     launch_corrector(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
@@ -2312,9 +2333,7 @@ static int capture_graphs(ndsph_ctx* ctx)
     graph_drop(ctx);
     if (!ctx->st2) CK(cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking));
     if (!ctx->d_live) CK(cudaMalloc(&ctx->d_live, sizeof(int) * NF));
-    std::vector<int> live;
-    for (int f : STATE_FIELDS) live.push_back(f);
-    for (int f : INCOPY_FIELDS) live.push_back(f);
+    const std::vector<int> live = step_live_fields(ctx, false);
     ctx->nlive = (int)live.size();
     CK(cudaMemcpyAsync(ctx->d_live, live.data(), sizeof(int) * live.size(), cudaMemcpyHostToDevice, st));
     // cells of the captured link: 2 hmax gmargin wide, 3 spare layers on open sides
@@ -2360,9 +2379,7 @@ static int graph_redo(ndsph_ctx* ctx)
     cudaStream_t st = ctx->st;
     launch_copy(ctx->F.f[HH], ctx->F.f[HDEN0], ctx->n, st);
     CK(cudaMemsetAsync(&ctx->red->gfail, 0, sizeof(int), st));
-    std::vector<int> live;
-    for (int f : STATE_FIELDS) live.push_back(f);
-    for (int f : INCOPY_FIELDS) live.push_back(f);
+    const std::vector<int> live = step_live_fields(ctx, false);
     int rc = do_derivs(ctx, live.data(), (int)live.size());
     if (rc) return rc;
     launch_corrector(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
