@@ -85,6 +85,9 @@ struct ndsph_ctx {
     bool late_relayout = false;
     bool late_pending = false;
     bool dl_density_done = false, dl_prim_done = false;
+    // device-resident steps: the last step's corrector also ran this step's
+    // save and predictor (k_corrector_predictor)
+    bool predicted = false;
     // ndsph_step: the rates sweep runs in dl_pieces pieces, one per chunk of
     // the host arrays, and each chunk's last outputs go back while the later
     // pieces run (dl_tail: where they go; null: all after the corrector)
@@ -1730,12 +1733,16 @@ static void mlp_train(ndsph_ctx* ctx)
 }
 
 // one leapfrog step on the device state (stepND_leapfrog_mhd.f90:31-275)
-static int dev_step_once(ndsph_ctx* ctx)
+// fuse_next: another device-resident step follows in the same call, so the
+// corrector also runs that step's save and predictor
+static int dev_step_once(ndsph_ctx* ctx, bool fuse_next = false)
 {
     cudaStream_t st = ctx->st;
     // dt lives in the Reduce block
     CK(cudaMemcpyAsync(&ctx->red->dt, &ctx->dt, sizeof(double), cudaMemcpyHostToDevice, st));
-    if (ctx->late_pending)
+    if (ctx->predicted)
+        ctx->predicted = false;
+    else if (ctx->late_pending)
         launch_predictor_part(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, 1, st);   // the rest in wait_late
     else
         launch_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
@@ -1761,12 +1768,16 @@ static int dev_step_once(ndsph_ctx* ctx)
         }
         ctx->timing.mlp_updates = ctx->mlp_step;
     }
-    launch_corrector(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+    if (fuse_next)
+        launch_corrector_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, ctx->d_dtout + 6, st);
+    else
+        launch_corrector(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
     rc = sync_red(ctx);
     if (rc) return rc;
     ctx->time += ctx->dt;
     ctx->dt = ctx->h_dtout[6];
     ctx->nsteps++;
+    ctx->predicted = fuse_next;
     return 0;
 }
 
@@ -1882,11 +1893,18 @@ extern "C" int ndsph_dev_step(ndsph_ctx* ctx, int32_t nsteps, ndsph_dt* dts)
     CK(cudaEventRecord(ctx->ev[10], ctx->st));
     float rates_sum = 0.f, dens_sum = 0.f, link_sum = 0.f;
     int passes = 0;
+    // between two steps of the call the corrector and the next predictor run
+    // as one pass (one simulation without fixed particles: the predictor
+    // then reads only each particle's own fields); the call ends corrected
+    const bool fusable = !ctx->o.has_fixed && !ctx->o.batched;
     for (int k = 0; k < nsteps; k++) {
         tmark(ctx, 8);
-        int rc = dev_step_once(ctx);
+        int rc = dev_step_once(ctx, fusable && k + 1 < nsteps);
         tmark(ctx, 9);
-        if (rc) return rc;
+        if (rc) {
+            ctx->predicted = false;
+            return rc;
+        }
         if (ctx->profiling) {
             cudaEventSynchronize(ctx->ev[9]);
             ctx->timing.step_ms = tdiff(ctx, 8, 9);

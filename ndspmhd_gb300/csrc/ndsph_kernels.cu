@@ -669,11 +669,9 @@ __global__ void k_predictor2(FieldPtrs F, Side S, DevOpts o, int n, const Reduce
 // force, h, dh/dt, rho); 2: Bevol, energy and alpha (with their saves and the
 // saves of their rates) -- a host-buffer step uploads the latter while the
 // link and the density passes run
-__global__ void k_predictor_fused(FieldPtrs F, Side S, DevOpts o, int n, const Reduce* red, int part)
+__device__ __forceinline__ void predictor_one(const FieldPtrs& F, const Side& S, const DevOpts& o, double dt, int i,
+                                              int part)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double dt = o.batched ? o.sim_dt[S.sim[i]] : red->dt;
     const int t = S.itype[i];
     const bool fixed = (t == NDSPH_ITYPE_BND || t == NDSPH_ITYPE_BNDDUST);
     if (part != 2) {
@@ -709,6 +707,13 @@ __global__ void k_predictor_fused(FieldPtrs F, Side S, DevOpts o, int n, const R
         for (int d = 0; d < 3; d++)
             if (o.iavlim[d] != 0) F.f[AL0 + d][i] = fmin(al[d] + dt * dal[d], 1.0);
     }
+}
+__global__ void k_predictor_fused(FieldPtrs F, Side S, DevOpts o, int n, const Reduce* red, int part)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double dt = o.batched ? o.sim_dt[S.sim[i]] : red->dt;
+    predictor_one(F, S, o, dt, i, part);
 }
 
 void launch_predictor_part(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, int part, cudaStream_t st)
@@ -754,6 +759,35 @@ __global__ void k_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
 void launch_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st)
 {
     if (n > 0) NDSPH_COUNT_LAUNCH, k_corrector<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+}
+
+// one simulation without fixed particles, between two steps of a
+// device-resident run: this step's corrector and the next step's save and
+// predictor (with the next dt, dtnext) in one pass over the particles -- the
+// same arithmetic as k_corrector followed by k_predictor_fused
+__global__ void k_corrector_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, const double* dtnext)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Corrected c;
+    corrector_values(F, S, o, red->dt, i, c);
+    if (!(c.h > 0.0)) raise_err(red, NDSPH_E_H_NONPOS, S.id[i]);
+    for (int d = 0; d < 3; d++) F.f[V0 + d][i] = c.v[d];
+    if (o.imhd != 0)
+        for (int d = 0; d < 3; d++) F.f[BE0 + d][i] = c.be[d];
+    for (int d = 0; d < 3; d++)
+        if (o.iavlim[d] != 0) F.f[AL0 + d][i] = c.al[d];
+    F.f[HH][i] = c.h;
+    if (o.iener != 0) F.f[EN][i] = c.en;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+        if (d < o.ndim && o.ibound[d] == 3) F.f[X0 + d][i] = c.x[d];
+    predictor_one(F, S, o, *dtnext, i, 0);
+}
+void launch_corrector_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, const double* dtnext,
+                                cudaStream_t st)
+{
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_corrector_predictor<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red, dtnext);
 }
 
 __global__ void k_read_words(const unsigned* __restrict__ src, unsigned* __restrict__ dst, int nw)

@@ -135,6 +135,10 @@ void launch_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaSt
 // states without fixed particles: part 1 = x, v, h; part 2 = Bevol, energy, alpha
 void launch_predictor_part(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, int part, cudaStream_t st);
 void launch_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st);
+// one simulation, no fixed particles: the corrector and the next step's save
+// and predictor (dt from dtnext, a device value) in one pass
+void launch_corrector_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, const double* dtnext,
+                                cudaStream_t st);
 // slots grouped by the host chunk of their particle (chunk c = particles
 // c*len .. (c+1)*len), ascending within a chunk: plist[c*len + r] is the
 // r-th slot of chunk c.  cnt: scratch of nchunk * ceil(n / 1024) ints

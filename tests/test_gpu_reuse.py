@@ -202,3 +202,36 @@ def test_host_step_streamed_skips_null_outputs(gpulib):
         assert np.all(part[k] == -7.0), k
     differ = [k for k in full if k not in dropped and not np.array_equal(full[k], part[k])]
     assert not differ, differ
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_device_steps_in_one_call_identical(precision, gpulib):
+    """Several device-resident steps in one call (the corrector and the next
+    predictor fused between them) leave the state bit-identical to the same
+    steps taken one call at a time."""
+    import numpy as np
+    from ndspmhd_gb300.gpu import GpuSPH
+    o, p = configs.mhd_box_3d(20, seed=5)
+    o = dict(o)
+    o["precision"] = precision
+    g0 = GpuSPH(o, configs.full_state(p, 3))
+    g0.primitive2conservative()
+    st = {k: v.copy() for k, v in g0.state.items()}
+    g0.close()
+    runs = []
+    for split in (False, True):
+        g = GpuSPH(o, {k: v.copy() for k, v in st.items()})
+        g.dev_upload()
+        g.set_dt(0.0)
+        if split:
+            for _ in range(6):
+                g.dev_step(1)
+        else:
+            g.dev_step(6)
+        g.dev_download()
+        runs.append(({k: v.copy() for k, v in g.state.items()}, g.dt.dt, g.dt.time))
+        g.close()
+    (a, dta, ta), (b, dtb, tb) = runs
+    assert dta == dtb and ta == tb
+    differ = [k for k in a if not np.array_equal(a[k], b[k])]
+    assert not differ, differ
