@@ -49,3 +49,37 @@ def test_default_opts_match_reference_defaults():
               "alphaBmin", "beta", "avdecayconst", "C_cour", "C_force"):
         assert getattr(o, k) == d[k], k
     assert list(o.iavlim) == d["iavlim"]
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The ctypes mirrors of the public structs have the header's sizes and
+    field offsets (a C program built against include/ndsph.h prints them)."""
+    import ctypes as C
+    import shutil
+    from ndspmhd_gb300 import abi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    pairs = [("ndsph_opts", abi.NdsphOpts), ("ndsph_particles", abi.NdsphParticles), ("ndsph_dt", abi.NdsphDt),
+             ("ndsph_timing", abi.NdsphTiming), ("ndsph_tuning", abi.NdsphTuning)]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ndsph.h"', 'int main(void) {']
+    for cname, py in pairs:
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ['return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for ln in out:
+        if ln.strip():
+            a, b, c = ln.split()
+            got[(a, b)] = int(c)
+    for cname, py in pairs:
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
