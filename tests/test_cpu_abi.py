@@ -83,3 +83,39 @@ def test_ctypes_structs_match_the_header(tmp_path):
         assert got[(cname, "size")] == C.sizeof(py), cname
         for fname, _ in py._fields_:
             assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def _c_struct_fields(txt, name):
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), txt, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    out = []
+    for m in re.finditer(r"\b(int32_t|int64_t|double|float)\s*(\*?)\s*(\w+)\s*(?:\[(\d+)\])?\s*;", body):
+        kind = "ptr" if m.group(2) else m.group(1)
+        out.append((m.group(3).lower(), kind, int(m.group(4) or 1)))
+    return out
+
+
+def _f_type_fields(txt, name):
+    body = re.search(r"type, bind\(C\) :: %s\n(.*?)\n\s*end type" % name, txt, re.S).group(1)
+    kinds = {"integer(c_int32_t)": "int32_t", "integer(c_int64_t)": "int64_t", "real(c_double)": "double",
+             "real(c_float)": "float", "type(c_ptr)": "ptr"}
+    out = []
+    for line in body.split("\n"):
+        line = line.split("!")[0].strip()
+        if not line:
+            continue
+        decl, names = [x.strip() for x in line.split("::")]
+        for m in re.finditer(r"(\w+)\s*(?:\((\d+)\))?", names):
+            out.append((m.group(1).lower(), kinds[decl.replace(" ", "")], int(m.group(2) or 1)))
+    return out
+
+
+def test_fortran_shim_types_match_the_header():
+    """The bind(C) derived types of the Fortran shim list the header's fields
+    in the same order with the matching C kinds (the shim is not compiled
+    here, so its layout is checked against the declarations as text)."""
+    c = open(os.path.join(ROOT, "include", "ndsph.h")).read()
+    f = open(os.path.join(ROOT, "ndspmhd_gb300", "fortran", "gpu_sph.f90")).read()
+    for cname in ("ndsph_opts", "ndsph_particles", "ndsph_dt", "ndsph_tuning"):
+        cf, ff = _c_struct_fields(c, cname), _f_type_fields(f, cname + "_t")
+        assert cf and cf == ff, (cname, cf, ff)
