@@ -286,6 +286,39 @@ def run_batched(steps: int, warmup: int, ntubes: int = 4096):
     return res
 
 
+def fp32_error(steps: int = 4, tolh: float = 1e-6):
+    """Error of the FP32 form against the FP64 (parity) form on the headline
+    workload: both from the same FP64 primitive2conservative state, `steps`
+    device-resident steps each (each form takes its own dt), then per field
+    max |fp32 - fp64| / max(max |fp64|, rms(fp64)).  Both forms iterate h to
+    `tolh` = 1e-6: at the workload's 1e-3 a particle whose Newton-Raphson
+    residual sits at the tolerance converges one pass apart in the two forms
+    and moves its h by up to ~1e-3, which would hide the arithmetic error."""
+    import numpy as np
+    from ndspmhd_gb300.gpu import GpuSPH
+    fields = ("x", "vel", "hh", "rho", "en", "Bevol", "force", "dudt", "dBevoldt")
+    o64, st64 = make_problem(N1D, 0)
+    o64["tolh"] = tolh
+    g = init_state(o64, st64)
+    st0 = {k: v.copy() for k, v in g.state.items()}
+    g.close()
+    out = {}
+    for prec in (0, 1):
+        g = GpuSPH(dict(o64, precision=prec), {k: v.copy() for k, v in st0.items()})
+        g.dev_upload()
+        g.set_dt(0.0)
+        g.dev_step(steps)
+        g.dev_download()
+        out[prec] = {k: g.state[k].copy() for k in fields}
+        g.close()
+    res = {"steps": steps, "tolh": tolh, "metric": "max |fp32 - fp64| / max(max |fp64|, rms fp64), per field"}
+    for k in fields:
+        ref = out[0][k]
+        scale = max(float(np.max(np.abs(ref))), float(np.sqrt(np.mean(ref * ref))))
+        res[k] = float(np.max(np.abs(out[1][k] - ref)) / scale) if scale > 0 else 0.0
+    return res
+
+
 def run_learned(n1d: int, steps: int, warmup: int):
     """Learned-h workload: isothermal log-normal turbulent box, tolh = 1e-4,
     FP32 pairs; NR density work and step rate with the reference's predictor
@@ -598,6 +631,8 @@ def main():
                         "speedup_fp32_over_fp64": round(ms64 / ms32, 2)}
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if not args.no_fp64 and world == 1:
+        line["fp32_error_vs_fp64"] = fp32_error()
     if not args.no_extra and world == 1:
         line["batched"] = run_batched(200, 3)
         if not args.no_cpu:
