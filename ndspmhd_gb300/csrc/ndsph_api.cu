@@ -93,6 +93,7 @@ struct ndsph_ctx {
     // pieces run (dl_tail: where they go; null: all after the corrector)
     ndsph_particles* dl_tail = nullptr;
     bool dl_tail_done = false;
+    bool dl_x_done = false;      // positions went back before the density passes
     int dl_pieces = 8;
     int* d_plist = nullptr;      // slots grouped by host chunk
     int* d_pcnt = nullptr;       // its scratch: dl_pieces counts per 1024 slots
@@ -735,6 +736,23 @@ static int download_aos(ndsph_ctx* ctx, double* host, int f0, int ncomp, int str
     CK(cudaMemcpyAsync(host, dst, sizeof(double) * need, cudaMemcpyDeviceToHost, ctx->st_cp));
     return 0;
 }
+// as download_aos, with the gather on the main stream (ordered before what
+// the main stream does next, e.g. a relink that rewrites pos_of_id) and the
+// copy on the copy stream
+static int download_aos_ordered(ndsph_ctx* ctx, double* host, int f0, int ncomp, int stride, int n)
+{
+    if (!host) return 0;
+    const size_t need = (size_t)stride * n;
+    int rc = arena_reserve(ctx, need);
+    if (rc) return rc;
+    double* dst = ctx->d_arena + ctx->arena_used;
+    ctx->arena_used += need;
+    launch_slab_to_aos(dst, stride, ctx->F, f0, ncomp, ctx->S.pos_of_id, n, ctx->st);
+    CK(cudaEventRecord(ctx->ev_dl, ctx->st));
+    CK(cudaStreamWaitEvent(ctx->st_cp, ctx->ev_dl, 0));
+    CK(cudaMemcpyAsync(host, dst, sizeof(double) * need, cudaMemcpyDeviceToHost, ctx->st_cp));
+    return 0;
+}
 static int download_end(ndsph_ctx* ctx)
 {
     CK(cudaStreamSynchronize(ctx->st));
@@ -1281,8 +1299,10 @@ static int rates_streamed(ndsph_ctx* ctx, SweepArgs a)
     const int len = (n + K - 1) / K;
     StepTail t;
     struct Out { double* host; double** stage; int stride; };
-    Out outs[] = {{p->x, &t.x, nd}, {p->vel, &t.v, 3}, {p->Bevol, &t.be, 3}, {p->en, &t.en, 1},
-                  {p->hh, &t.hh, 1}, {p->alpha, &t.al, 3}, {p->drhodt, &t.drhodt, 1}, {p->dhdt, &t.dhdt, 1},
+    // (the positions went back before the density passes when dl_x_done)
+    Out outs[] = {{ctx->dl_x_done ? nullptr : p->x, &t.x, nd}, {p->vel, &t.v, 3}, {p->Bevol, &t.be, 3},
+                  {p->en, &t.en, 1}, {p->hh, &t.hh, 1}, {p->alpha, &t.al, 3}, {p->drhodt, &t.drhodt, 1},
+                  {p->dhdt, &t.dhdt, 1},
                   {p->force, &t.force, 3}, {p->dBevoldt, &t.db, 3}, {p->dudt, &t.dudt, 1},
                   {p->dendt, &t.dendt, 1}, {p->daldt, &t.dal, 3}, {p->divB, &t.divb, 1},
                   {p->curlB, &t.curlb, 3}, {p->del2u, &t.del2u, 1}, {p->graddivv, &t.gdv, 3}};
@@ -1371,6 +1391,14 @@ static int do_derivs(ndsph_ctx* ctx, const int* fields, int nfields)
     if (anyb) launch_boundary_wrap(ctx->F, ctx->o, ctx->n, st);
     int rc = do_link(ctx, fields, nfields, false, true);
     if (rc) return rc;
+    // a streamed host-buffer step: the positions are final here (wrapped; the
+    // corrector's wrap leaves them), so they go back while the density
+    // passes run
+    if (ctx->dl_tail && ctx->dl_tail->x) {
+        rc = download_aos_ordered(ctx, ctx->dl_tail->x, X0, ctx->o.ndim, ctx->o.ndim, ctx->n);
+        if (rc) return rc;
+        ctx->dl_x_done = true;
+    }
     tmark(ctx, 1);
     launch_reduce_reset(ctx->red, st);
     if (ctx->o.batched) launch_sim_reset(ctx->o, st);
@@ -2050,7 +2078,7 @@ extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, nds
     const bool streamed = early && !ctx->host_access && !ctx->o.batched && ctx->dl_pieces > 1 &&
                           npart >= (1 << 16);
     ctx->dl_tail = streamed ? p : nullptr;
-    ctx->dl_density_done = ctx->dl_prim_done = ctx->dl_tail_done = false;
+    ctx->dl_density_done = ctx->dl_prim_done = ctx->dl_tail_done = ctx->dl_x_done = false;
     ctx->arena_used = 0;
     rc = dev_step_once(ctx);
     if (rc) {
@@ -2060,14 +2088,14 @@ extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, nds
         ctx->late_pending = false;
         ctx->dl_early = nullptr;
         ctx->dl_tail = nullptr;
-        ctx->dl_density_done = ctx->dl_prim_done = ctx->dl_tail_done = false;
+        ctx->dl_density_done = ctx->dl_prim_done = ctx->dl_tail_done = ctx->dl_x_done = false;
         return rc;
     }
     ctx->dl_early = p;   // also: pmass is not copied back (the step never writes it)
     rc = download_all(ctx, p);
     ctx->dl_early = nullptr;
     ctx->dl_tail = nullptr;
-    ctx->dl_density_done = ctx->dl_prim_done = ctx->dl_tail_done = false;
+    ctx->dl_density_done = ctx->dl_prim_done = ctx->dl_tail_done = ctx->dl_x_done = false;
     ctx->timing.launches = (int32_t)(ndsph_launch_counter().load() - l0);
     fill_dt(ctx, dts);
     return rc;
