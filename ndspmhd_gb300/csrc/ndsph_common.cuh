@@ -37,6 +37,7 @@ enum Field : int {
     HPRED, YPREV, FT0, FT1, FT2, FT3, FT4, FT5,   // learned-h predictor: h_pred, last z, features
     HDEN0,      // h at entry of iterate_density (hhin, iterate_density.f90:87)
     HNEXT,      // NR scratch: next h of the first pass
+    RHO1,       // 1/rho of the FP64 rates sweep (written with the EOS)
     NF
 };
 

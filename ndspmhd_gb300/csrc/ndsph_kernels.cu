@@ -532,6 +532,9 @@ __global__ void k_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
     if (k < n) {
         double rho = F.f[RHO][k];
         F.f[DENS][k] = rho;
+        // the FP64 rates sweep reads 1/rho of every neighbour: one division
+        // per particle instead of one per pair
+        if (o.precision == NDSPH_PREC_FP64) F.f[RHO1][k] = 1.0 / rho;
         double B[3] = {0.0, 0.0, 0.0};
         if (o.imhd >= 11) {
             for (int d = 0; d < 3; d++) B[d] = F.f[BE0 + d][k];
@@ -603,7 +606,7 @@ __global__ void k_fixed_copy(FieldPtrs F, Side S, int n)
     int j = S.pos_of_id[src_id];
     const int fl[] = {PM, RHO, RHOALT, HH, UU, EN, BE0, BE1, BE2, BF0, BF1, BF2, AL0, AL1, AL2, GRADH, GRADHN,
                       GRADGRADH, CS, PR, DENS, F0, F1, F2, DRHODT, DUDT, DENDT, DB0, DB1, DB2, DHDT, DAL0, DAL1,
-                      DAL2, DIVB, CB0, CB1, CB2};
+                      DAL2, DIVB, CB0, CB1, CB2, RHO1};
     for (unsigned q = 0; q < sizeof(fl) / sizeof(fl[0]); q++) F.f[fl[q]][k] = F.f[fl[q]][j];
 }
 void launch_fixed_copy(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st)

@@ -744,6 +744,9 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
     Acc<R> fx, fy, fz, dbx, dby, dbz, du, dvb, cbx, cby, cbz;
     AccPlain<R> d2u, gx, gy, gz;
     R dtc = (R)1.e6, dtav = (R)3.0e38, vsmax = 0, tsmin = (R)3.0e38, hcsts = 0;
+    // FP64 form: the two timestep minima as the pair (h, v) of the smallest
+    // h / v, compared by cross-multiplication and divided once per particle
+    R dtc_h = (R)1.e6, dtc_v = 1, dtav_h = (R)3.0e38, dtav_v = 1;
 
     Stencil<NDIM> stn(a.S.cell[i], g);
     const int ncand = live ? a.S.nl_cnt[i] : 0;
@@ -762,6 +765,7 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
             const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
             const float hm = fmaxf(hif, xsj.w);
             R dr[3], rij, q2i, q2j, hj1;
+            double irij = 0.0;   // FP64 form: 1/rij, reused by the conduction term
             if constexpr (PREC == NDSPH_PREC_FP64) {
                 const float rc = 2.0f * hm * 1.0002f + abs_tol;
                 if (r2f > rc * rc) return;
@@ -776,9 +780,11 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
                     if (a.S.itype[j] == typei && rijd < 2.2250738585072014e-308 && typei != 2)
                         raise_err(a.red, NDSPH_E_CLUMP, a.S.id[i]);
                     dr[0] = dr[1] = dr[2] = 0;
+                    irij = 1.0 / rijd;
                 } else {
                     const double ir = 1.0 / rijd;
                     dr[0] = dx[0] * ir; dr[1] = dx[1] * ir; dr[2] = dx[2] * ir;
+                    irij = ir;
                 }
                 rij = rijd; q2i = q2id; q2j = q2jd; hj1 = hj1d;
             } else {
@@ -834,7 +840,7 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
                 const R grkernj = gwj * hfacgrkj * pj.gradh;
                 const R grkern = (R)0.5 * (grkerni + grkernj);
                 const R dvdotr = dvel[0] * dr[0] + dvel[1] * dr[1] + dvel[2] * dr[2];
-                const R rho1j = rcp(rhoj);
+                const R rho1j = (PREC == NDSPH_PREC_FP64) ? (R)F.f[RHO1][j] : rcp(rhoj);
                 const R rho21j = rho1j * rho1j;
                 const R rhoav1 = (R)0.5 * (rho1i + rho1j);
                 const R prj = pj.pr;
@@ -878,7 +884,13 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
                     vsig = 0; vsigu = 0;
                 } else {
                     vsmax = fmax(vsmax, vsigdtc);
-                    if (vsigdtc > (R)1.e-10) dtc = fmin(dtc, divp(hmin, vsigdtc));
+                    if (vsigdtc > (R)1.e-10) {
+                        if (PREC == NDSPH_PREC_FP64) {
+                            if (hmin * dtc_v < dtc_h * vsigdtc) { dtc_h = hmin; dtc_v = vsigdtc; }
+                        } else {
+                            dtc = fmin(dtc, divp(hmin, vsigdtc));
+                        }
+                    }
                 }
                 R fxi = 0, fyi = 0, fzi = 0;
                 // ---------------- artificial_dissipation ----------------
@@ -911,7 +923,13 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
                             vissB = -alphaB * (R)0.5 * (dB[0] * dB[0] + dB[1] * dB[1] + dB[2] * dB[2]) * rhoav1;
                         du.add(mj * (term * vissv + termu * vissu + termB * vissB));
                     }
-                    if (vsigav > (R)1.e-10) dtav = fmin(dtav, divp(hmin, vsigav));
+                    if (vsigav > (R)1.e-10) {
+                        if (PREC == NDSPH_PREC_FP64) {
+                            if (hmin * dtav_v < dtav_h * vsigav) { dtav_h = hmin; dtav_v = vsigav; }
+                        } else {
+                            dtav = fmin(dtav, divp(hmin, vsigav));
+                        }
+                    }
                 }
                 // ---------------- pressure ----------------
                 const R prterm = Prho2i * grkerni + Prho2j * grkernj;
@@ -941,7 +959,7 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
                 fx.add(fxi); fy.add(fyi); fz.add(fzi);
                 if (o.iav > 0) {
                     if (o.iavlim[1] > 0) {
-                        const R graduterm = (ui - pj.u) * rcp(rij);
+                        const R graduterm = (ui - pj.u) * ((PREC == NDSPH_PREC_FP64) ? (R)irij : rcp(rij));
                         d2u.add(mj * rho1j * graduterm * grkerni);
                     }
                     if (o.iavlim[0] != 3) {
@@ -1043,6 +1061,11 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
             }
             for (int q = 0; q < na; q++) pair_terms(mine[q * RATES_BS]);
         }
+    }
+
+    if (PREC == NDSPH_PREC_FP64) {
+        dtc = dtc_h / dtc_v;
+        dtav = dtav_h / dtav_v;
     }
 
     // ---- per-particle post pass ratesND_mhd.f90:532-965 (in the pair
