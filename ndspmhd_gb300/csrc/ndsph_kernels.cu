@@ -617,61 +617,13 @@ void launch_fixed_copy(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st)
 // ---------------------------------------------------------------------------
 // leapfrog stepND_leapfrog_mhd.f90:31-275
 // ---------------------------------------------------------------------------
-__global__ void k_predictor(FieldPtrs F, Side S, DevOpts o, int n, const Reduce* red)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    // save (:70-101)
-    for (int d = 0; d < o.ndim; d++) F.f[XIN0 + d][i] = F.f[X0 + d][i];
-    for (int d = 0; d < 3; d++) {
-        F.f[VIN0 + d][i] = F.f[V0 + d][i];
-        F.f[BIN0 + d][i] = F.f[BE0 + d][i];
-        F.f[ALIN0 + d][i] = F.f[AL0 + d][i];
-        F.f[FIN0 + d][i] = F.f[F0 + d][i];
-        F.f[DBIN0 + d][i] = F.f[DB0 + d][i];
-        F.f[DALIN0 + d][i] = F.f[DAL0 + d][i];
-    }
-    F.f[HIN][i] = F.f[HH][i];
-    F.f[ENIN][i] = F.f[EN][i];
-    F.f[RHOIN][i] = F.f[RHO][i];
-    F.f[DHIN][i] = F.f[DHDT][i];
-    F.f[DENIN][i] = F.f[DENDT][i];
-}
-
-__global__ void k_predictor2(FieldPtrs F, Side S, DevOpts o, int n, const Reduce* red)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double dt = o.batched ? o.sim_dt[S.sim[i]] : red->dt;
-    int t = S.itype[i];
-    if (t == NDSPH_ITYPE_BND || t == NDSPH_ITYPE_BNDDUST) {
-        int j = (S.ireal[i] >= 0) ? S.pos_of_id[S.ireal[i]] : i;
-        for (int d = 0; d < o.ndim; d++)
-            F.f[X0 + d][i] = F.f[XIN0 + d][i] + dt * F.f[VIN0 + d][j] + 0.5 * dt * dt * F.f[FIN0 + d][j];
-        for (int d = 0; d < 3; d++) F.f[BE0 + d][i] = F.f[BIN0 + d][i];
-        F.f[RHO][i] = F.f[RHOIN][i];
-        F.f[HH][i] = F.f[HIN][i];
-        F.f[EN][i] = F.f[ENIN][i];
-        for (int d = 0; d < 3; d++) F.f[AL0 + d][i] = F.f[ALIN0 + d][i];
-    } else {
-        for (int d = 0; d < o.ndim; d++)
-            F.f[X0 + d][i] = F.f[XIN0 + d][i] + dt * F.f[VIN0 + d][i] + 0.5 * dt * dt * F.f[FIN0 + d][i];
-        for (int d = 0; d < 3; d++) F.f[V0 + d][i] = (F.f[VIN0 + d][i] + dt * F.f[FIN0 + d][i]) / (1.0 + 0.0);
-        if (o.imhd != 0)
-            for (int d = 0; d < 3; d++) F.f[BE0 + d][i] = F.f[BIN0 + d][i] + dt * F.f[DBIN0 + d][i];
-        F.f[HH][i] = F.f[HIN][i] + dt * F.f[DHIN][i];
-        if (o.iener != 0) F.f[EN][i] = F.f[ENIN][i] + dt * F.f[DENIN][i];
-        for (int d = 0; d < 3; d++)
-            if (o.iavlim[d] != 0) F.f[AL0 + d][i] = fmin(F.f[ALIN0 + d][i] + dt * F.f[DALIN0 + d][i], 1.0);
-    }
-}
-// save and predictor in one pass, for states without fixed particles (no
-// particle reads another's saved velocity and force, so no grid-wide order
-// is needed between the two); same arithmetic as k_predictor + k_predictor2.
-// part 0: every field; 1: position, velocity and h (with the saves of x, v,
-// force, h, dh/dt, rho); 2: Bevol, energy and alpha (with their saves and the
-// saves of their rates) -- a host-buffer step uploads the latter while the
-// link and the density passes run
+// leapfrog save and predictor (stepND_leapfrog_mhd.f90:70-101, :107-160) in one pass:
+// each particle reads only its own fields (a fixed particle's position,
+// which follows its source particle's saves, is set afterwards by
+// k_predictor_fixed_x).  part 0: every field; 1: position, velocity and h
+// (with the saves of x, v, force, h, dh/dt, rho); 2: Bevol, energy and alpha
+// (with their saves and the saves of their rates) -- a host-buffer step
+// uploads the latter while the link and the density passes run
 __device__ __forceinline__ void predictor_one(const FieldPtrs& F, const Side& S, const DevOpts& o, double dt, int i,
                                               int part)
 {
@@ -724,15 +676,28 @@ void launch_predictor_part(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, i
     if (n > 0) NDSPH_COUNT_LAUNCH, k_predictor_fused<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red, part);
 }
 
+// fixed particles after k_predictor_fused: the position moves by the source
+// particle's saved velocity and force (stepND_leapfrog_mhd.f90:110-116);
+// every other field of theirs is held, as k_predictor_fused leaves it
+__global__ void k_predictor_fixed_x(FieldPtrs F, Side S, DevOpts o, int n, const Reduce* red)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int t = S.itype[i];
+    if (t != NDSPH_ITYPE_BND && t != NDSPH_ITYPE_BNDDUST) return;
+    const double dt = o.batched ? o.sim_dt[S.sim[i]] : red->dt;
+    const int j = (S.ireal[i] >= 0) ? S.pos_of_id[S.ireal[i]] : i;
+    for (int d = 0; d < o.ndim; d++)
+        F.f[X0 + d][i] = F.f[XIN0 + d][i] + dt * F.f[VIN0 + d][j] + 0.5 * dt * dt * F.f[FIN0 + d][j];
+}
+
 void launch_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaStream_t st)
 {
     if (n <= 0) return;
-    if (!o.has_fixed) {
-        NDSPH_COUNT_LAUNCH, k_predictor_fused<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red, 0);
-        return;
-    }
-    NDSPH_COUNT_LAUNCH, k_predictor<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
-    NDSPH_COUNT_LAUNCH, k_predictor2<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
+    // save and predictor in one pass; with fixed particles their positions
+    // then follow their sources' saves (complete when the first kernel ends)
+    NDSPH_COUNT_LAUNCH, k_predictor_fused<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red, 0);
+    if (o.has_fixed) NDSPH_COUNT_LAUNCH, k_predictor_fixed_x<<<nblk(n, 256), 256, 0, st>>>(F, S, o, n, red);
 }
 
 __global__ void k_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
