@@ -119,3 +119,59 @@ def test_fortran_shim_types_match_the_header():
     for cname in ("ndsph_opts", "ndsph_particles", "ndsph_dt", "ndsph_tuning"):
         cf, ff = _c_struct_fields(c, cname), _f_type_fields(f, cname + "_t")
         assert cf and cf == ff, (cname, cf, ff)
+
+
+# option sets the reference supports but the device path does not take: each is
+# refused by ndsph_init with NDSPH_E_ARG before any CUDA call
+_OUT_OF_SCOPE = [
+    (dict(ndim=4), "ndim"),
+    (dict(ibound=[2, 0, 0]), "ibound"),
+    (dict(ibound=[3, 0, 0], xmin=[1.0, 0.0, 0.0], xmax=[1.0, 1.0, 1.0]), "xmax <= xmin"),
+    (dict(imhd=2), "imhd"),
+    (dict(imhd=1, imagforce=1), "imagforce"),
+    (dict(iener=1), "iener"),
+    (dict(iav=1), "iav"),
+    (dict(idust=1), "idust"),
+    (dict(idust=2, idrag_nature=2), "idrag_nature"),
+    (dict(iavlim=[3, 1, 0]), "iavlim"),
+    (dict(iavlim=[2, 1, 1]), "iavlim"),
+    (dict(precision=7), "precision"),
+]
+
+
+def test_out_of_scope_options_are_refused():
+    import pytest
+    from ndspmhd_gb300 import gpu
+    from ndspmhd_gb300.configs import default_opts
+    for change, word in _OUT_OF_SCOPE:
+        o = default_opts(3)
+        o.update(change)
+        with pytest.raises(gpu.NdsphError) as e:
+            gpu.GpuSPH(o, n=64)
+        assert e.value.code == 1, (change, str(e.value))
+        assert word in str(e.value), (change, str(e.value))
+
+
+def test_without_a_gpu_the_context_fails_loudly():
+    """A valid option set on a machine without a GPU ends in NDSPH_E_CUDA from
+    ndsph_init: there is no host fallback behind the C-ABI."""
+    import pytest
+    import torch
+    from ndspmhd_gb300 import gpu
+    from ndspmhd_gb300.configs import default_opts
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    for ndim in (1, 2, 3):
+        with pytest.raises(gpu.NdsphError) as e:
+            gpu.GpuSPH(default_opts(ndim), n=64)
+        assert e.value.code == 2, str(e.value)
+
+
+def test_kernel_tables_refuse_bad_dimension():
+    import ctypes as C
+    from ndspmhd_gb300 import gpu
+    out = np.zeros(5 * 4001)
+    ptr = out.ctypes.data_as(C.POINTER(C.c_double))
+    for ndim in (0, 4):
+        assert gpu.lib().ndsph_kernel_tables(ndim, ptr) == 1
+    assert gpu.lib().ndsph_kernel_tables(3, None) == 1
