@@ -2325,7 +2325,8 @@ static int capture_one(ndsph_ctx* ctx, cudaGraphExec_t* out, long long* nmain, l
     const cudaGraphNode_t* deps = nullptr;
     size_t ndeps = 0;
     GCK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &cgraph, &deps, nullptr, &ndeps));
-    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = hc;
     cp.conditional.type = cudaGraphCondTypeWhile;
     cp.conditional.size = 1;

@@ -44,6 +44,7 @@ constexpr size_t NA_OFF_BSUM = NA_OFF_START + NOALLOC_MAX_CELLS + 1;
 constexpr size_t NA_OFF_RED = NA_OFF_BSUM + NA_MAX_BLOCKS;
 constexpr size_t NA_INTS = NA_OFF_RED + 16;
 constexpr size_t NA_BYTES = NA_INTS * sizeof(int);   // about 5 MB
+static_assert(NA_BYTES < (size_t(8) << 20), "the static scratch stays under 8 MB");
 
 static __device__ __align__(256) int g_noalloc_scratch[NA_INTS];
 static __device__ __align__(256) double2 g_noalloc_tab[3 * NTAB];   // W, dW/dq, d2W/dq2 (value, slope)
@@ -416,10 +417,7 @@ extern "C" int ndsph_density_noalloc(const ndsph_opts* opts, const double* d_x, 
     DevOpts o;
     memset(&o, 0, sizeof o);
     o.ndim = nd;
-    Grid g;
-    memset(&g, 0, sizeof g);
-    g.sw = 3;
-    g.nlshift = 5;
+    Grid g{};   // zero sizes; the 3^ndim stencil (sw 3, nlshift 5)
     const double cmin = 2.0 * hmax * (1.0 + 1.e-9);
     long ncells = 1;
     for (int d = 0; d < 3; d++) {
