@@ -59,3 +59,29 @@ def test_batched_cpu_baseline_spreads_tubes_over_processes():
     assert f"({n} particles)" in res["sample"]
     upd, el = bench._cpu_tube_worker(([counts[0]], 4, 1))
     assert upd == configs.brio_wu_tube(counts[0])[1]["x"].shape[0] * 4 and el > 0
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    """`bench.py --impl reference` prints one JSON line with the native arm's
+    metric and unit, its CPU sample described in cpu_baseline and an e2e
+    object with no host-device bytes; ranks other than 0 print nothing."""
+    import argparse
+    import json
+    monkeypatch.setattr(bench, "CPU_SAMPLE_N1D", 8)
+    monkeypatch.setattr(bench.os, "cpu_count", lambda: 2)
+    args = argparse.Namespace(gpus=2, steps=1, warmup=0)
+    monkeypatch.setenv("RANK", "1")
+    bench.reference_arm(args)
+    assert capsys.readouterr().out == ""
+    monkeypatch.setenv("RANK", "0")
+    bench.reference_arm(args)
+    lines = [ln for ln in capsys.readouterr().out.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
+    assert d["higher_is_better"] is True and d["n_gpus"] == 2
+    assert d["value"] > 0 and d["cpu_baseline"]["value"] == d["value"]
+    assert d["cpu_baseline"]["cores"] == 2 and d["cpu_baseline"]["kind"] == "port"
+    assert d["e2e"] == {"value": d["value"], "unit": bench.UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
