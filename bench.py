@@ -197,15 +197,25 @@ def run_device(o, st, steps: int, warmup: int, dist=None, tuning=None):
     return total_ms / steps, tim, dts, clocks
 
 
+# outputs of ndsph_step that no later step reads: the Fortran shim's gpu_step
+# passes them as null between the steps whose results output/evwrite read
+INFO_ONLY = ("rho", "rhoalt", "drhodt", "gradh", "gradhn", "gradgradh", "numneigh", "dens", "uu", "pr",
+             "spsound", "Bfield", "dudt", "divB", "curlB", "del2u", "graddivv")
+
+
 def run_e2e(o, steps: int, warmup: int, tuning=None):
-    """Reference-facing C-ABI call with pinned host buffers: ndsph_step."""
+    """Reference-facing C-ABI call with pinned host buffers: ndsph_step, one
+    leapfrog step per call, every input uploaded and every result copied back
+    inside the timed loop.  Two output sets: the integrator's (x, vel, Bevol,
+    en, hh, alpha and their rates: what the next step reads, and what the
+    Fortran shim's gpu_step returns between output steps) and all 47.5
+    doubles a particle ndsph_step can return (the shim's output steps).
+    Returns {set: (value, h2d bytes, d2h bytes)} and the in-place-access rate."""
     import numpy as np
     import torch
-    from ndspmhd_gb300.abi import alloc_state
     from ndspmhd_gb300.gpu import GpuSPH
     o2, st = make_problem(N1D, o["precision"])
     g0 = init_state(o2, st)
-    dt0 = g0.dts()
     g0.close()
     n = st["x"].shape[0]
     # pinned host copies of every array ndsph_step reads and writes
@@ -216,16 +226,18 @@ def run_e2e(o, steps: int, warmup: int, tuning=None):
         a[...] = v
         pinned[k] = (t, a)
     host = {k: a for k, (t, a) in pinned.items()}
-    rates = {}
-    for mode in (1, 0):
-        # 0 (the library default): staging copies on a copy stream, overlapped
-        # with the layout kernels and, for outputs final before the rates
-        # sweep, with the sweep; 1: the layout kernels read and write the
-        # pinned arrays in place over the CPU-GPU link (slower here: the
-        # permuted writes do not fill whole lines)
+
+    def timed(mode, drop):
+        # mode 0 (the library default): staging copies on a copy stream,
+        # overlapped with the layout kernels and, for outputs final before the
+        # rates sweep, with the sweep; 1: the layout kernels read and write
+        # the pinned arrays in place over the CPU-GPU link
         for k, (t, a) in pinned.items():
             a[...] = st[k]
         g = GpuSPH(o2, host)
+        if drop:
+            for k in INFO_ONLY:
+                setattr(g._p, k, None)
         if tuning:
             g.set_tuning(**tuning)
         g.set_host_access(mode)
@@ -238,17 +250,21 @@ def run_e2e(o, steps: int, warmup: int, tuning=None):
         for _ in range(steps):
             g.step()
         torch.cuda.synchronize()
-        rates[mode] = n * steps / (time.perf_counter() - t0)
+        r = n * steps / (time.perf_counter() - t0)
         g.close()
+        return r
+
     # bytes per particle: ndsph_step uploads the step's inputs x(3) v(3) Bevol(3)
-    # en hh pmass alpha(3) dhdt force(3) dBevoldt(3) dendt daldt(3) + itype,
-    # and downloads every array the step writes: x v Bevol en hh alpha, rho
-    # rhoalt drhodt dhdt gradh gradhn gradgradh, dens uu pr spsound Bfield(3),
-    # force dBevoldt dudt dendt daldt divB curlB(3) del2u graddivv(3) + numneigh
+    # en hh pmass alpha(3) dhdt force(3) dBevoldt(3) dendt daldt(3) + itype
     d_up = (3 + 3 + 3 + 1 + 1 + 1 + 3 + 1 + 3 + 3 + 1 + 3) * 8 + 4
-    d_dn = (3 + 3 + 3 + 1 + 1 + 3 + 7 + 4 + 3 + 3 + 3 + 1 + 1 + 3 + 1 + 3 + 1 + 3) * 8 + 4
-    del dt0
-    return rates[0], d_up * n, d_dn * n, rates[1]
+    # integrator set: x v Bevol en hh alpha dhdt force dBevoldt dendt daldt
+    d_dn_int = (3 + 3 + 3 + 1 + 1 + 3 + 1 + 3 + 3 + 1 + 3) * 8
+    # every output: the above plus rho rhoalt drhodt gradh gradhn gradgradh,
+    # dens uu pr spsound Bfield(3), dudt divB curlB(3) del2u graddivv(3) + numneigh
+    d_dn_all = d_dn_int + (6 + 4 + 3 + 1 + 1 + 3 + 1 + 3) * 8 + 4
+    out = {"integrator": (timed(0, True), d_up * n, d_dn_int * n),
+           "all": (timed(0, False), d_up * n, d_dn_all * n)}
+    return out, timed(1, False)
 
 
 def run_batched(steps: int, warmup: int, ntubes: int = 4096):
@@ -286,37 +302,65 @@ def run_batched(steps: int, warmup: int, ntubes: int = 4096):
     return res
 
 
-def fp32_error(steps: int = 4, tolh: float = 1e-6):
-    """Error of the FP32 form against the FP64 (parity) form on the headline
-    workload: both from the same FP64 primitive2conservative state, `steps`
-    device-resident steps each (each form takes its own dt), then per field
-    max |fp32 - fp64| / max(max |fp64|, rms(fp64)).  Both forms iterate h to
-    `tolh` = 1e-6: at the workload's 1e-3 a particle whose Newton-Raphson
-    residual sits at the tolerance converges one pass apart in the two forms
-    and moves its h by up to ~1e-3, which would hide the arithmetic error."""
+def _fp32_vs_fp64(st0, o64, steps: int, tolh: float, timed_steps: int = 0):
+    """Both forms from the same FP64 state, `steps` device-resident steps each
+    (each form takes its own dt); then, if timed_steps, that many more steps
+    timed.  Per field: max |fp32 - fp64| / max(max |fp64|, rms fp64), and the
+    99.99th percentile of the same per-particle ratio."""
     import numpy as np
     from ndspmhd_gb300.gpu import GpuSPH
     fields = ("x", "vel", "hh", "rho", "en", "Bevol", "force", "dudt", "dBevoldt")
-    o64, st64 = make_problem(N1D, 0)
-    o64["tolh"] = tolh
-    g = init_state(o64, st64)
-    st0 = {k: v.copy() for k, v in g.state.items()}
-    g.close()
-    out = {}
+    out, ms = {}, {}
     for prec in (0, 1):
-        g = GpuSPH(dict(o64, precision=prec), {k: v.copy() for k, v in st0.items()})
+        g = GpuSPH(dict(o64, precision=prec, tolh=tolh), {k: v.copy() for k, v in st0.items()})
         g.dev_upload()
         g.set_dt(0.0)
         g.dev_step(steps)
         g.dev_download()
         out[prec] = {k: g.state[k].copy() for k in fields}
+        if timed_steps:
+            g.dev_step(timed_steps)
+            ms[prec] = g.timing()["total_ms"] / timed_steps
         g.close()
-    res = {"steps": steps, "tolh": tolh, "metric": "max |fp32 - fp64| / max(max |fp64|, rms fp64), per field"}
+    res = {"steps": steps, "tolh": tolh}
     for k in fields:
         ref = out[0][k]
         scale = max(float(np.max(np.abs(ref))), float(np.sqrt(np.mean(ref * ref))))
-        res[k] = float(np.max(np.abs(out[1][k] - ref)) / scale) if scale > 0 else 0.0
+        d = np.abs(out[1][k] - ref)
+        if d.ndim > 1:
+            d = d.max(axis=1)
+        res[k] = float(d.max() / scale) if scale > 0 else 0.0
+        res[k + "_p9999"] = float(np.quantile(d, 0.9999) / scale) if scale > 0 else 0.0
+    # particles whose h differs by more than 1e-5 relative: those whose
+    # Newton-Raphson residual sat at the tolerance and converged one pass apart
+    dh = np.abs(out[1]["hh"] - out[0]["hh"]) / out[0]["hh"]
+    res["particles_h_differ_1e-5"] = int(np.sum(dh > 1e-5))
+    if ms:
+        res["ms_per_step"] = {"fp64": round(ms[0], 3), "fp32": round(ms[1], 3),
+                              "speedup_fp32_over_fp64": round(ms[0] / ms[1], 2), "timed_steps": timed_steps}
     return res
+
+
+def fp32_error(steps: int = 4):
+    """Error of the FP32 form against the FP64 (parity) form on the headline
+    workload, at two Newton-Raphson tolerances (the same in both forms):
+
+    * tolh 1e-3, the headline's: a particle whose residual sits within the
+      FP32 form's ~5e-7 density error of the tolerance converges one pass
+      apart in the two forms, and its h then differs by up to ~tolh; the max
+      error is set by those few particles (counted), the 99.99th percentile
+      by the arithmetic;
+    * tolh 1e-6: the decisions agree closely enough that the max error is
+      the arithmetic's own (<= 1e-5); both forms are also timed there, so the
+      FP32/FP64 speed ratio is quoted at a tolerance where that bound holds.
+    """
+    o64, st64 = make_problem(N1D, 0)
+    g = init_state(o64, st64)
+    st0 = {k: v.copy() for k, v in g.state.items()}
+    g.close()
+    return {"metric": "max |fp32 - fp64| / max(max |fp64|, rms fp64), per field (and its 99.99th percentile)",
+            "at_headline_tolh": _fp32_vs_fp64(st0, o64, steps, 1e-3),
+            "at_tolh_1e-6": _fp32_vs_fp64(st0, o64, steps, 1e-6, timed_steps=4)}
 
 
 def run_learned(n1d: int, steps: int, warmup: int):
@@ -588,7 +632,8 @@ def main():
     ms32 = max_over_ranks(ms32, dist, "cuda")
     value = replica_value(n, world, ms32)
 
-    e2e_val, h2d, d2h, e2e_staged = run_e2e(o32, max(3, args.steps), 3, tuning)
+    e2e_sets, e2e_inplace = run_e2e(o32, max(3, args.steps), 3, tuning)
+    e2e_val, h2d, d2h = e2e_sets["integrator"]
 
     peak, peak_kind = _load_peaks()
     rates_ms = tim32["rates_ms"]
@@ -622,8 +667,13 @@ def main():
         "roofline": roofline,
         "clocks": clocks,
         "e2e": {"value": round(e2e_val, 1), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "call": "ndsph_step with pinned host buffers (staging copies overlapped with the kernels)",
-                "in_place_access_value": round(e2e_staged, 1)},
+                "call": "ndsph_step with pinned host buffers (staging copies overlapped with the kernels), "
+                        "returning the integrator's arrays (x, vel, Bevol, en, hh, alpha and their rates) as "
+                        "the Fortran shim's gpu_step does between output steps",
+                "all_outputs": {"value": round(e2e_sets["all"][0], 1), "h2d_bytes_per_step": e2e_sets["all"][1],
+                                "d2h_bytes_per_step": e2e_sets["all"][2],
+                                "call": "the same, returning all 47.5 doubles a particle (output steps)"},
+                "in_place_access_value": round(e2e_inplace, 1)},
     }
     if ms64 is not None:
         line["fp64"] = {"value": round(n / (ms64 * 1e-3), 1), "ms_per_step": round(ms64, 3),

@@ -44,6 +44,7 @@ extern "C" {
 #define NDSPH_E_CELLS          8   /* cell grid invalid (box < 3 cells, h > box) */
 #define NDSPH_E_CLUMP          9   /* dx = 0 pair  ratesND_mhd.f90:419-424       */
 #define NDSPH_E_CAPACITY      10   /* size above a fixed maximum                 */
+#define NDSPH_E_U_NEG         11   /* u_therm < 0  eos.f90:66-72 (iener /= 0)    */
 
 /* ---- particle types (variablesND.f90:165-171) ------------------------------ */
 #define NDSPH_ITYPE_GAS      0
@@ -264,18 +265,25 @@ NDSPH_API int ndsph_kernel_tables(int32_t ndim, double* out);
  * arrays itself; real-time loops that must not take cudaMalloc's implicit
  * synchronisation; applications that reserve all device memory up front).
  * It runs the first density pass of iterate_density with every particle
- * treated as converged (the maxdensits = 0 case): rho, gradh (= 1/omega),
- * drhodt (normalised by gradh) and numneigh for particles that are not fixed.
+ * treated as converged (the maxdensits = 0 case): rho, gradh (= 1/omega) and
+ * drhodt (normalised by gradh) for particles that are not fixed (the outputs
+ * of fixed particles are left as they are: the caller copies them from their
+ * sources as set_fixedbound does), numneigh for every particle.
  * All pointers are DEVICE pointers in the host layout of ndsph_particles
  * (x(ndim,n), vel(3,n)); `stream` is a cudaStream_t (NULL = legacy stream);
- * the call returns after the stream has finished its work.
- * Scratch: one file-scope __device__ array of about 5 MB (held by every GPU
- * that loads the library until exit); npart <= 262144 and cells <= 262144,
- * larger sizes return NDSPH_E_CAPACITY (message on stderr).  Calls share
+ * the call returns after the stream has finished its work.  Options: ndim,
+ * ibound (0, 1 or 3, as ndsph_init), xmin/xmax; the rest take no part.
+ * Scratch: one file-scope __device__ array of about 6 MB plus the kernel
+ * tables (576 KB), held by every GPU that loads the library until exit;
+ * npart <= 262144 and cells <= 262144 (cells of 2 hmax over the bounding box
+ * or periodic box), larger sizes return NDSPH_E_CAPACITY.  Errors (also h <= 0
+ * -> NDSPH_E_H_NONPOS, rho <= 0 -> NDSPH_E_RHO_NONPOS, a non-finite position
+ * -> NDSPH_E_NAN) leave their message in ndsph_last_error(NULL).  Calls share
  * the scratch, so calls that overlap on the GPU race; each call clears what
  * must start at zero.  The first call on a device takes the scratch's device
- * address (cudaGetSymbolAddress) and uploads the kernel table: make it before
- * any stream capture.  No cudaMalloc, cudaFree or allocating library call.   */
+ * address (cudaGetSymbolAddress) and uploads the kernel tables of the three
+ * dimensions: make it before any stream capture.  No cudaMalloc, cudaFree or
+ * allocating library call.                                                   */
 NDSPH_API int ndsph_density_noalloc(const ndsph_opts* opts, const double* d_x, const double* d_hh,
                                     const double* d_pmass, const double* d_vel, const int32_t* d_itype,
                                     int32_t npart, double* d_rho, double* d_drhodt, double* d_gradh,

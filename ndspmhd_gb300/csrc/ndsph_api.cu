@@ -170,6 +170,11 @@ struct ndsph_ctx {
 };
 
 static thread_local std::string g_err;
+namespace ndsph {
+// the message ndsph_last_error(NULL) returns, for entry points without a
+// context (ndsph_density_noalloc)
+void set_global_error(const char* msg) { g_err = msg ? msg : ""; }
+}  // namespace ndsph
 static int build_nlist(ndsph_ctx* ctx);
 static void link_sort_gather(ndsph_ctx* ctx, const int* d_fields, int nfields, cudaStream_t st);
 static int download_density_group(ndsph_ctx* ctx, ndsph_particles* p);
@@ -594,15 +599,33 @@ static cudaError_t read_dtout(ndsph_ctx* ctx, cudaStream_t st)
     return cudaMemcpyAsync(ctx->h_dtout, ctx->d_dtout, sizeof(double) * 8, cudaMemcpyDeviceToHost, st);
 }
 
+// the message of a status raised by a kernel, naming the reference's stop
+// site and the (1-based) particle that raised it first
+static std::string device_err_msg(int code, int index)
+{
+    const char* what = "device error";
+    switch (code) {
+    case NDSPH_E_H_NONPOS: what = "h <= 0 in density call (iterate_density.f90:99-102)"; break;
+    case NDSPH_E_RHO_NONPOS: what = "rho <= 0 (iterate_density.f90:168-170)"; break;
+    case NDSPH_E_NOT_CONVERGED: what = "density not converged (iterate_density.f90:349-351)"; break;
+    case NDSPH_E_VSIG_DET: what = "rates: vsig det < 0 (ratesND_mhd.f90:1422-1429)"; break;
+    case NDSPH_E_NAN: what = "non-finite value"; break;
+    case NDSPH_E_CLUMP: what = "rates: dx = 0 between particles of one type (ratesND_mhd.f90:419-424)"; break;
+    case NDSPH_E_U_NEG: what = "eos: u_therm -ve (eos.f90:66-72)"; break;
+    default: break;
+    }
+    char buf[200];
+    snprintf(buf, sizeof buf, "%s: status %d at particle %d", what, code, index + 1);
+    return buf;
+}
+
 static int sync_red(ndsph_ctx* ctx)
 {
     CK(read_red(ctx, ctx->red, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     if (ctx->h_red->err) {
-        int code = ctx->h_red->err;
-        char buf[160];
-        snprintf(buf, sizeof buf, "device error %d at particle %d", code, ctx->h_red->err_index + 1);
-        ctx->err = buf;
+        const int code = ctx->h_red->err;
+        ctx->err = device_err_msg(code, ctx->h_red->err_index);
         return code;
     }
     return 0;
@@ -2449,9 +2472,7 @@ static int batch_step_graph(ndsph_ctx* ctx)
     ctx->gsteps++;
     ndsph_launch_counter().fetch_add(ctx->gl_main[p] + (long long)std::max(ctx->h_red->g_its - 1, 0) * ctx->gl_body[p]);
     if (ctx->h_red->err) {
-        char buf[160];
-        snprintf(buf, sizeof buf, "device error %d at particle %d", ctx->h_red->err, ctx->h_red->err_index + 1);
-        ctx->err = buf;
+        ctx->err = device_err_msg(ctx->h_red->err, ctx->h_red->err_index);
         return ctx->h_red->err;
     }
     if (ctx->h_red->gfail) {

@@ -21,6 +21,9 @@ inline std::atomic<long long>& ndsph_launch_counter()
 
 namespace ndsph {
 
+// sets the message ndsph_last_error(NULL) returns (the calling thread's)
+void set_global_error(const char* msg);
+
 constexpr int IKERN = 4000;            // kernelND.f90:37
 constexpr int NTAB = IKERN + 1;
 

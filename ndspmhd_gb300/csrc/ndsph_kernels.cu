@@ -546,6 +546,8 @@ __global__ void k_eos(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red)
         double uu = F.f[EN][k];
         double pr = F.f[PR][k], cs = F.f[CS][k];
         int it = S.itype[k];
+        // the reference stops on a negative thermal energy (eos.f90:66-72)
+        if (o.iener != 0 && uu < 0.0) raise_err(red, NDSPH_E_U_NEG, S.id[k]);
         if (o.iener == 0) {
             if (rho > 0.0 && it == NDSPH_ITYPE_GAS) {
                 // rho^gamma: FP64 pow in the parity form; in the FP32 form the

@@ -13,11 +13,15 @@
 // for as long as the library is loaded (on every GPU that loads it).
 //
 // Limits: npart <= NOALLOC_MAX_N and cells <= NOALLOC_MAX_CELLS (else
-// NDSPH_E_CAPACITY).  The scratch is shared by every call: calls that
-// overlap on the GPU (two streams, two host threads) race on it.  Each call
-// clears the parts that must start at zero.  The first call on a device
-// fetches the scratch's device address with cudaGetSymbolAddress and
-// uploads the kernel tables; make that first call before any stream capture.
+// NDSPH_E_CAPACITY; the cell count is worked out in floating point and
+// checked before any integer conversion, so a very wide or non-finite
+// bounding box is refused, never wrapped).  The scratch is shared by every
+// call: calls that overlap on the GPU (two streams, two host threads) race
+// on it.  Each call clears the parts that must start at zero.  The first
+// call on a device fetches the scratch's device address with
+// cudaGetSymbolAddress and uploads the kernel tables of all three
+// dimensions; make that first call before any stream capture.  Errors come
+// back as status codes, with the message in ndsph_last_error(NULL).
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -34,43 +38,47 @@ constexpr int NOALLOC_MAX_CELLS = 1 << 18;    // 262,144 cells
 constexpr int NA_TILE = 1024;                 // scan tile (one thread per entry)
 constexpr int NA_MAX_BLOCKS = (NOALLOC_MAX_CELLS + NA_TILE - 1) / NA_TILE + 1;
 
-// scratch layout (ints): key[N] slot[N] perm[N] count[C] start[C+1] bsum[B] red[16]
+// scratch layout (ints): key[N] slot[N] perm2[N] perm[N] count[C] start[C+1]
+// bsum[B] red[16] (7 order-preserving 64-bit words and the error code/index)
 constexpr size_t NA_OFF_KEY = 0;
 constexpr size_t NA_OFF_SLOT = NA_OFF_KEY + NOALLOC_MAX_N;
-constexpr size_t NA_OFF_PERM = NA_OFF_SLOT + NOALLOC_MAX_N;
+constexpr size_t NA_OFF_PERM2 = NA_OFF_SLOT + NOALLOC_MAX_N;
+constexpr size_t NA_OFF_PERM = NA_OFF_PERM2 + NOALLOC_MAX_N;
 constexpr size_t NA_OFF_COUNT = NA_OFF_PERM + NOALLOC_MAX_N;
 constexpr size_t NA_OFF_START = NA_OFF_COUNT + NOALLOC_MAX_CELLS;
 constexpr size_t NA_OFF_BSUM = NA_OFF_START + NOALLOC_MAX_CELLS + 1;
 constexpr size_t NA_OFF_RED = NA_OFF_BSUM + NA_MAX_BLOCKS;
 constexpr size_t NA_INTS = NA_OFF_RED + 16;
-constexpr size_t NA_BYTES = NA_INTS * sizeof(int);   // about 5 MB
+constexpr size_t NA_BYTES = NA_INTS * sizeof(int);   // about 6 MB
 static_assert(NA_BYTES < (size_t(8) << 20), "the static scratch stays under 8 MB");
 
 static __device__ __align__(256) int g_noalloc_scratch[NA_INTS];
-static __device__ __align__(256) double2 g_noalloc_tab[3 * NTAB];   // W, dW/dq, d2W/dq2 (value, slope)
+// W, dW/dq, d2W/dq2 (value, slope) of the cubic spline for ndim = 1, 2, 3
+static __device__ __align__(256) double2 g_noalloc_tab[3 * 3 * NTAB];
 
 struct NaPtrs {
     int* key;
     int* slot;
+    int* perm2;   // slots in atomic arrival order, before the per-cell rank
     int* perm;
     int* count;
     int* start;
     int* bsum;
     unsigned long long* red;   // [0] = hmax bits, [1..3] xlo, [4..6] xhi (order-preserving)
+    int* err;                  // [0] first status raised by a kernel, [1] its particle
 };
 
 struct DeviceSetup {
     bool done = false;
     int* scratch = nullptr;
     double2* tab = nullptr;
-    int ndim = 0;
 };
 DeviceSetup g_setup[64];
-// errors are reported by status code; the message also goes to stderr
+// errors are reported by status code, the message through ndsph_last_error(NULL)
 struct NaErr {
     NaErr& operator=(const std::string& m)
     {
-        fprintf(stderr, "%s\n", m.c_str());
+        set_global_error(m.c_str());
         return *this;
     }
     NaErr& operator=(const char* m) { return *this = std::string(m); }
@@ -94,7 +102,13 @@ __global__ void na_reset(NaPtrs p)
     if (threadIdx.x == 0) {
         p.red[0] = 0ull;
         for (int d = 0; d < 3; d++) { p.red[1 + d] = ~0ull; p.red[4 + d] = 0ull; }
+        p.err[0] = 0;
+        p.err[1] = 0;
     }
+}
+__device__ inline void na_raise(NaPtrs p, int code, int i)
+{
+    if (atomicCAS(&p.err[0], 0, code) == 0) p.err[1] = i;
 }
 
 __global__ void na_hmax_bbox(const double* __restrict__ x, const double* __restrict__ h, int ndim, int n,
@@ -189,18 +203,20 @@ __global__ void na_scan_final(NaPtrs p, int nc, int n)
 __global__ void na_scatter(NaPtrs p, int n)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p.perm[p.start[p.key[i]] + p.slot[i]] = i;
+    if (i < n) p.perm2[p.start[p.key[i]] + p.slot[i]] = i;
 }
-__global__ void na_cell_sort(NaPtrs p, int nc)
+// each slot takes its rank by index among its cell's slots, so the order
+// inside a cell does not depend on the atomics' arrival order
+__global__ void na_cell_rank(NaPtrs p, int n)
 {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nc) return;
-    int a = p.start[c], b = p.start[c + 1];
-    for (int k = a + 1; k < b; k++) {
-        int v = p.perm[k], m = k - 1;
-        while (m >= a && p.perm[m] > v) { p.perm[m + 1] = p.perm[m]; m--; }
-        p.perm[m + 1] = v;
-    }
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int v = p.perm2[k];
+    const int c = p.key[v];
+    const int a = p.start[c], b = p.start[c + 1];
+    int r = 0;
+    for (int j = a; j < b; j++) r += (p.perm2[j] < v);
+    p.perm[a + r] = v;
 }
 
 __device__ inline bool na_match(int ti, int tj)
@@ -226,6 +242,11 @@ __global__ void na_density(const double* __restrict__ x, const double* __restric
     double xi[3] = {0, 0, 0};
     for (int d = 0; d < nd; d++) xi[d] = x[(size_t)i * nd + d];
     const double hi = h[i];
+    // iterate_density.f90:99-102
+    if (!(hi > 2.2250738585072014e-308)) {
+        na_raise(p, NDSPH_E_H_NONPOS, i);
+        return;
+    }
     const double hi1 = 1.0 / hi;
     const double hi21 = __dmul_rn(hi1, hi1);
     const int ti = itype[i];
@@ -301,6 +322,11 @@ __global__ void na_density(const double* __restrict__ x, const double* __restric
     if (nd >= 2) hfac *= hi1;
     if (nd >= 3) hfac *= hi1;
     const double rho = hfac * sw;
+    // iterate_density.f90:168-170
+    if (rho <= 1.e-6 && rho <= 0.0) {
+        na_raise(p, NDSPH_E_RHO_NONPOS, i);
+        return;
+    }
     const double gsum = -hfac * hi1 * sg;
     const double dhdrhoi = -hi / ((double)nd * rho);
     double omegai = 1.0 - dhdrhoi * gsum;
@@ -311,7 +337,8 @@ __global__ void na_density(const double* __restrict__ x, const double* __restric
     drhodt_out[i] = hfac * hi1 * sd * gradh;
 }
 
-void build_tabs(int ndim, std::vector<double2>& out, double& dq2, double& ddq2)
+// the value/slope table of one dimension into out[0 .. 3*NTAB)
+void build_tabs(int ndim, double2* out, double& dq2, double& ddq2)
 {
     // cubic spline table (kernelND.f90:4143-4192, :4279-4289), as the main path builds it
     const double pi = 3.141592653589;
@@ -339,7 +366,6 @@ void build_tabs(int ndim, std::vector<double2>& out, double& dq2, double& ddq2)
         w[i] = cn * a; gw[i] = cn * b; ggw[i] = cn * c;
     }
     ddq2 = 1. / dq2;
-    out.resize(3 * NTAB);
     const std::vector<double>* t[3] = {&w, &gw, &ggw};
     for (int k = 0; k < 3; k++)
         for (int i = 0; i <= IKERN; i++) {
@@ -361,6 +387,17 @@ extern "C" int ndsph_density_noalloc(const ndsph_opts* opts, const double* d_x, 
         g_na_err = "ndsph_density_noalloc: bad arguments";
         return NDSPH_E_ARG;
     }
+    // the boundary options ndsph_init accepts: none, fixed particles, periodic
+    for (int d = 0; d < opts->ndim; d++) {
+        if (opts->ibound[d] != 0 && opts->ibound[d] != 1 && opts->ibound[d] != 3) {
+            g_na_err = "ndsph_density_noalloc: ibound must be 0, 1 or 3 (reflective/shearing ghosts are out of scope)";
+            return NDSPH_E_ARG;
+        }
+        if (opts->ibound[d] == 3 && !(opts->xmax[d] > opts->xmin[d])) {
+            g_na_err = "ndsph_density_noalloc: periodic box with xmax <= xmin";
+            return NDSPH_E_ARG;
+        }
+    }
     if (npart > NOALLOC_MAX_N) {
         char buf[160];
         snprintf(buf, sizeof buf, "ndsph_density_noalloc: npart %d above the fixed maximum %d", npart,
@@ -369,6 +406,10 @@ extern "C" int ndsph_density_noalloc(const ndsph_opts* opts, const double* d_x, 
         return NDSPH_E_CAPACITY;
     }
     if (npart == 0) return 0;
+    if (!d_x || !d_hh || !d_pmass || !d_vel || !d_itype || !d_rho || !d_drhodt || !d_gradh || !d_numneigh) {
+        g_na_err = "ndsph_density_noalloc: null device pointer";
+        return NDSPH_E_ARG;
+    }
     cudaStream_t st = (cudaStream_t)stream;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
@@ -376,30 +417,32 @@ extern "C" int ndsph_density_noalloc(const ndsph_opts* opts, const double* d_x, 
         return NDSPH_E_CUDA;
     }
     DeviceSetup& su = g_setup[dev];
-    if (!su.done || su.ndim != opts->ndim) {
+    if (!su.done) {
         // once per device (with that device current): device addresses of the
-        // static arrays, and the kernel table for this dimension
+        // static arrays, and the kernel tables of the three dimensions
         cudaError_t e = cudaGetSymbolAddress((void**)&su.scratch, g_noalloc_scratch);
         if (e != cudaSuccess) { g_na_err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e); return NDSPH_E_CUDA; }
         e = cudaGetSymbolAddress((void**)&su.tab, g_noalloc_tab);
         if (e != cudaSuccess) { g_na_err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e); return NDSPH_E_CUDA; }
-        std::vector<double2> tabs;
+        std::vector<double2> tabs(3 * 3 * NTAB);
         double dq2, ddq2;
-        build_tabs(opts->ndim, tabs, dq2, ddq2);
-        e = cudaMemcpyToSymbol(g_noalloc_tab, tabs.data(), sizeof(double2) * 3 * NTAB);
+        for (int nd = 1; nd <= 3; nd++) build_tabs(nd, tabs.data() + (size_t)(nd - 1) * 3 * NTAB, dq2, ddq2);
+        e = cudaMemcpyToSymbol(g_noalloc_tab, tabs.data(), sizeof(double2) * tabs.size());
         if (e != cudaSuccess) { g_na_err = std::string("cudaMemcpyToSymbol: ") + cudaGetErrorString(e); return NDSPH_E_CUDA; }
-        su.ndim = opts->ndim;
         su.done = true;
     }
     NaPtrs p;
     p.key = su.scratch + NA_OFF_KEY;
     p.slot = su.scratch + NA_OFF_SLOT;
+    p.perm2 = su.scratch + NA_OFF_PERM2;
     p.perm = su.scratch + NA_OFF_PERM;
     p.count = su.scratch + NA_OFF_COUNT;
     p.start = su.scratch + NA_OFF_START;
     p.bsum = su.scratch + NA_OFF_BSUM;
     p.red = (unsigned long long*)(su.scratch + NA_OFF_RED);
+    p.err = su.scratch + NA_OFF_RED + 14;
     const int nd = opts->ndim;
+    const double2* tab = su.tab + (size_t)(nd - 1) * 3 * NTAB;
     const int bs = 256, nb = (npart + bs - 1) / bs;
 
     NDSPH_COUNT_LAUNCH, na_reset<<<1, 32, 0, st>>>(p);
@@ -410,46 +453,58 @@ extern "C" int ndsph_density_noalloc(const ndsph_opts* opts, const double* d_x, 
     if (e != cudaSuccess) { g_na_err = cudaGetErrorString(e); return NDSPH_E_CUDA; }
     double hmax;
     memcpy(&hmax, &red[0], 8);
-    if (!(hmax > 0.0) || !std::isfinite(hmax)) { g_na_err = "ndsph_density_noalloc: max h <= 0"; return NDSPH_E_H_NONPOS; }
+    if (!(hmax > 0.0) || !std::isfinite(hmax)) { g_na_err = "ndsph_density_noalloc: max h <= 0 or not finite"; return NDSPH_E_H_NONPOS; }
 
     // cell grid (same rule as the main path: periodic dims tile the box with
-    // cells >= 2 hmax, open dims pad the bounding box by one cell)
+    // cells >= 2 hmax, open dims pad the bounding box by one cell).  Counts
+    // are taken in double and checked against the maximum before any
+    // conversion to int.
+    for (int d = 0; d < nd; d++) {
+        if (!std::isfinite(na_unord(red[1 + d])) || !std::isfinite(na_unord(red[4 + d]))) {
+            g_na_err = "ndsph_density_noalloc: non-finite position";
+            return NDSPH_E_NAN;
+        }
+    }
     DevOpts o;
     memset(&o, 0, sizeof o);
     o.ndim = nd;
     Grid g{};   // zero sizes; the 3^ndim stencil (sw 3, nlshift 5)
     const double cmin = 2.0 * hmax * (1.0 + 1.e-9);
-    long ncells = 1;
+    double ncells_d = 1.0;
     for (int d = 0; d < 3; d++) {
         o.ibound[d] = d < nd ? opts->ibound[d] : 0;
         o.periodic[d] = (d < nd && opts->ibound[d] == 3);
         o.xmin[d] = opts->xmin[d];
         o.xmax[d] = opts->xmax[d];
-        if (d >= nd) { g.nc[d] = 1; g.cs[d] = 1.0; g.origin[d] = 0.0; }
-        else if (o.periodic[d]) {
+        double ncd = 1.0;
+        if (d >= nd) {
+            g.cs[d] = 1.0; g.origin[d] = 0.0;
+        } else if (o.periodic[d]) {
             const double L = opts->xmax[d] - opts->xmin[d];
-            long nc = (long)floor(L / cmin);
-            if (nc < 3) { g_na_err = "ndsph_density_noalloc: periodic box smaller than 3 cells"; return NDSPH_E_CELLS; }
-            g.nc[d] = (int)(nc > 4096 ? 4096 : nc);
+            ncd = std::floor(L / cmin);
+            if (!(ncd >= 3.0)) { g_na_err = "ndsph_density_noalloc: periodic box smaller than 3 cells of 2 hmax"; return NDSPH_E_CELLS; }
+            if (ncd > 4096.0) ncd = 4096.0;
             g.origin[d] = opts->xmin[d];
-            g.cs[d] = L / g.nc[d];
+            g.cs[d] = L / ncd;
         } else {
             const double lo = na_unord(red[1 + d]), hi = na_unord(red[4 + d]);
-            g.nc[d] = (int)floor(((hi - lo) + 2.0 * cmin) / cmin) + 1;
+            ncd = std::floor(((hi - lo) + 2.0 * cmin) / cmin) + 1.0;
             g.cs[d] = cmin;
             g.origin[d] = lo - cmin;
         }
+        if (!(ncd >= 1.0) || ncd > (double)NOALLOC_MAX_CELLS) ncd = (double)NOALLOC_MAX_CELLS + 1.0;
+        ncells_d *= ncd;
+        g.nc[d] = (ncd <= (double)NOALLOC_MAX_CELLS) ? (int)ncd : 1;
         g.inv_cs[d] = 1.0 / g.cs[d];
-        ncells *= g.nc[d];
     }
-    if (ncells > NOALLOC_MAX_CELLS) {
-        char buf[160];
-        snprintf(buf, sizeof buf, "ndsph_density_noalloc: %ld cells above the fixed maximum %d", ncells,
+    if (!(ncells_d <= (double)NOALLOC_MAX_CELLS)) {
+        char buf[200];
+        snprintf(buf, sizeof buf, "ndsph_density_noalloc: %.0f cells above the fixed maximum %d", ncells_d,
                  NOALLOC_MAX_CELLS);
         g_na_err = buf;
         return NDSPH_E_CAPACITY;
     }
-    g.ncells = (int)ncells;
+    g.ncells = (int)ncells_d;
     const int nc = g.ncells;
 
     // the counts must start at zero on every call (the scratch keeps the last call's contents)
@@ -461,12 +516,23 @@ extern "C" int ndsph_density_noalloc(const ndsph_opts* opts, const double* d_x, 
     NDSPH_COUNT_LAUNCH, na_scan_bsum<<<1, NA_TILE, 0, st>>>(p, ntiles);
     NDSPH_COUNT_LAUNCH, na_scan_final<<<ntiles, NA_TILE, 0, st>>>(p, nc, npart);
     NDSPH_COUNT_LAUNCH, na_scatter<<<nb, bs, 0, st>>>(p, npart);
-    NDSPH_COUNT_LAUNCH, na_cell_sort<<<(nc + 127) / 128, 128, 0, st>>>(p, nc);
+    NDSPH_COUNT_LAUNCH, na_cell_rank<<<nb, bs, 0, st>>>(p, npart);
     const double dq2 = 4.0 / (double)IKERN, ddq2 = 1.0 / dq2;
     NDSPH_COUNT_LAUNCH, na_density<<<(npart + 127) / 128, 128, 0, st>>>(d_x, d_hh, d_pmass, d_vel, d_itype, npart, g, o, 2.0 * hmax,
-                                                    dq2, ddq2, p, su.tab, d_rho, d_drhodt, d_gradh, d_numneigh);
+                                                    dq2, ddq2, p, tab, d_rho, d_drhodt, d_gradh, d_numneigh);
+    int err[2] = {0, 0};
     e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(err, p.err, sizeof(err), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { g_na_err = cudaGetErrorString(e); return NDSPH_E_CUDA; }
+    if (err[0]) {
+        char buf[160];
+        snprintf(buf, sizeof buf, "ndsph_density_noalloc: %s at particle %d",
+                 err[0] == NDSPH_E_H_NONPOS ? "h <= 0 in density call (iterate_density.f90:99-102)"
+                                            : "rho <= 0 (iterate_density.f90:168-170)",
+                 err[1] + 1);
+        g_na_err = buf;
+        return err[0];
+    }
     return 0;
 }

@@ -112,6 +112,12 @@ module gpu_sph
  type(c_ptr), save :: ctx = c_null_ptr
  ! pair-sum form of the context: 0 plain FP64 (the parity form), 1 FP32 pairs
  integer, save :: gpu_precision = 0
+ ! gpu_step copies back only what the next step reads (x, vel, Bevol, en, hh,
+ ! alpha and their rates: 25 doubles a particle) unless this is set; the
+ ! caller sets it before a step whose results output or evwrite will read
+ ! (evolve.f90:136-166), which then also gets rho, the density terms, the
+ ! primitives, div B, curl B and the switch sources (47.5 doubles a particle)
+ logical, save :: gpu_step_all_outputs = .false.
 
 contains
 
@@ -227,6 +233,15 @@ contains
   type(ndsph_dt_t) :: d
   call gpu_ensure()
   call gpu_particles(p)
+  if (.not.gpu_step_all_outputs) then
+     ! outputs no later step reads: left as they are on the host
+     p%rho = c_null_ptr;  p%rhoalt = c_null_ptr;  p%drhodt = c_null_ptr
+     p%gradh = c_null_ptr;  p%gradhn = c_null_ptr;  p%gradgradh = c_null_ptr
+     p%numneigh = c_null_ptr;  p%dens = c_null_ptr;  p%uu = c_null_ptr
+     p%pr = c_null_ptr;  p%spsound = c_null_ptr;  p%Bfield = c_null_ptr
+     p%dudt = c_null_ptr;  p%divB = c_null_ptr;  p%curlB = c_null_ptr
+     p%del2u = c_null_ptr;  p%graddivv = c_null_ptr
+  endif
   d%dt = dt;  d%time = time;  d%nsteps = int(nsteps,c_int32_t)
   call gpu_check(ndsph_step(ctx, p, int(npart,c_int32_t), d), 'step')
   ntotal = npart

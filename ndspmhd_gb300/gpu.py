@@ -35,7 +35,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libndsph_gpu.so")
 ERRORS = {
     1: "bad argument", 2: "CUDA error", 3: "h <= 0", 4: "rho <= 0", 5: "density not converged",
     6: "MHD signal-speed determinant < 0", 7: "non-finite value", 8: "cell grid invalid",
-    9: "coincident particles", 10: "capacity exceeded",
+    9: "coincident particles", 10: "capacity exceeded", 11: "thermal energy < 0",
 }
 
 _lib = None

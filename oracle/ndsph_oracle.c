@@ -746,10 +746,20 @@ out:
     return s->err;
 }
 
-/* equation_of_state eos.f90:40-106 on 1..npart */
+/* equation_of_state eos.f90:40-106 on 1..npart; stops on u < 0 when
+ * iener /= 0 (eos.f90:66-72) */
 static void equation_of_state(orc_sim* s)
 {
     double gamma = s->o.gamma, gamma1 = gamma - 1.;
+    if (s->o.iener != 0) {
+        for (int i = 0; i < s->npart; i++) {
+            if (s->uu[i] < 0.) {
+                s->err = NDSPH_E_U_NEG;
+                snprintf(s->msg, sizeof s->msg, "eos: u_therm -ve at %d", i + 1);
+                return;
+            }
+        }
+    }
     for (int i = 0; i < s->npart; i++) {
         double rho = s->rho[i];
         if (s->o.iener == 0) {
@@ -1299,6 +1309,7 @@ static int derivs(orc_sim* s)
     if (set_linklist(s)) return s->err;
     if (iterate_density(s)) return s->err;
     conservative2primitive(s);
+    if (s->err) return s->err;
     if (get_rates(s)) return s->err;
     return 0;
 }
@@ -1509,6 +1520,7 @@ int orc_get_rates(void* h)
     }
     if (set_linklist(s)) return s->err;
     conservative2primitive(s);
+    if (s->err) return s->err;
     return get_rates(s);
 }
 

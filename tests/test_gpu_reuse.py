@@ -204,6 +204,49 @@ def test_host_step_streamed_skips_null_outputs(gpulib):
     assert not differ, differ
 
 
+# outputs the Fortran shim's gpu_step leaves on the host between the steps
+# whose results output/evwrite read (gpu_step_all_outputs = .false.)
+INFO_ONLY = ("rho", "rhoalt", "drhodt", "gradh", "gradhn", "gradgradh", "numneigh", "dens", "uu", "pr",
+             "spsound", "Bfield", "dudt", "divB", "curlB", "del2u", "graddivv")
+
+
+@pytest.mark.parametrize("precision", [1, 0])
+def test_host_step_integrator_outputs_only(precision, gpulib):
+    """ndsph_step with every info-only output null (what gpu_step passes
+    between output steps): the next step reads only x, vel, Bevol, en, hh,
+    alpha and their rates, so three steps give bitwise the particles of three
+    steps that return everything, and the null arrays stay untouched."""
+    import numpy as np
+    from ndspmhd_gb300.gpu import GpuSPH
+    o, p = configs.mhd_box_3d(48, seed=7)
+    o = dict(o, precision=precision)
+    g0 = GpuSPH(o, configs.full_state(p, 3))
+    g0.primitive2conservative()
+    st = {k: v.copy() for k, v in g0.state.items()}
+    g0.close()
+    runs = []
+    for drop in (False, True):
+        s = {k: v.copy() for k, v in st.items()}
+        if drop:
+            for k in INFO_ONLY:
+                s[k][...] = -7
+        g = GpuSPH(o, s)
+        if drop:
+            for k in INFO_ONLY:
+                setattr(g._p, k, None)
+        g.dt.dt, g.dt.time, g.dt.nsteps = 0.0, 0.0, 0
+        for _ in range(3):
+            g.step()
+        runs.append(({k: v.copy() for k, v in g.state.items()}, g.dts()))
+        g.close()
+    (full, dfull), (part, dpart) = runs
+    for k in INFO_ONLY:
+        assert np.all(part[k] == -7), k
+    differ = [k for k in full if k not in INFO_ONLY and not np.array_equal(full[k], part[k])]
+    assert not differ, differ
+    assert dfull["dt"] == dpart["dt"] and dfull["time"] == dpart["time"]
+
+
 @pytest.mark.parametrize("precision", [1, 0])
 def test_device_steps_in_one_call_identical(precision, gpulib):
     """Several device-resident steps in one call (the corrector and the next
