@@ -2471,11 +2471,18 @@ static int batch_step_graph(ndsph_ctx* ctx)
     ctx->gparity = 1 - p;
     ctx->gsteps++;
     ndsph_launch_counter().fetch_add(ctx->gl_main[p] + (long long)std::max(ctx->h_red->g_its - 1, 0) * ctx->gl_body[p]);
-    if (ctx->h_red->err) {
+    if (ctx->h_red->err && !ctx->h_red->gfail) {
         ctx->err = device_err_msg(ctx->h_red->err, ctx->h_red->err_index);
         return ctx->h_red->err;
     }
     if (ctx->h_red->gfail) {
+        // the captured step left its cells, rows or pass budget: what it
+        // computed (a status it raised included) is redone on the eager path
+        // from the step's predicted state, which raises any real error again
+        if (ctx->h_red->err) {
+            CK(cudaMemsetAsync(&ctx->red->err, 0, 2 * sizeof(int), ctx->st));
+            ctx->h_red->err = 0;
+        }
         ctx->gredo++;
         graph_drop(ctx);
         int rc = graph_redo(ctx);

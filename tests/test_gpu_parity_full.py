@@ -11,7 +11,8 @@ too:
   within its 1e-5 bound;
 * 3D MHD box: 64^3 neighbour sets bit-exact; at 128^3 = 2,097,152 particles
   one derivs at 1e-12 with numneigh exact (so every particle's neighbour count
-  over both criteria agrees) and the FP32 form's derivs within 1e-5;
+  over both criteria agrees) and the FP32 form's derivs within 1e-5 (at the
+  workload's tolh, bar the few particles whose convergence pass differs);
 * a 1,600-particle Brio-Wu tube with fixed ends (the largest tube of the
   batched workload): neighbour sets, derivs, four steps;
 * the two-fluid dust box at 2 x 24^3 (every gas-dust drag pair): derivs and
@@ -93,6 +94,42 @@ def _check_fp32(o, st, ref, name):
     g.close()
 
 
+def _check_fp32_many(o, st, ref, name):
+    """The FP32 form on a set of millions of particles.  At the workload's
+    tolh (1e-3) a particle whose Newton-Raphson residual sits within the FP32
+    form's ~5e-7 density error of the tolerance stops one pass earlier or
+    later than in the FP64 arithmetic, and its h then differs by up to
+    ~tolh: against the oracle, those particles (a few per million) and their
+    neighbours are allowed up to tolh, every other particle 1e-5.  At tolh
+    1e-6 no decision differs and every particle holds 1e-5, checked against
+    the FP64 form (itself within 1e-12 of the oracle, above)."""
+    from ndspmhd_gb300.gpu import GpuSPH
+    from tests.helpers import field_scales
+    g = GpuSPH(dict(o, precision=1), {k: v.copy() for k, v in st.items()})
+    g.derivs()
+    sc = field_scales(ref.state)
+    dh = np.abs(g.state["hh"] - ref.state["hh"]) / ref.state["hh"]
+    flipped = dh > 1e-5
+    assert flipped.sum() <= 1e-5 * len(dh) + 2, (name, int(flipped.sum()))
+    assert dh.max() <= 1.05 * o["tolh"], (name, float(dh.max()))
+    for k in FP32_FIELDS:
+        a, b = g.state[k], ref.state[k]
+        rms = float(np.sqrt(np.mean(b ** 2)))
+        e = np.abs(a - b) / np.maximum(np.abs(b), max(rms, sc.get(k, 0.0)))
+        e = e.max(axis=1) if e.ndim > 1 else e
+        assert np.mean(e > 1e-5) <= 1e-3, (name, k, float(np.mean(e > 1e-5)))
+        assert e.max() <= 2.0 * o["tolh"], (name, k, float(e.max()))
+    g.close()
+    res = {}
+    for prec in (0, 1):
+        g = GpuSPH(dict(o, precision=prec, tolh=1e-6), {k: v.copy() for k, v in st.items()})
+        g.derivs()
+        res[prec] = g.state
+        g.close()
+    errs, bad = compare_fields(res[1], res[0], FP32_FIELDS, 1e-5)
+    assert not bad, f"{name} FP32 form at tolh 1e-6: {errs}"
+
+
 def _check_steps(o, st, name, nsteps=4):
     from ndspmhd_gb300.gpu import GpuSPH
     from oracle.oracle import Oracle
@@ -169,7 +206,7 @@ def test_mhd_box_128_derivs(gpulib):
     g, ref = _derivs_pair(o, st)
     _check_derivs(g, ref, o, "box 128^3")
     g.close()
-    _check_fp32(o, st, ref, "box 128^3")
+    _check_fp32_many(o, st, ref, "box 128^3")
 
 
 def test_brio_wu_1600_tube(gpulib):
