@@ -623,6 +623,12 @@ def main():
     tuned = tune(o32, st32)
     tuning = tuned["tuning"]
     ms32, tim32, dts32, clocks = run_device(o32, st32, args.steps, warmup, dist, tuning)
+    # the same workload with the learned h predictor in front of the
+    # Newton-Raphson iteration (FP32 pairs + learned h, the form the metric
+    # names); same tolh, same search settings
+    msl = timl = dtsl = None
+    if not args.no_extra:
+        msl, timl, dtsl, _ = run_device(dict(o32, learned_h=1), st32, args.steps, warmup, dist, tuning)
     ms64 = tim64 = None
     if not args.no_fp64:
         o64, st64 = make_problem(N1D, 0)
@@ -675,6 +681,15 @@ def main():
                                 "call": "the same, returning all 47.5 doubles a particle (output steps)"},
                 "in_place_access_value": round(e2e_inplace, 1)},
     }
+    if msl is not None:
+        line["fp32_learned_h"] = {
+            "value": round(replica_value(n, world, msl), 1), "ms_per_step": round(msl, 4),
+            "particle_passes_last_step": round(dtsl["ncalctotal"] / n, 4),
+            "particle_passes_last_step_predictor": round(dts32["ncalctotal"] / n, 4),
+            "nr_passes_last_step": dtsl["its"],
+            "kernels_ms_per_step": {"rates": round(timl["rates_ms"], 3), "density_all_passes": round(timl["density_ms"], 3),
+                                    "mlp": round(timl["mlp_ms"], 3)},
+            "speedup_over_fp32_predictor": round(ms32 / msl, 4)}
     if ms64 is not None:
         line["fp64"] = {"value": round(n / (ms64 * 1e-3), 1), "ms_per_step": round(ms64, 3),
                         "rates_ms": round(tim64["rates_ms"], 3), "density_ms": round(tim64["density_ms"], 3),

@@ -88,6 +88,7 @@ struct ndsph_ctx {
     // device-resident steps: the last step's corrector also ran this step's
     // save and predictor (k_corrector_predictor)
     bool predicted = false;
+    bool packs_valid = false;    // FP32 packs hold the last rates sweep's values of each slot
     // ndsph_step: the rates sweep runs in dl_pieces pieces, one per chunk of
     // the host arrays, and each chunk's last outputs go back while the later
     // pieces run (dl_tail: where they go; null: all after the corrector)
@@ -125,9 +126,9 @@ struct ndsph_ctx {
     float* mlp_loss = nullptr;
     MlpFrag* mlp_frag = nullptr; // BF16 tensor-core operands
     int mlp_step = 0;
-    float mlp_lr = 3.e-3f;
-    int mlp_batch = 32768;
-    int mlp_iters = 4;
+    float mlp_lr = 2.e-3f;
+    int mlp_batch = 16384;
+    int mlp_iters = 1;
     // batched form
     int nsim = 0;
     int* sim2 = nullptr;             // gather partner of S.sim
@@ -338,6 +339,7 @@ static void set_devopts(ndsph_ctx* ctx)
     o.avfact = (fabs(p.gamma - 1.) > 1.e-3) ? log(4.) / (log((p.gamma + 1.) / (p.gamma - 1.))) : 1.0;
     o.idust = p.idust; o.idrag_nature = p.idrag_nature; o.Kdrag = p.Kdrag;
     o.C_cour = p.C_cour; o.C_force = p.C_force; o.precision = p.precision;
+    o.learned = p.learned_h ? 1 : 0;
 }
 
 static void free_particles(ndsph_ctx* ctx)
@@ -531,6 +533,8 @@ extern "C" int ndsph_init(ndsph_ctx** out, const ndsph_opts* opts, int32_t nmax)
         cudaMemcpy(ctx->mlp_p, p0.data(), sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice);
         cudaMemset(ctx->mlp_m, 0, sizeof(float) * MLP_NPARAM);
         cudaMemset(ctx->mlp_v, 0, sizeof(float) * MLP_NPARAM);
+        cudaMemset(ctx->mlp_g, 0, sizeof(float) * MLP_NPARAM);
+        cudaMemset(ctx->mlp_loss, 0, sizeof(float));
         launch_mlp_pack(ctx->mlp_p, ctx->mlp_frag, ctx->st);
         cudaStreamSynchronize(ctx->st);
     }
@@ -821,6 +825,7 @@ static const int INCOPY_FIELDS[] = {XIN0, XIN1, XIN2, VIN0, VIN1, VIN2, BIN0, BI
 static int upload_inputs(ndsph_ctx* ctx, const ndsph_particles* p, int n, bool with_density, bool with_prim)
 {
     const int nd = ctx->o.ndim;
+    ctx->packs_valid = false;
     int rc = ensure_capacity(ctx, n);
     if (rc) return rc;
     ctx->n = n;
@@ -1082,6 +1087,7 @@ static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hma
 // `d_fields` into the other slab and the swap of the slabs and side arrays
 static void link_sort_gather(ndsph_ctx* ctx, const int* d_fields, int nfields, cudaStream_t st)
 {
+    ctx->packs_valid = false;
     const int n = ctx->n;
     launch_cell_key(ctx->F, ctx->g, ctx->o, n, ctx->srt, ctx->red, st);
     launch_scan(ctx->srt, ctx->g.ncells, st);
@@ -1385,6 +1391,7 @@ static int do_rates(ndsph_ctx* ctx)
         launch_rates(a, st);
     }
     tmark(ctx, 5);
+    ctx->packs_valid = (ctx->o.precision == NDSPH_PREC_FP32);
     launch_finalize_dt(ctx->red, ctx->o, ctx->d_dtout, st);
     if (ctx->o.batched) launch_sim_finalize(ctx->o, ctx->d_sim_dtnext, ctx->d_sim_out, st);
     CK(cudaGetLastError());
@@ -1692,7 +1699,7 @@ extern "C" int ndsph_primitive2conservative(ndsph_ctx* ctx, ndsph_particles* p, 
     return rc;
 }
 
-static const int MLP_FIELDS[] = {HPRED, YPREV, FT0, FT1, FT2, FT3, FT4, FT5};
+static const int MLP_FIELDS[] = {HPRED, HROOT, FT0, FT1, FT2};
 
 // fields the link at the start of a step's derivs carries into the new slot
 // order: the state and the step's saves, without position components beyond
@@ -1742,12 +1749,16 @@ static void mlp_infer(ndsph_ctx* ctx)
     a.drhodt = ctx->F.f[DRHODT];
     a.cs = ctx->F.f[CS];
     a.pmass = ctx->F.f[PM];
-    a.yprev = ctx->F.f[YPREV];
+    a.hroot = ctx->F.f[HROOT];
+    // the packs hold the previous rates sweep's values of each slot (no link
+    // since; FP32 form only)
+    a.pk_v = (ctx->o.precision == NDSPH_PREC_FP32 && ctx->packs_valid) ? ctx->S.pk_v : nullptr;
+    a.pk_t = a.pk_v ? ctx->S.pk_t : nullptr;
     a.numneigh = ctx->S.numneigh;
     a.itype = ctx->S.itype;
     a.hh = ctx->F.f[HH];
     a.hpred = ctx->F.f[HPRED];
-    for (int k = 0; k < MLP_NIN; k++) a.feat[k] = ctx->F.f[FT0 + k];
+    for (int k = 0; k < MLP_NFW; k++) a.feat[k] = reinterpret_cast<float2*>(ctx->F.f[FT0 + k]);
     launch_mlp_infer(ctx->mlp_frag, a, ctx->st);
 }
 
@@ -1756,10 +1767,8 @@ static void mlp_train(ndsph_ctx* ctx)
 {
     cudaStream_t st = ctx->st;
     const long long n = ctx->n;
-    if (ctx->mlp_iters > 0) {
-        CK_VOID(cudaMemsetAsync(ctx->mlp_g, 0, sizeof(float) * MLP_NPARAM, st));
-        CK_VOID(cudaMemsetAsync(ctx->mlp_loss, 0, sizeof(float), st));
-    }
+    // the gradient starts at zero: set so at init, and the Adam kernel
+    // clears it after every use
     for (int it = 0; it < ctx->mlp_iters; it++) {
         MlpTrainArgs a;
         memset(&a, 0, sizeof a);
@@ -1771,8 +1780,8 @@ static void mlp_train(ndsph_ctx* ctx)
         while (stride > 1 && std::__gcd(stride, n) != 1) stride--;
         a.stride = stride;
         a.offset = (long long)(ctx->mlp_step * 7919LL + it * 104729LL) % n;
-        for (int k = 0; k < MLP_NIN; k++) a.feat[k] = ctx->F.f[FT0 + k];
-        a.hconv = ctx->F.f[HH];
+        for (int k = 0; k < MLP_NFW; k++) a.feat[k] = reinterpret_cast<const float2*>(ctx->F.f[FT0 + k]);
+        a.hconv = ctx->F.f[HROOT];
         a.hpred = ctx->F.f[HPRED];
         if (it == ctx->mlp_iters - 1) CK_VOID(cudaMemsetAsync(ctx->mlp_loss, 0, sizeof(float), st));
         launch_mlp_grad(ctx->mlp_p, a, ctx->mlp_g, ctx->mlp_loss, st);
@@ -1780,7 +1789,6 @@ static void mlp_train(ndsph_ctx* ctx)
         launch_mlp_adam(ctx->mlp_p, ctx->mlp_m, ctx->mlp_v, ctx->mlp_g, ctx->mlp_step, ctx->mlp_lr, st);
     }
     launch_mlp_pack(ctx->mlp_p, ctx->mlp_frag, st);
-    launch_mlp_store_y(ctx->F.f[HH], ctx->F.f[HPRED], ctx->F.f[YPREV], ctx->n, st);
 }
 
 // one leapfrog step on the device state (stepND_leapfrog_mhd.f90:31-275)
@@ -2007,6 +2015,7 @@ extern "C" int ndsph_dev_derivs(ndsph_ctx* ctx, ndsph_dt* dts)
 // or maxdensits = 0 (no density pass), where everything is uploaded.
 static int step_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
 {
+    ctx->packs_valid = false;
     if (ctx->o.has_fixed || ctx->o.maxdensits < 1) return dev_upload_impl(ctx, p, npart, false);
     // when the last step's link may be kept, the caller's arrays go straight
     // into that step's slot order (slot k <- particle id[k]); the link's

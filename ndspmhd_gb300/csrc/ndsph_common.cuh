@@ -37,10 +37,13 @@ enum Field : int {
     // leapfrog saves (part_in module, stepND_leapfrog_mhd.f90:70-101)
     XIN0, XIN1, XIN2, VIN0, VIN1, VIN2, BIN0, BIN1, BIN2, HIN, ENIN, RHOIN, ALIN0, ALIN1, ALIN2,
     FIN0, FIN1, FIN2, DBIN0, DBIN1, DBIN2, DHIN, DENIN, DALIN0, DALIN1, DALIN2,
-    HPRED, YPREV, FT0, FT1, FT2, FT3, FT4, FT5,   // learned-h predictor: h_pred, last z, features
+    // learned-h predictor: h_pred, and the six FP32 features packed two to
+    // a field (bit patterns: the permutation gather moves 8-byte words)
+    HPRED, FT0, FT1, FT2,
     HDEN0,      // h at entry of iterate_density (hhin, iterate_density.f90:87)
     HNEXT,      // NR scratch: next h of the first pass
     RHO1,       // 1/rho of the FP64 rates sweep (written with the EOS)
+    HROOT,      // learned h: the Newton-Raphson estimate of the root at convergence
     NF
 };
 
@@ -60,6 +63,7 @@ struct DevOpts {
     double C_cour, C_force;
     int precision;
     int has_fixed;      // any ibound == 1 (fixed particles with ireal copies)
+    int learned;        // learned-h predictor on: the density passes keep HROOT
     // batched form: nsim independent simulations in one state
     int batched;
     int nsim;

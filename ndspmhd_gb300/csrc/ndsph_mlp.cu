@@ -3,14 +3,20 @@
 // A 6 -> 32 -> 32 -> 1 MLP (tanh hidden layers) predicts, per particle, the
 // correction z = 100 log(h_conv / h_pred) between the Newton-Raphson
 // converged h and the leapfrog predictor's h_pred = hhin + dt dhdt
-// (stepND_leapfrog_mhd.f90:152-153, ihvar = 2).  The prediction only moves
+// (stepND_leapfrog_mhd.f90:152-153, ihvar = 2), as the previous step's
+// correction y_prev plus the network's output: y_prev passes in FP32, so the
+// BF16 activations only carry the (smaller) change of the correction from
+// one step to the next.  The prediction only moves
 // the starting point of iterate_density: NR keeps the same tolerance and
 // decides convergence, so a wrong prediction costs extra passes, never accuracy.
 //
 //  * inference: BF16 weights and activations, FP32 accumulation, on the
 //    tensor cores with mma.sync.m16n8k16 (one warp = 16 particles per tile);
 //  * training: online, after every step, on minibatches of the particles'
-//    own (features, converged h) pairs; forward/backward in FP32 with the
+//    own features and the Newton-Raphson estimate of the root of f(h) at
+//    convergence (the Newton step from the converged h: the converged h
+//    itself only lies within ~tolh of the root, which put a floor of ~tolh
+//    under the prediction error); forward/backward in FP32 with the
 //    BF16-rounded weights the inference uses; Adam on FP32 master weights.
 //
 // Parameter vector (FP32, NPARAM = 1313): W1[32][6], b1[32], W2[32][32],
@@ -167,22 +173,40 @@ __device__ __forceinline__ void slot_features(const MlpInferArgs& a, int i, floa
 {
     // FP32 throughout: the features are rounded to BF16 anyway, and FP64
     // transcendentals are expensive on this part
+    // FP32 arithmetic from FP32 inputs where the FP32 form has them (FP64
+    // conversions and divisions run on this part's narrow FP64 pipe)
     const float hprev = (float)a.hin[i], hpred = (float)a.hh[i];
-    const float rho = (float)a.rho[i];
+    float rho, cs, m;
+    if (a.pk_t) {
+        const float4 t = a.pk_t[i];
+        rho = t.x;
+        cs = t.z;
+        m = a.pk_v[i].w;
+    } else {
+        rho = (float)a.rho[i];
+        cs = (float)a.cs[i];
+        m = (float)a.pmass[i];
+    }
     const float divv = -(float)a.drhodt[i] / rho;
     float hf = 1.f;
     const float hb = hprev / (float)a.hfact;
     for (int d = 0; d < a.ndim; d++) hf *= hb;
-    f[0] = 100.f * logf(hpred / hprev);
+    f[0] = 100.f * __logf(hpred / hprev);
     f[1] = 100.f * (float)a.dt * divv;
     f[2] = 10.f * ((float)a.numneigh[i] / (float)a.nn_ref - 1.f);
-    f[3] = 10.f * (float)a.dt * (float)a.cs[i] / hprev;
-    f[4] = 100.f * logf(rho * hf / (float)a.pmass[i]) / (float)a.ndim;
-    f[5] = (float)a.yprev[i];
+    f[3] = 10.f * (float)a.dt * cs / hprev;
+    f[4] = 100.f * __logf(rho * hf / m) / (float)a.ndim;
+    // the previous step's correction, from its h_pred and root estimate
+    // (none before the first learned step: both are 0 then)
+    const float hp0 = (float)a.hpred[i], hr0 = (float)a.hroot[i];
+    f[5] = (hp0 > 0.f && hr0 > 0.f) ? 100.f * __logf(hr0 / hp0) : 0.f;
 }
 
 // per step, before the link: h <- h_pred exp(z/100), features and h_pred kept
-// for the training after the density iteration
+// for the training after the density iteration.  A warp takes 32 slots at a
+// time: each lane loads and computes its own slot's features (coalesced), the
+// two 16-row tiles go through the network on the tensor cores, and each lane
+// stores its own slot's results.
 __global__ void k_mlp_infer(const MlpFrag* __restrict__ frp, MlpInferArgs a)
 {
     __shared__ MlpFrag fr;
@@ -192,37 +216,44 @@ __global__ void k_mlp_infer(const MlpFrag* __restrict__ frp, MlpInferArgs a)
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int tile = warp; tile * 16 < a.n; tile += nwarps) {
-        const int r0 = tile * 16 + g, r1 = r0 + 8;
-        // lanes t = 0 and 1 compute the features of rows g and g+8 once;
-        // every lane then picks its two columns by shuffle
+    for (int base = warp * 32; base < a.n; base += nwarps * 32) {
+        const int i = base + lane;
         float fa[MLP_NIN] = {0, 0, 0, 0, 0, 0};
-        const int myrow = (t == 0) ? r0 : r1;
-        if (t < 2 && myrow < a.n) slot_features(a, myrow, fa);
-        float f00 = 0.f, f01 = 0.f, f10 = 0.f, f11 = 0.f;
+        if (i < a.n) slot_features(a, i, fa);
+        // A fragments of the two tiles: lane (g, t) holds columns 2t, 2t+1 of
+        // rows g and g+8 (tile 0: slots base..base+15, tile 1: the next 16);
+        // column pair (2k, 2k+1) comes by shuffle from the rows' lanes
+        float x[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            // column pair (2k, 2k+1) belongs to lane t == k
-            const float ra0 = __shfl_sync(0xffffffffu, fa[2 * k], lane & ~3);
-            const float ra1 = __shfl_sync(0xffffffffu, fa[2 * k + 1], lane & ~3);
-            const float rb0 = __shfl_sync(0xffffffffu, fa[2 * k], (lane & ~3) | 1);
-            const float rb1 = __shfl_sync(0xffffffffu, fa[2 * k + 1], (lane & ~3) | 1);
-            if (t == k) { f00 = ra0; f01 = ra1; f10 = rb0; f11 = rb1; }
+#pragma unroll
+            for (int tl = 0; tl < 2; tl++) {
+                const float r00 = __shfl_sync(0xffffffffu, fa[2 * k], 16 * tl + g);
+                const float r01 = __shfl_sync(0xffffffffu, fa[2 * k + 1], 16 * tl + g);
+                const float r10 = __shfl_sync(0xffffffffu, fa[2 * k], 16 * tl + g + 8);
+                const float r11 = __shfl_sync(0xffffffffu, fa[2 * k + 1], 16 * tl + g + 8);
+                if (t == k) { x[tl][0] = r00; x[tl][1] = r01; x[tl][2] = r10; x[tl][3] = r11; }
+            }
         }
-        float z0, z1;
-        mlp_tile(fr, pack_bf16(f00, f01), pack_bf16(f10, f11), z0, z1);
-        // lane t = 0 finishes row g, lane t = 1 row g+8
-        if (t < 2) {
-            const int i = myrow;
-            const float zz = (t == 0) ? z0 : z1;
-            if (i < a.n) {
-                for (int k = 0; k < MLP_NIN; k++) a.feat[k][i] = fa[k];
-                const double hpred = a.hh[i];
-                a.hpred[i] = hpred;
-                if (!(a.fixed && a.itype[i] == 1)) {
-                    const float z = fminf(fmaxf(zz, -(float)a.zclip), (float)a.zclip);
-                    if (a.apply) a.hh[i] = hpred * (double)expf(0.01f * z);
-                }
+        float z00, z08, z10, z18;
+        mlp_tile(fr, pack_bf16(x[0][0], x[0][1]), pack_bf16(x[0][2], x[0][3]), z00, z08);
+        mlp_tile(fr, pack_bf16(x[1][0], x[1][1]), pack_bf16(x[1][2], x[1][3]), z10, z18);
+        // every lane of quad q holds z of rows q and q+8 of both tiles: lane
+        // L takes its own slot's value from lane 4 (L mod 8)
+        const int src = 4 * (lane & 7);
+        const float a00 = __shfl_sync(0xffffffffu, z00, src);
+        const float a08 = __shfl_sync(0xffffffffu, z08, src);
+        const float a10 = __shfl_sync(0xffffffffu, z10, src);
+        const float a18 = __shfl_sync(0xffffffffu, z18, src);
+        const float zz = (lane < 8) ? a00 : (lane < 16) ? a08 : (lane < 24) ? a10 : a18;
+        if (i < a.n) {
+            for (int k = 0; k < MLP_NFW; k++) a.feat[k][i] = make_float2(fa[2 * k], fa[2 * k + 1]);
+            const double hpred = a.hh[i];
+            a.hpred[i] = hpred;
+            if (!(a.fixed && a.itype[i] == 1)) {
+                // the network predicts the change of the correction
+                const float z = fminf(fmaxf(fa[5] + zz, -(float)a.zclip), (float)a.zclip);
+                if (a.apply) a.hh[i] = hpred * (double)__expf(0.01f * z);
             }
         }
     }
@@ -270,8 +301,14 @@ __global__ void __launch_bounds__(TRAIN_BS) k_mlp_grad(const float* __restrict__
                 y = a.targets[s];
             } else {            // strided sample of the slots
                 const long long i = ((long long)s * a.stride + a.offset) % a.n;
-                for (int k = 0; k < MLP_NIN; k++) x[k] = (float)a.feat[k][i];
-                y = 100.f * logf((float)a.hconv[i] / (float)a.hpred[i]);
+                for (int k = 0; k < MLP_NFW; k++) {
+                    const float2 v = a.feat[k][i];
+                    x[2 * k] = v.x;
+                    x[2 * k + 1] = v.y;
+                }
+                // target: the change of the correction from the previous step
+                // (feature 5, y_prev, unrounded), as the inference applies it
+                y = 100.f * logf((float)a.hconv[i] / (float)a.hpred[i]) - x[5];
             }
             for (int k = 0; k < MLP_NIN; k++) x[k] = bf16r(x[k]);
         } else {
@@ -359,13 +396,6 @@ __global__ void k_mlp_adam(float* p, float* m, float* v, float* g, int step, flo
     g[q] = 0.f;   // ready for the next minibatch without a memset
 }
 
-// y_prev <- 100 log(h_conv / h_pred) for the next step's features
-__global__ void k_mlp_store_y(const double* hconv, const double* hpred, double* yprev, int n)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) yprev[i] = (double)(100.f * logf((float)hconv[i] / (float)hpred[i]));
-}
-
 // ---------------------------------------------------------------------------
 void mlp_init_params(std::vector<float>& p, unsigned seed)
 {
@@ -394,8 +424,8 @@ void launch_mlp_forward(const MlpFrag* fr, const float* feats, int n, float* out
 void launch_mlp_infer(const MlpFrag* fr, const MlpInferArgs& a, cudaStream_t st)
 {
     if (a.n <= 0) return;
-    const int tiles = (a.n + 15) / 16;
-    int blocks = (tiles + 7) / 8;
+    const int groups = (a.n + 31) / 32;   // 32 slots per warp and pass
+    int blocks = (groups + 7) / 8;
     if (blocks > 152 * 16) blocks = 152 * 16;
     NDSPH_COUNT_LAUNCH, k_mlp_infer<<<blocks, 256, 0, st>>>(fr, a);
 }
@@ -410,10 +440,6 @@ void launch_mlp_grad(const float* p, const MlpTrainArgs& a, float* grad, float* 
 void launch_mlp_adam(float* p, float* m, float* v, float* g, int step, float lr, cudaStream_t st)
 {
     NDSPH_COUNT_LAUNCH, k_mlp_adam<<<(MLP_NPARAM + 255) / 256, 256, 0, st>>>(p, m, v, g, step, lr);
-}
-void launch_mlp_store_y(const double* hconv, const double* hpred, double* yprev, int n, cudaStream_t st)
-{
-    if (n > 0) NDSPH_COUNT_LAUNCH, k_mlp_store_y<<<(n + 255) / 256, 256, 0, st>>>(hconv, hpred, yprev, n);
 }
 
 }  // namespace ndsph

@@ -466,7 +466,10 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
         }
     }
     a.S.numneigh[i] = nn;
-    if (fixed_i) return;
+    if (fixed_i) {
+        if (o.learned) F.f[HROOT][i] = hi;
+        return;
+    }
 
     // ---- sums in reference units and the Newton-Raphson update
     // (iterate_density.f90:163-278).  FP64 for the parity form.  The FP32
@@ -585,6 +588,10 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
     } else {
         drhodt = drhodt * gradh;
         F.f[DHDT][i] = (double)(dhdrhoi * drhodt);
+        // learned h: the training target is the Newton step from the
+        // converged h, the root to second order, not h itself (which the
+        // tolerance leaves up to ~tolh from it)
+        if (o.learned) F.f[HROOT][i] = hnew;
     }
     if (relink) a.red->redolink = 1;
     F.f[RHO][i] = (double)rho;
