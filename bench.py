@@ -9,10 +9,14 @@ plus a 1% transverse perturbation, gamma = 5/3, cubic-spline kernel,
 hfact = 1.2, tolh = 1e-3.  Synthetic data generated in-process.
 
 Metric: particle-updates/s = N x steps / device time of the step loop.
-``value`` is the chosen FP32-pair form with the state resident in HBM;
-``fp64`` reports the plain FP64 form (the parity form) on the same workload;
-``e2e`` times the reference-facing C-ABI call ndsph_step with the state in
-pinned host buffers (H2D of the state and D2H of the result every step).
+``value`` is the chosen form -- FP32 pair sums with the learned h predictor
+in front of the Newton-Raphson iteration -- with the state resident in HBM;
+``fp32_predictor`` the FP32 form with the reference's own predictor;
+``fp64`` the plain FP64 form (the parity form) on the same workload;
+``fp32_error_vs_fp64`` the FP32 forms' error against the FP64 form (tolh 1e-3
+and 1e-6, with the speed ratio at 1e-6); ``e2e`` times the reference-facing
+C-ABI call ndsph_step with the state in pinned host buffers (H2D of the state
+and D2H of the result every step).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 (N>1 under torchrun: independent replicas, one box per rank, weak scaling.)
@@ -34,7 +38,7 @@ sys.path.insert(0, ROOT)
 N1D = int(os.environ.get("NDSPH_BENCH_N1D", "128"))
 CPU_SAMPLE_N1D = 48          # CPU baseline sample: 48^3 box, 2 steps
 CPU_SAMPLE_STEPS = 2
-METRIC = "SPH particle-updates/s on 1 GB300 (3D MHD 128^3 box, full leapfrog step)"
+METRIC = "SPH particle-updates/s on 1 GB300: FP32+learned-h vs plain FP64 at stated error"
 UNIT = "particle-updates/s"
 
 # algorithmic bytes per particle of the rates sweep: reads x(3) v(3) m h rho P
@@ -303,55 +307,65 @@ def run_batched(steps: int, warmup: int, ntubes: int = 4096):
 
 
 def _fp32_vs_fp64(st0, o64, steps: int, tolh: float, timed_steps: int = 0):
-    """Both forms from the same FP64 state, `steps` device-resident steps each
-    (each form takes its own dt); then, if timed_steps, that many more steps
-    timed.  Per field: max |fp32 - fp64| / max(max |fp64|, rms fp64), and the
-    99.99th percentile of the same per-particle ratio."""
+    """The FP32 forms (reference predictor; learned h) against the FP64 form
+    from the same FP64 state, `steps` device-resident steps each (each form
+    takes its own dt); then, if timed_steps, that many more steps timed.  Per
+    field: max |fp32 - fp64| / max(max |fp64|, rms fp64), and the 99.99th
+    percentile of the same per-particle ratio."""
     import numpy as np
     from ndspmhd_gb300.gpu import GpuSPH
     fields = ("x", "vel", "hh", "rho", "en", "Bevol", "force", "dudt", "dBevoldt")
+    forms = {"fp64": dict(precision=0, learned_h=0), "fp32": dict(precision=1, learned_h=0),
+             "fp32_learned_h": dict(precision=1, learned_h=1)}
     out, ms = {}, {}
-    for prec in (0, 1):
-        g = GpuSPH(dict(o64, precision=prec, tolh=tolh), {k: v.copy() for k, v in st0.items()})
+    for key, f in forms.items():
+        g = GpuSPH(dict(o64, tolh=tolh, **f), {k: v.copy() for k, v in st0.items()})
         g.dev_upload()
         g.set_dt(0.0)
         g.dev_step(steps)
         g.dev_download()
-        out[prec] = {k: g.state[k].copy() for k in fields}
+        out[key] = {k: g.state[k].copy() for k in fields}
         if timed_steps:
             g.dev_step(timed_steps)
-            ms[prec] = g.timing()["total_ms"] / timed_steps
+            ms[key] = g.timing()["total_ms"] / timed_steps
         g.close()
     res = {"steps": steps, "tolh": tolh}
-    for k in fields:
-        ref = out[0][k]
-        scale = max(float(np.max(np.abs(ref))), float(np.sqrt(np.mean(ref * ref))))
-        d = np.abs(out[1][k] - ref)
-        if d.ndim > 1:
-            d = d.max(axis=1)
-        res[k] = float(d.max() / scale) if scale > 0 else 0.0
-        res[k + "_p9999"] = float(np.quantile(d, 0.9999) / scale) if scale > 0 else 0.0
-    # particles whose h differs by more than 1e-5 relative: those whose
-    # Newton-Raphson residual sat at the tolerance and converged one pass apart
-    dh = np.abs(out[1]["hh"] - out[0]["hh"]) / out[0]["hh"]
-    res["particles_h_differ_1e-5"] = int(np.sum(dh > 1e-5))
+    for key in ("fp32", "fp32_learned_h"):
+        r = {}
+        for k in fields:
+            ref = out["fp64"][k]
+            scale = max(float(np.max(np.abs(ref))), float(np.sqrt(np.mean(ref * ref))))
+            d = np.abs(out[key][k] - ref)
+            if d.ndim > 1:
+                d = d.max(axis=1)
+            r[k] = float(d.max() / scale) if scale > 0 else 0.0
+            r[k + "_p9999"] = float(np.quantile(d, 0.9999) / scale) if scale > 0 else 0.0
+        # particles whose h differs by more than 1e-5 relative: those whose
+        # Newton-Raphson residual sat at the tolerance and converged one pass
+        # apart (or, with learned h, from another starting point)
+        dh = np.abs(out[key]["hh"] - out["fp64"]["hh"]) / out["fp64"]["hh"]
+        r["particles_h_differ_1e-5"] = int(np.sum(dh > 1e-5))
+        res[key] = r
     if ms:
-        res["ms_per_step"] = {"fp64": round(ms[0], 3), "fp32": round(ms[1], 3),
-                              "speedup_fp32_over_fp64": round(ms[0] / ms[1], 2), "timed_steps": timed_steps}
+        res["ms_per_step"] = {k: round(v, 3) for k, v in ms.items()}
+        res["ms_per_step"]["timed_steps"] = timed_steps
+        res["ms_per_step"]["speedup_fp32_over_fp64"] = round(ms["fp64"] / ms["fp32"], 2)
+        res["ms_per_step"]["speedup_fp32_learned_h_over_fp64"] = round(ms["fp64"] / ms["fp32_learned_h"], 2)
     return res
 
 
 def fp32_error(steps: int = 4):
-    """Error of the FP32 form against the FP64 (parity) form on the headline
-    workload, at two Newton-Raphson tolerances (the same in both forms):
+    """Error of the FP32 forms against the FP64 (parity) form on the headline
+    workload, at two Newton-Raphson tolerances (the same in every form):
 
     * tolh 1e-3, the headline's: a particle whose residual sits within the
       FP32 form's ~5e-7 density error of the tolerance converges one pass
-      apart in the two forms, and its h then differs by up to ~tolh; the max
-      error is set by those few particles (counted), the 99.99th percentile
-      by the arithmetic;
-    * tolh 1e-6: the decisions agree closely enough that the max error is
-      the arithmetic's own (<= 1e-5); both forms are also timed there, so the
+      apart in the two forms (with learned h the starting point differs as
+      well), and its h then differs by up to ~tolh; the max error is set by
+      those few particles (counted) and their neighbours, the 99.99th
+      percentile by the arithmetic;
+    * tolh 1e-6: the decisions agree closely enough that the error is the
+      arithmetic's own (<= 1e-5); the forms are also timed there, so the
       FP32/FP64 speed ratio is quoted at a tolerance where that bound holds.
     """
     o64, st64 = make_problem(N1D, 0)
@@ -622,13 +636,13 @@ def main():
     n = st32["x"].shape[0]
     tuned = tune(o32, st32)
     tuning = tuned["tuning"]
-    ms32, tim32, dts32, clocks = run_device(o32, st32, args.steps, warmup, dist, tuning)
-    # the same workload with the learned h predictor in front of the
-    # Newton-Raphson iteration (FP32 pairs + learned h, the form the metric
-    # names); same tolh, same search settings
-    msl = timl = dtsl = None
-    if not args.no_extra:
-        msl, timl, dtsl, _ = run_device(dict(o32, learned_h=1), st32, args.steps, warmup, dist, tuning)
+    # the headline form: FP32 pairs + the learned h predictor in front of the
+    # Newton-Raphson iteration (the form the metric names), then the same
+    # workload with the reference's own predictor; same tolh, same search
+    # settings (tuned on the reference predictor)
+    o32l = dict(o32, learned_h=1)
+    ms32, tim32, dts32, clocks = run_device(o32l, st32, args.steps, warmup, dist, tuning)
+    msp, timp, dtsp, _ = run_device(o32, st32, args.steps, warmup, dist, tuning)
     ms64 = tim64 = None
     if not args.no_fp64:
         o64, st64 = make_problem(N1D, 0)
@@ -638,7 +652,7 @@ def main():
     ms32 = max_over_ranks(ms32, dist, "cuda")
     value = replica_value(n, world, ms32)
 
-    e2e_sets, e2e_inplace = run_e2e(o32, max(3, args.steps), 3, tuning)
+    e2e_sets, e2e_inplace = run_e2e(o32l, max(3, args.steps), 3, tuning)
     e2e_val, h2d, d2h = e2e_sets["integrator"]
 
     peak, peak_kind = _load_peaks()
@@ -661,7 +675,8 @@ def main():
         "vs_baseline": None, "dtype": "f32 pairs / f64 state",
         "data": "synthetic (seeded jittered 128^3 MHD box, generated in-process)",
         "config": {"workload": f"3D MHD box {N1D}^3 = {n} particles, periodic, full leapfrog step",
-                   "form": "FP32 pair sums (compensated), FP64 state/integration",
+                   "form": "FP32 pair sums (compensated), FP64 state/integration, learned h predictor "
+                           "(MLP, trained online) in front of the Newton-Raphson iteration at tolh 1e-3",
                    "l2": "inputs larger than L2 (state slab ~1.3 GB)", "parallelism": f"replicas x{world}",
                    "nr_passes_per_step": tim32["density_passes"],
                    "steps_keeping_the_link": tim32["kept_link_steps"], "row_builds": tim32["row_builds"],
@@ -669,7 +684,9 @@ def main():
                    "autotune_trials": [[t["tuning"], t["ms_per_step"]] for t in tuned["trials"]]},
         "gpu_launches": None,
         "kernels_ms_per_step": {"rates": round(tim32["rates_ms"], 3), "density_all_passes": round(tim32["density_ms"], 3),
-                                "link": round(tim32["link_ms"], 3), "step_total": round(tim32["step_ms"], 3)},
+                                "link": round(tim32["link_ms"], 3), "mlp": round(tim32["mlp_ms"], 3),
+                                "step_total": round(tim32["step_ms"], 3)},
+        "particle_passes_last_step": round(dts32["ncalctotal"] / n, 4),
         "roofline": roofline,
         "clocks": clocks,
         "e2e": {"value": round(e2e_val, 1), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -681,15 +698,14 @@ def main():
                                 "call": "the same, returning all 47.5 doubles a particle (output steps)"},
                 "in_place_access_value": round(e2e_inplace, 1)},
     }
-    if msl is not None:
-        line["fp32_learned_h"] = {
-            "value": round(replica_value(n, world, msl), 1), "ms_per_step": round(msl, 4),
-            "particle_passes_last_step": round(dtsl["ncalctotal"] / n, 4),
-            "particle_passes_last_step_predictor": round(dts32["ncalctotal"] / n, 4),
-            "nr_passes_last_step": dtsl["its"],
-            "kernels_ms_per_step": {"rates": round(timl["rates_ms"], 3), "density_all_passes": round(timl["density_ms"], 3),
-                                    "mlp": round(timl["mlp_ms"], 3)},
-            "speedup_over_fp32_predictor": round(ms32 / msl, 4)}
+    msp = max_over_ranks(msp, dist, "cuda")
+    line["fp32_predictor"] = {
+        "value": round(replica_value(n, world, msp), 1), "ms_per_step": round(msp, 4),
+        "form": "FP32 pairs with the reference's predictor h + dt dh/dt (stepND_leapfrog_mhd.f90:152-153)",
+        "particle_passes_last_step": round(dtsp["ncalctotal"] / n, 4), "nr_passes_last_step": dtsp["its"],
+        "kernels_ms_per_step": {"rates": round(timp["rates_ms"], 3), "density_all_passes": round(timp["density_ms"], 3),
+                                "link": round(timp["link_ms"], 3), "step_total": round(timp["step_ms"], 3)},
+        "learned_speedup": round(msp / ms32, 4)}
     if ms64 is not None:
         line["fp64"] = {"value": round(n / (ms64 * 1e-3), 1), "ms_per_step": round(ms64, 3),
                         "rates_ms": round(tim64["rates_ms"], 3), "density_ms": round(tim64["density_ms"], 3),

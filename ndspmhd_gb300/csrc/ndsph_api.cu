@@ -2023,9 +2023,14 @@ static int step_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
     // still hold every pair, so arrays the caller changed are safe
     const bool keep = ctx->nl_valid && ctx->linked && npart == ctx->n && reuse_on(ctx);
     int rc = 0;
+    // the learned-h predictor's inputs from the previous step that are not
+    // among the uploaded arrays follow each particle into this upload's order
+    bool carry_mlp = false;
     if (!keep) {
+        const int n_prev = ctx->n;
         rc = ensure_capacity(ctx, npart);
         if (rc) return rc;
+        carry_mlp = ctx->opts.learned_h && ctx->linked && n_prev == npart;
         ctx->n = npart;
         ctx->nl_valid = false;
     }
@@ -2084,6 +2089,22 @@ static int step_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
             launch_int_shift(ctx->S.itype, v, n, 0, ctx->st);
         else
             CK(cudaMemcpyAsync(ctx->S.itype, p->itype, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
+        if (carry_mlp) {
+            // slot k takes particle k: gather the previous step's values the
+            // predictor reads (its h_pred and root estimate, drho/dt, c_s,
+            // numneigh) from the old slot pos_of_id[k] into the other slab,
+            // then copy back
+            static const int mf[4] = {HPRED, HROOT, DRHODT, CS};
+            CK(cudaMemcpyAsync(ctx->d_fields, mf, sizeof mf, cudaMemcpyHostToDevice, ctx->st));
+            FieldPtrs tmp;
+            double* other = ctx->slab[1 - ctx->cur];
+            for (int f = 0; f < NF; f++) tmp.f[f] = other + (size_t)(ctx->F.f[f] - ctx->slab[ctx->cur]);
+            launch_gather_fields(tmp, ctx->F, ctx->d_fields, 4, ctx->S.pos_of_id, n, ctx->st);
+            for (int f : mf) launch_copy(ctx->F.f[f], tmp.f[f], n, ctx->st);
+            launch_gather_int(ctx->d_istage, ctx->S.numneigh, ctx->S.pos_of_id, n, ctx->st);
+            CK(cudaMemcpyAsync(ctx->S.numneigh, ctx->d_istage, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice,
+                               ctx->st));
+        }
         launch_iota(ctx->S.id, n, ctx->st);
         launch_iota(ctx->S.pos_of_id, n, ctx->st);
         ctx->linked = false;
@@ -2103,7 +2124,7 @@ extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, nds
     if (dts) { ctx->dt = dts->dt; ctx->time = dts->time; ctx->nsteps = dts->nsteps; }
     // without fixed particles the density outputs and the primitives are
     // final before the rates sweep: copy them back while it runs
-    const bool early = !ctx->o.has_fixed && !ctx->opts.learned_h;
+    const bool early = !ctx->o.has_fixed;
     ctx->dl_early = early ? p : nullptr;
     // the rest streams with the rates pieces when the copies are staged and
     // the arrays are large enough for the pieces to pay

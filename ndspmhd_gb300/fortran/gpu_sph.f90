@@ -112,6 +112,10 @@ module gpu_sph
  type(c_ptr), save :: ctx = c_null_ptr
  ! pair-sum form of the context: 0 plain FP64 (the parity form), 1 FP32 pairs
  integer, save :: gpu_precision = 0
+ ! 1: the learned h predictor (an MLP trained online on the device) sets the
+ ! starting h of each step's density iteration in gpu_step; the iteration and
+ ! its tolerance are unchanged
+ integer, save :: gpu_learned_h = 0
  ! gpu_step copies back only what the next step reads (x, vel, Bevol, en, hh,
  ! alpha and their rates: 25 doubles a particle) unless this is set; the
  ! caller sets it before a step whose results output or evwrite will read
@@ -141,7 +145,7 @@ contains
   o%beta = beta;  o%avdecayconst = avdecayconst;  o%gamma = gamma;  o%polyk = polyk
   o%idust = idust;  o%idrag_nature = idrag_nature;  o%Kdrag = Kdrag
   o%C_cour = C_cour;  o%C_force = C_force
-  o%precision = gpu_precision;  o%learned_h = 0
+  o%precision = gpu_precision;  o%learned_h = gpu_learned_h
  end subroutine gpu_opts
 
  subroutine gpu_particles(p)

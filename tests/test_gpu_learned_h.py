@@ -95,3 +95,37 @@ def test_learned_h_reduces_density_work(gpulib):
     assert t1["mlp_updates"] > 0
     # measured on GB300: ~1.92 -> ~1.65 particle passes per step (second half)
     assert lrn < 0.95 * base
+
+
+def test_learned_h_through_the_host_buffer_step(gpulib):
+    """ndsph_step with the learned predictor (the form the bench's e2e number
+    times): the predictor's per-particle history (its last h_pred and root
+    estimate, drho/dt, c_s, numneigh) follows each particle into the host
+    order of every upload.  The Newton-Raphson iteration stays the judge, so
+    after six steps the particles agree with the reference predictor's to
+    within a few times tolh, and the learned steps need fewer density
+    passes."""
+    import numpy as np
+    from ndspmhd_gb300.gpu import GpuSPH
+    o, p = configs.mhd_box_3d(32, seed=7)
+    o = dict(o, precision=1)
+    g0 = GpuSPH(o, configs.full_state(p, 3))
+    g0.primitive2conservative()
+    st = {k: v.copy() for k, v in g0.state.items()}
+    g0.close()
+    res, work = {}, {}
+    for learned in (0, 1):
+        g = GpuSPH(dict(o, learned_h=learned), {k: v.copy() for k, v in st.items()})
+        g.dt.dt, g.dt.time, g.dt.nsteps = 0.0, 0.0, 0
+        w = []
+        for _ in range(6):
+            g.step()
+            w.append(g.dts()["ncalctotal"])
+        res[learned] = {k: v.copy() for k, v in g.state.items()}
+        work[learned] = sum(w[2:])
+        g.close()
+    for k in ("x", "vel", "hh", "rho", "en"):
+        a, b = res[1][k], res[0][k]
+        scale = max(float(np.max(np.abs(b))), 1e-30)
+        assert float(np.max(np.abs(a - b))) <= 10 * o["tolh"] * scale, k
+    assert work[1] < work[0], work
