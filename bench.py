@@ -274,8 +274,10 @@ def run_e2e(o, steps: int, warmup: int, tuning=None):
 def run_batched(steps: int, warmup: int, ntubes: int = 4096):
     """Batched form: 4096 independent 1D Brio-Wu tubes, 200-1600 particles
     each (seeded), one device state, per-tube dt; FP32 pair sums.  `steps`
-    timed steps as captured CUDA graphs (one launch per step), then the same
-    problem on the eager host loop for comparison."""
+    timed steps of the fused per-tube kernel (one launch per step, one block
+    per tube), then the same problem as captured CUDA graphs of the per-kernel
+    step (one graph launch per step, search settings from the autotuner) and
+    on the eager host loop, for comparison."""
     from ndspmhd_gb300 import autotune, configs
     from ndspmhd_gb300.gpu import GpuSPH
     o, p, sim, counts = configs.brio_wu_batch(ntubes)
@@ -285,7 +287,7 @@ def run_batched(steps: int, warmup: int, ntubes: int = 4096):
     tuned = autotune.tune_batched(o, configs.full_state(p, 1), sim, len(counts), candidates=cands,
                                   steps=20, warmup=3)
     out = {}
-    for mode, nst in ((1, steps), (0, max(steps // 4, 5))):
+    for mode, nst in ((1, steps), (2, max(steps // 4, 20)), (0, max(steps // 4, 5))):
         g = GpuSPH(o, configs.full_state(p, 1))
         g.set_tuning(**tuned["tuning"])
         g.batch_upload(sim, len(counts), initialise=True)
@@ -297,11 +299,12 @@ def run_batched(steps: int, warmup: int, ntubes: int = 4096):
         g.close()
         out[mode] = {"value": round(n * nst / (ms * 1e-3), 1), "ms_per_step": round(ms / nst, 3), "steps": nst,
                      "launches_per_step": round(tim["launches"] / nst, 1),
-                     "graph_steps": tim["graph_steps"], "graph_redos": tim["graph_redos"]}
+                     "fused_steps": tim["fused_steps"], "graph_steps": tim["graph_steps"],
+                     "graph_redos": tim["graph_redos"]}
     res = dict(out[1])
     res.update({"unit": UNIT, "config": f"{ntubes} Brio-Wu tubes, {n} particles, FP32 pairs, per-tube dt, "
-                                        f"one captured graph launch per step",
-                "eager": out[0], "search_tuning": tuned["tuning"],
+                                        f"one fused launch per step (one block per tube)",
+                "captured_graph": out[2], "eager": out[0], "graph_search_tuning": tuned["tuning"],
                 "autotune_trials": [[t["tuning"], t["ms_per_step"]] for t in tuned["trials"]]})
     return res
 

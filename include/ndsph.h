@@ -237,11 +237,15 @@ NDSPH_API int ndsph_batch_download(ndsph_ctx* ctx, ndsph_particles* p);
  * it, as Grace over NVLink-C2C does), else through staging copies; 0 always
  * staging copies.  The results are the same either way.                      */
 NDSPH_API int ndsph_set_host_access(ndsph_ctx* ctx, int32_t mode);
-/* how ndsph_batch_step runs a step: 1 (default) one captured CUDA graph per
- * step -- link, neighbour rows, the Newton-Raphson passes under a device-driven
- * WHILE node, EOS, rates, leapfrog and the per-simulation dt in one launch, with
- * steps the graph cannot finish (cells or rows outgrown, a relink, the pass
- * limit) redone on the eager path; 0 the eager host loop (one host
+/* how ndsph_batch_step runs a step: 1 (default) one launch per step -- for a
+ * 1D batch whose simulations hold at most 4096 particles each, a fused kernel
+ * with one block per simulation that runs its whole leapfrog step (predictor,
+ * order by x, every Newton-Raphson pass, EOS, rates, its dt, corrector) with
+ * no global sort or neighbour rows; otherwise as 2; 2 one captured CUDA graph
+ * per step -- link, neighbour rows, the Newton-Raphson passes under a
+ * device-driven WHILE node, EOS, rates, leapfrog and the per-simulation dt,
+ * with steps the graph cannot finish (cells or rows outgrown, a relink, the
+ * pass limit) redone on the eager path; 0 the eager host loop (one host
  * synchronisation per Newton-Raphson pass).  Replaces the one-run-per-input
  * loop of multi/multirun.f90; no reference counterpart for the mode itself.  */
 NDSPH_API int ndsph_batch_set_graph(ndsph_ctx* ctx, int32_t mode);
@@ -303,6 +307,7 @@ typedef struct ndsph_timing {
     int32_t graph_steps;     /* batched steps run as a captured CUDA graph      */
     int32_t graph_redos;     /* of those, steps redone on the eager path        */
     int32_t nl_reused;       /* steps that kept the previous link and rows      */
+    int32_t fused_steps;     /* batched steps run by the fused per-tube kernel   */
 } ndsph_timing;
 NDSPH_API int ndsph_get_timing(ndsph_ctx* ctx, ndsph_timing* t);
 

@@ -66,6 +66,7 @@ class NdsphTiming(C.Structure):
         ("launches", C.c_int32), ("pairs_density", C.c_int64), ("pairs_rates", C.c_int64),
         ("mlp_loss", C.c_float), ("mlp_ms", C.c_float), ("mlp_updates", C.c_int32), ("nl_builds", C.c_int32),
         ("graph_steps", C.c_int32), ("graph_redos", C.c_int32), ("nl_reused", C.c_int32),
+        ("fused_steps", C.c_int32),
     ]
 
     def as_dict(self) -> dict:

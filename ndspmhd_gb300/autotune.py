@@ -137,6 +137,7 @@ def _time_batched(opts: dict, state: dict, sim, nsim: int, tuning: dict, steps: 
     try:
         g.set_tuning(**tuning)
         g.batch_upload(sim, nsim, initialise=True)
+        g.batch_set_graph(2)   # the captured step, whose cells the knobs size
         g.batch_step(warmup)
         g.batch_step(steps)
         return g.timing()["total_ms"] / steps
@@ -146,8 +147,10 @@ def _time_batched(opts: dict, state: dict, sim, nsim: int, tuning: dict, steps: 
 
 def tune_batched(opts: dict, state: dict, sim, nsim: int, candidates=None, steps: int = 20,
                  warmup: int = 3, use_cache: bool = True) -> dict:
-    """Fastest tuning of the batched captured step (cell margin, skin) for
-    this batch; ``state`` holds the primitive inputs batch_upload takes."""
+    """Fastest tuning of the batched captured-graph step (cell margin, skin)
+    for this batch; ``state`` holds the primitive inputs batch_upload takes.
+    (The fused per-tube step of 1D batches has no such knobs: its cells are
+    each tube's own.)"""
     key = signature(opts, state["x"].shape[0], batched=True)
     if use_cache:
         hit = load_cache().get(key)

@@ -150,7 +150,15 @@ struct ndsph_ctx {
     PtrState gptr[2];
     int gparity = 0;
     bool gvalid = false;
-    int graph_mode = 1;          // 1: batched steps run as captured graphs when possible
+    int graph_mode = 1;          // 1: one launch per batched step (fused per-tube kernel for 1D
+                                 //    batches, else a captured graph); 2: captured graph; 0: eager
+    // fused per-tube step (1D batches): tube slot ranges and launch order
+    int* d_tube_start = nullptr;
+    int* d_tube_order = nullptr;
+    int tube_maxm = 0;           // largest tube; 0: the batch does not qualify
+    int tube_cap = 0;
+    int fsteps = 0;              // steps run by the fused per-tube kernel
+    bool tubes_valid = false;    // ranges match the slot order (reset by every link)
     int gredo = 0;               // captured steps redone on the eager path
     int gsteps = 0;              // captured steps launched
     double g_hmax = 0.0;         // max h the graph's cells were sized for
@@ -573,6 +581,8 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
                             ctx->ev_pfork, ctx->ev_pjoin, ctx->ev_g})
         if (ev) cudaEventDestroy(ev);
     if (ctx->d_live) cudaFree(ctx->d_live);
+    if (ctx->d_tube_start) cudaFree(ctx->d_tube_start);
+    if (ctx->d_tube_order) cudaFree(ctx->d_tube_order);
     if (ctx->st2) cudaStreamDestroy(ctx->st2);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -1088,6 +1098,7 @@ static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hma
 static void link_sort_gather(ndsph_ctx* ctx, const int* d_fields, int nfields, cudaStream_t st)
 {
     ctx->packs_valid = false;
+    ctx->tubes_valid = false;
     const int n = ctx->n;
     launch_cell_key(ctx->F, ctx->g, ctx->o, n, ctx->srt, ctx->red, st);
     launch_scan(ctx->srt, ctx->g.ncells, st);
@@ -2282,7 +2293,7 @@ static void graph_drop(ndsph_ctx* ctx)
 
 static bool graph_usable(const ndsph_ctx* ctx)
 {
-    return ctx->graph_mode == 1 && ctx->o.batched && !ctx->opts.learned_h && !ctx->profiling &&
+    return ctx->graph_mode >= 1 && ctx->o.batched && !ctx->opts.learned_h && !ctx->profiling &&
            ctx->o.maxdensits >= 1 && ctx->n > 0;
 }
 
@@ -2525,6 +2536,77 @@ static int batch_step_graph(ndsph_ctx* ctx)
     return 0;
 }
 
+// The fused per-tube step needs every simulation's particles in one run of
+// slots, simulations in order (as the link leaves a 1D batch: simulation s
+// sits at x offset s (2 L + 1)), and each tube small enough for one block's
+// shared memory.  Ranges and a largest-first launch order are set up after
+// every link.
+static int tubes_prepare(ndsph_ctx* ctx)
+{
+    if (ctx->tubes_valid) return 0;
+    ctx->tube_maxm = 0;
+    ctx->tubes_valid = true;
+    const int n = ctx->n, ns = ctx->nsim;
+    if (n <= 0 || ns <= 0) return 0;
+    std::vector<int> sim(n);
+    CK(cudaStreamSynchronize(ctx->st));
+    CK(cudaMemcpy(sim.data(), ctx->S.sim, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+    std::vector<int> start(ns + 1, 0), cnt(ns, 0);
+    for (int k = 0; k < n; k++) {
+        if (sim[k] < 0 || sim[k] >= ns || (k > 0 && sim[k] < sim[k - 1])) return 0;   // not in order
+        cnt[sim[k]]++;
+    }
+    int maxm = 0;
+    for (int q = 0; q < ns; q++) {
+        if (cnt[q] == 0) return 0;
+        start[q + 1] = start[q] + cnt[q];
+        maxm = std::max(maxm, cnt[q]);
+    }
+    if (maxm > TUBE_MAX) return 0;
+    std::vector<int> order(ns);
+    for (int q = 0; q < ns; q++) order[q] = q;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cnt[x] > cnt[y]; });
+    if (!ctx->d_tube_start) {
+        CK(cudaMalloc(&ctx->d_tube_start, sizeof(int) * (size_t)(ns + 1)));
+        CK(cudaMalloc(&ctx->d_tube_order, sizeof(int) * (size_t)ns));
+        ctx->tube_cap = ns;
+    } else if (ns > ctx->tube_cap) {
+        cudaFree(ctx->d_tube_start);
+        cudaFree(ctx->d_tube_order);
+        ctx->d_tube_start = ctx->d_tube_order = nullptr;
+        CK(cudaMalloc(&ctx->d_tube_start, sizeof(int) * (size_t)(ns + 1)));
+        CK(cudaMalloc(&ctx->d_tube_order, sizeof(int) * (size_t)ns));
+        ctx->tube_cap = ns;
+    }
+    CK(cudaMemcpy(ctx->d_tube_start, start.data(), sizeof(int) * (size_t)(ns + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_tube_order, order.data(), sizeof(int) * (size_t)ns, cudaMemcpyHostToDevice));
+    ctx->tube_maxm = maxm;
+    return 0;
+}
+
+static bool fused_usable(const ndsph_ctx* ctx)
+{
+    return ctx->graph_mode == 1 && ctx->o.batched && ctx->o.ndim == 1 && !ctx->opts.learned_h &&
+           !ctx->profiling && ctx->o.maxdensits >= 1 && ctx->n > 0 && ctx->linked;
+}
+
+// one leapfrog step of every tube in one launch (k_tube_step); false in
+// *done when the batch does not qualify
+static int batch_step_fused(ndsph_ctx* ctx, bool* done)
+{
+    *done = false;
+    int rc = tubes_prepare(ctx);
+    if (rc) return rc;
+    if (ctx->tube_maxm <= 0) return 0;
+    SweepArgs a = sweep_args(ctx);
+    launch_tube_step(a, ctx->d_tube_start, ctx->d_tube_order, ctx->nsim, ctx->d_sim_dtnext, ctx->d_sim_out,
+                     ctx->tube_maxm, ctx->st);
+    CK(cudaGetLastError());
+    *done = true;
+    ctx->fsteps++;
+    return sync_red(ctx);
+}
+
 extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, double* time_out)
 {
     GUARD_CTX();
@@ -2533,8 +2615,15 @@ extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, 
     const long long l0 = ndsph_launch_counter().load();
     CK(cudaEventRecord(ctx->ev[10], st));
     for (int k = 0; k < nsteps; k++) {
-        const int rc = graph_usable(ctx) ? batch_step_graph(ctx) : batch_step_eager(ctx);
-        if (rc) return rc;
+        bool done = false;
+        if (fused_usable(ctx)) {
+            const int rc = batch_step_fused(ctx, &done);
+            if (rc) return rc;
+        }
+        if (!done) {
+            const int rc = graph_usable(ctx) ? batch_step_graph(ctx) : batch_step_eager(ctx);
+            if (rc) return rc;
+        }
         ctx->nsteps++;
     }
     CK(cudaEventRecord(ctx->ev[11], st));
@@ -2547,6 +2636,7 @@ extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, 
     ctx->timing.launches = (int32_t)(ndsph_launch_counter().load() - l0);
     ctx->timing.graph_steps = ctx->gsteps;
     ctx->timing.graph_redos = ctx->gredo;
+    ctx->timing.fused_steps = ctx->fsteps;
     for (int s2 = 0; s2 < ctx->nsim; s2++) {
         if (dt_out) dt_out[s2] = ctx->h_sim_out[s2 * 4 + 2];
         if (time_out) time_out[s2] = ctx->h_sim_out[s2 * 4 + 3];
@@ -2566,7 +2656,7 @@ extern "C" int ndsph_set_host_access(ndsph_ctx* ctx, int32_t mode)
 extern "C" int ndsph_batch_set_graph(ndsph_ctx* ctx, int32_t mode)
 {
     GUARD_CTX();
-    if (mode != 0 && mode != 1) { ctx->err = "graph mode must be 0 or 1"; return NDSPH_E_ARG; }
+    if (mode < 0 || mode > 2) { ctx->err = "batched step mode must be 0, 1 or 2"; return NDSPH_E_ARG; }
     graph_drop(ctx);
     ctx->graph_mode = mode;
     return 0;

@@ -168,6 +168,12 @@ void launch_sim_dt_advance(double* dt, const double* dtnext, int nsim, const Red
 // ---- sweeps (ndsph_sweeps.cu) --------------------------------------------
 void launch_density(const SweepArgs& a, bool full, cudaStream_t st);
 void launch_rates(const SweepArgs& a, cudaStream_t st);
+// fused step of a 1D batch, one block per tube (tubes contiguous in slots;
+// tube_start[nsim+1], order[nsim] largest first; maxm the largest tube)
+constexpr int TUBE_MAX = 4096;
+size_t tube_smem_bytes(int maxm);
+void launch_tube_step(const SweepArgs& a, const int* tube_start, const int* order, int nsim, double* dt_next,
+                      double* sim_out, int maxm, cudaStream_t st);
 void launch_pack_v(const SweepArgs& a, cudaStream_t st);
 void launch_build_nlist(const SweepArgs& a, cudaStream_t st);
 void launch_pack_rates(const SweepArgs& a, cudaStream_t st);

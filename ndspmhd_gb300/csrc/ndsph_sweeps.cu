@@ -295,19 +295,17 @@ struct KSum {
 // ===========================================================================
 // density + Newton-Raphson
 // ===========================================================================
-template <int NDIM, bool FULL, int PREC>
-__global__ void __launch_bounds__(128) k_density(SweepArgs a)
+// Candidate sources of the two sweeps: RowSrc walks the slot's neighbour row
+// (the sweeps' own loops, below); a source with kRows = false supplies the
+// candidates itself through for_each(i, f), calling f(pk) with entries
+// packed as in the rows, (j << shift) | stencil offset of j's cell.
+struct RowSrc {
+    static constexpr bool kRows = true;
+};
+
+template <int NDIM, bool FULL, int PREC, class Src>
+__device__ __forceinline__ void density_body(const SweepArgs& a, const int i, const Src& src)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    int i;
-    if (FULL) {
-        if (t >= a.n) return;
-        i = t;
-    } else {
-        const int nlist = a.d_nlist ? *a.d_nlist : a.nlist;
-        if (t >= nlist) return;
-        i = a.S.active[t];
-    }
     const FieldPtrs& F = a.F;
     const DevOpts& o = a.o;
     const Grid& g = a.g;
@@ -339,8 +337,6 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
     int nn = 0;
 
     Stencil<NDIM> stn(a.S.cell[i], g);
-    const int ncand = a.S.nl_cnt[i];
-    const unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
     // one candidate: its list entry, position and type, and (FP32 form) its
     // velocity/mass pack, loaded by the caller
     const unsigned shift = (NDIM == 3) ? (unsigned)g.nlshift : 5u, omask = (1u << shift) - 1u;
@@ -428,7 +424,16 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
             sums32(j, q2i, dxf, pvj);
         }
     };
-    if (PREC == NDSPH_PREC_FP64) {
+    if constexpr (!Src::kRows) {
+        const bool typed = (PREC == NDSPH_PREC_FP64 || o.idust != 0);
+        src.for_each(i, [&](unsigned pk) {
+            const int j = (int)(pk >> shift);
+            pair(pk, a.S.xs[j], typed ? a.S.itype[j] : typei,
+                 PREC == NDSPH_PREC_FP64 ? make_float4(0.f, 0.f, 0.f, 0.f) : a.S.pk_v[j]);
+        });
+    } else if (PREC == NDSPH_PREC_FP64) {
+        const int ncand = a.S.nl_cnt[i];
+        const unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int k = 0; k < ncand; k++) {
             const unsigned pk = row[k];
@@ -436,6 +441,8 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
             pair(pk, a.S.xs[j], a.S.itype[j], z4);
         }
     } else {
+        const int ncand = a.S.nl_cnt[i];
+        const unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
         // FP32 form: four candidates' loads in flight at once (the pair work
         // is short, so the loop is bound by load latency otherwise)
         // rows are 16-byte aligned with a stride of a multiple of 4 entries
@@ -584,7 +591,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
             }
         }
         if (hnew > bitsd(a.red->hmax_ghost)) relink = true;
-        if ((float)hnew + a.nl_dmax > a.S.hb[i] * a.nl_skin) a.red->nl_stale = 1;
+        if (Src::kRows && (float)hnew + a.nl_dmax > a.S.hb[i] * a.nl_skin) a.red->nl_stale = 1;
     } else {
         drhodt = drhodt * gradh;
         F.f[DHDT][i] = (double)(dhdrhoi * drhodt);
@@ -600,6 +607,22 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
     F.f[GRADH][i] = (double)gradh;
     F.f[GRADHN][i] = (double)gradhn;
     F.f[GRADGRADH][i] = (double)gradgradh;
+}
+
+template <int NDIM, bool FULL, int PREC>
+__global__ void __launch_bounds__(128) k_density(SweepArgs a)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int i;
+    if (FULL) {
+        if (t >= a.n) return;
+        i = t;
+    } else {
+        const int nlist = a.d_nlist ? *a.d_nlist : a.nlist;
+        if (t >= nlist) return;
+        i = a.S.active[t];
+    }
+    density_body<NDIM, FULL, PREC>(a, i, RowSrc{});
 }
 
 void launch_density(const SweepArgs& a, bool full, cudaStream_t st)
@@ -694,15 +717,13 @@ constexpr int RATES_BS = 128;      // threads per block of the rates sweep
 // accepted entries per thread per chunk of the 3D FP32 rows (~90 candidates)
 template <int NDIM>
 constexpr int rates_chunk() { return NDSPH_RATES_CHUNK; }
-template <int NDIM, int PREC>
-__global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_rates(SweepArgs a)
+// every lane of a warp calls it together (the reductions at its end are warp
+// shuffles, and block-wide in a one-simulation FP32 sweep): `live` false runs
+// an empty candidate set on slot i
+template <int NDIM, int PREC, class Src>
+__device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, const bool live, const Src& src)
 {
     typedef typename std::conditional<PREC == NDSPH_PREC_FP64, double, float>::type R;
-    // no early return: every lane of the warp takes part in the final
-    // shuffle reductions; lanes past n run an empty stencil on slot 0
-    const int ithread = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = ithread < (a.plist ? a.pn : a.n);
-    const int i = live ? (a.plist ? a.plist[a.pi0 + ithread] : ithread) : 0;
     const FieldPtrs& F = a.F;
     const DevOpts& o = a.o;
     const Grid& g = a.g;
@@ -762,8 +783,6 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
     R dtc_h = (R)1.e6, dtc_v = 1, dtav_h = (R)3.0e38, dtav_v = 1;
 
     Stencil<NDIM> stn(a.S.cell[i], g);
-    const int ncand = live ? a.S.nl_cnt[i] : 0;
-    const unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
     // the terms of one candidate pair (rates_core, artificial_dissipation,
     // mhd_terms, drag_forces for the pair (i, j)); returns early when the
     // pair is out of range
@@ -1040,11 +1059,17 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
                 if (typei == NDSPH_ITYPE_GAS) du.add(mj * dragterm_en);
             }
     };
-    if constexpr (PREC == NDSPH_PREC_FP64 || NDIM < 3) {
+    if constexpr (!Src::kRows) {
+        if (live) src.for_each(i, [&](unsigned pk) { pair_terms(pk, nullptr, 0); });
+    } else if constexpr (PREC == NDSPH_PREC_FP64 || NDIM < 3) {
         // the FP64 form, and short 1D/2D rows (~8 / ~25 entries, most of them
         // accepted), take one pass over the row
+        const int ncand = live ? a.S.nl_cnt[i] : 0;
+        const unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
         for (int k = 0; k < ncand; k++) pair_terms(row[k], nullptr, 0);
     } else {
+        const int ncand = live ? a.S.nl_cnt[i] : 0;
+        const unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
         // Two phases per chunk of the row: screen the candidates (four row
         // entries and positions in flight at a time) and keep the accepted
         // entries in shared memory, then run the pair terms over those only,
@@ -1267,22 +1292,28 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
 
 // FP32 packs (FP32 form): velocities + masses before the density passes,
 // everything the rates sweep reads after the EOS
-__global__ void k_pack_v(SweepArgs a)
+__device__ __forceinline__ void pack_v_one(const SweepArgs& a, int k)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.n) return;
     const FieldPtrs& F = a.F;
     a.S.pk_v[k] = make_float4((float)F.f[V0][k], (float)F.f[V1][k], (float)F.f[V2][k], (float)F.f[PM][k]);
 }
-__global__ void k_pack_rates(SweepArgs a)
+__device__ __forceinline__ void pack_rates_one(const SweepArgs& a, int k)
 {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.n) return;
     const FieldPtrs& F = a.F;
     a.S.pk_v[k] = make_float4((float)F.f[V0][k], (float)F.f[V1][k], (float)F.f[V2][k], (float)F.f[PM][k]);
     a.S.pk_t[k] = make_float4((float)F.f[RHO][k], (float)fmax(F.f[PR][k], 0.0), (float)F.f[CS][k], (float)F.f[UU][k]);
     a.S.pk_b[k] = make_float4((float)F.f[BF0][k], (float)F.f[BF1][k], (float)F.f[BF2][k], (float)F.f[GRADH][k]);
     a.S.pk_a[k] = make_float4((float)F.f[AL0][k], (float)F.f[AL1][k], (float)F.f[AL2][k], (float)F.f[HH][k]);
+}
+__global__ void k_pack_v(SweepArgs a)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < a.n) pack_v_one(a, k);
+}
+__global__ void k_pack_rates(SweepArgs a)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < a.n) pack_rates_one(a, k);
 }
 void launch_pack_v(const SweepArgs& a, cudaStream_t st)
 {
@@ -1291,6 +1322,17 @@ void launch_pack_v(const SweepArgs& a, cudaStream_t st)
 void launch_pack_rates(const SweepArgs& a, cudaStream_t st)
 {
     if (a.n > 0) NDSPH_COUNT_LAUNCH, k_pack_rates<<<nblk(a.n, 256), 256, 0, st>>>(a);
+}
+
+template <int NDIM, int PREC>
+__global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_rates(SweepArgs a)
+{
+    // no early return: every lane of the warp takes part in the final
+    // shuffle reductions; lanes past n run an empty stencil on slot 0
+    const int ithread = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = ithread < (a.plist ? a.pn : a.n);
+    const int i = live ? (a.plist ? a.plist[a.pi0 + ithread] : ithread) : 0;
+    rates_body<NDIM, PREC>(a, i, live, RowSrc{});
 }
 
 void launch_rates(const SweepArgs& a, cudaStream_t st)
@@ -1310,6 +1352,380 @@ void launch_rates(const SweepArgs& a, cudaStream_t st)
     }
 }
 
+
+
+// ===========================================================================
+// Fused step of a batch of 1D simulations (the tubes of a parameter sweep):
+// one block per tube runs the whole leapfrog step of its tube -- predictor,
+// order by x, every Newton-Raphson density pass, EOS, rates, the tube's dt
+// and the corrector -- in one launch for all tubes, with no global sort,
+// permutation gather or neighbour rows (stepND_leapfrog_mhd.f90:31-275 with
+// derivs.f90:27-287 per tube, as the reference runs one tube per process,
+// multi/multirun.f90).  The particles stay in their slots; each tube keeps
+// an order by x in shared memory, and a particle's candidates are the run of
+// that order within 2 max(h_i, h_j) of it: scanning away from it stops at the
+// first particle farther than twice the largest h of every particle beyond
+// (prefix / suffix maxima of h), so no pair is missed.  The candidates reach
+// the density and rates sweeps' own per-particle bodies packed as neighbour-
+// row entries, over cells of the tube's own grid (8 cells to 2 hmax), so the
+// pair arithmetic and the Newton-Raphson semantics are the sweeps'.
+// ===========================================================================
+constexpr int TUBE_BS = 128;
+
+// candidates of slot i of a tube in x order (see above)
+struct TubeWin {
+    static constexpr bool kRows = false;
+    const float* X;      // [m] x - (tube's smallest x), in x order
+    const float* H;      // [m] h rounded up, in x order
+    const float* PMX;    // [m] prefix max of H
+    const float* SMX;    // [m] suffix max of H
+    const int* idx;      // [m] x order -> slot
+    const int* pos;      // [m] slot - t0 -> x order
+    const int* cell;     // cell of each slot (tube grid)
+    const int* id;
+    Reduce* red;
+    int t0, m;
+    template <class Fn>
+    __device__ __forceinline__ void for_each(int i, Fn&& f) const
+    {
+        const int k = pos[i - t0];
+        const int ci = cell[i];
+        const float xk = X[k], hk = H[k];
+        auto emit = [&](int j) {
+            const int d = cell[j] - ci;
+            // the tube grid puts every candidate within 8 cells (checked)
+            if (d < -8 || d > 8) {
+                raise_err(red, NDSPH_E_CELLS, id[i]);
+                return;
+            }
+            f(((unsigned)j << 5) | (unsigned)(d + 8));
+        };
+        // in increasing x, the order the cell-sorted rows give (sums in a
+        // shock tube are sensitive to their order: the cell path, the
+        // reference and this one then round alike)
+        int q0 = k;
+        while (q0 > 0 && xk - X[q0 - 1] < 2.0f * fmaxf(hk, PMX[q0 - 1]) * 1.001f + 2e-6f) q0--;
+        for (int q = q0; q < k; q++) emit(idx[q]);
+        emit(i);
+        for (int q = k + 1; q < m; q++) {
+            if (X[q] - xk >= 2.0f * fmaxf(hk, SMX[q]) * 1.001f + 2e-6f) break;
+            emit(idx[q]);
+        }
+    }
+};
+
+struct TubeShared {
+    double cs;       // cell size of the tube grid in use (0: none yet)
+    int ncalc, bad;
+};
+
+// block-wide max / min of one double per thread
+__device__ __forceinline__ double tube_block_max(double v, double* scratch)
+{
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = scratch[0];
+    for (int w = 1; w < TUBE_BS / 32; w++) r = fmax(r, scratch[w]);
+    __syncthreads();
+    return r;
+}
+__device__ __forceinline__ double tube_block_min(double v, double* scratch)
+{
+    return -tube_block_max(-v, scratch);
+}
+
+// inclusive running max of a[0..m) from the front (dir = +1) or the back
+// (dir = -1) into out: each thread scans a contiguous chunk, the chunk
+// maxima are combined, then applied
+__device__ __forceinline__ void tube_running_max(const float* a, float* out, int m, int dir, float* part)
+{
+    const int per = (m + TUBE_BS - 1) / TUBE_BS;
+    const int c0 = threadIdx.x * per, c1 = min(c0 + per, m);
+    float run = 0.f;
+    for (int q = c0; q < c1; q++) {
+        const int k = (dir > 0) ? q : (m - 1 - q);
+        run = fmaxf(run, a[k]);
+        out[k] = run;
+    }
+    part[threadIdx.x] = run;
+    __syncthreads();
+    float before = 0.f;
+    for (int t = 0; t < (int)threadIdx.x; t++) before = fmaxf(before, part[t]);
+    for (int q = c0; q < c1; q++) {
+        const int k = (dir > 0) ? q : (m - 1 - q);
+        out[k] = fmaxf(out[k], before);
+    }
+    __syncthreads();
+}
+
+struct TubeArgs {
+    SweepArgs a;
+    const int* tube_start;   // [nsim + 1] first slot of each tube (tubes are contiguous)
+    const int* order;        // [nsim] tubes, largest first
+    double* dt_next;         // [nsim] the next step's dt of each tube
+    double* sim_out;         // [nsim * 4] dtcourant, dtforce, dt next, time
+};
+
+template <int PREC>
+__global__ void __launch_bounds__(TUBE_BS) k_tube_step(TubeArgs T)
+{
+    extern __shared__ __align__(16) unsigned char tube_smem[];
+    __shared__ TubeShared sh;
+    __shared__ double red_scratch[TUBE_BS / 32];
+    __shared__ float part[TUBE_BS];
+    // the sweeps' arguments with this tube's grid, pass number and active
+    // list: one copy per block in shared memory, changed by thread 0 between
+    // barriers
+    __shared__ __align__(16) unsigned char a_raw[sizeof(SweepArgs)];
+    SweepArgs& a = *reinterpret_cast<SweepArgs*>(a_raw);
+    const int s = T.order[blockIdx.x];
+    const int t0 = T.tube_start[s], m = T.tube_start[s + 1] - t0;
+    const int tid = threadIdx.x;
+    if (tid == 0) a = T.a;
+    __syncthreads();
+    const FieldPtrs& F = T.a.F;
+    const Side& S = T.a.S;
+    const DevOpts& o = T.a.o;
+    float* X = reinterpret_cast<float*>(tube_smem);
+    float* H = X + m;
+    float* PMX = H + m;
+    float* SMX = PMX + m;
+    int* idx = reinterpret_cast<int*>(SMX + m);
+    int* pos = idx + m;
+    const double dt = o.sim_dt[s];
+
+    // ---- reductions of this tube start afresh; predictor
+    if (tid == 0) {
+        unsigned long long* r = o.sim_red + (size_t)s * SIMRED;
+        r[SR_DTC] = dbits(1.e6);
+        r[SR_DTAV] = dbits(1.7976931348623157e308);
+        r[SR_VSIG] = 0ull;
+        r[SR_TS] = dbits(1.7976931348623157e308);
+        r[SR_FH] = 0ull;
+        r[SR_STRESS] = 0ull;
+        sh.bad = 0;
+    }
+    for (int k = tid; k < m; k += TUBE_BS) predictor_one(F, S, o, dt, t0 + k, 0);
+    __syncthreads();
+    if (o.has_fixed) {
+        for (int k = tid; k < m; k += TUBE_BS) predictor_fixed_x_one(F, S, o, dt, t0 + k);
+        __syncthreads();
+    }
+
+    // ---- x order of the tube (a particle seldom passes another: checked,
+    // and ranked afresh when one has)
+    double xmin = 1.7976931348623157e308;
+    int bad = 0, unsorted = 0;
+    for (int k = tid; k < m; k += TUBE_BS) {
+        const double x = F.f[X0][t0 + k];
+        if (!isfinite(x)) bad = 1;
+        xmin = fmin(xmin, x);
+        if (k + 1 < m && F.f[X0][t0 + k + 1] < x) unsorted = 1;
+    }
+    if (__syncthreads_or(bad)) {
+        if (tid == 0) raise_err(a.red, NDSPH_E_NAN, S.id[t0]);
+        return;
+    }
+    xmin = tube_block_min(xmin, red_scratch);
+    if (__syncthreads_or(unsorted)) {
+        for (int k = tid; k < m; k += TUBE_BS) {
+            const double xk = F.f[X0][t0 + k];
+            int r = 0;
+            for (int q = 0; q < m; q++) {
+                const double xq = F.f[X0][t0 + q];
+                r += (xq < xk) || (xq == xk && q < k);
+            }
+            idx[r] = t0 + k;
+        }
+    } else {
+        for (int k = tid; k < m; k += TUBE_BS) idx[k] = t0 + k;
+    }
+    __syncthreads();
+    for (int k = tid; k < m; k += TUBE_BS) {
+        pos[idx[k] - t0] = k;
+        X[k] = (float)(F.f[X0][idx[k]] - xmin);
+    }
+    __syncthreads();
+
+    // ---- per pass: the tube grid and the window bounds from the current h
+    TubeWin win;
+    win.X = X; win.H = H; win.PMX = PMX; win.SMX = SMX; win.idx = idx; win.pos = pos;
+    win.cell = S.cell; win.id = S.id; win.red = a.red; win.t0 = t0; win.m = m;
+    // The cells (8 to 2 hmax with the window's margins) are set once a step
+    // with 10 % room for h to grow and set again only when some h outgrows
+    // them; 1/h and the FP32 h follow every pass.
+    if (tid == 0) sh.cs = 0.0;
+    auto prep = [&]() -> bool {
+        float hmf = 0.f;
+        for (int k = tid; k < m; k += TUBE_BS) {
+            const float h = (float)F.f[HH][idx[k]] * 1.000001f;
+            H[k] = h;
+            hmf = fmaxf(hmf, h);
+        }
+        const double hm = tube_block_max((double)hmf, red_scratch);
+        if (!(hm > 0.0) || !isfinite(hm)) return false;
+        const bool regrid = (2.0 * hm * 1.002 + 4e-6) > 7.5 * sh.cs;
+        if (regrid) {
+            const double cs = (2.0 * hm * 1.1 + 4e-6) / 7.5;
+            const double origin = xmin - cs;
+            const double inv_cs = 1.0 / cs;
+            for (int k = tid; k < m; k += TUBE_BS) {
+                const int i = t0 + k;
+                const double x = F.f[X0][i];
+                const int c = (int)floor((x - origin) * inv_cs);
+                S.cell[i] = c;
+                S.xs[i] = make_float4((float)(x - (origin + (double)c * cs)), 0.f, 0.f, 0.f);
+            }
+            __syncthreads();
+            if (tid == 0) {
+                sh.cs = cs;
+                a.g.nc[0] = 1 << 30; a.g.nc[1] = 1; a.g.nc[2] = 1;
+                a.g.ncells = 1 << 30;
+                a.g.origin[0] = origin; a.g.cs[0] = cs; a.g.inv_cs[0] = inv_cs; a.g.csf[0] = (float)cs;
+                a.g.sw = 17;
+                a.g.nlshift = 5;
+            }
+        }
+        for (int k = tid; k < m; k += TUBE_BS) {
+            const int i = t0 + k;
+            const double h = F.f[HH][i];
+            S.xs[i].w = (float)h;
+            S.h1[i] = 1.0 / h;
+        }
+        tube_running_max(H, PMX, m, +1, part);
+        tube_running_max(H, SMX, m, -1, part);
+        return true;
+    };
+
+    // ---- iterate_density (iterate_density.f90:43-360) over the tube
+    for (int k = tid; k < m; k += TUBE_BS) {
+        density_init_one(F, S, t0 + k, a.red);
+        if (PREC == NDSPH_PREC_FP32) pack_v_one(a, t0 + k);
+    }
+    if (tid == 0) {
+        a.d_its = nullptr;
+        a.d_nlist = nullptr;
+        a.ncalc_next = &sh.ncalc;
+    }
+    __syncthreads();
+    int* act = S.active + t0;
+    int* act_next = S.active_next + t0;
+    int its = 0, ncalc = m;
+    while (ncalc > 0 && its <= o.maxdensits) {
+        its++;
+        const bool full = (ncalc == m);
+        if (full && its > 1) {
+            for (int k = tid; k < m; k += TUBE_BS) F.f[HNEXT][t0 + k] = F.f[HH][t0 + k];
+        }
+        if (!prep()) {
+            if (tid == 0) raise_err(a.red, NDSPH_E_H_NONPOS, S.id[t0]);
+            return;
+        }
+        if (tid == 0) {
+            sh.ncalc = 0;
+            a.its = its;
+            a.S.active_next = act_next;
+        }
+        __syncthreads();
+        if (full) {
+            for (int k = tid; k < m; k += TUBE_BS) density_body<1, true, PREC>(a, idx[k], win);
+        } else {
+            for (int k = tid; k < ncalc; k += TUBE_BS) density_body<1, false, PREC>(a, act[k], win);
+        }
+        __syncthreads();
+        if (full)
+            for (int k = tid; k < m; k += TUBE_BS) F.f[HH][t0 + k] = F.f[HNEXT][t0 + k];
+        __syncthreads();
+        if (o.has_fixed) {
+            for (int k = tid; k < m; k += TUBE_BS) fixed_density_copy_one(F, S, t0 + k);
+            __syncthreads();
+        }
+        ncalc = sh.ncalc;
+        int* tmp = act; act = act_next; act_next = tmp;
+        __syncthreads();
+    }
+    if (its > o.maxdensits && o.maxdensits > 0) {
+        if (tid == 0) raise_err(a.red, NDSPH_E_NOT_CONVERGED, S.id[t0]);
+        return;
+    }
+
+    // ---- conservative2primitive + EOS, fixed-particle copies
+    double st = 0.0;
+    for (int k = tid; k < m; k += TUBE_BS) st = fmax(st, eos_one(F, S, o, t0 + k, a.red));
+    st = tube_block_max(st, red_scratch);
+    if (tid == 0 && st > 0.0) o.sim_red[(size_t)s * SIMRED + SR_STRESS] = dbits(st);
+    if (o.has_fixed) {
+        for (int k = tid; k < m; k += TUBE_BS) fixed_copy_one(F, S, t0 + k);
+        __syncthreads();
+    }
+    if (PREC == NDSPH_PREC_FP32) {
+        for (int k = tid; k < m; k += TUBE_BS) pack_rates_one(a, t0 + k);
+    }
+    __syncthreads();
+
+    // ---- get_rates over the tube (every lane of each warp takes part)
+    if (!prep()) {
+        if (tid == 0) raise_err(a.red, NDSPH_E_H_NONPOS, S.id[t0]);
+        return;
+    }
+    __syncthreads();
+    for (int k0 = 0; k0 < m; k0 += TUBE_BS) {
+        const int k = k0 + tid;
+        const bool live = k < m;
+        rates_body<1, PREC>(a, live ? idx[k] : idx[0], live, win);
+    }
+    __syncthreads();
+
+    // ---- the tube's next dt (stepND_leapfrog_mhd.f90:252) and its clock
+    if (tid == 0) {
+        const unsigned long long* r = o.sim_red + (size_t)s * SIMRED;
+        const double dtcourant = bitsd(r[SR_DTC]);
+        const double fhmax = bitsd(r[SR_FH]);
+        double dtforce = 1.7976931348623157e308;
+        if (fhmax > 0.0) dtforce = fmin(dtforce, sqrt(1.0 / fhmax));
+        double dtdrag = 1.7976931348623157e308;
+        if (o.idust == 2 && o.idrag_nature != 0 && (o.Kdrag > 0.0 || o.idrag_nature > 1))
+            dtdrag = fmin(dtdrag, bitsd(r[SR_TS]));
+        double dtn = o.C_force * dtforce;
+        dtn = fmin(dtn, o.C_cour * dtcourant);
+        dtn = fmin(dtn, 0.9 * dtdrag);
+        dtn = fmin(dtn, o.C_force * 1.7976931348623157e308);
+        T.dt_next[s] = dtn;
+        T.sim_out[s * 4 + 0] = dtcourant;
+        T.sim_out[s * 4 + 1] = dtforce;
+        T.sim_out[s * 4 + 2] = dtn;
+        T.sim_out[s * 4 + 3] += dt;
+    }
+    // ---- corrector
+    for (int k = tid; k < m; k += TUBE_BS) corrector_one(F, S, o, dt, t0 + k, a.red);
+    __syncthreads();
+    if (tid == 0) o.sim_dt[s] = T.dt_next[s];
+}
+
+size_t tube_smem_bytes(int maxm) { return (size_t)maxm * (4 * sizeof(float) + 2 * sizeof(int)); }
+
+void launch_tube_step(const SweepArgs& a, const int* tube_start, const int* order, int nsim, double* dt_next,
+                      double* sim_out, int maxm, cudaStream_t st)
+{
+    TubeArgs T;
+    T.a = a;
+    T.tube_start = tube_start;
+    T.order = order;
+    T.dt_next = dt_next;
+    T.sim_out = sim_out;
+    const size_t smem = tube_smem_bytes(maxm);
+    // (128 registers a thread: 4 blocks, 16 warps per SM; forcing 5 blocks
+    // spilled and was 8 % slower)
+    if (a.o.precision == NDSPH_PREC_FP64) {
+        cudaFuncSetAttribute(k_tube_step<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        NDSPH_COUNT_LAUNCH, k_tube_step<0><<<nsim, TUBE_BS, smem, st>>>(T);
+    } else {
+        cudaFuncSetAttribute(k_tube_step<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        NDSPH_COUNT_LAUNCH, k_tube_step<1><<<nsim, TUBE_BS, smem, st>>>(T);
+    }
+}
 
 // ===========================================================================
 // neighbour lists: every candidate j (self included) of slot i with
