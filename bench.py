@@ -46,7 +46,13 @@ UNIT = "particle-updates/s"
 # force(3) dBevol/dt(3) du/dt de/dt dalpha/dt(3) divB curlB(3) del2u
 # graddivv(3) drhodt dhdt (21 doubles) once each
 RATES_BYTES_PER_PARTICLE = (26 + 21) * 8
-RATES_DRAM_BYTES_64 = 146.7e6
+# ncu of one k_rates<3,FP32> launch of the 64^3 box (profiles/k_rates_mhd_box3d_64cubed_fp32.md):
+# DRAM bytes read + written, warp instructions issued, and the ratios that explain it
+RATES_DRAM_BYTES_64 = 146.3e6
+RATES_WARP_INSTR_64 = 280.6e6
+RATES_NCU_64 = {"issue_active_frac": 0.598, "threads_per_instruction": 29.4, "warps_active_frac": 0.223,
+                "fma_pipe_frac": 0.419, "top_stalls_per_issue": {"long_scoreboard": 1.47, "wait": 1.46}}
+SMS, SMSP_PER_SM = 152, 4
 # density pass: reads x(3) h m v(3) (8 doubles) writes rho rhoalt drhodt dhdt
 # gradh gradhn gradgradh h (8 doubles) + numneigh (4 B)
 DENSITY_BYTES_PER_PARTICLE = 16 * 8 + 4
@@ -664,12 +670,20 @@ def main():
     # DRAM bytes of one k_rates<3,FP32> launch from an ncu capture of the 64^3 box
     # (127.8 MB read + 18.7 MB written), scaled by the particle count
     traffic = round(RATES_DRAM_BYTES_64 * n / 64 ** 3)
+    # the sweep's issue rate, live: warp instructions of one launch (the 64^3
+    # capture scaled by N) over the slots of 152 SMs x 4 schedulers at the
+    # clock sampled during the timed steps
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    warp_instr = RATES_WARP_INSTR_64 * n / 64 ** 3
+    issue_frac = warp_instr / (rates_ms * 1e-3 * SMS * SMSP_PER_SM * sm_mhz * 1e6) if rates_ms > 0 else 0.0
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": traffic, "traffic_note": "ncu dram bytes of the 64^3 launch x N/64^3",
                 "kernel": "k_rates<3,FP32> (rates sweep)",
-                "issue_view": {"issue_active_frac": 0.564, "threads_per_instruction": 29.4, "warps_active_frac": 0.222,
-                               "source": "ncu --set full of the 64^3 launch: the sweep is bound by instruction "
-                                         "issue and load latency"},
+                "issue_view": dict(RATES_NCU_64, **{
+                    "issue_frac_live": round(issue_frac, 4),
+                    "issue_note": "the sweep is bound by FP32 instruction issue: issue_frac_live = warp instructions "
+                                  "per launch / (rates time x 152 SMs x 4 schedulers x SM clock); the other "
+                                  "figures from ncu --set full of the 64^3 launch"}),
                 "note": f"peak of {peak_kind} (MEASURED_PEAKS.json hbm_gbs); algorithmic bytes "
                         f"{RATES_BYTES_PER_PARTICLE} B/particle x {n}; the sweep is FP32-issue bound"}
     line = {
