@@ -219,8 +219,10 @@ NDSPH_API int ndsph_dev_set_time(ndsph_ctx* ctx, double dt, double time, int32_t
 
 /* ---- batched form --------------------------------------------------------------
  * `nsim` independent simulations with the same options (open or fixed
- * boundaries), in one device state: the batched counterpart of running the
- * reference once per input file (ndspmhd.f90:312-359, multi/multirun.f90).
+ * boundaries, or periodic in every dimension: each simulation then keeps its
+ * own periodic box, the same xmin/xmax for all), in one device state: the
+ * batched counterpart of running the reference once per input file
+ * (ndspmhd.f90:312-359, multi/multirun.f90).
  * sim[i] (0-based) names the simulation of particle i; ireal stays 1-based
  * over the whole array.  Each simulation keeps its own dt and clock (first
  * step dt = 0 as evolve.f90:50-56); reductions (dtcourant, dtforce,
@@ -237,6 +239,14 @@ NDSPH_API int ndsph_batch_download(ndsph_ctx* ctx, ndsph_particles* p);
  * it, as Grace over NVLink-C2C does), else through staging copies; 0 always
  * staging copies.  The results are the same either way.                      */
 NDSPH_API int ndsph_set_host_access(ndsph_ctx* ctx, int32_t mode);
+/* per-simulation drag constants K (dust.f90:91, idrag_nature = 1: the
+ * stopping time rho_i rho_j / (K (rho_i + rho_j))) of a batch whose runs
+ * differ in K, as their input files would: kdrag holds nsim values >= 0.
+ * Call it before ndsph_batch_upload so that the initialising derivs use them
+ * (they are kept for every later upload of nsim simulations); called on an
+ * uploaded batch of nsim simulations it also changes the next steps.
+ * Without it every simulation takes the options' Kdrag.                     */
+NDSPH_API int ndsph_batch_set_kdrag(ndsph_ctx* ctx, int32_t nsim, const double* kdrag);
 /* how ndsph_batch_step runs a step: 1 (default) one launch per step -- for a
  * 1D batch whose simulations hold at most 4096 particles each, a fused kernel
  * with one block per simulation that runs its whole leapfrog step (predictor,

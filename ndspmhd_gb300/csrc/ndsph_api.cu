@@ -138,6 +138,8 @@ struct ndsph_ctx {
     double* d_sim_out = nullptr;     // [nsim][4] dtcourant, dtforce, dtnext, time
     double* d_sim_off = nullptr;
     double* h_sim_out = nullptr;
+    unsigned long long* d_sim_aux = nullptr;   // [nsim][SIMAUX] drag constant, ghosts' hhmax
+    std::vector<double> h_kdrag;     // per-simulation drag constants set by the caller
     // captured batched step: two CUDA graphs (the link swaps the slabs, so
     // consecutive steps alternate between two pointer states)
     struct PtrState {
@@ -563,7 +565,7 @@ extern "C" int ndsph_finalize(ndsph_ctx* ctx)
     void* ptrs[] = {ctx->tab64, ctx->tab32, ctx->red, ctx->d_dtout, ctx->d_ncalc, ctx->d_fields,
                     ctx->srt.count, ctx->srt.start, ctx->srt.blocksums, ctx->srt.cell_h, ctx->mlp_p, ctx->mlp_m, ctx->mlp_v,
                     ctx->mlp_g, ctx->mlp_loss, ctx->mlp_frag, ctx->d_sim_red, ctx->d_sim_dt, ctx->d_sim_dtnext,
-                    ctx->d_sim_out, ctx->d_sim_off};
+                    ctx->d_sim_out, ctx->d_sim_off, ctx->d_sim_aux};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (ctx->h_red) cudaFreeHost(ctx->h_red);
     if (ctx->d_arena) cudaFree(ctx->d_arena);
@@ -890,7 +892,7 @@ static int upload_inputs(ndsph_ctx* ctx, const ndsph_particles* p, int n, bool w
 // by one cell each side (like linkND.f90:80-89)
 static bool reuse_on(const ndsph_ctx* ctx)
 {
-    return ctx->nl_reuse && ctx->o.precision == NDSPH_PREC_FP32 && !ctx->o.batched;
+    return ctx->nl_reuse && ctx->o.precision == NDSPH_PREC_FP32 && (!ctx->o.batched || ctx->o.stacked);
 }
 
 static int build_grid(ndsph_ctx* ctx, double hmax, const double* lo, const double* hi)
@@ -911,8 +913,8 @@ static int build_grid(ndsph_ctx* ctx, double hmax, const double* lo, const doubl
     // sparsest tube sets
     int wide = 3;
     if (ctx->nl_sw5 && ctx->o.ndim == 1) wide = 17;
-    else if (ctx->nl_sw5 && ctx->o.ndim == 3 && ctx->o.precision == NDSPH_PREC_FP32 && !ctx->o.batched &&
-             ctx->n < (1 << 25))
+    else if (ctx->nl_sw5 && ctx->o.ndim == 3 && ctx->o.precision == NDSPH_PREC_FP32 &&
+             (!ctx->o.batched || ctx->o.stacked) && ctx->n < (1 << 25))
         wide = 5;
     const int tries_sw[3] = {wide, 3, 3};
     const double tries_cf[3] = {skin_cf, skin_cf, 1.0};
@@ -957,6 +959,10 @@ static int build_grid(ndsph_ctx* ctx, double hmax, const double* lo, const doubl
         g.csf[d] = (float)g.cs[d];
         ncells *= g.nc[d];
     }
+    // a periodic batch: one grid per simulation, stacked
+    g.ncs = (int)std::min(ncells, 200000001L);
+    g.nstack = ctx->o.stacked ? ctx->o.nsim : 1;
+    ncells *= g.nstack;
     if (ncells > 200000000L) { ctx->err = "too many cells"; return NDSPH_E_CELLS; }
     g.ncells = (int)ncells;
     ctx->cell_hmax = hmax;
@@ -1033,6 +1039,7 @@ static bool try_keep_link(ndsph_ctx* ctx, bool keep_hmax_ghost, int* rc)
             *rc = NDSPH_E_CUDA;
             return false;
         }
+        if (ctx->o.stacked) launch_sim_ghost_h(ctx->F, ctx->S.sim, ctx->o, ctx->n, 1, st);
     }
     // the check covers every particle's current h: no row is stale
     if (cudaMemsetAsync(&r->nl_stale, 0, sizeof(int), st) != cudaSuccess) {
@@ -1085,6 +1092,8 @@ static int do_link(ndsph_ctx* ctx, const int* fields, int nfields, bool keep_hma
         ctx->h_red->hmax_ghost = dbits(hmax);
         CK(cudaMemcpyAsync(&ctx->red->hmax_ghost, &ctx->h_red->hmax_ghost, sizeof(unsigned long long),
                            cudaMemcpyHostToDevice, st));
+        // a periodic batch: each simulation's ghosts take its own max h
+        if (ctx->o.stacked) launch_sim_ghost_h(ctx->F, ctx->S.sim, ctx->o, n, 1, st);
     }
     CK(cudaMemcpyAsync(ctx->d_fields, fields, sizeof(int) * (size_t)nfields, cudaMemcpyHostToDevice, st));
     link_sort_gather(ctx, ctx->d_fields, nfields, st);
@@ -1100,7 +1109,7 @@ static void link_sort_gather(ndsph_ctx* ctx, const int* d_fields, int nfields, c
     ctx->packs_valid = false;
     ctx->tubes_valid = false;
     const int n = ctx->n;
-    launch_cell_key(ctx->F, ctx->g, ctx->o, n, ctx->srt, ctx->red, st);
+    launch_cell_key(ctx->F, ctx->g, ctx->o, n, ctx->S.sim, ctx->srt, ctx->red, st);
     launch_scan(ctx->srt, ctx->g.ncells, st);
     launch_scatter_sort(ctx->srt, n, ctx->g.ncells, st);
     FieldPtrs dst;
@@ -1236,15 +1245,19 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
             const double cap = 0.5 * stencil_cover(ctx) / (1.0 + 1.e-9) - (double)ctx->nl_dmax;
             if (hmax_now <= cap && !rows_relink) {
                 CK(cudaMemcpyAsync(&ctx->red->hmax_ghost, &hb, sizeof(hb), cudaMemcpyHostToDevice, st));
+                // a periodic batch: the simulations that asked take their own max h
+                if (ctx->o.stacked) launch_sim_ghost_h(ctx->F, ctx->S.sim, ctx->o, n, 0, st);
             } else {
                 // active list -> ids
                 std::vector<int> act(ncalc), ids(n);
                 CK(cudaMemcpy(act.data(), ctx->S.active, sizeof(int) * (size_t)ncalc, cudaMemcpyDeviceToHost));
                 CK(cudaMemcpy(ids.data(), ctx->S.id, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
                 for (int k = 0; k < ncalc; k++) act[k] = ids[act[k]];
-                // a relink asked for by the rows alone keeps the ghosts' hhmax
-                int rc = link_all(ctx, !redolink);
+                // a relink asked for by the rows alone keeps the ghosts' hhmax;
+                // in a periodic batch only the simulations that asked refresh it
+                int rc = link_all(ctx, !redolink || ctx->o.stacked);
                 if (rc) return rc;
+                if (redolink && ctx->o.stacked) launch_sim_ghost_h(ctx->F, ctx->S.sim, ctx->o, n, 0, st);
                 relinked = true;
                 std::vector<int> pos(n);
                 CK(cudaMemcpy(pos.data(), ctx->S.pos_of_id, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
@@ -2166,16 +2179,28 @@ extern "C" int ndsph_step(ndsph_ctx* ctx, ndsph_particles* p, int32_t npart, nds
 }
 
 // ---------------------------------------------------------------------------
-// batched form: nsim independent simulations (open/fixed boundaries) laid
-// side by side along x, one device state, per-simulation dt and clock
+// batched form: nsim independent simulations in one device state with
+// per-simulation dt, clock, reductions and drag constant.  Open/fixed
+// boundaries: the simulations lie side by side along x.  Periodic in every
+// dimension: each simulation keeps its own box and a cell grid of its own,
+// the grids stacked (cell = sim * cells per grid + local cell), so the
+// periodic wrap of the search stays inside each simulation.
 // ---------------------------------------------------------------------------
 extern "C" int ndsph_batch_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart, const int32_t* sim,
                                   int32_t nsim, int32_t initialise)
 {
     GUARD_CTX();
     if (!p || !sim || npart <= 0 || nsim <= 0) { ctx->err = "bad batch arguments"; return NDSPH_E_ARG; }
-    for (int d = 0; d < ctx->o.ndim; d++)
-        if (ctx->o.ibound[d] > 1) { ctx->err = "batched form needs open or fixed boundaries"; return NDSPH_E_ARG; }
+    int nper = 0;
+    for (int d = 0; d < ctx->o.ndim; d++) {
+        if (ctx->o.ibound[d] == 2) { ctx->err = "batched form: reflective boundaries are not supported"; return NDSPH_E_ARG; }
+        nper += ctx->o.periodic[d];
+    }
+    if (nper != 0 && nper != ctx->o.ndim) {
+        ctx->err = "batched form needs open or fixed boundaries, or periodic ones in every dimension";
+        return NDSPH_E_ARG;
+    }
+    const bool stacked = (nper == ctx->o.ndim);
     for (int i = 0; i < npart; i++)
         if (sim[i] < 0 || sim[i] >= nsim) { ctx->err = "simulation index out of range"; return NDSPH_E_ARG; }
     int rc = upload_inputs(ctx, p, npart, true, !initialise);
@@ -2194,7 +2219,8 @@ extern "C" int ndsph_batch_upload(ndsph_ctx* ctx, const ndsph_particles* p, int3
     if (rc) return rc;
     // per-simulation arrays
     if (nsim != ctx->nsim) {
-        void* old[] = {ctx->d_sim_red, ctx->d_sim_dt, ctx->d_sim_dtnext, ctx->d_sim_out, ctx->d_sim_off};
+        void* old[] = {ctx->d_sim_red, ctx->d_sim_dt, ctx->d_sim_dtnext, ctx->d_sim_out, ctx->d_sim_off,
+                       ctx->d_sim_aux};
         for (void* q : old) if (q) cudaFree(q);
         if (ctx->h_sim_out) cudaFreeHost(ctx->h_sim_out);
         CK(cudaMalloc(&ctx->d_sim_red, sizeof(unsigned long long) * SIMRED * (size_t)nsim));
@@ -2202,20 +2228,33 @@ extern "C" int ndsph_batch_upload(ndsph_ctx* ctx, const ndsph_particles* p, int3
         CK(cudaMalloc(&ctx->d_sim_dtnext, sizeof(double) * (size_t)nsim));
         CK(cudaMalloc(&ctx->d_sim_out, sizeof(double) * 4 * (size_t)nsim));
         CK(cudaMalloc(&ctx->d_sim_off, sizeof(double) * (size_t)nsim));
+        CK(cudaMalloc(&ctx->d_sim_aux, sizeof(unsigned long long) * SIMAUX * (size_t)nsim));
         CK(cudaMallocHost(&ctx->h_sim_out, sizeof(double) * 4 * (size_t)nsim));
         ctx->nsim = nsim;
     }
     CK(cudaMemsetAsync(ctx->d_sim_dt, 0, sizeof(double) * (size_t)nsim, ctx->st));
     CK(cudaMemsetAsync(ctx->d_sim_out, 0, sizeof(double) * 4 * (size_t)nsim, ctx->st));
-    std::vector<double> off(nsim);
+    std::vector<double> off(nsim, 0.0);
     const double span = 2.0 * (ctx->o.xmax[0] - ctx->o.xmin[0]) + 1.0;
-    for (int s2 = 0; s2 < nsim; s2++) off[s2] = span * s2;
+    if (!stacked)
+        for (int s2 = 0; s2 < nsim; s2++) off[s2] = span * s2;
+    // drag constants: the caller's per-simulation values, else the options'
+    const bool own_k = ctx->h_kdrag.size() == (size_t)nsim;
+    std::vector<unsigned long long> aux((size_t)SIMAUX * nsim, 0ull);
+    for (int s2 = 0; s2 < nsim; s2++)
+        aux[(size_t)s2 * SIMAUX + SA_KDRAG] = dbits(own_k ? ctx->h_kdrag[s2] : ctx->o.Kdrag);
+    CK(cudaMemcpyAsync(ctx->d_sim_aux, aux.data(), sizeof(unsigned long long) * aux.size(), cudaMemcpyHostToDevice,
+                       ctx->st));
     CK(cudaMemcpyAsync(ctx->d_sim_off, off.data(), sizeof(double) * (size_t)nsim, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(ctx->S.sim, sim, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, ctx->st));
     ctx->o.batched = 1;
     ctx->o.nsim = nsim;
     ctx->o.sim_red = ctx->d_sim_red;
     ctx->o.sim_dt = ctx->d_sim_dt;
+    ctx->o.sim_aux = ctx->d_sim_aux;
+    ctx->o.stacked = stacked ? 1 : 0;
+    ctx->nl_valid = false;
+    ctx->linked = false;
     launch_add_offset(ctx->F, ctx->S.sim, ctx->d_sim_off, n, +1, ctx->st);
     if (initialise) {
         launch_p2c_init(ctx->F, ctx->S, ctx->o, n, ctx->st);
@@ -2293,7 +2332,7 @@ static void graph_drop(ndsph_ctx* ctx)
 
 static bool graph_usable(const ndsph_ctx* ctx)
 {
-    return ctx->graph_mode >= 1 && ctx->o.batched && !ctx->opts.learned_h && !ctx->profiling &&
+    return ctx->graph_mode >= 1 && ctx->o.batched && !ctx->o.stacked && !ctx->opts.learned_h && !ctx->profiling &&
            ctx->o.maxdensits >= 1 && ctx->n > 0;
 }
 
@@ -2586,7 +2625,7 @@ static int tubes_prepare(ndsph_ctx* ctx)
 
 static bool fused_usable(const ndsph_ctx* ctx)
 {
-    return ctx->graph_mode == 1 && ctx->o.batched && ctx->o.ndim == 1 && !ctx->opts.learned_h &&
+    return ctx->graph_mode == 1 && ctx->o.batched && !ctx->o.stacked && ctx->o.ndim == 1 && !ctx->opts.learned_h &&
            !ctx->profiling && ctx->o.maxdensits >= 1 && ctx->n > 0 && ctx->linked;
 }
 
@@ -2650,6 +2689,23 @@ extern "C" int ndsph_set_host_access(ndsph_ctx* ctx, int32_t mode)
     if (mode != 0 && mode != 1) { ctx->err = "host access mode must be 0 or 1"; return NDSPH_E_ARG; }
     CK(cudaStreamSynchronize(ctx->st));
     ctx->host_access = mode;
+    return 0;
+}
+
+extern "C" int ndsph_batch_set_kdrag(ndsph_ctx* ctx, int32_t nsim, const double* kdrag)
+{
+    GUARD_CTX();
+    if (nsim <= 0 || !kdrag) { ctx->err = "bad drag constants"; return NDSPH_E_ARG; }
+    for (int s2 = 0; s2 < nsim; s2++)
+        if (!(kdrag[s2] >= 0.0) || !std::isfinite(kdrag[s2])) { ctx->err = "drag constant negative or not finite"; return NDSPH_E_ARG; }
+    ctx->h_kdrag.assign(kdrag, kdrag + nsim);
+    if (ctx->o.batched && ctx->nsim == nsim) {
+        CK(cudaStreamSynchronize(ctx->st));
+        std::vector<unsigned long long> aux((size_t)SIMAUX * nsim);
+        CK(cudaMemcpy(aux.data(), ctx->d_sim_aux, sizeof(unsigned long long) * aux.size(), cudaMemcpyDeviceToHost));
+        for (int s2 = 0; s2 < nsim; s2++) aux[(size_t)s2 * SIMAUX + SA_KDRAG] = dbits(kdrag[s2]);
+        CK(cudaMemcpy(ctx->d_sim_aux, aux.data(), sizeof(unsigned long long) * aux.size(), cudaMemcpyHostToDevice));
+    }
     return 0;
 }
 

@@ -69,14 +69,25 @@ struct DevOpts {
     int nsim;
     unsigned long long* sim_red;   // [nsim][SIMRED] per-simulation reductions
     double* sim_dt;                // [nsim] dt of the current step
+    unsigned long long* sim_aux;   // [nsim][SIMAUX] per-simulation drag constant and ghost hhmax
+    int stacked;                   // periodic batch: one cell grid per simulation, stacked
 };
 // per-simulation reduction slots (batched form)
 enum SimRed : int { SR_DTC = 0, SR_DTAV, SR_VSIG, SR_TS, SR_FH, SR_STRESS, SIMRED = 8 };
+// per-simulation settings and link state (batched form, bit patterns of
+// doubles): the drag constant K (dust.f90:91), the ghosts' hhmax of the
+// simulation's last (re)link, the scratch max h of a relink, and the relink
+// request of its last Newton-Raphson pass (iterate_density.f90:122-126)
+enum SimAux : int { SA_KDRAG = 0, SA_HG, SA_HNOW, SA_RELINK, SIMAUX = 4 };
 
 // cell grid (periodic dims wrap, the others are padded bounding boxes)
 struct Grid {
     int nc[3];          // cells per dim (1 for unused dims)
     int ncells;
+    // a periodic batch stacks one grid of ncs cells per simulation:
+    // cell = sim * ncs + local cell (nstack = 1: one simulation)
+    int ncs = 0;
+    int nstack = 1;
     double origin[3];   // lower corner
     double cs[3];       // cell size per dim (>= 2 hmax / reach)
     double inv_cs[3];
@@ -87,6 +98,21 @@ struct Grid {
     int sw = 3;
     int nlshift = 5;
 };
+
+// coordinates of cell c within its simulation's grid and the id of that
+// grid's first cell
+__host__ __device__ inline void cell_coords(int c, const Grid& g, int cc[3], int* base = nullptr)
+{
+    int b = 0;
+    if (g.nstack > 1) {
+        b = (c / g.ncs) * g.ncs;
+        c -= b;
+    }
+    cc[0] = c % g.nc[0];
+    cc[1] = (c / g.nc[0]) % g.nc[1];
+    cc[2] = c / (g.nc[0] * g.nc[1]);
+    if (base) *base = b;
+}
 
 // kernel tables: value and slope per entry, slope(i) = (t(i+1)-t(i))*ddq2table
 // exactly as interpolate_kernel* form it (kernelND.f90:4382-4391)

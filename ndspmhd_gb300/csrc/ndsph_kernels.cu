@@ -104,21 +104,23 @@ __device__ inline int cell_coord(double x, double origin, double inv_cs, int nc)
     return c;
 }
 
-__global__ void k_cell_key(FieldPtrs F, Grid g, int ndim, int n, SortScratch s)
+__global__ void k_cell_key(FieldPtrs F, Grid g, int ndim, int n, const int* sim, SortScratch s)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int c[3] = {0, 0, 0};
     for (int d = 0; d < ndim; d++) c[d] = cell_coord(F.f[X0 + d][i], g.origin[d], g.inv_cs[d], g.nc[d]);
     int key = (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
+    if (g.nstack > 1) key += sim[i] * g.ncs;   // the simulation's own grid
     s.key[i] = key;
     s.slot[i] = atomicAdd(&s.count[key], 1);
 }
-void launch_cell_key(FieldPtrs F, Grid g, DevOpts o, int n, SortScratch s, Reduce* red, cudaStream_t st)
+void launch_cell_key(FieldPtrs F, Grid g, DevOpts o, int n, const int* sim, SortScratch s, Reduce* red,
+                     cudaStream_t st)
 {
     (void)red;
     cudaMemsetAsync(s.count, 0, sizeof(int) * (size_t)g.ncells, st);
-    if (n > 0) NDSPH_COUNT_LAUNCH, k_cell_key<<<nblk(n, 256), 256, 0, st>>>(F, g, o.ndim, n, s);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_cell_key<<<nblk(n, 256), 256, 0, st>>>(F, g, o.ndim, n, sim, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -280,11 +282,8 @@ __global__ void k_xs(FieldPtrs F, Side S, Grid g, int ndim, int n)
 {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    int c = S.cell[k];
     int cc[3];
-    cc[0] = c % g.nc[0];
-    cc[1] = (c / g.nc[0]) % g.nc[1];
-    cc[2] = c / (g.nc[0] * g.nc[1]);
+    cell_coords(S.cell[k], g, cc);
     float r[3] = {0.f, 0.f, 0.f};
     for (int d = 0; d < ndim; d++) r[d] = (float)(F.f[X0 + d][k] - (g.origin[d] + cc[d] * g.cs[d]));
     S.xs[k] = make_float4(r[0], r[1], r[2], (float)F.f[HH][k]);
@@ -318,11 +317,8 @@ __global__ void k_reuse_check(FieldPtrs F, Side S, Grid g, DevOpts o, int n, flo
     float d2 = 0.f, slack = 3.0e38f;
     double h = 0.0;
     if (k < n) {
-        const int c = S.cell[k];
         int cc[3];
-        cc[0] = c % g.nc[0];
-        cc[1] = (c / g.nc[0]) % g.nc[1];
-        cc[2] = c / (g.nc[0] * g.nc[1]);
+        cell_coords(S.cell[k], g, cc);
         float r[3] = {0.f, 0.f, 0.f};
         for (int d = 0; d < o.ndim; d++) {
             double v = F.f[X0 + d][k] - (g.origin[d] + cc[d] * g.cs[d]);
@@ -788,7 +784,8 @@ __global__ void k_sim_finalize(DevOpts o, double* dt_next, double* sim_out)
     double dtforce = 1.7976931348623157e308;
     if (fhmax > 0.0) dtforce = fmin(dtforce, sqrt(1.0 / fhmax));
     double dtdrag = 1.7976931348623157e308;
-    if (o.idust == 2 && o.idrag_nature != 0 && (o.Kdrag > 0.0 || o.idrag_nature > 1)) dtdrag = fmin(dtdrag, bitsd(r[SR_TS]));
+    const double kdrag = o.sim_aux ? bitsd(o.sim_aux[(size_t)s * SIMAUX + SA_KDRAG]) : o.Kdrag;
+    if (o.idust == 2 && o.idrag_nature != 0 && (kdrag > 0.0 || o.idrag_nature > 1)) dtdrag = fmin(dtdrag, bitsd(r[SR_TS]));
     double dtn = o.C_force * dtforce;
     dtn = fmin(dtn, o.C_cour * dtcourant);
     dtn = fmin(dtn, 0.9 * dtdrag);
@@ -804,6 +801,43 @@ void launch_sim_finalize(DevOpts o, double* dt_next, double* sim_out, cudaStream
 {
     if (o.nsim > 0) NDSPH_COUNT_LAUNCH, k_sim_finalize<<<nblk(o.nsim, 256), 256, 0, st>>>(o, dt_next, sim_out);
 }
+// ghosts' hhmax per simulation of a periodic batch: the largest h of each
+// simulation at its link (ghostND_mhd.f90:218 takes hhmax of the run's own
+// particles), for every simulation (all = 1) or for the simulations whose
+// last Newton-Raphson pass asked for a relink (iterate_density.f90:122-126)
+__global__ void k_sim_hmax(FieldPtrs F, const int* __restrict__ sim, int n, DevOpts o)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int si = (i < n) ? sim[i] : -1;
+    unsigned long long hb = (i < n) ? dbits(fmax(F.f[HH][i], 0.0)) : 0ull;
+    // one atomic per warp when the warp holds one simulation (slots are
+    // sorted by simulation)
+    const int s0 = __shfl_sync(0xffffffffu, si, 0);
+    if (__all_sync(0xffffffffu, si == s0 || si < 0)) {
+        for (int off = 16; off > 0; off >>= 1) {
+            const unsigned long long q = __shfl_down_sync(0xffffffffu, hb, off);
+            hb = q > hb ? q : hb;
+        }
+        if ((threadIdx.x & 31) == 0 && s0 >= 0) atomicMax(&o.sim_aux[(size_t)s0 * SIMAUX + SA_HNOW], hb);
+    } else if (si >= 0) {
+        atomicMax(&o.sim_aux[(size_t)si * SIMAUX + SA_HNOW], hb);
+    }
+}
+__global__ void k_sim_hg_apply(DevOpts o, int all)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= o.nsim) return;
+    unsigned long long* x = o.sim_aux + (size_t)s * SIMAUX;
+    if (all || x[SA_RELINK]) x[SA_HG] = x[SA_HNOW];
+    x[SA_RELINK] = 0ull;
+    x[SA_HNOW] = 0ull;
+}
+void launch_sim_ghost_h(FieldPtrs F, const int* sim, DevOpts o, int n, int all, cudaStream_t st)
+{
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_sim_hmax<<<nblk(n, 256), 256, 0, st>>>(F, sim, n, o);
+    if (o.nsim > 0) NDSPH_COUNT_LAUNCH, k_sim_hg_apply<<<nblk(o.nsim, 256), 256, 0, st>>>(o, all);
+}
+
 // x += sign * off[sim]  (tubes laid side by side along x)
 __global__ void k_add_offset(FieldPtrs F, const int* sim, const double* off, int n, int sign)
 {

@@ -95,7 +95,8 @@ void launch_boundary_wrap(FieldPtrs F, DevOpts o, int n, cudaStream_t st);
 // max h and bounding box; skipped when `gate` is set and points to 0
 void launch_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, cudaStream_t st,
                       const int* gate = nullptr);
-void launch_cell_key(FieldPtrs F, Grid g, DevOpts o, int n, SortScratch s, Reduce* red, cudaStream_t st);
+void launch_cell_key(FieldPtrs F, Grid g, DevOpts o, int n, const int* sim, SortScratch s, Reduce* red,
+                     cudaStream_t st);
 void launch_scan(SortScratch s, int ncells, cudaStream_t st);
 void launch_scatter_sort(SortScratch s, int n, int ncells, cudaStream_t st);
 void launch_gather_fields(FieldPtrs dst, FieldPtrs src, const int* fields, int nfields, const int* perm,
@@ -153,6 +154,7 @@ void launch_p2c_post(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
 // batched form
 void launch_sim_reset(DevOpts o, cudaStream_t st);
 void launch_sim_finalize(DevOpts o, double* dt_next, double* sim_out, cudaStream_t st);
+void launch_sim_ghost_h(FieldPtrs F, const int* sim, DevOpts o, int n, int all, cudaStream_t st);
 void launch_add_offset(FieldPtrs F, const int* sim, const double* off, int n, int sign, cudaStream_t st);
 // captured step (CUDA graph) control kernels
 void launch_link_reset(Reduce* red, cudaStream_t st);

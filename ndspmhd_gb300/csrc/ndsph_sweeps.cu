@@ -36,6 +36,13 @@ namespace ndsph {
 
 static inline int nblk(long n, int bs) { return (int)((n + bs - 1) / bs); }
 
+// the ghosts' hhmax of particle i's simulation: the max h at its last
+// (re)link (ghostND_mhd.f90:218); per simulation in a periodic batch
+__device__ __forceinline__ double ghost_hmax(const SweepArgs& a, int i)
+{
+    return a.o.stacked ? bitsd(a.o.sim_aux[(size_t)a.S.sim[i] * SIMAUX + SA_HG]) : bitsd(a.red->hmax_ghost);
+}
+
 __device__ __forceinline__ bool type_match(int ti, int tj)
 {
     return (tj == ti) || (ti == NDSPH_ITYPE_GAS && tj == NDSPH_ITYPE_BND) ||
@@ -141,12 +148,8 @@ __device__ __forceinline__ void stencil_d(unsigned o, int sw, int d[3])
 template <int NDIM>
 struct Stencil {
     int cc[3];
-    __device__ Stencil(int cell, const Grid& g)
-    {
-        cc[0] = cell % g.nc[0];
-        cc[1] = (cell / g.nc[0]) % g.nc[1];
-        cc[2] = cell / (g.nc[0] * g.nc[1]);
-    }
+    int base;   // first cell of the simulation's grid (stacked periodic batch)
+    __device__ Stencil(int cell, const Grid& g) { cell_coords(cell, g, cc, &base); }
     // cell at offset d (a stencil of any width) with periodic wrap flags;
     // false if outside an open dimension
     __device__ __forceinline__ bool cell_at_d(const int d[3], const Grid& g, const DevOpts& op, int& cid,
@@ -169,7 +172,7 @@ struct Stencil {
                 }
             }
         }
-        cid = (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
+        cid = base + (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
         return true;
     }
     // offsets and wrap flags of a stored row entry's stencil index
@@ -328,7 +331,7 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
         const float4 pvi = a.S.pk_v[i];
         vif[0] = pvi.x; vif[1] = pvi.y; vif[2] = pvi.z;
     }
-    const double dxbound = 2.0 * bitsd(a.red->hmax_ghost);
+    const double dxbound = 2.0 * ghost_hmax(a, i);
     const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
 
     // FP64 sums (PREC 0) or compensated FP32 sums (PREC 1), in kernel units
@@ -590,7 +593,10 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
                 a.S.xs[i] = xw;
             }
         }
-        if (hnew > bitsd(a.red->hmax_ghost)) relink = true;
+        if (hnew > ghost_hmax(a, i)) {
+            relink = true;
+            if (o.stacked) o.sim_aux[(size_t)a.S.sim[i] * SIMAUX + SA_RELINK] = 1ull;
+        }
         if (Src::kRows && (float)hnew + a.nl_dmax > a.S.hb[i] * a.nl_skin) a.red->nl_stale = 1;
     } else {
         drhodt = drhodt * gradh;
@@ -737,7 +743,7 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
     const double hi21_d = hi1_d * hi1_d;
     const float4 xsi = a.S.xs[i];
     const float hif = xsi.w;
-    const double dxbound = 2.0 * bitsd(a.red->hmax_ghost);
+    const double dxbound = 2.0 * ghost_hmax(a, i);
     const float abs_tol = 1e-6f * fmaxf(g.csf[0], fmaxf(g.csf[1], g.csf[2]));
 
     PData<R> pi;
@@ -772,7 +778,6 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
     const R stressmax = (R)bitsd(o.batched ? o.sim_red[(size_t)a.S.sim[i] * SIMRED + SR_STRESS]
                                            : a.red->stressmax);
     const R beta = (R)o.beta;
-    const R Kdrag = (R)o.Kdrag;
     const bool i_dust = (typei == NDSPH_ITYPE_DUST);
 
     Acc<R> fx, fy, fz, dbx, dby, dbz, du, dvb, cbx, cby, cbz;
@@ -1025,6 +1030,8 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                     drd[0] = dr[0]; drd[1] = dr[1]; drd[2] = dr[2];
                 }
                 const R rsum = rhoi + rhoj;
+                // the simulation's drag constant (per simulation in a batch)
+                const R Kdrag = (R)(o.sim_aux ? bitsd(o.sim_aux[(size_t)a.S.sim[i] * SIMAUX + SA_KDRAG]) : o.Kdrag);
                 const R ts = divp(rhoj * rhoi, Kdrag * rsum);
                 R wgas, csg;
                 if (typei == NDSPH_ITYPE_GAS || typei == NDSPH_ITYPE_BND) {
@@ -1686,7 +1693,8 @@ __global__ void __launch_bounds__(TUBE_BS) k_tube_step(TubeArgs T)
         double dtforce = 1.7976931348623157e308;
         if (fhmax > 0.0) dtforce = fmin(dtforce, sqrt(1.0 / fhmax));
         double dtdrag = 1.7976931348623157e308;
-        if (o.idust == 2 && o.idrag_nature != 0 && (o.Kdrag > 0.0 || o.idrag_nature > 1))
+        const double kdrag = o.sim_aux ? bitsd(o.sim_aux[(size_t)s * SIMAUX + SA_KDRAG]) : o.Kdrag;
+        if (o.idust == 2 && o.idrag_nature != 0 && (kdrag > 0.0 || o.idrag_nature > 1))
             dtdrag = fmin(dtdrag, bitsd(r[SR_TS]));
         double dtn = o.C_force * dtforce;
         dtn = fmin(dtn, o.C_cour * dtcourant);
@@ -1815,10 +1823,11 @@ __global__ void k_xg(Side S, Grid g, int n)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const int c = S.cell[k];
-    const int cx = c % g.nc[0], cy = (c / g.nc[0]) % g.nc[1], cz = c / (g.nc[0] * g.nc[1]);
+    int cc[3];
+    cell_coords(S.cell[k], g, cc);
     const float4 x = S.xs[k];
-    S.xg[k] = make_float4((float)cx * g.csf[0] + x.x, (float)cy * g.csf[1] + x.y, (float)cz * g.csf[2] + x.z, x.w);
+    S.xg[k] = make_float4((float)cc[0] * g.csf[0] + x.x, (float)cc[1] * g.csf[1] + x.y,
+                          (float)cc[2] * g.csf[2] + x.z, x.w);
 }
 
 // One thread per particle.  For each (dy, dz) row of the stencil, the cells
@@ -1941,8 +1950,8 @@ void launch_build_nlist(const SweepArgs& a, cudaStream_t st)
     const int nbp = nblk(a.n, 128);
     if (a.o.ndim == 1) NDSPH_COUNT_LAUNCH, k_build_nlist<1><<<nbp, 128, 0, st>>>(a);
     else if (a.o.ndim == 2) NDSPH_COUNT_LAUNCH, k_build_nlist<2><<<nbp, 128, 0, st>>>(a);
-    else if (!a.o.batched && a.g.nc[0] <= 1024 && a.g.nc[1] <= 1024 && a.g.nc[2] <= 1024) {
-        // one 3D simulation of at most 1024 cells a side: the scan runs on
+    else if ((!a.o.batched || a.o.stacked) && a.g.nc[0] <= 1024 && a.g.nc[1] <= 1024 && a.g.nc[2] <= 1024) {
+        // 3D simulations of at most 1024 cells a side: the scan runs on
         // FP32 positions relative to the grid origin, which carry an error of
         // at most ~6e-8 x 1024 cells, well inside the rows' 2e-4 radius margin
         NDSPH_COUNT_LAUNCH, k_xg<<<nbp, 128, 0, st>>>(a.S, a.g, a.n);
@@ -1966,7 +1975,7 @@ __global__ void k_neigh(SweepArgs a, int mode, const long long* offsets, long lo
     const double hi1 = a.S.h1[i];
     const double hi21 = __dmul_rn(hi1, hi1);
     const int typei = a.S.itype[i];
-    const double dxbound = 2.0 * bitsd(a.red->hmax_ghost);
+    const double dxbound = 2.0 * ghost_hmax(a, i);
     Stencil<NDIM> stn(a.S.cell[i], a.g);
     const int sw = a.g.sw, r = (sw - 1) >> 1;
     const int nst = (NDIM == 1) ? sw : (NDIM == 2 ? sw * sw : sw * sw * sw);

@@ -79,6 +79,7 @@ def lib() -> C.CDLL:
     L.ndsph_batch_upload.argtypes = [P, parts, C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.c_int32]
     L.ndsph_batch_step.argtypes = [P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.ndsph_batch_download.argtypes = [P, parts]
+    L.ndsph_batch_set_kdrag.argtypes = [P, C.c_int32, C.POINTER(C.c_double)]
     L.ndsph_set_tuning.argtypes = [P, C.POINTER(NdsphTuning)]
     L.ndsph_get_tuning.argtypes = [P, C.POINTER(NdsphTuning)]
     _lib = L
@@ -189,6 +190,12 @@ class GpuSPH:
 
     def set_host_access(self, mode: int):
         self._check(lib().ndsph_set_host_access(self._h, int(mode)))
+
+    def batch_set_kdrag(self, kdrag):
+        """Per-simulation drag constants K; call before batch_upload so the
+        initialising derivs use them."""
+        k = np.ascontiguousarray(kdrag, dtype=np.float64)
+        self._check(lib().ndsph_batch_set_kdrag(self._h, len(k), k.ctypes.data_as(C.POINTER(C.c_double))))
 
     def batch_set_graph(self, mode: int):
         self._check(lib().ndsph_batch_set_graph(self._h, int(mode)))
