@@ -224,7 +224,9 @@ def run_e2e(o, steps: int, warmup: int, tuning=None):
     import numpy as np
     import torch
     from ndspmhd_gb300.gpu import GpuSPH
-    o2, st = make_problem(N1D, o["precision"])
+    # the caller's form (precision, learned h) on the same particle set
+    o2 = dict(o)
+    _, st = make_problem(N1D, o["precision"])
     g0 = init_state(o2, st)
     g0.close()
     n = st["x"].shape[0]

@@ -2062,8 +2062,7 @@ static int step_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
     const int* idm = keep ? ctx->S.id : nullptr;
     // late inputs (Bevol, energy, alpha and their rates: the EOS and their
     // part of the predictor) on the upload stream, overlapping the link and
-    // the density passes; the learned-h form reads them before the link
-    const bool split = !ctx->opts.learned_h;
+    // the density passes (and the learned-h inference, which reads none of them)
     // early inputs (the predictor of x, v, h; the link; the density passes).
     // rho is recomputed for every particle by the first density pass and
     // read before it only as the save of fixed particles (none here) and as
@@ -2072,35 +2071,25 @@ static int step_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
     rc |= upload_aos(ctx, p->vel, V0, 3, 3, n, idm);
     rc |= upload_aos(ctx, p->hh, HH, 1, 1, n, idm);
     rc |= upload_aos(ctx, p->pmass, PM, 1, 1, n, idm);
-    if (!split) rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n, idm);
+    if (ctx->opts.learned_h) rc |= upload_aos(ctx, p->rho, RHO, 1, 1, n, idm);
     rc |= upload_aos(ctx, p->dhdt, DHDT, 1, 1, n, idm);
     rc |= upload_aos(ctx, p->force, F0, 3, 3, n, idm);
     if (rc) return rc;
-    if (split) {
-        // behind the early copies, so they do not share the link's bandwidth
-        CK(cudaEventRecord(ctx->ev_up0, ctx->st_cp));
-        CK(cudaStreamWaitEvent(ctx->st_up, ctx->ev_up0, 0));
-        ctx->late_nf = 0;
-        ctx->late_used = 0;
-        ctx->late_relayout = false;
-        rc |= upload_aos_late(ctx, p->Bevol, BE0, 3, 3, n, idm);
-        rc |= upload_aos_late(ctx, p->en, EN, 1, 1, n, idm);
-        rc |= upload_aos_late(ctx, p->alpha, AL0, 3, 3, n, idm);
-        rc |= upload_aos_late(ctx, p->dBevoldt, DB0, 3, 3, n, idm);
-        rc |= upload_aos_late(ctx, p->dendt, DENDT, 1, 1, n, idm);
-        rc |= upload_aos_late(ctx, p->daldt, DAL0, 3, 3, n, idm);
-        if (rc) return rc;
-        CK(cudaEventRecord(ctx->ev_late, ctx->st_up));
-        ctx->late_pending = true;
-    } else {
-        rc |= upload_aos(ctx, p->Bevol, BE0, 3, 3, n, idm);
-        rc |= upload_aos(ctx, p->en, EN, 1, 1, n, idm);
-        rc |= upload_aos(ctx, p->alpha, AL0, 3, 3, n, idm);
-        rc |= upload_aos(ctx, p->dBevoldt, DB0, 3, 3, n, idm);
-        rc |= upload_aos(ctx, p->dendt, DENDT, 1, 1, n, idm);
-        rc |= upload_aos(ctx, p->daldt, DAL0, 3, 3, n, idm);
-        if (rc) return rc;
-    }
+    // behind the early copies, so they do not share the link's bandwidth
+    CK(cudaEventRecord(ctx->ev_up0, ctx->st_cp));
+    CK(cudaStreamWaitEvent(ctx->st_up, ctx->ev_up0, 0));
+    ctx->late_nf = 0;
+    ctx->late_used = 0;
+    ctx->late_relayout = false;
+    rc |= upload_aos_late(ctx, p->Bevol, BE0, 3, 3, n, idm);
+    rc |= upload_aos_late(ctx, p->en, EN, 1, 1, n, idm);
+    rc |= upload_aos_late(ctx, p->alpha, AL0, 3, 3, n, idm);
+    rc |= upload_aos_late(ctx, p->dBevoldt, DB0, 3, 3, n, idm);
+    rc |= upload_aos_late(ctx, p->dendt, DENDT, 1, 1, n, idm);
+    rc |= upload_aos_late(ctx, p->daldt, DAL0, 3, 3, n, idm);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->ev_late, ctx->st_up));
+    ctx->late_pending = true;
     if (keep) {
         const int* v = (const int*)host_view(ctx, p->itype);
         if (!v) {
@@ -2116,15 +2105,16 @@ static int step_upload(ndsph_ctx* ctx, const ndsph_particles* p, int32_t npart)
         if (carry_mlp) {
             // slot k takes particle k: gather the previous step's values the
             // predictor reads (its h_pred and root estimate, drho/dt, c_s,
-            // numneigh) from the old slot pos_of_id[k] into the other slab,
-            // then copy back
-            static const int mf[4] = {HPRED, HROOT, DRHODT, CS};
-            CK(cudaMemcpyAsync(ctx->d_fields, mf, sizeof mf, cudaMemcpyHostToDevice, ctx->st));
+            // numneigh, and rho when the caller passes none) from the old
+            // slot pos_of_id[k] into the other slab, then copy back
+            static const int mf[5] = {HPRED, HROOT, DRHODT, CS, RHO};
+            const int nmf = p->rho ? 4 : 5;
+            CK(cudaMemcpyAsync(ctx->d_fields, mf, sizeof(int) * nmf, cudaMemcpyHostToDevice, ctx->st));
             FieldPtrs tmp;
             double* other = ctx->slab[1 - ctx->cur];
             for (int f = 0; f < NF; f++) tmp.f[f] = other + (size_t)(ctx->F.f[f] - ctx->slab[ctx->cur]);
-            launch_gather_fields(tmp, ctx->F, ctx->d_fields, 4, ctx->S.pos_of_id, n, ctx->st);
-            for (int f : mf) launch_copy(ctx->F.f[f], tmp.f[f], n, ctx->st);
+            launch_gather_fields(tmp, ctx->F, ctx->d_fields, nmf, ctx->S.pos_of_id, n, ctx->st);
+            for (int k = 0; k < nmf; k++) launch_copy(ctx->F.f[mf[k]], tmp.f[mf[k]], n, ctx->st);
             launch_gather_int(ctx->d_istage, ctx->S.numneigh, ctx->S.pos_of_id, n, ctx->st);
             CK(cudaMemcpyAsync(ctx->S.numneigh, ctx->d_istage, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice,
                                ctx->st));

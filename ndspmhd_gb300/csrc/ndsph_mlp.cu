@@ -168,8 +168,10 @@ __global__ void k_mlp_forward(const MlpFrag* __restrict__ frp, const float* __re
     }
 }
 
-// features of one slot (all FP32, scaled to O(1)) -- see ndsph_mlp.h
-__device__ __forceinline__ void slot_features(const MlpInferArgs& a, int i, float f[MLP_NIN])
+// features of one slot (all FP32, scaled to O(1)) -- see ndsph_mlp.h;
+// false when one is not finite (a slot without a density yet: rho = 0 before
+// the first density pass of a context whose caller passed none)
+__device__ __forceinline__ bool slot_features(const MlpInferArgs& a, int i, float f[MLP_NIN])
 {
     // FP32 throughout: the features are rounded to BF16 anyway, and FP64
     // transcendentals are expensive on this part
@@ -200,6 +202,10 @@ __device__ __forceinline__ void slot_features(const MlpInferArgs& a, int i, floa
     // (none before the first learned step: both are 0 then)
     const float hp0 = (float)a.hpred[i], hr0 = (float)a.hroot[i];
     f[5] = (hp0 > 0.f && hr0 > 0.f) ? 100.f * __logf(hr0 / hp0) : 0.f;
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < MLP_NIN; k++) ok = ok && isfinite(f[k]);
+    return ok;
 }
 
 // per step, before the link: h <- h_pred exp(z/100), features and h_pred kept
@@ -219,7 +225,10 @@ __global__ void k_mlp_infer(const MlpFrag* __restrict__ frp, MlpInferArgs a)
     for (int base = warp * 32; base < a.n; base += nwarps * 32) {
         const int i = base + lane;
         float fa[MLP_NIN] = {0, 0, 0, 0, 0, 0};
-        if (i < a.n) slot_features(a, i, fa);
+        bool ok = true;
+        if (i < a.n) ok = slot_features(a, i, fa);
+        if (!ok)
+            for (int k = 0; k < MLP_NIN; k++) fa[k] = 0.f;   // the slot keeps h_pred (below)
         // A fragments of the two tiles: lane (g, t) holds columns 2t, 2t+1 of
         // rows g and g+8 (tile 0: slots base..base+15, tile 1: the next 16);
         // column pair (2k, 2k+1) comes by shuffle from the rows' lanes
@@ -248,9 +257,11 @@ __global__ void k_mlp_infer(const MlpFrag* __restrict__ frp, MlpInferArgs a)
         const float zz = (lane < 8) ? a00 : (lane < 16) ? a08 : (lane < 24) ? a10 : a18;
         if (i < a.n) {
             for (int k = 0; k < MLP_NFW; k++) a.feat[k][i] = make_float2(fa[2 * k], fa[2 * k + 1]);
+            // a slot without valid features is left out of the training
+            if (!ok) a.feat[0][i] = make_float2(__int_as_float(0x7fc00000), 0.f);
             const double hpred = a.hh[i];
             a.hpred[i] = hpred;
-            if (!(a.fixed && a.itype[i] == 1)) {
+            if (ok && !(a.fixed && a.itype[i] == 1)) {
                 // the network predicts the change of the correction
                 const float z = fminf(fmaxf(fa[5] + zz, -(float)a.zclip), (float)a.zclip);
                 if (a.apply) a.hh[i] = hpred * (double)__expf(0.01f * z);
@@ -314,6 +325,14 @@ __global__ void __launch_bounds__(TRAIN_BS) k_mlp_grad(const float* __restrict__
         } else {
             for (int k = 0; k < MLP_NIN; k++) x[k] = 0.f;
         }
+        // samples without valid features or target (a slot the inference
+        // marked, or one without a converged h) add nothing
+        bool good = valid && isfinite(y);
+        for (int k = 0; k < MLP_NIN; k++) good = good && isfinite(x[k]);
+        if (!good) {
+            for (int k = 0; k < MLP_NIN; k++) x[k] = 0.f;
+            y = 0.f;
+        }
         float h1[32], h2[32];
         for (int n = 0; n < 32; n++) {
             float z = B1[n];
@@ -327,7 +346,7 @@ __global__ void __launch_bounds__(TRAIN_BS) k_mlp_grad(const float* __restrict__
         }
         float out = b3;
         for (int k = 0; k < 32; k++) out += W3[k] * h2[k];
-        const float r = valid ? (out - y) : 0.f;
+        const float r = good ? (out - y) : 0.f;
         const float dz3 = 2.f * r * inv;
         lacc += r * r * inv;
         float dz2[32];
@@ -386,6 +405,8 @@ __global__ void k_mlp_adam(float* p, float* m, float* v, float* g, int step, flo
     if (q >= MLP_NPARAM) return;
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     const float gq = g[q];
+    g[q] = 0.f;   // ready for the next minibatch without a memset
+    if (!isfinite(gq)) return;   // never let a non-finite gradient into the weights
     const float mq = b1 * m[q] + (1.f - b1) * gq;
     const float vq = b2 * v[q] + (1.f - b2) * gq * gq;
     m[q] = mq;
@@ -393,7 +414,6 @@ __global__ void k_mlp_adam(float* p, float* m, float* v, float* g, int step, flo
     const float mh = mq / (1.f - powf(b1, (float)step));
     const float vh = vq / (1.f - powf(b2, (float)step));
     p[q] -= lr * mh / (sqrtf(vh) + eps);
-    g[q] = 0.f;   // ready for the next minibatch without a memset
 }
 
 // ---------------------------------------------------------------------------

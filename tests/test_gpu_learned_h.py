@@ -124,8 +124,47 @@ def test_learned_h_through_the_host_buffer_step(gpulib):
         res[learned] = {k: v.copy() for k, v in g.state.items()}
         work[learned] = sum(w[2:])
         g.close()
-    for k in ("x", "vel", "hh", "rho", "en"):
+    for k in ("x", "vel", "hh", "rho", "en", "Bevol", "alpha", "force", "dBevoldt", "dudt"):
         a, b = res[1][k], res[0][k]
         scale = max(float(np.max(np.abs(b))), 1e-30)
         assert float(np.max(np.abs(a - b))) <= 10 * o["tolh"] * scale, k
     assert work[1] < work[0], work
+
+
+def test_learned_h_host_step_without_density_outputs(gpulib):
+    """The host-buffer step with the density outputs left out (NULL rho,
+    drho/dt, numneigh, c_s ...: the integrator's set of the Fortran shim's
+    gpu_step): the predictor's rho then follows each particle from the
+    previous step, and the first step, which has no rho yet, keeps h_pred
+    and trains on nothing, so the network never sees a non-finite feature.
+    The learned steps then need no more density work than with every output
+    passed."""
+    import numpy as np
+    from ndspmhd_gb300.gpu import GpuSPH
+    o, p = configs.mhd_box_3d(32, seed=11)
+    o = dict(o, precision=1, learned_h=1)
+    g0 = GpuSPH(o, configs.full_state(p, 3))
+    g0.primitive2conservative()
+    st = {k: v.copy() for k, v in g0.state.items()}
+    g0.close()
+    info_only = ("rho", "rhoalt", "drhodt", "gradh", "gradhn", "gradgradh", "numneigh", "dens", "uu", "pr",
+                 "spsound", "Bfield", "dudt", "divB", "curlB", "del2u", "graddivv")
+    work, res = {}, {}
+    for drop in (False, True):
+        g = GpuSPH(o, {k: v.copy() for k, v in st.items()})
+        if drop:
+            for k in info_only:
+                setattr(g._p, k, None)
+        g.set_tuning(nl_reuse=0)   # every upload goes through the host order
+        g.dt.dt, g.dt.time, g.dt.nsteps = 0.0, 0.0, 0
+        w = []
+        for _ in range(8):
+            g.step()
+            w.append(g.dts()["ncalctotal"] / g.n)
+        work[drop] = float(np.mean(w[3:]))
+        res[drop] = {k: g.state[k].copy() for k in ("x", "hh", "vel")}
+        g.close()
+    assert work[True] <= 1.1 * work[False] + 0.02, work
+    for k in ("x", "hh", "vel"):
+        scale = max(float(np.max(np.abs(res[False][k]))), 1e-30)
+        assert float(np.max(np.abs(res[True][k] - res[False][k]))) <= 10 * o["tolh"] * scale, k
