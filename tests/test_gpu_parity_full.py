@@ -16,7 +16,8 @@ too:
 * a 1,600-particle Brio-Wu tube with fixed ends (the largest tube of the
   batched workload): neighbour sets, derivs, four steps;
 * the two-fluid dust box at 2 x 24^3 (every gas-dust drag pair): derivs and
-  four steps.
+  four steps; at its own size, 2 x 96^3, one derivs in both forms; and the
+  batch of its 8 settings (14.2 M particles) against each setting run alone.
 
 Both codes start from the same state (primitive2conservative of the GPU
 FP64 form for the 128^3 box, whose oracle set-up would take half a minute;
@@ -223,6 +224,64 @@ def test_brio_wu_1600_tube(gpulib):
     _check_derivs(g, ref, o, "brio-wu 1600")
     g.close()
     _check_steps(o, st, "brio-wu 1600")
+
+
+def test_dust_box_full_2x96(gpulib):
+    """The dust workload at its own size (2 x 96^3 = 1,769,472 particles, one
+    of its settings): one derivs, FP64 form against the oracle at 1e-12 with
+    numneigh exact and dtdrag, the FP32 form within its stated bounds."""
+    from ndspmhd_gb300.gpu import GpuSPH
+    o, p = configs.dust_gas_box_3d(96, eps=0.3, tstop=0.02, seed=77)
+    g = GpuSPH(o, configs.full_state(p, 3))
+    g.primitive2conservative()
+    st = {k: v.copy() for k, v in g.state.items()}
+    g.close()
+    g, ref = _derivs_pair(o, st)
+    _check_derivs(g, ref, o, "dust 2x96^3")
+    g.close()
+    _check_fp32_many(o, st, ref, "dust 2x96^3")
+
+
+def test_dust_batch_full_8_settings(gpulib):
+    """The batched dust workload at its own size: 8 (eps, t_s) settings of
+    2 x 96^3 in one periodic batch (14,155,776 particles), FP32 form.  After
+    two steps every setting agrees with the same setting run alone (FP32 form)
+    within 1e-5: the batch's shared cells change only the order of each pair
+    sum.  At tolh 1e-6, as in _check_fp32_many: at the workload's 1e-3 a few
+    particles per million sit within rounding of the tolerance and stop one
+    Newton-Raphson pass apart in the two orders, which moves their h by up to
+    tolh."""
+    from ndspmhd_gb300.gpu import GpuSPH
+    rng = np.random.default_rng(99)
+    eps = np.exp(rng.uniform(np.log(0.01), np.log(1.0), 8))
+    ts = np.exp(rng.uniform(np.log(1e-3), np.log(1.0), 8))
+    runs = [configs.dust_gas_box_3d(96, eps=float(eps[k]), tstop=float(ts[k]), seed=77 + k) for k in range(8)]
+    parts = [q for _, q in runs]
+    cat = {k: np.concatenate([q[k] for q in parts], axis=0) for k in parts[0]}
+    sim = np.concatenate([np.full(q["x"].shape[0], s, np.int32) for s, q in enumerate(parts)])
+    runs = [(dict(o, tolh=1e-6), q) for o, q in runs]
+    o0 = dict(runs[0][0], precision=1)
+    g = GpuSPH(o0, configs.full_state(cat, 3))
+    g.batch_set_kdrag([o["Kdrag"] for o, _ in runs])
+    g.batch_upload(sim, 8, initialise=True)
+    _, t = g.batch_step(2)
+    g.batch_download()
+    out = {k: g.state[k].copy() for k in STEP_FIELDS}
+    g.close()
+    start = 0
+    for k, (o, q) in enumerate(runs):
+        n = q["x"].shape[0]
+        a = GpuSPH(dict(o, precision=1), configs.full_state(q, 3))
+        a.primitive2conservative()
+        a.dev_upload()
+        a.set_dt(0.0)
+        a.dev_step(2)
+        a.dev_download()
+        assert abs(a.dts()["time"] - t[k]) <= 1e-6 * t[k], (k, a.dts()["time"], t[k])
+        errs, bad = compare_fields({f: out[f][start:start + n] for f in STEP_FIELDS}, a.state, STEP_FIELDS, 1e-5)
+        assert not bad, (k, errs)
+        a.close()
+        start += n
 
 
 def test_dust_box_2x24(gpulib):
