@@ -725,8 +725,9 @@ template <int NDIM>
 constexpr int rates_chunk() { return NDSPH_RATES_CHUNK; }
 // every lane of a warp calls it together (the reductions at its end are warp
 // shuffles, and block-wide in a one-simulation FP32 sweep): `live` false runs
-// an empty candidate set on slot i
-template <int NDIM, int PREC, class Src>
+// an empty candidate set on slot i.  TYPED: two particle types (the 3D FP32
+// sweep of a gas + dust run), see the two runs of accepted entries below.
+template <int NDIM, int PREC, class Src, bool TYPED = false>
 __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, const bool live, const Src& src)
 {
     typedef typename std::conditional<PREC == NDSPH_PREC_FP64, double, float>::type R;
@@ -1083,13 +1084,20 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
         // so the lanes of a warp do not idle on rejected candidates in the
         // long part.  The accepted pairs, their order and the screen
         // arithmetic are those of a single pass over the row.
+        // With two particle types (gas and dust: TYPED) the accepted entries are
+        // kept in two runs, the pairs of matching types from the front of the
+        // chunk and the gas-dust (drag) pairs from its back, and the second
+        // phase runs the two runs one after the other: the lanes of a warp
+        // then take the same branch of the pair terms instead of alternating
+        // between the hydro/MHD terms and the drag terms pair by pair.
         constexpr int RATES_CHUNK = rates_chunk<NDIM>();
         __shared__ unsigned acc_buf[RATES_CHUNK * RATES_BS];
         unsigned* mine = acc_buf + threadIdx.x;
+        const bool typed = (o.idust != 0);
         int k = 0;   // a multiple of 4 whenever a vector row load is issued
         while (k < ncand) {
-            int na = 0;
-            while (na + 4 <= RATES_CHUNK && k < ncand) {
+            int na = 0, nb = 0;
+            while (na + nb + 4 <= RATES_CHUNK && k < ncand) {
                 unsigned pq[4];
                 int m = 4;
                 if (k + 4 <= ncand) {
@@ -1101,8 +1109,12 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                     for (int u = 0; u < 4; u++) pq[u] = (u < m) ? row[k + u] : ((unsigned)i << shift);
                 }
                 float4 xq[4];
+                int tq[4];
 #pragma unroll
-                for (int u = 0; u < 4; u++) xq[u] = a.S.xs[pq[u] >> shift];
+                for (int u = 0; u < 4; u++) {
+                    xq[u] = a.S.xs[pq[u] >> shift];
+                    tq[u] = TYPED ? a.S.itype[pq[u] >> shift] : typei;
+                }
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
                     int d[3], w[3];
@@ -1111,8 +1123,13 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                     const float r2f = screen_r2<NDIM>(xsi, xq[u], d, g, dxf);
                     const float hm = fmaxf(hif, xq[u].w);
                     if ((int)(pq[u] >> shift) != i && r2f < 4.0f * hm * hm) {
-                        mine[na * RATES_BS] = pq[u];
-                        na++;
+                        if (!TYPED || type_match(typei, tq[u])) {
+                            mine[na * RATES_BS] = pq[u];
+                            na++;
+                        } else {
+                            nb++;
+                            mine[(RATES_CHUNK - nb) * RATES_BS] = pq[u];
+                        }
                     }
                 }
                 k += m;
@@ -1123,9 +1140,9 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
             // 2.83 -> 2.64 ms at 128^3).  Loading the next entry's data while
             // this one's terms run needs 20 more registers and spilled
             // (3.14 ms).
-            const bool typed = (o.idust != 0);
-            for (int q = 0; q < na; q++) {
-                const unsigned pk = mine[q * RATES_BS];
+            for (int q = 0; q < na + nb; q++) {
+                // the matching-type run, then the drag run in the order found
+                const unsigned pk = mine[(!TYPED || q < na ? q : RATES_CHUNK - 1 - (q - na)) * RATES_BS];
                 const int j = (int)(pk >> shift);
                 float4 cur[5];
                 cur[0] = a.S.xs[j];
@@ -1331,7 +1348,7 @@ void launch_pack_rates(const SweepArgs& a, cudaStream_t st)
     if (a.n > 0) NDSPH_COUNT_LAUNCH, k_pack_rates<<<nblk(a.n, 256), 256, 0, st>>>(a);
 }
 
-template <int NDIM, int PREC>
+template <int NDIM, int PREC, bool TYPED = false>
 __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MINB) k_rates(SweepArgs a)
 {
     // no early return: every lane of the warp takes part in the final
@@ -1339,7 +1356,7 @@ __global__ void __launch_bounds__(RATES_BS, PREC == 0 ? 2 : NDSPH_RATES_FP32_MIN
     const int ithread = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = ithread < (a.plist ? a.pn : a.n);
     const int i = live ? (a.plist ? a.plist[a.pi0 + ithread] : ithread) : 0;
-    rates_body<NDIM, PREC>(a, i, live, RowSrc{});
+    rates_body<NDIM, PREC, RowSrc, TYPED>(a, i, live, RowSrc{});
 }
 
 void launch_rates(const SweepArgs& a, cudaStream_t st)
@@ -1355,6 +1372,7 @@ void launch_rates(const SweepArgs& a, cudaStream_t st)
     } else {
         if (a.o.ndim == 1) NDSPH_COUNT_LAUNCH, k_rates<1, 1><<<nb, bs, 0, st>>>(a);
         else if (a.o.ndim == 2) NDSPH_COUNT_LAUNCH, k_rates<2, 1><<<nb, bs, 0, st>>>(a);
+        else if (a.o.idust != 0) NDSPH_COUNT_LAUNCH, k_rates<3, 1, true><<<nb, bs, 0, st>>>(a);
         else NDSPH_COUNT_LAUNCH, k_rates<3, 1><<<nb, bs, 0, st>>>(a);
     }
 }
