@@ -639,9 +639,24 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-form measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and learned-h workloads")
+    ap.add_argument("--only", choices=["batched", "dust", "learned", "ot2d"],
+                    help="run one secondary workload alone and print its JSON (for profiling it)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.only:
+        import torch
+        torch.cuda.set_device(0)
+        if args.only == "batched":
+            r = run_batched(args.steps, max(args.warmup, 3))
+        elif args.only == "dust":
+            r = run_dust(96 if N1D >= 128 else 32, args.steps, max(args.warmup, 3), serial=False)
+        elif args.only == "learned":
+            r = run_learned(min(N1D, 128), args.steps, 40)
+        else:
+            r = run_ot2d()
+        print(json.dumps({"workload": args.only, **r}), flush=True)
         return
 
     import torch
