@@ -222,7 +222,8 @@ NDSPH_API int ndsph_dev_set_time(ndsph_ctx* ctx, double dt, double time, int32_t
  * boundaries, or periodic in every dimension: each simulation then keeps its
  * own periodic box, the same xmin/xmax for all), in one device state: the
  * batched counterpart of running the reference once per input file
- * (ndspmhd.f90:312-359, multi/multirun.f90).
+ * (ndspmhd.f90:312-359, multi/multirun.f90).  Batched steps predict h as
+ * the reference does (the learned-h option applies to one simulation).
  * sim[i] (0-based) names the simulation of particle i; ireal stays 1-based
  * over the whole array.  Each simulation keeps its own dt and clock (first
  * step dt = 0 as evolve.f90:50-56); reductions (dtcourant, dtforce,

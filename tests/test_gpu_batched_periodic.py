@@ -12,7 +12,8 @@ run alone through the oracle (one reference run per input file):
   ghosts' hhmax (ghostND_mhd.f90:218) and relinks;
 * the FP32 form of the batch within its 1e-5 bound of the oracle, and after
   six steps within 1e-5 of the same boxes run one at a time in the FP32 form
-  (the batch's cells differ, so only the order of each pair sum does).
+  (the batch's cells differ, so only the order of each pair sum does);
+* a 2D periodic batch (Orszag-Tang at two resolutions) against the oracle.
 """
 import numpy as np
 import pytest
@@ -144,6 +145,36 @@ def test_dust_batch_fp32_form(gpulib):
         errs, bad = compare_fields(got, g.state, STEP_FIELDS, 1e-5)
         assert not bad, (k, errs)
         g.close()
+
+
+def test_orszag_tang_2d_batch_match_oracle(gpulib):
+    """A 2D periodic batch (the grids stacked along y): the Orszag-Tang vortex
+    at two resolutions (32 x 36 and 48 x 56 particles on their own hcp
+    lattices), MHD, against two oracle runs after 3 steps."""
+    from ndspmhd_gb300.gpu import GpuSPH
+    from oracle.oracle import Oracle
+    runs = [configs.orszag_tang_2d(nx) for nx in (32, 48)]
+    parts = [q for _, q in runs]
+    cat = {k: np.concatenate([q[k] for q in parts], axis=0) for k in parts[0]}
+    sim = np.concatenate([np.full(q["x"].shape[0], s, np.int32) for s, q in enumerate(parts)])
+    o = dict(runs[0][0], psep=min(r[0]["psep"] for r in runs))
+    g = GpuSPH(o, configs.full_state(cat, 2))
+    g.batch_upload(sim, 2, initialise=True)
+    dt, t = g.batch_step(3)
+    g.batch_download()
+    start = 0
+    for k, (ok, pk) in enumerate(runs):
+        n = pk["x"].shape[0]
+        orc = Oracle(ok, configs.full_state(pk, 2))
+        orc.primitive2conservative()
+        orc.step(3)
+        got = {f: g.state[f][start:start + n] for f in STEP_FIELDS}
+        errs, bad = compare_fields(got, orc.state, STEP_FIELDS, 1e-9)
+        assert not bad, (k, errs)
+        d = orc.dts()
+        assert abs(t[k] - d["time"]) <= 1e-10 * d["time"], (k, t[k], d["time"])
+        start += n
+    g.close()
 
 
 def test_batch_refuses_mixed_boundaries(gpulib):
