@@ -358,7 +358,7 @@ static void free_particles(ndsph_ctx* ctx)
                     ctx->S.numneigh, ctx->S.cell, ctx->S.xs, ctx->S.h1, ctx->S.active, ctx->S.active_next,
                     ctx->S.flag, ctx->itype2, ctx->id2, ctx->ireal2, ctx->srt.key, ctx->srt.slot, ctx->srt.perm, ctx->srt.perm2,
                     ctx->d_stage, ctx->d_stage_late, ctx->d_istage, ctx->S.pk_v, ctx->S.pk_t, ctx->S.pk_b, ctx->S.pk_a,
-                    ctx->S.nl, ctx->S.nl_cnt, ctx->S.hb, ctx->S.xsb, ctx->S.xg, ctx->S.sim, ctx->sim2, ctx->d_plist,
+                    ctx->S.nl, ctx->S.nl_cnt, ctx->S.nl2, ctx->S.nl_cnt2, ctx->S.hb, ctx->S.xsb, ctx->S.xg, ctx->S.sim, ctx->sim2, ctx->d_plist,
                     ctx->d_pcnt};
     for (void* p : ptrs) if (p) cudaFree(p);
     ctx->slab[0] = ctx->slab[1] = nullptr;
@@ -401,6 +401,7 @@ static int ensure_capacity(ndsph_ctx* ctx, int n)
     CK(cudaMalloc(&ctx->S.pk_b, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.pk_a, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.nl_cnt, ib));
+    CK(cudaMalloc(&ctx->S.nl_cnt2, ib));
     CK(cudaMalloc(&ctx->S.sim, ib));
     CK(cudaMalloc(&ctx->sim2, ib));
     CK(cudaMalloc(&ctx->d_plist, ib));
@@ -410,6 +411,7 @@ static int ensure_capacity(ndsph_ctx* ctx, int n)
     CK(cudaMalloc(&ctx->S.xsb, sizeof(float4) * (size_t)cap));
     CK(cudaMalloc(&ctx->S.xg, sizeof(float4) * (size_t)cap));
     ctx->S.nl = nullptr;
+    ctx->S.nl2 = nullptr;
     ctx->nl_valid = false;
     ctx->nl_stride = 0;
     CK(cudaMalloc(&ctx->d_istage, ib));
@@ -1142,6 +1144,13 @@ static int link_all(ndsph_ctx* ctx, bool keep_hmax_ghost)
     return do_link(ctx, all.data(), NF, keep_hmax_ghost);
 }
 
+// neighbour rows split by particle type: two types (gas + dust) in the 3D
+// FP32 form, whose density passes then read only the rows of their own type
+static bool typed_rows_wanted(const ndsph_ctx* ctx)
+{
+    return ctx->o.idust != 0 && ctx->o.precision == NDSPH_PREC_FP32 && ctx->o.ndim == 3;
+}
+
 static SweepArgs sweep_args(ndsph_ctx* ctx)
 {
     SweepArgs a;
@@ -1161,6 +1170,7 @@ static SweepArgs sweep_args(ndsph_ctx* ctx)
     a.nl_stride = ctx->nl_stride;
     a.nl_skin = ctx->nl_skin;
     a.nl_dmax = ctx->nl_dmax;
+    a.typed_rows = (typed_rows_wanted(ctx) && ctx->S.nl2) ? 1 : 0;
     a.d_its = nullptr;
     a.d_nlist = nullptr;
     a.gate = nullptr;
@@ -1178,11 +1188,13 @@ static int build_nlist(ndsph_ctx* ctx)
 {
     cudaStream_t st = ctx->st;
     ctx->nl_valid = false;
+    const bool typed = typed_rows_wanted(ctx);
     if (ctx->nl_stride == 0) {
         int s0 = ctx->o.ndim == 1 ? 32 : (ctx->o.ndim == 2 ? 64 : 160);
         CK(cudaMalloc(&ctx->S.nl, sizeof(unsigned) * (size_t)s0 * ctx->cap));
         ctx->nl_stride = s0;
     }
+    if (typed && !ctx->S.nl2) CK(cudaMalloc(&ctx->S.nl2, sizeof(unsigned) * (size_t)ctx->nl_stride * ctx->cap));
     for (int attempt = 0; attempt < 4; attempt++) {
         int z[3] = {0, 0, 0};
         CK(cudaMemcpyAsync(&ctx->red->nl_stale, z, sizeof(int) * 3, cudaMemcpyHostToDevice, st));
@@ -1203,6 +1215,11 @@ static int build_nlist(ndsph_ctx* ctx)
         CK(cudaFree(ctx->S.nl));
         ctx->S.nl = nullptr;
         CK(cudaMalloc(&ctx->S.nl, sizeof(unsigned) * (size_t)ns * ctx->cap));
+        if (ctx->S.nl2) {
+            CK(cudaFree(ctx->S.nl2));
+            ctx->S.nl2 = nullptr;
+            CK(cudaMalloc(&ctx->S.nl2, sizeof(unsigned) * (size_t)ns * ctx->cap));
+        }
         ctx->nl_stride = ns;
     }
     ctx->err = "neighbour list stride did not converge";

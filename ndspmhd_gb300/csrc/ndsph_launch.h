@@ -31,6 +31,11 @@ struct Side {
     // each entry packs (j << 5) | stencil offset of j's cell
     unsigned* nl;
     int* nl_cnt;
+    // two particle types (gas + dust, 3D FP32 form): nl/nl_cnt then hold the
+    // candidates of the slot's own type (the ones the density sums see) and
+    // nl2/nl_cnt2 those of the other type (the drag pairs of the rates sweep)
+    unsigned* nl2;
+    int* nl_cnt2;
     float* hb;        // h of each slot when its list was built
     float4* xsb;      // xs of each slot when its list was built (reuse check)
     float4* xg;       // FP32 position relative to the grid origin + h (3D row build)
@@ -74,6 +79,7 @@ struct SweepArgs {
     int nl_stride;           // entries per particle
     float nl_skin;           // list radius = 2 max(h_i,h_j) skin (h may grow by skin before a rebuild)
     float nl_dmax;           // largest displacement since the rows were built (0 right after a build)
+    int typed_rows;          // rows split by type (nl: matching types, nl2: the other type)
     // device-side control (captured step): when set, the pass number, the
     // active count and the row-build gate are read from device memory
     const int* d_its;

@@ -449,7 +449,9 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
         // FP32 form: four candidates' loads in flight at once (the pair work
         // is short, so the loop is bound by load latency otherwise)
         // rows are 16-byte aligned with a stride of a multiple of 4 entries
-        const bool typed = (o.idust != 0);   // without dust every type pair matches
+        // without dust every type pair matches; rows split by type hold only
+        // the slot's own type here
+        const bool typed = (o.idust != 0) && !a.typed_rows;
         // the next four row entries are loaded while this group's positions
         // and packs are fetched and summed (1.20 -> 1.16 ms of density
         // passes per 128^3 step)
@@ -726,7 +728,7 @@ constexpr int rates_chunk() { return NDSPH_RATES_CHUNK; }
 // every lane of a warp calls it together (the reductions at its end are warp
 // shuffles, and block-wide in a one-simulation FP32 sweep): `live` false runs
 // an empty candidate set on slot i.  TYPED: two particle types (the 3D FP32
-// sweep of a gas + dust run), see the two runs of accepted entries below.
+// sweep of a gas + dust run, rows split by type), see the two runs below.
 template <int NDIM, int PREC, class Src, bool TYPED = false>
 __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, const bool live, const Src& src)
 {
@@ -1076,83 +1078,74 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
         const unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
         for (int k = 0; k < ncand; k++) pair_terms(row[k], nullptr, 0);
     } else {
-        const int ncand = live ? a.S.nl_cnt[i] : 0;
-        const unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
         // Two phases per chunk of the row: screen the candidates (four row
         // entries and positions in flight at a time) and keep the accepted
         // entries in shared memory, then run the pair terms over those only,
         // so the lanes of a warp do not idle on rejected candidates in the
         // long part.  The accepted pairs, their order and the screen
         // arithmetic are those of a single pass over the row.
-        // With two particle types (gas and dust: TYPED) the accepted entries are
-        // kept in two runs, the pairs of matching types from the front of the
-        // chunk and the gas-dust (drag) pairs from its back, and the second
-        // phase runs the two runs one after the other: the lanes of a warp
-        // then take the same branch of the pair terms instead of alternating
-        // between the hydro/MHD terms and the drag terms pair by pair.
         constexpr int RATES_CHUNK = rates_chunk<NDIM>();
         __shared__ unsigned acc_buf[RATES_CHUNK * RATES_BS];
         unsigned* mine = acc_buf + threadIdx.x;
         const bool typed = (o.idust != 0);
-        int k = 0;   // a multiple of 4 whenever a vector row load is issued
-        while (k < ncand) {
-            int na = 0, nb = 0;
-            while (na + nb + 4 <= RATES_CHUNK && k < ncand) {
-                unsigned pq[4];
-                int m = 4;
-                if (k + 4 <= ncand) {
-                    const uint4 r4 = *reinterpret_cast<const uint4*>(row + k);
-                    pq[0] = r4.x; pq[1] = r4.y; pq[2] = r4.z; pq[3] = r4.w;
-                } else {
-                    m = ncand - k;
+        auto sweep_row = [&](const unsigned* row, const int ncand) {
+            int k = 0;   // a multiple of 4 whenever a vector row load is issued
+            while (k < ncand) {
+                int na = 0;
+                while (na + 4 <= RATES_CHUNK && k < ncand) {
+                    unsigned pq[4];
+                    int m = 4;
+                    if (k + 4 <= ncand) {
+                        const uint4 r4 = *reinterpret_cast<const uint4*>(row + k);
+                        pq[0] = r4.x; pq[1] = r4.y; pq[2] = r4.z; pq[3] = r4.w;
+                    } else {
+                        m = ncand - k;
 #pragma unroll
-                    for (int u = 0; u < 4; u++) pq[u] = (u < m) ? row[k + u] : ((unsigned)i << shift);
-                }
-                float4 xq[4];
-                int tq[4];
+                        for (int u = 0; u < 4; u++) pq[u] = (u < m) ? row[k + u] : ((unsigned)i << shift);
+                    }
+                    float4 xq[4];
 #pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    xq[u] = a.S.xs[pq[u] >> shift];
-                    tq[u] = TYPED ? a.S.itype[pq[u] >> shift] : typei;
-                }
+                    for (int u = 0; u < 4; u++) xq[u] = a.S.xs[pq[u] >> shift];
 #pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    int d[3], w[3];
-                    stn.offset(pq[u] & omask, g, d, w);
-                    float dxf[3];
-                    const float r2f = screen_r2<NDIM>(xsi, xq[u], d, g, dxf);
-                    const float hm = fmaxf(hif, xq[u].w);
-                    if ((int)(pq[u] >> shift) != i && r2f < 4.0f * hm * hm) {
-                        if (!TYPED || type_match(typei, tq[u])) {
+                    for (int u = 0; u < 4; u++) {
+                        int d[3], w[3];
+                        stn.offset(pq[u] & omask, g, d, w);
+                        float dxf[3];
+                        const float r2f = screen_r2<NDIM>(xsi, xq[u], d, g, dxf);
+                        const float hm = fmaxf(hif, xq[u].w);
+                        if ((int)(pq[u] >> shift) != i && r2f < 4.0f * hm * hm) {
                             mine[na * RATES_BS] = pq[u];
                             na++;
-                        } else {
-                            nb++;
-                            mine[(RATES_CHUNK - nb) * RATES_BS] = pq[u];
                         }
                     }
+                    k += m;
                 }
-                k += m;
+                // the accepted entries: each one's position and four packs
+                // are loaded together, one round trip to L1/L2 per pair
+                // (loaded inside the pair terms, the packs waited for the
+                // position's screen: 2.83 -> 2.64 ms at 128^3).  Loading the
+                // next entry's data while this one's terms run needs 20 more
+                // registers and spilled (3.14 ms).
+                for (int q = 0; q < na; q++) {
+                    const unsigned pk = mine[q * RATES_BS];
+                    const int j = (int)(pk >> shift);
+                    float4 cur[5];
+                    cur[0] = a.S.xs[j];
+                    cur[1] = a.S.pk_v[j];
+                    cur[2] = a.S.pk_t[j];
+                    cur[3] = a.S.pk_b[j];
+                    cur[4] = a.S.pk_a[j];
+                    pair_terms(pk, cur, typed ? a.S.itype[j] : typei);
+                }
             }
-            // the accepted entries: each one's position and four packs are
-            // loaded together, one round trip to L1/L2 per pair (loaded inside
-            // the pair terms, the packs waited for the position's screen:
-            // 2.83 -> 2.64 ms at 128^3).  Loading the next entry's data while
-            // this one's terms run needs 20 more registers and spilled
-            // (3.14 ms).
-            for (int q = 0; q < na + nb; q++) {
-                // the matching-type run, then the drag run in the order found
-                const unsigned pk = mine[(!TYPED || q < na ? q : RATES_CHUNK - 1 - (q - na)) * RATES_BS];
-                const int j = (int)(pk >> shift);
-                float4 cur[5];
-                cur[0] = a.S.xs[j];
-                cur[1] = a.S.pk_v[j];
-                cur[2] = a.S.pk_t[j];
-                cur[3] = a.S.pk_b[j];
-                cur[4] = a.S.pk_a[j];
-                pair_terms(pk, cur, typed ? a.S.itype[j] : typei);
-            }
-        }
+        };
+        sweep_row(a.S.nl + (size_t)i * a.nl_stride, live ? a.S.nl_cnt[i] : 0);
+        // two particle types (gas and dust: TYPED, rows split by type): the
+        // rows of the other type, the drag pairs, follow as a second run, so
+        // the lanes of a warp take one branch of the pair terms at a time
+        // instead of alternating between the hydro/MHD terms and the drag
+        // terms pair by pair
+        if constexpr (TYPED) sweep_row(a.S.nl2 + (size_t)i * a.nl_stride, live ? a.S.nl_cnt2[i] : 0);
     }
 
     if (PREC == NDSPH_PREC_FP64) {
@@ -1372,7 +1365,7 @@ void launch_rates(const SweepArgs& a, cudaStream_t st)
     } else {
         if (a.o.ndim == 1) NDSPH_COUNT_LAUNCH, k_rates<1, 1><<<nb, bs, 0, st>>>(a);
         else if (a.o.ndim == 2) NDSPH_COUNT_LAUNCH, k_rates<2, 1><<<nb, bs, 0, st>>>(a);
-        else if (a.o.idust != 0) NDSPH_COUNT_LAUNCH, k_rates<3, 1, true><<<nb, bs, 0, st>>>(a);
+        else if (a.typed_rows) NDSPH_COUNT_LAUNCH, k_rates<3, 1, true><<<nb, bs, 0, st>>>(a);
         else NDSPH_COUNT_LAUNCH, k_rates<3, 1><<<nb, bs, 0, st>>>(a);
     }
 }
@@ -1768,23 +1761,48 @@ __device__ __forceinline__ float slab_dist(float x, int dc, float cs)
     return fmaxf(fmaxf(lo - x, x - (lo + cs)), 0.0f);
 }
 
+// the rows a build writes for one slot: its own row and count, and with
+// TYPED (two particle types) the row and count of the other type's entries
+struct RowOut {
+    unsigned* row;
+    int cnt;
+    unsigned* row2;
+    int cnt2;
+    int typei;
+};
+template <bool TYPED>
+__device__ __forceinline__ void row_put(const SweepArgs& a, RowOut& out, int tj, unsigned e)
+{
+    if (TYPED && !type_match(out.typei, tj)) {
+        if (out.cnt2 < a.nl_stride) out.row2[out.cnt2] = e;
+        out.cnt2++;
+    } else {
+        if (out.cnt < a.nl_stride) out.row[out.cnt] = e;
+        out.cnt++;
+    }
+}
+
 // candidates of slot i in the slot range [jb, je) of a run of x-adjacent
 // cells starting at x offset dx0: the x offset of j's cell steps up at each
 // of the run's inner cell starts b[0..3] (je where the run is shorter); the
 // stencil index is obase + dx + r.  Loads are issued four at a time so that
 // their latencies overlap.
-template <int NDIM>
+template <int NDIM, bool TYPED = false>
 __device__ __forceinline__ void nl_scan_run(const SweepArgs& a, const float4& xsi, float hi, float sk,
                                             float abs_tol, int jb, int je, const int b[4], int dx0, float oy,
-                                            float oz, unsigned obase, unsigned* row, int& cnt)
+                                            float oz, unsigned obase, RowOut& out)
 {
     const Grid& g = a.g;
     const unsigned shift = (NDIM == 3) ? (unsigned)g.nlshift : 5u;
     const int r = (NDIM == 2) ? 1 : (g.sw - 1) >> 1;
     for (int j0 = jb; j0 < je; j0 += 4) {
         float4 q[4];
+        int tq[4] = {0, 0, 0, 0};
 #pragma unroll
-        for (int u = 0; u < 4; u++) q[u] = (j0 + u < je) ? a.S.xs[j0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int u = 0; u < 4; u++) {
+            q[u] = (j0 + u < je) ? a.S.xs[j0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (TYPED) tq[u] = (j0 + u < je) ? a.S.itype[j0 + u] : 0;
+        }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const int j = j0 + u;
@@ -1796,8 +1814,7 @@ __device__ __forceinline__ void nl_scan_run(const SweepArgs& a, const float4& xs
             if (NDIM >= 3) { const float t = (xsi.z - q[u].z) - oz; r2 += t * t; }
             const float rc = sk * fmaxf(hi, q[u].w) + abs_tol;
             if (r2 > rc * rc) continue;
-            if (cnt < a.nl_stride) row[cnt] = ((unsigned)j << shift) | (obase + (unsigned)(dx + r));
-            cnt++;
+            row_put<TYPED>(a, out, tq[u], ((unsigned)j << shift) | (obase + (unsigned)(dx + r)));
         }
     }
 }
@@ -1806,17 +1823,22 @@ __device__ __forceinline__ void nl_scan_run(const SweepArgs& a, const float4& xs
 // simulation): the separation is a plain difference (ox: the periodic image
 // shift of the run's cells), and the x cell offset is counted only for the
 // entries written
+template <bool TYPED = false>
 __device__ __forceinline__ void nl_scan_run_g(const SweepArgs& a, const float4& xgi, float hi, float sk,
                                               float abs_tol, int jb, int je, const int b[4], int dx0, float ox,
-                                              float oy, float oz, unsigned obase, unsigned* row, int& cnt)
+                                              float oy, float oz, unsigned obase, RowOut& out)
 {
     const unsigned shift = (unsigned)a.g.nlshift;
     const int r = (a.g.sw - 1) >> 1;
     const float xi = xgi.x - ox, yi = xgi.y - oy, zi = xgi.z - oz;
     for (int j0 = jb; j0 < je; j0 += 4) {
         float4 q[4];
+        int tq[4] = {0, 0, 0, 0};
 #pragma unroll
-        for (int u = 0; u < 4; u++) q[u] = (j0 + u < je) ? a.S.xg[j0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int u = 0; u < 4; u++) {
+            q[u] = (j0 + u < je) ? a.S.xg[j0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (TYPED) tq[u] = (j0 + u < je) ? a.S.itype[j0 + u] : 0;
+        }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const int j = j0 + u;
@@ -1825,11 +1847,8 @@ __device__ __forceinline__ void nl_scan_run_g(const SweepArgs& a, const float4& 
             const float r2 = tx * tx + ty * ty + tz * tz;
             const float rc = sk * fmaxf(hi, q[u].w) + abs_tol;
             if (r2 > rc * rc) continue;
-            if (cnt < a.nl_stride) {
-                const int dx = dx0 + (j >= b[0]) + (j >= b[1]) + (j >= b[2]) + (j >= b[3]);
-                row[cnt] = ((unsigned)j << shift) | (obase + (unsigned)(dx + r));
-            }
-            cnt++;
+            const int dx = dx0 + (j >= b[0]) + (j >= b[1]) + (j >= b[2]) + (j >= b[3]);
+            row_put<TYPED>(a, out, tq[u], ((unsigned)j << shift) | (obase + (unsigned)(dx + r)));
         }
     }
 }
@@ -1853,7 +1872,7 @@ __global__ void k_xg(Side S, Grid g, int n)
 // pair a sweep may need is within it) form a run of x-adjacent cells, one
 // slot range unless it wraps or leaves an open box; rows and cells beyond
 // the reach are skipped.
-template <int NDIM, bool XG = false>
+template <int NDIM, bool XG = false, bool TYPED = false>
 __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1870,8 +1889,12 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
     const float reach = (float)r * csmin * 1.001f + abs_tol;
     const float reach2 = reach * reach;
     Stencil<NDIM> stn(a.S.cell[i], g);
-    unsigned* row = a.S.nl + (size_t)i * a.nl_stride;
-    int cnt = 0;
+    RowOut out;
+    out.row = a.S.nl + (size_t)i * a.nl_stride;
+    out.cnt = 0;
+    out.row2 = TYPED ? a.S.nl2 + (size_t)i * a.nl_stride : nullptr;
+    out.cnt2 = 0;
+    out.typei = TYPED ? a.S.itype[i] : 0;
     if (NDIM == 1) {
         // 1D: cells of 2 hmax / r in a run of 2r + 1; a cell is searched only
         // within 2 skin max(h_i, largest h of the cell) of the particle, so a
@@ -1885,7 +1908,7 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
             if (!stn.cell_at_d(d, g, a.o, cid, w)) continue;
             if (ex > sk * fmaxf(hi, a.cell_h[cid]) + abs_tol) continue;
             nl_scan_run<NDIM>(a, xsi, hi, sk, abs_tol, a.cell_start[cid], a.cell_start[cid + 1], bnone, dx, 0.f, 0.f,
-                              0u, row, cnt);
+                              0u, out);
         }
     }
     const int zlo = (NDIM >= 3) ? -r : 0, ylo = (NDIM >= 2) ? -r : 0;
@@ -1920,11 +1943,11 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
 #pragma unroll
                 for (int k = 0; k < 4; k++) b[k] = (k < dx1 - dx0) ? a.cell_start[c0 + k + 1] : 0x7fffffff;
                 if (XG)
-                    nl_scan_run_g(a, xgi, hi, sk, abs_tol, a.cell_start[c0], a.cell_start[c1 + 1], b, dx0,
-                                  (float)w[0] * (float)a.o.L[0], gy, gz, obase, row, cnt);
+                    nl_scan_run_g<TYPED>(a, xgi, hi, sk, abs_tol, a.cell_start[c0], a.cell_start[c1 + 1], b, dx0,
+                                         (float)w[0] * (float)a.o.L[0], gy, gz, obase, out);
                 else
-                    nl_scan_run<NDIM>(a, xsi, hi, sk, abs_tol, a.cell_start[c0], a.cell_start[c1 + 1], b, dx0, oy,
-                                      oz, obase, row, cnt);
+                    nl_scan_run<NDIM, TYPED>(a, xsi, hi, sk, abs_tol, a.cell_start[c0], a.cell_start[c1 + 1], b,
+                                             dx0, oy, oz, obase, out);
             } else {
                 const int bnone[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
                 for (int dx = dx0; dx <= dx1; dx++) {
@@ -1932,20 +1955,22 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
                     int cid;
                     if (!stn.cell_at_d(d, g, a.o, cid, w)) continue;
                     if (XG)
-                        nl_scan_run_g(a, xgi, hi, sk, abs_tol, a.cell_start[cid], a.cell_start[cid + 1], bnone, dx,
-                                      (float)w[0] * (float)a.o.L[0], gy, gz, obase, row, cnt);
+                        nl_scan_run_g<TYPED>(a, xgi, hi, sk, abs_tol, a.cell_start[cid], a.cell_start[cid + 1],
+                                             bnone, dx, (float)w[0] * (float)a.o.L[0], gy, gz, obase, out);
                     else
-                        nl_scan_run<NDIM>(a, xsi, hi, sk, abs_tol, a.cell_start[cid], a.cell_start[cid + 1], bnone,
-                                          dx, oy, oz, obase, row, cnt);
+                        nl_scan_run<NDIM, TYPED>(a, xsi, hi, sk, abs_tol, a.cell_start[cid], a.cell_start[cid + 1],
+                                                 bnone, dx, oy, oz, obase, out);
                 }
             }
         }
     }
-    a.S.nl_cnt[i] = cnt < a.nl_stride ? cnt : a.nl_stride;
+    a.S.nl_cnt[i] = out.cnt < a.nl_stride ? out.cnt : a.nl_stride;
+    if (TYPED) a.S.nl_cnt2[i] = out.cnt2 < a.nl_stride ? out.cnt2 : a.nl_stride;
     a.S.hb[i] = hi;
     if (a.S.xsb) a.S.xsb[i] = xsi;
-    if (cnt > a.nl_stride) { a.red->nl_overflow = 1; if (a.graph) a.red->gfail |= 2; }
-    atomicMax(&a.red->nl_maxcnt, cnt);
+    const int cmax = max(out.cnt, out.cnt2);
+    if (cmax > a.nl_stride) { a.red->nl_overflow = 1; if (a.graph) a.red->gfail |= 2; }
+    atomicMax(&a.red->nl_maxcnt, cmax);
 }
 
 // largest h (the xs.w the build uses) of each cell's particles (1D pruning)
@@ -1973,8 +1998,10 @@ void launch_build_nlist(const SweepArgs& a, cudaStream_t st)
         // FP32 positions relative to the grid origin, which carry an error of
         // at most ~6e-8 x 1024 cells, well inside the rows' 2e-4 radius margin
         NDSPH_COUNT_LAUNCH, k_xg<<<nbp, 128, 0, st>>>(a.S, a.g, a.n);
-        NDSPH_COUNT_LAUNCH, k_build_nlist<3, true><<<nbp, 128, 0, st>>>(a);
-    } else NDSPH_COUNT_LAUNCH, k_build_nlist<3><<<nbp, 128, 0, st>>>(a);
+        if (a.typed_rows) NDSPH_COUNT_LAUNCH, k_build_nlist<3, true, true><<<nbp, 128, 0, st>>>(a);
+        else NDSPH_COUNT_LAUNCH, k_build_nlist<3, true><<<nbp, 128, 0, st>>>(a);
+    } else if (a.typed_rows) NDSPH_COUNT_LAUNCH, k_build_nlist<3, false, true><<<nbp, 128, 0, st>>>(a);
+    else NDSPH_COUNT_LAUNCH, k_build_nlist<3><<<nbp, 128, 0, st>>>(a);
 }
 
 // ===========================================================================
