@@ -724,6 +724,60 @@ struct TileSrc {
     float4 xs_self;
 };
 
+// the same brick, candidates from the particle's neighbour row (the rows'
+// exact candidate set) and their data from the staging: a row entry's
+// stencil offset names its cell in the neighbourhood, and its slot's rank in
+// that cell its place in the staging
+template <bool STAGED>
+struct TileRowSrc {
+    static constexpr bool kRows = false;
+    static constexpr bool kData = true;
+    static constexpr bool kRowsLater = true;
+    const TileSmem* t;
+    const float4* sxs;
+    const float4* spv;
+    const unsigned* row;
+    int ncand;
+    int lhome;               // the particle's cell in the neighbourhood (flat index)
+    unsigned shift;
+    const float4* gxs;
+    const float4* gpv;
+    template <class Fn>
+    __device__ __forceinline__ void for_each_data(int i, Fn&& f) const
+    {
+        const unsigned omask = (1u << shift) - 1u;
+        for (int k0 = 0; k0 < ncand; k0 += 4) {
+            unsigned pq[4];
+            if (k0 + 4 <= ncand) {
+                const uint4 r4 = *reinterpret_cast<const uint4*>(row + k0);
+                pq[0] = r4.x; pq[1] = r4.y; pq[2] = r4.z; pq[3] = r4.w;
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; u++) pq[u] = (k0 + u < ncand) ? row[k0 + u] : 0u;
+            }
+            float4 xq[4], vq[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int j = (int)(pq[u] >> shift);
+                if (STAGED) {
+                    int d[3];
+                    stencil_d<3>(pq[u] & omask, 5, d);
+                    const int L = lhome + (d[2] * TE_Y + d[1]) * TE_X + d[0];
+                    const int idx = (k0 + u < ncand) ? t->tab[L] + (j - t->gst[L]) : 0;
+                    xq[u] = sxs[idx];
+                    vq[u] = spv[idx];
+                } else {
+                    xq[u] = gxs[j];
+                    vq[u] = gpv[j];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (k0 + u < ncand) f(pq[u], xq[u], vq[u]);
+        }
+    }
+};
+
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
 __global__ void __launch_bounds__(TILE_BS, 2) k_density_tile(SweepArgs a, int ntx, int nty)
@@ -867,18 +921,22 @@ __global__ void __launch_bounds__(TILE_BS, 2) k_density_tile(SweepArgs a, int nt
         const int L = ((hz + TB_R) * TE_Y + (hy + TB_R)) * TE_X + (hx + TB_R);
         const int i = t.gst[L] + (k - t.hpre[lo]);
         if (staged) {
-            TileSrc<true> src;
-            src.t = &t; src.xs = sxs; src.pv = spv; src.g = &g;
-            src.hx = hx + TB_R; src.hy = hy + TB_R; src.hz = hz + TB_R;
+            TileRowSrc<true> src;
+            src.t = &t; src.sxs = sxs; src.spv = spv;
+            src.row = a.S.nl + (size_t)i * a.nl_stride;
+            src.ncand = a.S.nl_cnt[i];
+            src.lhome = L;
             src.shift = (unsigned)g.nlshift;
-            src.xs_self = a.S.xs[i];
+            src.gxs = a.S.xs; src.gpv = a.S.pk_v;
             density_body<3, true, NDSPH_PREC_FP32>(a, i, src);
         } else {
-            TileSrc<false> src;
-            src.t = &t; src.xs = a.S.xs; src.pv = a.S.pk_v; src.g = &g;
-            src.hx = hx + TB_R; src.hy = hy + TB_R; src.hz = hz + TB_R;
+            TileRowSrc<false> src;
+            src.t = &t; src.sxs = sxs; src.spv = spv;
+            src.row = a.S.nl + (size_t)i * a.nl_stride;
+            src.ncand = a.S.nl_cnt[i];
+            src.lhome = L;
             src.shift = (unsigned)g.nlshift;
-            src.xs_self = a.S.xs[i];
+            src.gxs = a.S.xs; src.gpv = a.S.pk_v;
             density_body<3, true, NDSPH_PREC_FP32>(a, i, src);
         }
     }
