@@ -28,7 +28,6 @@
 // places ghosts, rij2 = dx.dx without FMA, q2 = rij2*h^-2), so the neighbour
 // sets match the reference bit for bit.
 #include <cstdio>
-#include <cstdlib>
 #include <type_traits>
 #include "ndsph_launch.h"
 #include "ndsph_step.cuh"
@@ -302,15 +301,9 @@ struct KSum {
 // Candidate sources of the two sweeps: RowSrc walks the slot's neighbour row
 // (the sweeps' own loops, below); a source with kRows = false supplies the
 // candidates itself through for_each(i, f), calling f(pk) with entries
-// packed as in the rows, (j << shift) | stencil offset of j's cell, or (kData)
-// through for_each_data(i, f), calling f(pk, position, pack) with the
-// candidate's data already at hand.  kRowsLater: the neighbour rows serve
-// later sweeps of the step, so the density pass still flags an h that
-// outgrows them.
+// packed as in the rows, (j << shift) | stencil offset of j's cell.
 struct RowSrc {
     static constexpr bool kRows = true;
-    static constexpr bool kData = false;
-    static constexpr bool kRowsLater = true;
 };
 
 template <int NDIM, bool FULL, int PREC, class Src>
@@ -434,9 +427,7 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
             sums32(j, q2i, dxf, pvj);
         }
     };
-    if constexpr (Src::kData) {
-        src.for_each_data(i, [&](unsigned pk, const float4& xj, const float4& vj) { pair(pk, xj, typei, vj); });
-    } else if constexpr (!Src::kRows) {
+    if constexpr (!Src::kRows) {
         const bool typed = (PREC == NDSPH_PREC_FP64 || o.idust != 0);
         src.for_each(i, [&](unsigned pk) {
             const int j = (int)(pk >> shift);
@@ -608,7 +599,7 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
             relink = true;
             if (o.stacked) o.sim_aux[(size_t)a.S.sim[i] * SIMAUX + SA_RELINK] = 1ull;
         }
-        if (Src::kRowsLater && (float)hnew + a.nl_dmax > a.S.hb[i] * a.nl_skin) a.red->nl_stale = 1;
+        if (Src::kRows && (float)hnew + a.nl_dmax > a.S.hb[i] * a.nl_skin) a.red->nl_stale = 1;
     } else {
         drhodt = drhodt * gradh;
         F.f[DHDT][i] = (double)(dhdrhoi * drhodt);
@@ -642,327 +633,8 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
     density_body<NDIM, FULL, PREC>(a, i, RowSrc{});
 }
 
-// ===========================================================================
-// Cell-tile first density pass (3D FP32 form, one particle type, one
-// simulation, 5^3 stencil): a block takes a brick of TB_X x TB_Y x TB_Z
-// cells, stages the positions and (v, m) packs of every particle of the
-// brick's stencil neighbourhood (the brick widened by 2 cells each way) into
-// shared memory with bulk copies -- one cp.async.bulk per array and run of
-// x-adjacent cells, which are contiguous slots -- completing on one mbarrier,
-// and runs the density sums of the brick's particles over the staged
-// candidates, screening each particle's 5^3 cells (the cells beyond its
-// reach skipped as the row build skips them).  No neighbour row is read.
-// The pairs, and the arithmetic of each, are those of the row pass; only
-// the order of each particle's sum differs.  A brick whose neighbourhood
-// holds more particles than the staging takes reads them from global memory.
-// ===========================================================================
-constexpr int TB_X = 8, TB_Y = 4, TB_Z = 4;
-constexpr int TB_R = 2;
-constexpr int TE_X = TB_X + 2 * TB_R, TE_Y = TB_Y + 2 * TB_R, TE_Z = TB_Z + 2 * TB_R;
-constexpr int TE_N = TE_X * TE_Y * TE_Z;       // cells of the staged neighbourhood
-constexpr int TB_N = TB_X * TB_Y * TB_Z;       // home cells
-constexpr int TILE_BS = 256;
-constexpr int TILE_CAP = 3200;                 // staged particles (2 x 16 B each)
-struct TileSmem {
-    unsigned long long bar;
-    int bad;
-    int total;
-    int tab[TE_N + 1];       // local start of each neighbourhood cell (prefix)
-    int gst[TE_N];           // global first slot of each neighbourhood cell
-    int hpre[TB_N + 1];      // prefix of the home cells' particle counts
-};
-constexpr size_t tile_smem_bytes() { return ((sizeof(TileSmem) + 15) / 16) * 16 + 2 * (size_t)TILE_CAP * 16; }
-
-__device__ __forceinline__ float slab_dist(float x, int dc, float cs);
-
-template <bool STAGED>
-struct TileSrc {
-    static constexpr bool kRows = false;
-    static constexpr bool kData = true;
-    static constexpr bool kRowsLater = true;
-    const TileSmem* t;
-    const float4* xs;        // staged positions (STAGED) or the global array
-    const float4* pv;        // staged (v, m) packs or the global array
-    const Grid* g;
-    int hx, hy, hz;          // the particle's cell in neighbourhood coordinates
-    unsigned shift;
-    template <class Fn>
-    __device__ __forceinline__ void for_each_data(int i, Fn&& f) const
-    {
-        const float4 xsi = xs_self;
-        const float csx = g->csf[0], csy = g->csf[1], csz = g->csf[2];
-        const float csmin = fminf(csx, fminf(csy, csz));
-        const float abs_tol = 1e-6f * fmaxf(csx, fmaxf(csy, csz));
-        const float reach = (float)TB_R * csmin * 1.001f + abs_tol;
-        const float reach2 = reach * reach;
-        for (int dz = -TB_R; dz <= TB_R; dz++) {
-            const float ez = slab_dist(xsi.z, dz, csz);
-            for (int dy = -TB_R; dy <= TB_R; dy++) {
-                const float ey = slab_dist(xsi.y, dy, csy);
-                const float e2 = ey * ey + ez * ez;
-                if (e2 > reach2) continue;
-                const float ax = sqrtf(reach2 - e2) + abs_tol;
-                const int dx0 = max(-TB_R, (int)floorf((xsi.x - ax) / csx));
-                const int dx1 = min(TB_R, (int)floorf((xsi.x + ax) / csx));
-                const int lrow = ((hz + dz) * TE_Y + (hy + dy)) * TE_X + hx;
-                const unsigned obase = (unsigned)((dy + TB_R) * 5 + (dz + TB_R) * 25);
-                for (int dx = dx0; dx <= dx1; dx++) {
-                    const int L = lrow + dx;
-                    const int k0 = t->tab[L], k1 = t->tab[L + 1];
-                    const int base = STAGED ? 0 : t->gst[L] - k0;   // global slot of local k: base + k
-                    const int gj0 = t->gst[L] - k0;
-                    const unsigned off = obase + (unsigned)(dx + TB_R);
-                    for (int k = k0; k < k1; k++) {
-                        const float4 xj = xs[base + k];
-                        const float4 vj = pv[base + k];
-                        f(((unsigned)(gj0 + k) << shift) | off, xj, vj);
-                    }
-                }
-            }
-        }
-    }
-    float4 xs_self;
-};
-
-// the same brick, candidates from the particle's neighbour row (the rows'
-// exact candidate set) and their data from the staging: a row entry's
-// stencil offset names its cell in the neighbourhood, and its slot's rank in
-// that cell its place in the staging
-template <bool STAGED>
-struct TileRowSrc {
-    static constexpr bool kRows = false;
-    static constexpr bool kData = true;
-    static constexpr bool kRowsLater = true;
-    const TileSmem* t;
-    const float4* sxs;
-    const float4* spv;
-    const unsigned* row;
-    int ncand;
-    int lhome;               // the particle's cell in the neighbourhood (flat index)
-    unsigned shift;
-    const float4* gxs;
-    const float4* gpv;
-    template <class Fn>
-    __device__ __forceinline__ void for_each_data(int i, Fn&& f) const
-    {
-        const unsigned omask = (1u << shift) - 1u;
-        for (int k0 = 0; k0 < ncand; k0 += 4) {
-            unsigned pq[4];
-            if (k0 + 4 <= ncand) {
-                const uint4 r4 = *reinterpret_cast<const uint4*>(row + k0);
-                pq[0] = r4.x; pq[1] = r4.y; pq[2] = r4.z; pq[3] = r4.w;
-            } else {
-#pragma unroll
-                for (int u = 0; u < 4; u++) pq[u] = (k0 + u < ncand) ? row[k0 + u] : 0u;
-            }
-            float4 xq[4], vq[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int j = (int)(pq[u] >> shift);
-                if (STAGED) {
-                    int d[3];
-                    stencil_d<3>(pq[u] & omask, 5, d);
-                    const int L = lhome + (d[2] * TE_Y + d[1]) * TE_X + d[0];
-                    const int idx = (k0 + u < ncand) ? t->tab[L] + (j - t->gst[L]) : 0;
-                    xq[u] = sxs[idx];
-                    vq[u] = spv[idx];
-                } else {
-                    xq[u] = gxs[j];
-                    vq[u] = gpv[j];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-                if (k0 + u < ncand) f(pq[u], xq[u], vq[u]);
-        }
-    }
-};
-
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__global__ void __launch_bounds__(TILE_BS, 2) k_density_tile(SweepArgs a, int ntx, int nty)
-{
-    extern __shared__ __align__(16) unsigned char tile_raw[];
-    TileSmem& t = *reinterpret_cast<TileSmem*>(tile_raw);
-    float4* sxs = reinterpret_cast<float4*>(tile_raw + ((sizeof(TileSmem) + 15) / 16) * 16);
-    float4* spv = sxs + TILE_CAP;
-    const Grid& g = a.g;
-    const int bx = blockIdx.x % ntx, by = (blockIdx.x / ntx) % nty, bz = blockIdx.x / (ntx * nty);
-    const int x0 = bx * TB_X - TB_R, y0 = by * TB_Y - TB_R, z0 = bz * TB_Z - TB_R;   // neighbourhood origin
-    const int tid = threadIdx.x;
-    // global cell of neighbourhood cell (ex, ey, ez), -1 outside an open box
-    auto gcell = [&](int ex, int ey, int ez) {
-        int c[3] = {x0 + ex, y0 + ey, z0 + ez};
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            if (c[d] < 0 || c[d] >= g.nc[d]) {
-                if (!a.o.periodic[d]) return -1;
-                c[d] = (c[d] % g.nc[d] + g.nc[d]) % g.nc[d];
-            }
-        }
-        return (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
-    };
-    // cell counts and global starts of the neighbourhood, then their prefix
-    for (int L = tid; L < TE_N; L += TILE_BS) {
-        const int ex = L % TE_X, ey = (L / TE_X) % TE_Y, ez = L / (TE_X * TE_Y);
-        const int c = gcell(ex, ey, ez);
-        const int s0 = (c >= 0) ? a.cell_start[c] : 0;
-        t.gst[L] = s0;
-        t.tab[L + 1] = (c >= 0) ? a.cell_start[c + 1] - s0 : 0;
-    }
-    if (tid == 0) { t.tab[0] = 0; t.bad = 0; }
-    __syncthreads();
-    if (tid < 32) {
-        // prefix over the TE_N counts by one warp (TE_N / 32 per lane)
-        constexpr int PER = (TE_N + 31) / 32;
-        int sum = 0;
-        for (int q = 0; q < PER; q++) {
-            const int L = tid * PER + q;
-            if (L < TE_N) sum += t.tab[L + 1];
-        }
-        int incl = sum;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (tid >= o) incl += v;
-        }
-        int run = incl - sum;
-        for (int q = 0; q < PER; q++) {
-            const int L = tid * PER + q;
-            if (L < TE_N) { run += t.tab[L + 1]; t.tab[L + 1] = run; }
-        }
-        if (tid == 31) t.total = incl;
-    }
-    // home cells' counts
-    for (int hc = tid; hc < TB_N; hc += TILE_BS) {
-        const int hx = hc % TB_X, hy = (hc / TB_X) % TB_Y, hz = hc / (TB_X * TB_Y);
-        const bool inside = (bx * TB_X + hx < g.nc[0]) && (by * TB_Y + hy < g.nc[1]) && (bz * TB_Z + hz < g.nc[2]);
-        const int L = ((hz + TB_R) * TE_Y + (hy + TB_R)) * TE_X + (hx + TB_R);
-        t.hpre[hc + 1] = inside ? (a.cell_start[gcell(hx + TB_R, hy + TB_R, hz + TB_R) + 1] - t.gst[L]) : 0;
-    }
-    if (tid == 0) t.hpre[0] = 0;
-    __syncthreads();
-    if (tid < 32) {
-        constexpr int PER = TB_N / 32;
-        int sum = 0;
-        for (int q = 0; q < PER; q++) sum += t.hpre[tid * PER + q + 1];
-        int incl = sum;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (tid >= o) incl += v;
-        }
-        int run = incl - sum;
-        for (int q = 0; q < PER; q++) { run += t.hpre[tid * PER + q + 1]; t.hpre[tid * PER + q + 1] = run; }
-    }
-    __syncthreads();
-    const int total = t.total;
-    const bool staged = total <= TILE_CAP;
-    if (staged && total > 0) {
-        // bulk copies into the staging, completing on one mbarrier
-        const unsigned bar = smem_u32(&t.bar);
-        if (tid == 0) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
-        __syncthreads();
-        if (tid < 32) {
-            if (tid == 0)
-                asm volatile("{ .reg .b64 st; mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1; }" ::"r"(bar),
-                             "r"((unsigned)(total * 32)) : "memory");
-            __syncwarp();
-            // one lane per neighbourhood row (ey, ez): runs of cells whose
-            // global cells are consecutive
-            for (int row = tid; row < TE_Y * TE_Z; row += 32) {
-                const int Lr = row * TE_X, ey = row % TE_Y, ez = row / TE_Y;
-                int ex = 0;
-                while (ex < TE_X) {
-                    const int c0 = gcell(ex, ey, ez);
-                    if (c0 < 0) { ex++; continue; }   // outside an open box: no particles
-                    int e1 = ex + 1;
-                    while (e1 < TE_X && gcell(e1, ey, ez) == c0 + (e1 - ex)) e1++;
-                    const int k0 = t.tab[Lr + ex], k1 = t.tab[Lr + e1];
-                    if (k1 > k0) {
-                        const unsigned bytes = (unsigned)(k1 - k0) * 16u;
-                        const float4* gx = a.S.xs + t.gst[Lr + ex];
-                        const float4* gv = a.S.pk_v + t.gst[Lr + ex];
-                        asm volatile(
-                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                            ::"r"(smem_u32(sxs + k0)), "l"(gx), "r"(bytes), "r"(bar) : "memory");
-                        asm volatile(
-                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                            ::"r"(smem_u32(spv + k0)), "l"(gv), "r"(bytes), "r"(bar) : "memory");
-                    }
-                    ex = e1;
-                }
-            }
-        }
-        // every thread waits for phase 0, with an iteration limit
-        unsigned done = 0;
-        for (int it = 0; it < (1 << 22) && !done; it++)
-            asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
-                         : "=r"(done) : "r"(bar) : "memory");
-        if (!done) {
-            if (tid == 0) raise_err(a.red, NDSPH_E_CUDA, -1);
-            // the copies are the block's own: give them a second bounded wait
-            for (int it = 0; it < (1 << 22) && !done; it++)
-                asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
-                             : "=r"(done) : "r"(bar) : "memory");
-            return;
-        }
-    }
-    // the brick's particles, one per thread at a time
-    const int H = t.hpre[TB_N];
-    for (int k = tid; k < H; k += TILE_BS) {
-        int lo = 0, hi = TB_N;   // hpre[lo] <= k < hpre[lo + 1]
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (t.hpre[mid] <= k) lo = mid; else hi = mid;
-        }
-        const int hx = lo % TB_X, hy = (lo / TB_X) % TB_Y, hz = lo / (TB_X * TB_Y);
-        const int L = ((hz + TB_R) * TE_Y + (hy + TB_R)) * TE_X + (hx + TB_R);
-        const int i = t.gst[L] + (k - t.hpre[lo]);
-        if (staged) {
-            TileRowSrc<true> src;
-            src.t = &t; src.sxs = sxs; src.spv = spv;
-            src.row = a.S.nl + (size_t)i * a.nl_stride;
-            src.ncand = a.S.nl_cnt[i];
-            src.lhome = L;
-            src.shift = (unsigned)g.nlshift;
-            src.gxs = a.S.xs; src.gpv = a.S.pk_v;
-            density_body<3, true, NDSPH_PREC_FP32>(a, i, src);
-        } else {
-            TileRowSrc<false> src;
-            src.t = &t; src.sxs = sxs; src.spv = spv;
-            src.row = a.S.nl + (size_t)i * a.nl_stride;
-            src.ncand = a.S.nl_cnt[i];
-            src.lhome = L;
-            src.shift = (unsigned)g.nlshift;
-            src.gxs = a.S.xs; src.gpv = a.S.pk_v;
-            density_body<3, true, NDSPH_PREC_FP32>(a, i, src);
-        }
-    }
-}
-
-bool density_tile_ok(const SweepArgs& a)
-{
-    return a.o.ndim == 3 && a.o.precision == NDSPH_PREC_FP32 && !a.o.batched && a.o.idust == 0 && a.g.sw == 5 &&
-           a.g.nstack == 1 && a.n > 0 && getenv("NDSPH_DENSITY_TILES") != nullptr;
-}
-
-void launch_density_tile(const SweepArgs& a, cudaStream_t st)
-{
-    const int ntx = (a.g.nc[0] + TB_X - 1) / TB_X, nty = (a.g.nc[1] + TB_Y - 1) / TB_Y,
-              ntz = (a.g.nc[2] + TB_Z - 1) / TB_Z;
-    const size_t smem = tile_smem_bytes();
-    cudaFuncSetAttribute(k_density_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    NDSPH_COUNT_LAUNCH, k_density_tile<<<ntx * nty * ntz, TILE_BS, smem, st>>>(a, ntx, nty);
-}
-
 void launch_density(const SweepArgs& a, bool full, cudaStream_t st)
 {
-    if (full && !a.d_nlist && density_tile_ok(a)) {
-        launch_density_tile(a, st);
-        return;
-    }
     const int bs = 128;
     const int nthreads = full ? a.n : (a.d_nlist ? a.n : a.nlist);
     if (nthreads <= 0) return;
@@ -1721,8 +1393,6 @@ constexpr int TUBE_BS = 128;
 // candidates of slot i of a tube in x order (see above)
 struct TubeWin {
     static constexpr bool kRows = false;
-    static constexpr bool kData = false;
-    static constexpr bool kRowsLater = false;
     const float* X;      // [m] x - (tube's smallest x), in x order
     const float* H;      // [m] h rounded up, in x order
     const float* PMX;    // [m] prefix max of H
