@@ -1088,7 +1088,10 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
         __shared__ unsigned acc_buf[RATES_CHUNK * RATES_BS];
         unsigned* mine = acc_buf + threadIdx.x;
         const bool typed = (o.idust != 0);
-        auto sweep_row = [&](const unsigned* row, const int ncand) {
+        // drag_only: a row of the other type's entries, whose pair terms are
+        // the drag terms alone (they read no B, gradh or alpha of the
+        // neighbour, and its h is the position's h)
+        auto sweep_row = [&](const unsigned* row, const int ncand, auto drag_only) {
             int k = 0;   // a multiple of 4 whenever a vector row load is issued
             while (k < ncand) {
                 int na = 0;
@@ -1133,19 +1136,25 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                     cur[0] = a.S.xs[j];
                     cur[1] = a.S.pk_v[j];
                     cur[2] = a.S.pk_t[j];
-                    cur[3] = a.S.pk_b[j];
-                    cur[4] = a.S.pk_a[j];
+                    if constexpr (decltype(drag_only)::value) {
+                        cur[3] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        cur[4] = make_float4(0.f, 0.f, 0.f, cur[0].w);
+                    } else {
+                        cur[3] = a.S.pk_b[j];
+                        cur[4] = a.S.pk_a[j];
+                    }
                     pair_terms(pk, cur, typed ? a.S.itype[j] : typei);
                 }
             }
         };
-        sweep_row(a.S.nl + (size_t)i * a.nl_stride, live ? a.S.nl_cnt[i] : 0);
+        sweep_row(a.S.nl + (size_t)i * a.nl_stride, live ? a.S.nl_cnt[i] : 0, std::false_type{});
         // two particle types (gas and dust: TYPED, rows split by type): the
         // rows of the other type, the drag pairs, follow as a second run, so
         // the lanes of a warp take one branch of the pair terms at a time
         // instead of alternating between the hydro/MHD terms and the drag
         // terms pair by pair
-        if constexpr (TYPED) sweep_row(a.S.nl2 + (size_t)i * a.nl_stride, live ? a.S.nl_cnt2[i] : 0);
+        if constexpr (TYPED)
+            sweep_row(a.S.nl2 + (size_t)i * a.nl_stride, live ? a.S.nl_cnt2[i] : 0, std::true_type{});
     }
 
     if (PREC == NDSPH_PREC_FP64) {
