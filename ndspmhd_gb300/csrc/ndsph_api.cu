@@ -160,6 +160,7 @@ struct ndsph_ctx {
     int tube_maxm = 0;           // largest tube; 0: the batch does not qualify
     int tube_cap = 0;
     int fsteps = 0;              // steps run by the fused per-tube kernel
+    bool tubes_predicted = false;  // the last fused launch also ran the next step's predictor
     bool tubes_valid = false;    // ranges match the slot order (reset by every link)
     int gredo = 0;               // captured steps redone on the eager path
     int gsteps = 0;              // captured steps launched
@@ -2638,19 +2639,30 @@ static bool fused_usable(const ndsph_ctx* ctx)
 
 // one leapfrog step of every tube in one launch (k_tube_step); false in
 // *done when the batch does not qualify
-static int batch_step_fused(ndsph_ctx* ctx, bool* done)
+// predict_next: another fused step follows in the same call, so this
+// launch's corrector also runs that step's save and predictor; the state
+// between two such launches is the predicted one, and every call ends
+// corrected.  The host reads the status block every 16 steps and at the end.
+static int batch_step_fused(ndsph_ctx* ctx, bool* done, bool predict_next, bool check)
 {
     *done = false;
     int rc = tubes_prepare(ctx);
     if (rc) return rc;
-    if (ctx->tube_maxm <= 0) return 0;
+    if (ctx->tube_maxm <= 0) {
+        if (ctx->tubes_predicted) { ctx->err = "batched step: predicted state without the fused step"; return NDSPH_E_ARG; }
+        return 0;
+    }
     SweepArgs a = sweep_args(ctx);
     launch_tube_step(a, ctx->d_tube_start, ctx->d_tube_order, ctx->nsim, ctx->d_sim_dtnext, ctx->d_sim_out,
-                     ctx->tube_maxm, ctx->st);
+                     ctx->tube_maxm, ctx->tubes_predicted, predict_next, ctx->st);
     CK(cudaGetLastError());
+    ctx->tubes_predicted = predict_next;
     *done = true;
     ctx->fsteps++;
-    return sync_red(ctx);
+    if (!check) return 0;
+    rc = sync_red(ctx);
+    if (rc) ctx->tubes_predicted = false;
+    return rc;
 }
 
 extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, double* time_out)
@@ -2663,7 +2675,8 @@ extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, 
     for (int k = 0; k < nsteps; k++) {
         bool done = false;
         if (fused_usable(ctx)) {
-            const int rc = batch_step_fused(ctx, &done);
+            const bool last = (k + 1 == nsteps);
+            const int rc = batch_step_fused(ctx, &done, !last, last || (k % 16) == 15);
             if (rc) return rc;
         }
         if (!done) {

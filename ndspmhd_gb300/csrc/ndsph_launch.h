@@ -180,8 +180,11 @@ void launch_rates(const SweepArgs& a, cudaStream_t st);
 // tube_start[nsim+1], order[nsim] largest first; maxm the largest tube)
 constexpr int TUBE_MAX = 4096;
 size_t tube_smem_bytes(int maxm);
+// predicted: the previous launch already ran this step's save and predictor;
+// predict_next: the corrector also runs the next step's (several steps of one
+// ndsph_batch_step call)
 void launch_tube_step(const SweepArgs& a, const int* tube_start, const int* order, int nsim, double* dt_next,
-                      double* sim_out, int maxm, cudaStream_t st);
+                      double* sim_out, int maxm, bool predicted, bool predict_next, cudaStream_t st);
 void launch_pack_v(const SweepArgs& a, cudaStream_t st);
 void launch_build_nlist(const SweepArgs& a, cudaStream_t st);
 void launch_pack_rates(const SweepArgs& a, cudaStream_t st);

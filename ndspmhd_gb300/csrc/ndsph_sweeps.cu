@@ -1493,6 +1493,12 @@ struct TubeArgs {
     const int* order;        // [nsim] tubes, largest first
     double* dt_next;         // [nsim] the next step's dt of each tube
     double* sim_out;         // [nsim * 4] dtcourant, dtforce, dt next, time
+    // several steps in one call: the previous launch's corrector also ran
+    // this step's save and predictor (predicted), and this launch's corrector
+    // runs the next step's (predict_next) -- each particle's corrected state
+    // goes straight into the next save and predictor, one pass over its
+    // fields instead of two
+    int predicted, predict_next;
 };
 
 template <int PREC>
@@ -1534,10 +1540,14 @@ __global__ void __launch_bounds__(TUBE_BS) k_tube_step(TubeArgs T)
         r[SR_STRESS] = 0ull;
         sh.bad = 0;
     }
-    for (int k = tid; k < m; k += TUBE_BS) predictor_one(F, S, o, dt, t0 + k, 0);
-    __syncthreads();
-    if (o.has_fixed) {
-        for (int k = tid; k < m; k += TUBE_BS) predictor_fixed_x_one(F, S, o, dt, t0 + k);
+    if (!T.predicted) {
+        for (int k = tid; k < m; k += TUBE_BS) predictor_one(F, S, o, dt, t0 + k, 0);
+        __syncthreads();
+        if (o.has_fixed) {
+            for (int k = tid; k < m; k += TUBE_BS) predictor_fixed_x_one(F, S, o, dt, t0 + k);
+            __syncthreads();
+        }
+    } else {
         __syncthreads();
     }
 
@@ -1726,16 +1736,31 @@ __global__ void __launch_bounds__(TUBE_BS) k_tube_step(TubeArgs T)
         T.sim_out[s * 4 + 2] = dtn;
         T.sim_out[s * 4 + 3] += dt;
     }
-    // ---- corrector
-    for (int k = tid; k < m; k += TUBE_BS) corrector_one(F, S, o, dt, t0 + k, a.red);
-    __syncthreads();
+    // ---- corrector (and with predict_next the next step's save and
+    // predictor, with the dt just set)
+    if (T.predict_next) {
+        __syncthreads();
+        const double dtn = T.dt_next[s];
+        for (int k = tid; k < m; k += TUBE_BS) {
+            corrector_one(F, S, o, dt, t0 + k, a.red);
+            predictor_one(F, S, o, dtn, t0 + k, 0);
+        }
+        __syncthreads();
+        if (o.has_fixed) {
+            for (int k = tid; k < m; k += TUBE_BS) predictor_fixed_x_one(F, S, o, dtn, t0 + k);
+            __syncthreads();
+        }
+    } else {
+        for (int k = tid; k < m; k += TUBE_BS) corrector_one(F, S, o, dt, t0 + k, a.red);
+        __syncthreads();
+    }
     if (tid == 0) o.sim_dt[s] = T.dt_next[s];
 }
 
 size_t tube_smem_bytes(int maxm) { return (size_t)maxm * (4 * sizeof(float) + 2 * sizeof(int)); }
 
 void launch_tube_step(const SweepArgs& a, const int* tube_start, const int* order, int nsim, double* dt_next,
-                      double* sim_out, int maxm, cudaStream_t st)
+                      double* sim_out, int maxm, bool predicted, bool predict_next, cudaStream_t st)
 {
     TubeArgs T;
     T.a = a;
@@ -1743,6 +1768,8 @@ void launch_tube_step(const SweepArgs& a, const int* tube_start, const int* orde
     T.order = order;
     T.dt_next = dt_next;
     T.sim_out = sim_out;
+    T.predicted = predicted ? 1 : 0;
+    T.predict_next = predict_next ? 1 : 0;
     const size_t smem = tube_smem_bytes(maxm);
     // (128 registers a thread: 4 blocks, 16 warps per SM; forcing 5 blocks
     // spilled and was 8 % slower)
