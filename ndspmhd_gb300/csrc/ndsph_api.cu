@@ -2286,18 +2286,27 @@ extern "C" int ndsph_batch_upload(ndsph_ctx* ctx, const ndsph_particles* p, int3
 }
 
 // one eager batched step: predictor, derivs, corrector, next dt per simulation
-static int batch_step_eager(ndsph_ctx* ctx)
+// fuse_next (no fixed particles): another eager step follows in the same
+// call, so the corrector also runs that step's save and predictor with each
+// simulation's next dt (k_corrector_predictor); every call ends corrected
+static int batch_step_eager(ndsph_ctx* ctx, bool fuse_next)
 {
     cudaStream_t st = ctx->st;
-    launch_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+    if (ctx->predicted) ctx->predicted = false;
+    else launch_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
     const std::vector<int> live = step_live_fields(ctx, false);
     int rc = do_derivs(ctx, live.data(), (int)live.size());
     if (rc) return rc;
-    launch_corrector(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+    fuse_next = fuse_next && !ctx->o.has_fixed;
+    if (fuse_next) launch_corrector_predictor(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, ctx->d_sim_dtnext, st);
+    else launch_corrector(ctx->F, ctx->S, ctx->o, ctx->n, ctx->red, st);
+    ctx->predicted = fuse_next;
     // next dt of every simulation
     CK(cudaMemcpyAsync(ctx->d_sim_dt, ctx->d_sim_dtnext, sizeof(double) * (size_t)ctx->nsim,
                        cudaMemcpyDeviceToDevice, st));
-    return sync_red(ctx);
+    rc = sync_red(ctx);
+    if (rc) ctx->predicted = false;
+    return rc;
 }
 
 // ---------------------------------------------------------------------------
@@ -2680,7 +2689,7 @@ extern "C" int ndsph_batch_step(ndsph_ctx* ctx, int32_t nsteps, double* dt_out, 
             if (rc) return rc;
         }
         if (!done) {
-            const int rc = graph_usable(ctx) ? batch_step_graph(ctx) : batch_step_eager(ctx);
+            const int rc = graph_usable(ctx) ? batch_step_graph(ctx) : batch_step_eager(ctx, k + 1 < nsteps);
             if (rc) return rc;
         }
         ctx->nsteps++;

@@ -593,13 +593,16 @@ void launch_corrector(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, cudaSt
 // one simulation without fixed particles, between two steps of a
 // device-resident run: this step's corrector and the next step's save and
 // predictor (with the next dt, dtnext) in one pass over the particles -- the
-// same arithmetic as k_corrector followed by k_predictor_fused
+// same arithmetic as k_corrector followed by k_predictor_fused.  A batch
+// (no fixed particles) takes each simulation's dt and next dt (dtnext[sim]).
 __global__ void k_corrector_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, const double* dtnext)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const double dt = o.batched ? o.sim_dt[S.sim[i]] : red->dt;
+    const double dtn = o.batched ? dtnext[S.sim[i]] : *dtnext;
     Corrected c;
-    corrector_values(F, S, o, red->dt, i, c);
+    corrector_values(F, S, o, dt, i, c);
     if (!(c.h > 0.0)) raise_err(red, NDSPH_E_H_NONPOS, S.id[i]);
     for (int d = 0; d < 3; d++) F.f[V0 + d][i] = c.v[d];
     if (o.imhd != 0)
@@ -611,7 +614,7 @@ __global__ void k_corrector_predictor(FieldPtrs F, Side S, DevOpts o, int n, Red
 #pragma unroll
     for (int d = 0; d < 3; d++)
         if (d < o.ndim && o.ibound[d] == 3) F.f[X0 + d][i] = c.x[d];
-    predictor_one(F, S, o, *dtnext, i, 0);
+    predictor_one(F, S, o, dtn, i, 0);
 }
 void launch_corrector_predictor(FieldPtrs F, Side S, DevOpts o, int n, Reduce* red, const double* dtnext,
                                 cudaStream_t st)
