@@ -151,12 +151,16 @@ def write_infile(path: str, opts: dict) -> None:
 
 
 def _key(o: dict) -> tuple:
-    return tuple((k, tuple(v) if isinstance(v, list) else v) for k, v in sorted(o.items()) if k != "psep")
+    # psep and the drag constant may differ inside a batch (the drag
+    # constant goes per simulation)
+    return tuple((k, tuple(v) if isinstance(v, list) else v) for k, v in sorted(o.items())
+                 if k not in ("psep", "Kdrag"))
 
 
 def run_sweep(runs, nsteps: int, precision: int = 1):
-    """Run ``runs`` = [(opts, particles), ...] (open or fixed boundaries):
-    runs whose hot-path options agree (psep aside) share one batched launch.
+    """Run ``runs`` = [(opts, particles), ...] (open or fixed boundaries, or
+    periodic in every dimension): runs whose hot-path options agree (psep and
+    the drag constant K aside) share one batched launch, each with its own K.
     Returns the final particle dicts and per-run (time, dt), in input order."""
     import numpy as np
     from .configs import full_state
@@ -181,6 +185,7 @@ def run_sweep(runs, nsteps: int, precision: int = 1):
             start += n
         cat = {f: np.concatenate([q[f] for q in parts], axis=0) for f in parts[0]}
         g = GpuSPH(o0, full_state(cat, o0["ndim"]))
+        g.batch_set_kdrag([runs[k][0].get("Kdrag", 0.0) for k in idx])
         g.batch_upload(np.concatenate(sims), len(idx), initialise=True)
         dt, t = g.batch_step(nsteps)
         g.batch_download()

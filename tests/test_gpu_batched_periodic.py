@@ -189,3 +189,29 @@ def test_batch_refuses_mixed_boundaries(gpulib):
     with pytest.raises(NdsphError):
         g.batch_set_kdrag(np.array([1.0, -1.0]))
     g.close()
+
+
+def test_sweep_of_dust_infiles_batches_the_drag_constants(gpulib, tmp_path):
+    """The sweep driver batches runs whose options files differ only in the
+    drag constant (one periodic batch, one K per run) and each run evolves as
+    the oracle runs its file."""
+    from ndspmhd_gb300.infile import read_infile, run_sweep, write_infile
+    from oracle.oracle import Oracle
+    settings = [(8, 0.5, 0.05, 60), (8, 0.1, 0.3, 61)]
+    runs = []
+    for k, (n1d, eps, ts, seed) in enumerate(settings):
+        o, p = configs.dust_gas_box_3d(n1d, eps=eps, tstop=ts, seed=seed)
+        path = tmp_path / f"dust{k}.in"
+        write_infile(str(path), o)
+        runs.append((read_infile(str(path), 3, base=o), configs.full_state(p, 3)))
+    assert runs[0][0]["Kdrag"] != runs[1][0]["Kdrag"]
+    out = run_sweep(runs, 3, precision=0)
+    for k, (o, st) in enumerate(runs):
+        orc = Oracle(o, configs.full_state({f: st[f] for f in st}, 3))
+        orc.primitive2conservative()
+        orc.step(3)
+        got, t, dt = out[k]
+        errs, bad = compare_fields({f: got[f] for f in ("x", "vel", "hh", "en", "rho")}, orc.state,
+                                   ["x", "vel", "hh", "en", "rho"], 1e-9)
+        assert not bad, (k, errs)
+        assert abs(t - orc.dts()["time"]) <= 1e-10 * orc.dts()["time"]
