@@ -1172,6 +1172,7 @@ static SweepArgs sweep_args(ndsph_ctx* ctx)
     a.nl_skin = ctx->nl_skin;
     a.nl_dmax = ctx->nl_dmax;
     a.typed_rows = (typed_rows_wanted(ctx) && ctx->S.nl2) ? 1 : 0;
+    a.mixed = 0;
     a.d_its = nullptr;
     a.d_nlist = nullptr;
     a.gate = nullptr;
@@ -1237,7 +1238,8 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
     int zero = 0;
     CK(cudaMemcpyAsync(&ctx->red->redolink, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
     int its = 0, ncalc = n, ncalctotal = 0, nrelink = 0;
-    bool redolink = false, h1_stale = true, rows_stale = false;
+    bool redolink = false, h1_stale = true, rows_stale = false, any_full = false;
+    if (ctx->o.batched) launch_sim_nr_init(ctx->o, st);
     if (ctx->o.precision == NDSPH_PREC_FP32) {
         SweepArgs pa = sweep_args(ctx);
         launch_pack_v(pa, st);
@@ -1297,21 +1299,29 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
         }
         rows_stale = false;
         const bool full = (ncalc == n);
+        // a batch: a pass over the active list in which the simulations whose
+        // every particle is still unconverged take the full pass's rule, as
+        // each run alone would (the rest take the partial pass's)
+        const bool mixed = ctx->o.batched && !full && any_full;
+        const bool jacobi = full || mixed;
         // 1/h: after the start, a full pass (every h changed) or a relink; a
         // partial pass keeps it current for the particles it updates
         if (h1_stale) launch_h1(ctx->F, ctx->S, n, st);
-        h1_stale = full;
-        if (full && its > 1) launch_copy(ctx->F.f[HNEXT], ctx->F.f[HH], n, st);
+        h1_stale = jacobi;
+        if (jacobi && its > 1) launch_copy(ctx->F.f[HNEXT], ctx->F.f[HH], n, st);
         CK(cudaMemsetAsync(ctx->d_ncalc, 0, sizeof(int), st));
         CK(cudaMemsetAsync(&ctx->red->redolink, 0, sizeof(int), st));
+        if (ctx->o.batched) CK(cudaMemsetAsync(&ctx->red->sim_any_full, 0, sizeof(int), st));
         SweepArgs a = sweep_args(ctx);
         a.its = its;
         a.nlist = ncalc;
+        a.mixed = mixed ? 1 : 0;
         tmark(ctx, 2);
-        launch_density(a, full, st);
+        launch_density(a, jacobi, st);
         tmark(ctx, 3);
         CK(cudaGetLastError());
-        if (full) std::swap(ctx->F.f[HH], ctx->F.f[HNEXT]);
+        if (ctx->o.batched) launch_sim_full_update(ctx->o, ctx->red, st);
+        if (jacobi) std::swap(ctx->F.f[HH], ctx->F.f[HNEXT]);
         if (ctx->o.has_fixed) launch_fixed_density_copy(ctx->F, ctx->S, n, st);
         ncalctotal += ncalc;
         // the next pass's count comes back with the reductions, one wait
@@ -1326,6 +1336,7 @@ static int do_iterate_density(ndsph_ctx* ctx, int* its_out, int* ncalctotal_out,
             if (its == 1) pass1_ms = ms;
         }
         redolink = ctx->h_red->redolink != 0;
+        any_full = ctx->o.batched && ctx->h_red->sim_any_full != 0;
         ncalc = h_ncalc;
         std::swap(ctx->S.active, ctx->S.active_next);
         // rows outgrown by some h: rebuilt before the next pass (a particle

@@ -76,9 +76,13 @@ struct DevOpts {
 enum SimRed : int { SR_DTC = 0, SR_DTAV, SR_VSIG, SR_TS, SR_FH, SR_STRESS, SIMRED = 8 };
 // per-simulation settings and link state (batched form, bit patterns of
 // doubles): the drag constant K (dust.f90:91), the ghosts' hhmax of the
-// simulation's last (re)link, the scratch max h of a relink, and the relink
-// request of its last Newton-Raphson pass (iterate_density.f90:122-126)
-enum SimAux : int { SA_KDRAG = 0, SA_HG, SA_HNOW, SA_RELINK, SIMAUX = 4 };
+// simulation's last (re)link, the scratch max h of a relink, the relink
+// request of its last Newton-Raphson pass (iterate_density.f90:122-126), and
+// the full-pass rule of a run (iterate_density.f90:129-133: a pass is full
+// while every particle of the run is unconverged): SA_FULL whether the
+// simulation's next pass is full, SA_CONV whether a particle of it
+// converged (or is fixed) in the current pass
+enum SimAux : int { SA_KDRAG = 0, SA_HG, SA_HNOW, SA_RELINK, SA_FULL, SA_CONV, SIMAUX = 8 };
 
 // cell grid (periodic dims wrap, the others are padded bounding boxes)
 struct Grid {
@@ -166,6 +170,8 @@ struct Reduce {
     // neighbour-row reuse check of a step that skips the link
     unsigned reuse_d2;              // max squared displacement since the build (float bits)
     unsigned reuse_slack;           // min of skin*h_build - grow*h (order-preserving float bits)
+    int sim_any_full;               // batched: some simulation's next pass is full
+    int sim_pad;
 };
 
 __host__ __device__ inline unsigned long long dbits(double v)

@@ -841,6 +841,35 @@ void launch_sim_ghost_h(FieldPtrs F, const int* sim, DevOpts o, int n, int all, 
     if (o.nsim > 0) NDSPH_COUNT_LAUNCH, k_sim_hg_apply<<<nblk(o.nsim, 256), 256, 0, st>>>(o, all);
 }
 
+// the full-pass rule per simulation of a batch (iterate_density.f90:129-133
+// in each run): every simulation's first pass is full; its next pass is full
+// while no particle of it converged in a full pass
+__global__ void k_sim_nr_init(DevOpts o)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= o.nsim) return;
+    o.sim_aux[(size_t)s * SIMAUX + SA_FULL] = 1ull;
+    o.sim_aux[(size_t)s * SIMAUX + SA_CONV] = 0ull;
+}
+__global__ void k_sim_full_update(DevOpts o, Reduce* red)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= o.nsim) return;
+    unsigned long long* x = o.sim_aux + (size_t)s * SIMAUX;
+    const bool full = x[SA_FULL] != 0ull && x[SA_CONV] == 0ull;
+    x[SA_FULL] = full ? 1ull : 0ull;
+    x[SA_CONV] = 0ull;
+    if (full) red->sim_any_full = 1;
+}
+void launch_sim_nr_init(DevOpts o, cudaStream_t st)
+{
+    if (o.nsim > 0) NDSPH_COUNT_LAUNCH, k_sim_nr_init<<<nblk(o.nsim, 256), 256, 0, st>>>(o);
+}
+void launch_sim_full_update(DevOpts o, Reduce* red, cudaStream_t st)
+{
+    if (o.nsim > 0) NDSPH_COUNT_LAUNCH, k_sim_full_update<<<nblk(o.nsim, 256), 256, 0, st>>>(o, red);
+}
+
 // x += sign * off[sim]  (tubes laid side by side along x)
 __global__ void k_add_offset(FieldPtrs F, const int* sim, const double* off, int n, int sign)
 {

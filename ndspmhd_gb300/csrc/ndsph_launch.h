@@ -80,6 +80,8 @@ struct SweepArgs {
     float nl_skin;           // list radius = 2 max(h_i,h_j) skin (h may grow by skin before a rebuild)
     float nl_dmax;           // largest displacement since the rows were built (0 right after a build)
     int typed_rows;          // rows split by type (nl: matching types, nl2: the other type)
+    int mixed;               // batched full pass over the active list: the simulations whose
+                             // SA_FULL is set take the full pass's rule, the others a partial's
     // device-side control (captured step): when set, the pass number, the
     // active count and the row-build gate are read from device memory
     const int* d_its;
@@ -161,6 +163,8 @@ void launch_p2c_post(FieldPtrs F, Side S, DevOpts o, int n, cudaStream_t st);
 void launch_sim_reset(DevOpts o, cudaStream_t st);
 void launch_sim_finalize(DevOpts o, double* dt_next, double* sim_out, cudaStream_t st);
 void launch_sim_ghost_h(FieldPtrs F, const int* sim, DevOpts o, int n, int all, cudaStream_t st);
+void launch_sim_nr_init(DevOpts o, cudaStream_t st);
+void launch_sim_full_update(DevOpts o, Reduce* red, cudaStream_t st);
 void launch_add_offset(FieldPtrs F, const int* sim, const double* off, int n, int sign, cudaStream_t st);
 // captured step (CUDA graph) control kernels
 void launch_link_reset(Reduce* red, cudaStream_t st);

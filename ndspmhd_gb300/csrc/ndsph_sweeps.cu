@@ -340,6 +340,18 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
     int nn = 0;
 
     Stencil<NDIM> stn(a.S.cell[i], g);
+    // the full pass's rule for this particle (union criterion, Jacobi h):
+    // every particle of a full pass; in a batch's mixed pass only those of
+    // the simulations whose every particle is still unconverged
+    const bool uni = FULL && (!a.mixed || o.sim_aux[(size_t)a.S.sim[i] * SIMAUX + SA_FULL] != 0ull);
+    // a batch: a particle that converges (or is fixed) ends its simulation's
+    // full passes (iterate_density.f90:129-133 per run)
+    auto sim_converged = [&]() {
+        if (o.batched) {
+            unsigned long long* c = o.sim_aux + (size_t)a.S.sim[i] * SIMAUX + SA_CONV;
+            if (*c == 0ull) *c = 1ull;
+        }
+    };
     // one candidate: its list entry, position and type, and (FP32 form) its
     // velocity/mass pack, loaded by the caller
     const unsigned shift = (NDIM == 3) ? (unsigned)g.nlshift : 5u, omask = (1u << shift) - 1u;
@@ -377,7 +389,7 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
         stn.offset(pk & omask, g, d, w);
         float dxf[3];
         const float r2f = screen_r2<NDIM>(xsi, xsj, d, g, dxf);
-        const float hm = FULL ? fmaxf(hif, xsj.w) : hif;
+        const float hm = uni ? fmaxf(hif, xsj.w) : hif;
         if (PREC == NDSPH_PREC_FP64) {
             const float rc = 2.0f * hm * 1.0002f + abs_tol;
             if (r2f > rc * rc) return;
@@ -390,7 +402,7 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
             if (!exact_dx<NDIM>(F, j, xi, w, o, dxbound, dx, rij2)) return;
             const double q2i = __dmul_rn(rij2, hi21);
             bool inc;
-            if (FULL) {
+            if (uni) {
                 const double hj1 = a.S.h1[j];
                 const double q2j = __dmul_rn(__dmul_rn(rij2, hj1), hj1);
                 inc = (q2i < 4.0) || (q2j < 4.0);
@@ -480,6 +492,7 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
     a.S.numneigh[i] = nn;
     if (fixed_i) {
         if (o.learned) F.f[HROOT][i] = hi;
+        sim_converged();
         return;
     }
 
@@ -601,6 +614,7 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
         }
         if (Src::kRows && (float)hnew + a.nl_dmax > a.S.hb[i] * a.nl_skin) a.red->nl_stale = 1;
     } else {
+        sim_converged();
         drhodt = drhodt * gradh;
         F.f[DHDT][i] = (double)(dhdrhoi * drhodt);
         // learned h: the training target is the Newton step from the
@@ -622,7 +636,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     int i;
-    if (FULL) {
+    if (FULL && !a.mixed) {
         if (t >= a.n) return;
         i = t;
     } else {
@@ -636,7 +650,7 @@ __global__ void __launch_bounds__(128) k_density(SweepArgs a)
 void launch_density(const SweepArgs& a, bool full, cudaStream_t st)
 {
     const int bs = 128;
-    const int nthreads = full ? a.n : (a.d_nlist ? a.n : a.nlist);
+    const int nthreads = (full && !a.mixed) ? a.n : (a.d_nlist ? a.n : a.nlist);
     if (nthreads <= 0) return;
     const int nb = nblk(nthreads, bs);
 #define DLAUNCH(ND, FU, PR) NDSPH_COUNT_LAUNCH, k_density<ND, FU, PR><<<nb, bs, 0, st>>>(a)

@@ -215,3 +215,42 @@ def test_sweep_of_dust_infiles_batches_the_drag_constants(gpulib, tmp_path):
                                    ["x", "vel", "hh", "en", "rho"], 1e-9)
         assert not bad, (k, errs)
         assert abs(t - orc.dts()["time"]) <= 1e-10 * orc.dts()["time"]
+
+
+def test_batch_full_pass_rule_per_simulation(gpulib):
+    """A Newton-Raphson pass is full while every particle of the run is
+    unconverged (iterate_density.f90:129-133), which decides the union
+    criterion of numneigh and the particle set of the pass.  In a batch whose
+    first box starts 8 % off in h (no particle of it converges in the first
+    pass) and whose second starts converged, the second pass is full for the
+    first box only: both boxes must match their oracle runs, numneigh
+    included."""
+    from ndspmhd_gb300.gpu import GpuSPH
+    from oracle.oracle import Oracle
+    states, opts = [], None
+    for k in range(2):
+        o, p = configs.mhd_box_3d(10, seed=40 + k)
+        g = GpuSPH(o, configs.full_state(p, 3))
+        g.primitive2conservative()
+        states.append({f: v.copy() for f, v in g.state.items()})
+        g.close()
+        opts = o
+    states[0]["hh"] *= 1.08
+    cat = {f: np.concatenate([s[f] for s in states], axis=0) for f in states[0]}
+    sim = np.concatenate([np.full(s["x"].shape[0], k, np.int32) for k, s in enumerate(states)])
+    g = GpuSPH(opts, cat)
+    g.batch_upload(sim, 2, initialise=False)
+    g.batch_step(1)
+    g.batch_download()
+    start = 0
+    for k, s in enumerate(states):
+        n = s["x"].shape[0]
+        orc = Oracle(opts, {f: v.copy() for f, v in s.items()})
+        orc.step(1)
+        got = {f: g.state[f][start:start + n] for f in STEP_FIELDS + ["numneigh"]}
+        errs, bad = compare_fields(got, orc.state, STEP_FIELDS, 1e-9)
+        assert not bad, (k, errs)
+        nd = np.nonzero(got["numneigh"] != orc.state["numneigh"])[0]
+        assert len(nd) == 0, (k, len(nd), nd[:5])
+        start += n
+    g.close()
