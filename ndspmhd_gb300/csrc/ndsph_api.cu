@@ -2274,6 +2274,8 @@ extern "C" int ndsph_batch_upload(ndsph_ctx* ctx, const ndsph_particles* p, int3
     ctx->o.stacked = stacked ? 1 : 0;
     ctx->nl_valid = false;
     ctx->linked = false;
+    ctx->predicted = false;          // a new state: no step has predicted it
+    ctx->tubes_predicted = false;
     launch_add_offset(ctx->F, ctx->S.sim, ctx->d_sim_off, n, +1, ctx->st);
     if (initialise) {
         launch_p2c_init(ctx->F, ctx->S, ctx->o, n, ctx->st);
