@@ -39,6 +39,20 @@ def test_infile_round_trip(tmp_path):
     assert list(back["iavlim"]) == [2, 1, 1]
 
 
+def test_sweep_groups_runs_that_differ_only_in_psep_or_drag(tmp_path):
+    """The sweep driver's batch key: options files that differ only in psep
+    or the drag constant K share a batch (K goes per simulation); any other
+    difference splits them."""
+    from ndspmhd_gb300.infile import _key
+    o1, _ = configs.dust_gas_box_3d(8, eps=0.5, tstop=0.05)
+    o2, _ = configs.dust_gas_box_3d(8, eps=0.1, tstop=0.3)
+    assert o1["Kdrag"] != o2["Kdrag"]
+    assert _key(o1) == _key(o2)
+    assert _key(o1) == _key(dict(o1, psep=0.5))
+    assert _key(o1) != _key(dict(o1, gamma=1.4))
+    assert _key(o1) != _key(dict(o1, idrag_nature=2))
+
+
 def test_infile_rejects_unsupported_option(tmp_path):
     path = tmp_path / "bad.in"
     path.write_text("icty = 1 ! continuity by time derivative\n")
