@@ -101,7 +101,7 @@ def test_learned_h_through_the_host_buffer_step(gpulib):
     """ndsph_step with the learned predictor (the form the bench's e2e number
     times): the predictor's per-particle history (its last h_pred and root
     estimate, drho/dt, c_s, numneigh) follows each particle into the host
-    order of every upload.  The Newton-Raphson iteration stays the judge, so
+    order of every upload.  The Newton-Raphson iteration has the last word, so
     after six steps the particles agree with the reference predictor's to
     within a few times tolh, and the learned steps need fewer density
     passes."""
