@@ -686,7 +686,9 @@ struct Acc<float> {
 };
 // plain sum in the pair precision: the sources of the dissipation switches
 // (del2u, graddivv), which only enter dalpha/dt and carry no cancellation
-// the switches are sensitive to
+// the switches are sensitive to, and div B and curl B, outputs that no later
+// quantity of the step reads (each compensated sum costs three more adds a
+// pair: the four plain ones here took the 128^3 sweep from 2.52 to 2.47 ms)
 template <typename R>
 struct AccPlain {
     R v = 0;
@@ -705,6 +707,8 @@ __device__ __forceinline__ R accv(const A& x)
 }
 
 // per-particle quantities the rates sweep reads for either side of a pair
+// gradh: the grad-h term itself in the FP64 form; in the FP32 form the pack's
+// m gradh h^-(ndim+1)
 template <typename R>
 struct PData {
     R vx, vy, vz, m, rho, pr, cs, u, Bx, By, Bz, gradh, a0, a1, a2, h;
@@ -723,7 +727,7 @@ __device__ __forceinline__ void load_p(const SweepArgs& a, int j,
         const float4 v = a.S.pk_v[j], t = a.S.pk_t[j], b = a.S.pk_b[j], al = a.S.pk_a[j];
         q.vx = v.x; q.vy = v.y; q.vz = v.z; q.m = v.w;
         q.rho = t.x; q.pr = t.y; q.cs = t.z; q.u = t.w;
-        q.Bx = b.x; q.By = b.y; q.Bz = b.z; q.gradh = b.w;
+        q.Bx = b.x; q.By = b.y; q.Bz = b.z; q.gradh = b.w;   // m gradh h^-(ndim+1)
         q.a0 = al.x; q.a1 = al.y; q.a2 = al.z; q.h = al.w;
     }
 }
@@ -779,7 +783,10 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
     const R csi = pi.cs;
     const R ui = pi.u;
     const R alphai = pi.a0, alphaui = pi.a1, alphaBi = pi.a2;
-    const R gradhi = pi.gradh;
+    const R gradhi = (PREC == NDSPH_PREC_FP64) ? pi.gradh : (R)F.f[GRADH][i];
+    // FP32 form: h^-(ndim+1) gradh of i, the j-independent factor of i's
+    // kernel gradient
+    const R hgi = hfacgrki * gradhi;
     const bool mhd = (o.imhd != 0);
     R Bi[3] = {0, 0, 0}, Brhoi[3] = {0, 0, 0};
     R B2i = 0, Brho2i = 0, va2i = 0;
@@ -797,8 +804,8 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
     const R beta = (R)o.beta;
     const bool i_dust = (typei == NDSPH_ITYPE_DUST);
 
-    Acc<R> fx, fy, fz, dbx, dby, dbz, du, dvb, cbx, cby, cbz;
-    AccPlain<R> d2u, gx, gy, gz;
+    Acc<R> fx, fy, fz, dbx, dby, dbz, du;
+    AccPlain<R> d2u, gx, gy, gz, dvb, cbx, cby, cbz;
     R dtc = (R)1.e6, dtav = (R)3.0e38, vsmax = 0, tsmin = (R)3.0e38, hcsts = 0;
     // FP64 form: the two timestep minima as the pair (h, v) of the smallest
     // h / v, compared by cross-multiplication and divided once per particle
@@ -879,9 +886,9 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
             const R rhoj = pj.rho;
             if (type_match(typei, typej)) {
                 // ---------------- rates_core ----------------
-                R hfacgrkj = hj1 * hj1;
-                if (NDIM >= 2) hfacgrkj *= hj1;
-                if (NDIM >= 3) hfacgrkj *= hj1;
+                // mw: the mass factor of every hydro/MHD term below; the
+                // FP32 form has m_j in the kernel gradients already
+                const R mw = (PREC == NDSPH_PREC_FP64) ? mj : (R)1;
                 R gwi, gwj;
                 if constexpr (PREC == NDSPH_PREC_FP64) {
                     gwi = tab_val(a.t.gw, tab_index(a.t, q2i));
@@ -903,8 +910,19 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                         gwj = tab_valf(a.t.gwf, tab_indexf(a.t, q2j));
                     }
                 }
-                const R grkerni = gwi * hfacgrki * gradhi;
-                const R grkernj = gwj * hfacgrkj * pj.gradh;
+                R grkerni, grkernj;
+                if constexpr (PREC == NDSPH_PREC_FP64) {
+                    R hfacgrkj = hj1 * hj1;
+                    if (NDIM >= 2) hfacgrkj *= hj1;
+                    if (NDIM >= 3) hfacgrkj *= hj1;
+                    grkerni = gwi * hfacgrki * gradhi;
+                    grkernj = gwj * hfacgrkj * pj.gradh;
+                } else {
+                    // m_j times the two kernel gradients (pj.gradh is the
+                    // pack's m gradh h^-(ndim+1))
+                    grkerni = (gwi * hgi) * mj;
+                    grkernj = gwj * pj.gradh;
+                }
                 const R grkern = (R)0.5 * (grkerni + grkernj);
                 const R dvdotr = dvel[0] * dr[0] + dvel[1] * dr[1] + dvel[2] * dr[2];
                 const R rho1j = (PREC == NDSPH_PREC_FP64) ? (R)F.f[RHO1][j] : rcp(rhoj);
@@ -971,10 +989,10 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                     const R termB = vsigB * rhoav1 * grkern;
                     if (dvdotr < (R)0 && o.iav <= 3) {
                         const R visc = alphaav * term * (-dvdotr);
-                        fxi -= mj * visc * dr[0]; fyi -= mj * visc * dr[1]; fzi -= mj * visc * dr[2];
+                        fxi -= mw * visc * dr[0]; fyi -= mw * visc * dr[1]; fzi -= mw * visc * dr[2];
                     }
                     if (o.imhd > 0 && o.imhd != 10 && o.iav >= 2) {
-                        const R fb = rhoi * mj * alphaB * termB * rhoav1;
+                        const R fb = rhoi * mw * alphaB * termB * rhoav1;
                         dbx.add(fb * dB[0]); dby.add(fb * dB[1]); dbz.add(fb * dB[2]);
                     }
                     if (o.iener > 0 && o.iener != 3) {
@@ -988,7 +1006,7 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                         R vissB = 0;
                         if (o.imhd > 0 && o.imhd != 10 && o.iav >= 2)
                             vissB = -alphaB * (R)0.5 * (dB[0] * dB[0] + dB[1] * dB[1] + dB[2] * dB[2]) * rhoav1;
-                        du.add(mj * (term * vissv + termu * vissu + termB * vissB));
+                        du.add(mw * (term * vissv + termu * vissu + termB * vissB));
                     }
                     if (vsigav > (R)1.e-10) {
                         if (PREC == NDSPH_PREC_FP64) {
@@ -1000,7 +1018,7 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                 }
                 // ---------------- pressure ----------------
                 const R prterm = Prho2i * grkerni + Prho2j * grkernj;
-                fxi -= mj * prterm * dr[0]; fyi -= mj * prterm * dr[1]; fzi -= mj * prterm * dr[2];
+                fxi -= mw * prterm * dr[0]; fyi -= mw * prterm * dr[1]; fzi -= mw * prterm * dr[2];
                 // ---------------- mhd_terms ----------------
                 if (mhd) {
                     const R fiso = (R)0.5 * (Brho2i * grkerni + Brho2j * grkernj);
@@ -1008,18 +1026,18 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                     for (int c = 0; c < 3; c++) {
                         const R fan = (Brhoi[c] * projBrhoi - stressmax * dr[c] * rho21i) * grkerni +
                                       (Brhoj[c] * projBrhoj - stressmax * dr[c] * rho21j) * grkernj;
-                        const R fm = mj * (fan - fiso * dr[c]);
+                        const R fm = mw * (fan - fiso * dr[c]);
                         if (c == 0) fxi += fm; else if (c == 1) fyi += fm; else fzi += fm;
                     }
-                    dvb.add(-mj * projdB * grkern);
+                    dvb.add(-mw * projdB * grkern);
                     if (o.imhd > 0) {
                         const R c0 = dB[1] * dr[2] - dB[2] * dr[1];
                         const R c1 = dB[2] * dr[0] - dB[0] * dr[2];
                         const R c2 = dB[0] * dr[1] - dB[1] * dr[0];
-                        cbx.add(mj * c0 * grkern); cby.add(mj * c1 * grkern); cbz.add(mj * c2 * grkern);
+                        cbx.add(mw * c0 * grkern); cby.add(mw * c1 * grkern); cbz.add(mw * c2 * grkern);
                     }
                     if (o.imhd == 1 || o.imhd == 11) {
-                        const R fb = mj * projBrhoi * grkerni;
+                        const R fb = mw * projBrhoi * grkerni;
                         dbx.add(-fb * dvel[0]); dby.add(-fb * dvel[1]); dbz.add(-fb * dvel[2]);
                     }
                 }
@@ -1027,12 +1045,12 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                 if (o.iav > 0) {
                     if (o.iavlim[1] > 0) {
                         const R graduterm = (ui - pj.u) * ((PREC == NDSPH_PREC_FP64) ? (R)irij : rcp(rij));
-                        d2u.add(mj * rho1j * graduterm * grkerni);
+                        d2u.add(mw * rho1j * graduterm * grkerni);
                     }
                     if (o.iavlim[0] != 3) {
-                        gx.add(mj * (dvel[0] - dvdotr) * grkerni);
-                        gy.add(mj * (dvel[1] - dvdotr) * grkerni);
-                        gz.add(mj * (dvel[2] - dvdotr) * grkerni);
+                        gx.add(mw * (dvel[0] - dvdotr) * grkerni);
+                        gy.add(mw * (dvel[1] - dvdotr) * grkerni);
+                        gz.add(mw * (dvel[2] - dvdotr) * grkerni);
                     }
                 }
             } else if (o.idust == 2 && o.idrag_nature > 0) {
@@ -1337,13 +1355,24 @@ __device__ __forceinline__ void pack_v_one(const SweepArgs& a, int k)
     const FieldPtrs& F = a.F;
     a.S.pk_v[k] = make_float4((float)F.f[V0][k], (float)F.f[V1][k], (float)F.f[V2][k], (float)F.f[PM][k]);
 }
+// The fourth word of pk_b is m gradh h^-(ndim+1): the factor that turns the
+// kernel's dW/dq at q_j into particle j's mass-weighted grad-h gradient.
+// Every hydro/MHD pair term carries m_j times one of the kernel gradients,
+// so the FP32 sweep folds m_j in once per pair instead of once per term
+// (~20 fewer multiplies a pair: 2.57 -> 2.52 ms for the 128^3 sweep).
 __device__ __forceinline__ void pack_rates_one(const SweepArgs& a, int k)
 {
     const FieldPtrs& F = a.F;
-    a.S.pk_v[k] = make_float4((float)F.f[V0][k], (float)F.f[V1][k], (float)F.f[V2][k], (float)F.f[PM][k]);
+    const float m = (float)F.f[PM][k], hf = (float)F.f[HH][k];
+    const float h1 = rcp_ftz(hf);
+    float hfac = h1 * h1;
+    if (a.o.ndim >= 2) hfac *= h1;
+    if (a.o.ndim >= 3) hfac *= h1;
+    a.S.pk_v[k] = make_float4((float)F.f[V0][k], (float)F.f[V1][k], (float)F.f[V2][k], m);
     a.S.pk_t[k] = make_float4((float)F.f[RHO][k], (float)fmax(F.f[PR][k], 0.0), (float)F.f[CS][k], (float)F.f[UU][k]);
-    a.S.pk_b[k] = make_float4((float)F.f[BF0][k], (float)F.f[BF1][k], (float)F.f[BF2][k], (float)F.f[GRADH][k]);
-    a.S.pk_a[k] = make_float4((float)F.f[AL0][k], (float)F.f[AL1][k], (float)F.f[AL2][k], (float)F.f[HH][k]);
+    a.S.pk_b[k] = make_float4((float)F.f[BF0][k], (float)F.f[BF1][k], (float)F.f[BF2][k],
+                              (m * (float)F.f[GRADH][k]) * hfac);
+    a.S.pk_a[k] = make_float4((float)F.f[AL0][k], (float)F.f[AL1][k], (float)F.f[AL2][k], hf);
 }
 __global__ void k_pack_v(SweepArgs a)
 {
