@@ -829,6 +829,7 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
             const float hm = fmaxf(hif, xsj.w);
             R dr[3], rij, q2i, q2j, hj1;
             double irij = 0.0;   // FP64 form: 1/rij, reused by the conduction term
+            float irf = 0.f;     // FP32 form: the same, the screen's rsqrt
             if constexpr (PREC == NDSPH_PREC_FP64) {
                 const float rc = 2.0f * hm * 1.0002f + abs_tol;
                 if (r2f > rc * rc) return;
@@ -854,6 +855,7 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                 if (!(r2f < 4.0f * hm * hm)) return;
                 const float ir = rsqrt_ftz(fmaxf(r2f, 1e-37f));
                 const float rr = r2f * ir;
+                irf = ir;
                 if (rr <= 1e-30f) {
                     if (a.S.itype[j] == typei && typei != 2) raise_err(a.red, NDSPH_E_CLUMP, a.S.id[i]);
                     dr[0] = dr[1] = dr[2] = 0;
@@ -978,28 +980,53 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                     }
                 }
                 R fxi = 0, fyi = 0, fzi = 0;
+                // FP32 form: the pair's induction terms (resistivity and the
+                // dB/dt term), added to the compensated sums once
+                R dbp[3] = {0, 0, 0};
+                const bool resist = o.imhd > 0 && o.imhd != 10 && o.iav >= 2;
+                const bool induct = o.imhd == 1 || o.imhd == 11;
                 // ---------------- artificial_dissipation ----------------
                 if (o.iav > 0) {
                     const R alphaav = (R)0.5 * (alphai + pj.a0);
                     const R alphau = (R)0.5 * (alphaui + pj.a1);
                     const R alphaB = (R)0.5 * (alphaBi + pj.a2);
                     const R vsigav = fmax(fmax(alphaav, alphau), alphaB) * vsig;
-                    const R term = vsig * rhoav1 * grkern;
-                    const R termu = vsigu * rhoav1 * grkern;
-                    const R termB = vsigB * rhoav1 * grkern;
+                    R term, termu, termB;
+                    if constexpr (PREC == NDSPH_PREC_FP64) {
+                        term = vsig * rhoav1 * grkern;
+                        termu = vsigu * rhoav1 * grkern;
+                        termB = vsigB * rhoav1 * grkern;
+                    } else {
+                        const R rg = rhoav1 * grkern;
+                        term = vsig * rg;
+                        termu = vsigu * rg;
+                        termB = vsigB * rg;
+                    }
                     if (dvdotr < (R)0 && o.iav <= 3) {
                         const R visc = alphaav * term * (-dvdotr);
                         fxi -= mw * visc * dr[0]; fyi -= mw * visc * dr[1]; fzi -= mw * visc * dr[2];
                     }
-                    if (o.imhd > 0 && o.imhd != 10 && o.iav >= 2) {
+                    if (resist) {
                         const R fb = rhoi * mw * alphaB * termB * rhoav1;
-                        dbx.add(fb * dB[0]); dby.add(fb * dB[1]); dbz.add(fb * dB[2]);
+                        if constexpr (PREC == NDSPH_PREC_FP64) {
+                            dbx.add(fb * dB[0]); dby.add(fb * dB[1]); dbz.add(fb * dB[2]);
+                        } else {
+                            dbp[0] = fb * dB[0]; dbp[1] = fb * dB[1]; dbp[2] = fb * dB[2];
+                        }
                     }
                     if (o.iener > 0 && o.iener != 3) {
                         R vissv = 0;
                         if (dvdotr < (R)0 && o.iav <= 3) {
-                            const R tt = (vi[0] * dr[0] + vi[1] * dr[1] + vi[2] * dr[2]) -
-                                         (vj[0] * dr[0] + vj[1] * dr[1] + vj[2] * dr[2]);
+                            // v_i.r - v_j.r as the reference forms it; the
+                            // FP32 form takes the pair's dv.r (the same
+                            // quantity, one rounding instead of a difference
+                            // of two dot products)
+                            R tt;
+                            if constexpr (PREC == NDSPH_PREC_FP64)
+                                tt = (vi[0] * dr[0] + vi[1] * dr[1] + vi[2] * dr[2]) -
+                                     (vj[0] * dr[0] + vj[1] * dr[1] + vj[2] * dr[2]);
+                            else
+                                tt = dvdotr;
                             vissv = -alphaav * (R)0.5 * (tt * tt);
                         }
                         const R vissu = (o.iener == 1) ? (R)0 : alphau * (ui - pj.u);
@@ -1022,12 +1049,24 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                 // ---------------- mhd_terms ----------------
                 if (mhd) {
                     const R fiso = (R)0.5 * (Brho2i * grkerni + Brho2j * grkernj);
+                    if constexpr (PREC == NDSPH_PREC_FP64) {
 #pragma unroll
-                    for (int c = 0; c < 3; c++) {
-                        const R fan = (Brhoi[c] * projBrhoi - stressmax * dr[c] * rho21i) * grkerni +
-                                      (Brhoj[c] * projBrhoj - stressmax * dr[c] * rho21j) * grkernj;
-                        const R fm = mw * (fan - fiso * dr[c]);
-                        if (c == 0) fxi += fm; else if (c == 1) fyi += fm; else fzi += fm;
+                        for (int c = 0; c < 3; c++) {
+                            const R fan = (Brhoi[c] * projBrhoi - stressmax * dr[c] * rho21i) * grkerni +
+                                          (Brhoj[c] * projBrhoj - stressmax * dr[c] * rho21j) * grkernj;
+                            const R fm = mw * (fan - fiso * dr[c]);
+                            if (c == 0) fxi += fm; else if (c == 1) fyi += fm; else fzi += fm;
+                        }
+                    } else {
+                        // the same terms regrouped: B_i/rho_i (B_i.r/rho_i) grkerni
+                        // + B_j (B_j.r/rho_j)/rho_j grkernj - (stressmax (grkerni/rho_i^2
+                        // + grkernj/rho_j^2) + fiso) r
+                        const R pbi = projBrhoi * grkerni;
+                        const R pbj = projBrhoj * rho1j * grkernj;
+                        const R st = stressmax * (rho21i * grkerni + rho21j * grkernj) + fiso;
+                        fxi += Brhoi[0] * pbi + pj.Bx * pbj - st * dr[0];
+                        fyi += Brhoi[1] * pbi + pj.By * pbj - st * dr[1];
+                        fzi += Brhoi[2] * pbi + pj.Bz * pbj - st * dr[2];
                     }
                     dvb.add(-mw * projdB * grkern);
                     if (o.imhd > 0) {
@@ -1036,15 +1075,22 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                         const R c2 = dB[0] * dr[1] - dB[1] * dr[0];
                         cbx.add(mw * c0 * grkern); cby.add(mw * c1 * grkern); cbz.add(mw * c2 * grkern);
                     }
-                    if (o.imhd == 1 || o.imhd == 11) {
+                    if (induct) {
                         const R fb = mw * projBrhoi * grkerni;
-                        dbx.add(-fb * dvel[0]); dby.add(-fb * dvel[1]); dbz.add(-fb * dvel[2]);
+                        if constexpr (PREC == NDSPH_PREC_FP64) {
+                            dbx.add(-fb * dvel[0]); dby.add(-fb * dvel[1]); dbz.add(-fb * dvel[2]);
+                        } else {
+                            dbp[0] -= fb * dvel[0]; dbp[1] -= fb * dvel[1]; dbp[2] -= fb * dvel[2];
+                        }
                     }
                 }
                 fx.add(fxi); fy.add(fyi); fz.add(fzi);
+                if constexpr (PREC == NDSPH_PREC_FP32) {
+                    if ((resist && o.iav > 0) || induct) { dbx.add(dbp[0]); dby.add(dbp[1]); dbz.add(dbp[2]); }
+                }
                 if (o.iav > 0) {
                     if (o.iavlim[1] > 0) {
-                        const R graduterm = (ui - pj.u) * ((PREC == NDSPH_PREC_FP64) ? (R)irij : rcp(rij));
+                        const R graduterm = (ui - pj.u) * ((PREC == NDSPH_PREC_FP64) ? (R)irij : (R)irf);
                         d2u.add(mw * rho1j * graduterm * grkerni);
                     }
                     if (o.iavlim[0] != 3) {
