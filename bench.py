@@ -24,6 +24,7 @@ Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -220,7 +221,8 @@ def run_e2e(o, steps: int, warmup: int, tuning=None):
     en, hh, alpha and their rates: what the next step reads, and what the
     Fortran shim's gpu_step returns between output steps) and all 47.5
     doubles a particle ndsph_step can return (the shim's output steps).
-    Returns {set: (value, h2d bytes, d2h bytes)} and the in-place-access rate."""
+    Returns {set: (value, h2d bytes, d2h bytes, per-call ms min/median/max)}
+    and the in-place-access rate."""
     import numpy as np
     import torch
     from ndspmhd_gb300.gpu import GpuSPH
@@ -258,13 +260,26 @@ def run_e2e(o, steps: int, warmup: int, tuning=None):
         for _ in range(warmup):
             g.step()
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            g.step()
-        torch.cuda.synchronize()
-        r = n * steps / (time.perf_counter() - t0)
+        # no Python garbage collection inside the timed loop (a collection of
+        # the earlier legs' objects stalled single steps); each call returns
+        # with its results in the host arrays, so the per-call times add up
+        # to the loop's
+        gc.collect()
+        gc.disable()
+        try:
+            t0 = time.perf_counter()
+            tk = [t0]
+            for _ in range(steps):
+                g.step()
+                tk.append(time.perf_counter())
+            torch.cuda.synchronize()
+            r = n * steps / (time.perf_counter() - t0)
+        finally:
+            gc.enable()
         g.close()
-        return r
+        dts = sorted((b - a) * 1e3 for a, b in zip(tk, tk[1:]))
+        step_ms = {"min": round(dts[0], 3), "median": round(statistics.median(dts), 3), "max": round(dts[-1], 3)}
+        return r, step_ms
 
     # bytes per particle: ndsph_step uploads the step's inputs x(3) v(3) Bevol(3)
     # en hh pmass alpha(3) dhdt force(3) dBevoldt(3) dendt daldt(3) + itype
@@ -274,9 +289,11 @@ def run_e2e(o, steps: int, warmup: int, tuning=None):
     # every output: the above plus rho rhoalt drhodt gradh gradhn gradgradh,
     # dens uu pr spsound Bfield(3), dudt divB curlB(3) del2u graddivv(3) + numneigh
     d_dn_all = d_dn_int + (6 + 4 + 3 + 1 + 1 + 3 + 1 + 3) * 8 + 4
-    out = {"integrator": (timed(0, True), d_up * n, d_dn_int * n),
-           "all": (timed(0, False), d_up * n, d_dn_all * n)}
-    return out, timed(1, False)
+    ri, si = timed(0, True)
+    ra, sa = timed(0, False)
+    out = {"integrator": (ri, d_up * n, d_dn_int * n, si),
+           "all": (ra, d_up * n, d_dn_all * n, sa)}
+    return out, timed(1, False)[0]
 
 
 def run_batched(steps: int, warmup: int, ntubes: int = 4096):
@@ -699,7 +716,7 @@ def main():
     value = replica_value(n, world, ms32)
 
     e2e_sets, e2e_inplace = run_e2e(o32l, max(3, args.steps), 3, tuning)
-    e2e_val, h2d, d2h = e2e_sets["integrator"]
+    e2e_val, h2d, d2h, e2e_step_ms = e2e_sets["integrator"]
 
     peak, peak_kind = _load_peaks()
     rates_ms = tim32["rates_ms"]
@@ -747,8 +764,10 @@ def main():
                 "call": "ndsph_step with pinned host buffers (staging copies overlapped with the kernels), "
                         "returning the integrator's arrays (x, vel, Bevol, en, hh, alpha and their rates) as "
                         "the Fortran shim's gpu_step does between output steps",
+                "step_ms": dict(e2e_step_ms, note="host wall time of each call; the link is kept on every "
+                                                  "other step and rebuilt on the others"),
                 "all_outputs": {"value": round(e2e_sets["all"][0], 1), "h2d_bytes_per_step": e2e_sets["all"][1],
-                                "d2h_bytes_per_step": e2e_sets["all"][2],
+                                "d2h_bytes_per_step": e2e_sets["all"][2], "step_ms": e2e_sets["all"][3],
                                 "call": "the same, returning all 47.5 doubles a particle (output steps)"},
                 "in_place_access_value": round(e2e_inplace, 1)},
     }
