@@ -1207,11 +1207,21 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                 // position's screen: 2.83 -> 2.64 ms at 128^3).  Loading the
                 // next entry's data while this one's terms run needs 20 more
                 // registers and spilled (3.14 ms).
+                // The next entry's position is loaded one pair ahead (4
+                // registers), so the screen, the separation and the kernel
+                // gradients of a pair start without waiting and overlap the
+                // loads of its four packs.
+                unsigned pk_next = (na > 0) ? mine[0] : 0u;
+                float4 x_next = (na > 0) ? a.S.xs[pk_next >> shift] : make_float4(0.f, 0.f, 0.f, 0.f);
                 for (int q = 0; q < na; q++) {
-                    const unsigned pk = mine[q * RATES_BS];
+                    const unsigned pk = pk_next;
                     const int j = (int)(pk >> shift);
                     float4 cur[5];
-                    cur[0] = a.S.xs[j];
+                    cur[0] = x_next;
+                    if (q + 1 < na) {
+                        pk_next = mine[(q + 1) * RATES_BS];
+                        x_next = a.S.xs[pk_next >> shift];
+                    }
                     cur[1] = a.S.pk_v[j];
                     cur[2] = a.S.pk_t[j];
                     if constexpr (decltype(drag_only)::value) {
