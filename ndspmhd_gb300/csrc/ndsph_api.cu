@@ -999,8 +999,10 @@ static bool try_keep_link(ndsph_ctx* ctx, bool keep_hmax_ghost, int* rc)
     *rc = 0;
     if (!reuse_on(ctx) || !ctx->nl_valid || !ctx->linked || ctx->grid_cf <= 1.0 || !ctx->S.nl) return false;
     // where particles outrun the skin every step (a supersonic flow), the
-    // check fails each time: after two failures in a row it is tried again
-    // only every eighth step
+    // check fails each time: after two, three and four or more failures in a
+    // row it is tried again after one, three and seven steps (a single pair of
+    // failures, e.g. while a learned predictor is still untrained, then costs
+    // one forced relink, not seven)
     if (ctx->keep_skip > 0) {
         ctx->keep_skip--;
         return false;
@@ -1028,10 +1030,8 @@ static bool try_keep_link(ndsph_ctx* ctx, bool keep_hmax_ghost, int* rc)
     const float dmax = sqrtf(d2) * 1.001f + 2e-6f * csmax;
     if (!(hmax > 0.0) || !std::isfinite(hmax) || !(dmax <= slack) ||
         !(hmax * ctx->nl_grow + dmax <= 0.5 * stencil_cover(ctx) / (1.0 + 1.e-9))) {
-        if (++ctx->keep_fails >= 2) {
-            ctx->keep_skip = 7;
-            ctx->keep_fails = 0;
-        }
+        ctx->keep_fails = std::min(ctx->keep_fails + 1, 4);
+        if (ctx->keep_fails >= 2) ctx->keep_skip = (1 << (ctx->keep_fails - 1)) - 1;   // 1, 3, 7
         return false;
     }
     ctx->keep_fails = 0;

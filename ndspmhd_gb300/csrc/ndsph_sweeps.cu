@@ -1201,16 +1201,15 @@ __device__ __forceinline__ void rates_body(const SweepArgs& a, const int i, cons
                     }
                     k += m;
                 }
-                // the accepted entries: each one's position and four packs
-                // are loaded together, one round trip to L1/L2 per pair
+                // the accepted entries: each one's four packs are loaded
+                // together at the start of its pair, one round trip to L1/L2
                 // (loaded inside the pair terms, the packs waited for the
-                // position's screen: 2.83 -> 2.64 ms at 128^3).  Loading the
-                // next entry's data while this one's terms run needs 20 more
-                // registers and spilled (3.14 ms).
-                // The next entry's position is loaded one pair ahead (4
-                // registers), so the screen, the separation and the kernel
-                // gradients of a pair start without waiting and overlap the
-                // loads of its four packs.
+                // position's screen: 2.83 -> 2.64 ms at 128^3), and its
+                // position one pair ahead (4 registers), so the screen, the
+                // separation and the kernel gradients start without waiting
+                // and overlap the packs' loads (2.39 -> 2.33 ms).  Loading
+                // all of the next entry's data ahead needs 20 more registers
+                // and spilled (3.14 ms).
                 unsigned pk_next = (na > 0) ? mine[0] : 0u;
                 float4 x_next = (na > 0) ? a.S.xs[pk_next >> shift] : make_float4(0.f, 0.f, 0.f, 0.f);
                 for (int q = 0; q < na; q++) {
