@@ -49,10 +49,10 @@ UNIT = "particle-updates/s"
 RATES_BYTES_PER_PARTICLE = (26 + 21) * 8
 # ncu of one k_rates<3,FP32> launch of the 64^3 box (profiles/k_rates_mhd_box3d_64cubed_fp32.md):
 # DRAM bytes read + written, warp instructions issued, and the ratios that explain it
-RATES_DRAM_BYTES_64 = 148.2e6
-RATES_WARP_INSTR_64 = 259.9e6
-RATES_NCU_64 = {"issue_active_frac": 0.577, "threads_per_instruction": 29.4, "warps_active_frac": 0.222,
-                "fma_pipe_frac": 0.391, "top_stalls_per_issue": {"long_scoreboard": 1.63, "wait": 1.50}}
+RATES_DRAM_BYTES_64 = 148.6e6
+RATES_WARP_INSTR_64 = 253.8e6
+RATES_NCU_64 = {"issue_active_frac": 0.601, "threads_per_instruction": 29.7, "warps_active_frac": 0.223,
+                "fma_pipe_frac": 0.402, "top_stalls_per_issue": {"wait": 1.55, "long_scoreboard": 1.28}}
 SMS, SMSP_PER_SM = 152, 4
 # density pass: reads x(3) h m v(3) (8 doubles) writes rho rhoalt drhodt dhdt
 # gradh gradhn gradgradh h (8 doubles) + numneigh (4 B)
@@ -736,7 +736,7 @@ def main():
     rates_ms = tim32["rates_ms"]
     achieved = RATES_BYTES_PER_PARTICLE * n / (rates_ms * 1e-3) / 1e9 if rates_ms > 0 else 0.0
     # DRAM bytes of one k_rates<3,FP32> launch from an ncu capture of the 64^3 box
-    # (129.8 MB read + 18.4 MB written), scaled by the particle count
+    # (129.8 MB read + 18.8 MB written), scaled by the particle count
     traffic = round(RATES_DRAM_BYTES_64 * n / 64 ** 3)
     # the sweep's issue rate, live: warp instructions of one launch (the 64^3
     # capture scaled by N) over the slots of 152 SMs x 4 schedulers at the
