@@ -294,6 +294,15 @@ struct KSum {
     __device__ __forceinline__ double val() const { return (double)s - (double)c; }
     __device__ __forceinline__ float valf() const { return s - c; }
 };
+// plain FP32 sum with the same interface: the density outputs no later
+// quantity of the step reads (the number density, its h-derivative and the
+// second h-derivative term), where the compensation's three extra adds a
+// pair buy nothing the step uses
+struct FSum {
+    float s = 0.f;
+    __device__ __forceinline__ void add(float v) { s += v; }
+    __device__ __forceinline__ float valf() const { return s; }
+};
 
 // ===========================================================================
 // density + Newton-Raphson
@@ -336,7 +345,8 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
 
     // FP64 sums (PREC 0) or compensated FP32 sums (PREC 1), in kernel units
     double sw = 0.0, sn = 0.0, sg = 0.0, sgn = 0.0, sgg = 0.0, sd = 0.0;
-    KSum fw, fn, fg, fgn, fgg, fd;
+    KSum fw, fg, fd;
+    FSum fn, fgn, fgg;
     int nn = 0;
 
     Stencil<NDIM> stn(a.S.cell[i], g);
