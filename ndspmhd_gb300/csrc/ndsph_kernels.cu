@@ -4,6 +4,7 @@
 // All kernels are HBM-bound streaming passes over per-particle SoA arrays:
 // one thread per particle, grid = ceil(n/256) blocks (a multiple of the 152 SMs
 // for any n above ~40k), coalesced 8-byte loads and stores.
+#include <algorithm>
 #include <cstdio>
 #include <cmath>
 #include "ndsph_launch.h"
@@ -35,6 +36,14 @@ void launch_boundary_wrap(FieldPtrs F, DevOpts o, int n, cudaStream_t st)
     if (n > 0) NDSPH_COUNT_LAUNCH, k_boundary_wrap<<<nblk(n, 256), 256, 0, st>>>(F, o, n);
 }
 
+// The reductions below run a grid-stride loop on a grid of at most
+// RED_BLOCKS blocks: one block per particle group made every block's
+// atomics land on the same few words (8192 blocks at 2.1 M particles), and
+// the atomics, not the 32 B a particle, set the kernel's time.  Maxima and
+// minima do not depend on the order, so the results are the same.
+constexpr int RED_BLOCKS = 152 * 4;
+inline int red_blocks(int n) { return std::min(nblk(n, 256), RED_BLOCKS); }
+
 // max h (bound module hhmax, linkND.f90:70 / ghostND_mhd.f90:77) and the
 // particle bounding box (linkND.f90:80-89) in one pass
 __global__ void k_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, const int* gate)
@@ -43,15 +52,14 @@ __global__ void k_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned 
     // block-level reduction first: one set of atomics per block, not per warp
     __shared__ double sh[8];
     __shared__ unsigned long long slo[8][3], shi[8][3];
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double h = (i < n) ? F.f[HH][i] : 0.0;
-    unsigned long long lo[3], hi[3];
-    for (int d = 0; d < 3; d++) {
-        if (i < n && d < ndim) {
-            unsigned long long b = ord_bits(F.f[X0 + d][i]);
-            lo[d] = b; hi[d] = b;
-        } else {
-            lo[d] = ~0ull; hi[d] = 0ull;
+    double h = 0.0;
+    unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        h = fmax(h, F.f[HH][i]);
+        for (int d = 0; d < ndim; d++) {
+            const unsigned long long b = ord_bits(F.f[X0 + d][i]);
+            lo[d] = b < lo[d] ? b : lo[d];
+            hi[d] = b > hi[d] ? b : hi[d];
         }
     }
     for (int off = 16; off > 0; off >>= 1) {
@@ -88,7 +96,7 @@ __global__ void k_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned 
 void launch_hmax_bbox(FieldPtrs F, int ndim, int n, Reduce* red, unsigned long long* dst, cudaStream_t st,
                       const int* gate)
 {
-    if (n > 0) NDSPH_COUNT_LAUNCH, k_hmax_bbox<<<nblk(n, 256), 256, 0, st>>>(F, ndim, n, red, dst, gate);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_hmax_bbox<<<red_blocks(n), 256, 0, st>>>(F, ndim, n, red, dst, gate);
 }
 
 // ---------------------------------------------------------------------------
@@ -313,32 +321,39 @@ __global__ void k_reuse_check(FieldPtrs F, Side S, Grid g, DevOpts o, int n, flo
 {
     __shared__ float sd[8], ss[8];
     __shared__ unsigned long long sh[8];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     float d2 = 0.f, slack = 3.0e38f;
-    double h = 0.0;
-    if (k < n) {
+    // h as its bit pattern: h >= 0 orders like its bits (integer pipe)
+    unsigned long long hb = 0ull;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         int cc[3];
         cell_coords(S.cell[k], g, cc);
         float r[3] = {0.f, 0.f, 0.f};
         for (int d = 0; d < o.ndim; d++) {
-            double v = F.f[X0 + d][k] - (g.origin[d] + cc[d] * g.cs[d]);
-            if (o.periodic[d]) {
-                if (v > 0.5 * o.L[d]) v -= o.L[d];
-                else if (v < -0.5 * o.L[d]) v += o.L[d];
-            }
+            const double v = F.f[X0 + d][k] - (g.origin[d] + cc[d] * g.cs[d]);
             r[d] = (float)v;
+            // the periodic jump is undone only for a separation beyond half
+            // the box; |v| <= L/4 (tested in FP32, where it is conservative)
+            // never is one, so the FP64 tests run only for the rare rest
+            if (o.periodic[d] && !(fabsf(r[d]) <= 0.25f * (float)o.L[d])) {
+                double w = v;
+                if (w > 0.5 * o.L[d]) w -= o.L[d];
+                else if (w < -0.5 * o.L[d]) w += o.L[d];
+                r[d] = (float)w;
+            }
         }
-        h = F.f[HH][k];
+        const double h = F.f[HH][k];
         S.xs[k] = make_float4(r[0], r[1], r[2], (float)h);
         const float4 b = S.xsb[k];
         const float e0 = r[0] - b.x, e1 = r[1] - b.y, e2 = r[2] - b.z;
-        d2 = e0 * e0 + e1 * e1 + e2 * e2;
-        slack = skin * S.hb[k] - grow * (float)h;
-        if (!(d2 <= 3.0e38f)) d2 = 3.0e38f;          // non-finite position: fails the check
-        if (!(slack >= -3.0e38f)) slack = -3.0e38f;
+        float dk = e0 * e0 + e1 * e1 + e2 * e2;
+        float sk = skin * S.hb[k] - grow * (float)h;
+        if (!(dk <= 3.0e38f)) dk = 3.0e38f;          // non-finite position: fails the check
+        if (!(sk >= -3.0e38f)) sk = -3.0e38f;
+        d2 = fmaxf(d2, dk);
+        slack = fminf(slack, sk);
+        const unsigned long long hk = dbits(h);
+        hb = hk > hb ? hk : hb;
     }
-    // h as its bit pattern: h >= 0 orders like its bits (integer pipe)
-    unsigned long long hb = dbits(h);
     for (int off = 16; off > 0; off >>= 1) {
         d2 = fmaxf(d2, __shfl_down_sync(0xffffffffu, d2, off));
         slack = fminf(slack, __shfl_down_sync(0xffffffffu, slack, off));
@@ -362,7 +377,7 @@ __global__ void k_reuse_check(FieldPtrs F, Side S, Grid g, DevOpts o, int n, flo
 void launch_reuse_check(FieldPtrs F, Side S, Grid g, DevOpts o, int n, float skin, float grow, Reduce* red,
                         cudaStream_t st)
 {
-    if (n > 0) NDSPH_COUNT_LAUNCH, k_reuse_check<<<nblk(n, 256), 256, 0, st>>>(F, S, g, o, n, skin, grow, red);
+    if (n > 0) NDSPH_COUNT_LAUNCH, k_reuse_check<<<red_blocks(n), 256, 0, st>>>(F, S, g, o, n, skin, grow, red);
 }
 
 // ---------------------------------------------------------------------------
