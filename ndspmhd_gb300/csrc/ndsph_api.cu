@@ -129,6 +129,12 @@ struct ndsph_ctx {
     float mlp_lr = 2.e-3f;
     int mlp_batch = 16384;
     int mlp_iters = 1;
+    // the training runs on its own stream from the end of the density
+    // iteration to the corrector, beside the EOS and the rates sweep
+    cudaStream_t st_mlp = nullptr;
+    cudaEvent_t ev_mfork = nullptr, ev_mjoin = nullptr;
+    bool mlp_train_here = false;   // do_derivs starts the training after the iteration
+    bool mlp_pending = false;      // training issued, not yet joined
     // batched form
     int nsim = 0;
     int* sim2 = nullptr;             // gather partner of S.sim
@@ -563,6 +569,9 @@ extern "C" int ndsph_init(ndsph_ctx** out, const ndsph_opts* opts, int32_t nmax)
 extern "C" int ndsph_finalize(ndsph_ctx* ctx)
 {
     if (!ctx) return 0;
+    if (ctx->st_mlp) { cudaStreamSynchronize(ctx->st_mlp); cudaStreamDestroy(ctx->st_mlp); }
+    if (ctx->ev_mfork) cudaEventDestroy(ctx->ev_mfork);
+    if (ctx->ev_mjoin) cudaEventDestroy(ctx->ev_mjoin);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     free_particles(ctx);
     void* ptrs[] = {ctx->tab64, ctx->tab32, ctx->red, ctx->d_dtout, ctx->d_ncalc, ctx->d_fields,
@@ -1465,6 +1474,8 @@ static int do_rates(ndsph_ctx* ctx)
 }
 
 // derivs: boundary, link, iterate_density, cons2prim, get_rates
+static void mlp_train_async(ndsph_ctx* ctx);
+
 static int do_derivs(ndsph_ctx* ctx, const int* fields, int nfields)
 {
     cudaStream_t st = ctx->st;
@@ -1488,6 +1499,10 @@ static int do_derivs(ndsph_ctx* ctx, const int* fields, int nfields)
     int its = 0, nct = 0, nrl = 0;
     rc = do_iterate_density(ctx, &its, &nct, &nrl);
     if (rc) return rc;
+    if (ctx->mlp_train_here) {
+        ctx->mlp_train_here = false;
+        mlp_train_async(ctx);
+    }
     if (ctx->dl_early) {
         rc = download_density_group(ctx, ctx->dl_early);
         if (rc) return rc;
@@ -1816,9 +1831,8 @@ static void mlp_infer(ndsph_ctx* ctx)
 }
 
 // learned h, after the density iteration: train on (features, converged h)
-static void mlp_train(ndsph_ctx* ctx)
+static void mlp_train(ndsph_ctx* ctx, cudaStream_t st)
 {
-    cudaStream_t st = ctx->st;
     const long long n = ctx->n;
     // the gradient starts at zero: set so at init, and the Adam kernel
     // clears it after every use
@@ -1844,12 +1858,50 @@ static void mlp_train(ndsph_ctx* ctx)
     launch_mlp_pack(ctx->mlp_p, ctx->mlp_frag, st);
 }
 
+// The training reads the features, h_pred and the converged h, which nothing
+// between the end of the density iteration and the corrector writes, and
+// updates the weights, which the next step's inference reads: it runs on its
+// own stream over that stretch (the EOS and the rates sweep), and the main
+// stream waits for it before the corrector.  Without the stream it runs in
+// order on the main stream.
+static void mlp_train_async(ndsph_ctx* ctx)
+{
+    if (!ctx->st_mlp) {
+        if (cudaStreamCreateWithFlags(&ctx->st_mlp, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_mfork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_mjoin, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            if (ctx->st_mlp) { cudaStreamDestroy(ctx->st_mlp); ctx->st_mlp = nullptr; }
+            if (ctx->ev_mfork) { cudaEventDestroy(ctx->ev_mfork); ctx->ev_mfork = nullptr; }
+            if (ctx->ev_mjoin) { cudaEventDestroy(ctx->ev_mjoin); ctx->ev_mjoin = nullptr; }
+            mlp_train(ctx, ctx->st);
+            return;
+        }
+    }
+    if (cudaEventRecord(ctx->ev_mfork, ctx->st) != cudaSuccess ||
+        cudaStreamWaitEvent(ctx->st_mlp, ctx->ev_mfork, 0) != cudaSuccess) {
+        cudaGetLastError();
+        mlp_train(ctx, ctx->st);
+        return;
+    }
+    mlp_train(ctx, ctx->st_mlp);
+    cudaEventRecord(ctx->ev_mjoin, ctx->st_mlp);
+    ctx->mlp_pending = true;
+}
+static void mlp_join(ndsph_ctx* ctx)
+{
+    if (!ctx->mlp_pending) return;
+    cudaStreamWaitEvent(ctx->st, ctx->ev_mjoin, 0);
+    ctx->mlp_pending = false;
+}
+
 // one leapfrog step on the device state (stepND_leapfrog_mhd.f90:31-275)
 // fuse_next: another device-resident step follows in the same call, so the
 // corrector also runs that step's save and predictor
 static int dev_step_once(ndsph_ctx* ctx, bool fuse_next = false)
 {
     cudaStream_t st = ctx->st;
+    mlp_join(ctx);   // a training left by a step that stopped with an error
     // dt lives in the Reduce block
     CK(cudaMemcpyAsync(&ctx->red->dt, &ctx->dt, sizeof(double), cudaMemcpyHostToDevice, st));
     if (ctx->predicted)
@@ -1865,13 +1917,18 @@ static int dev_step_once(ndsph_ctx* ctx, bool fuse_next = false)
         tmark(ctx, 13);
     }
     const std::vector<int> live = step_live_fields(ctx, learned);
+    // the training overlaps the EOS and the rates sweep; a profiled step
+    // runs it in order so that its time can be taken
+    ctx->mlp_train_here = learned && !ctx->profiling;
     int rc = do_derivs(ctx, live.data(), (int)live.size());
+    ctx->mlp_train_here = false;
     if (rc) return rc;
+    mlp_join(ctx);
     if (learned) {
-        tmark(ctx, 14);
-        mlp_train(ctx);
-        tmark(ctx, 15);
         if (ctx->profiling) {
+            tmark(ctx, 14);
+            mlp_train(ctx, st);
+            tmark(ctx, 15);
             float loss = 0.f;
             cudaMemcpyAsync(&loss, ctx->mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, st);
             cudaStreamSynchronize(st);
