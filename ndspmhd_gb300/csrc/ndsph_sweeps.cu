@@ -366,9 +366,12 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
     // velocity/mass pack, loaded by the caller
     const unsigned shift = (NDIM == 3) ? (unsigned)g.nlshift : 5u, omask = (1u << shift) - 1u;
     // FP32 form: the kernel sums of one accepted pair (q_i < 2)
+    // 1/h of i for the FP32 pair sums: with the rsqrt of q^2 it gives 1/r
+    const float hi1f = rcp_ftz(hif);
     auto sums32 = [&](int j, float q2i, const float dxf[3], const float4& pvj) {
         const float mj = pvj.w;
-        const float q = sqrtp(q2i);
+        const float rq = rsqrt_ftz(fmaxf(q2i, 1e-37f));   // 1/q (the sqrt's own rsqrt)
+        const float q = q2i * rq;
         float wv, gw, ggw;
         if (q2i >= KERN_Q2_DIRECT) {
             const KerF kf = kern_cubic(q, a.t.cnormf);
@@ -386,11 +389,12 @@ __device__ __forceinline__ void density_body(const SweepArgs& a, const int i, co
         fgn.add(tg);
         fgg.add(mj * ((float)(NDIM * (NDIM + 1)) * wv + (float)(2 * (NDIM + 1)) * q * gw + q2i * ggw));
         if (j != i) {
-            const float rij = q * hif;
+            // 1/r_ij = (1/q)(1/h_i), no reciprocal of its own (a coincident
+            // pair has dv.r = 0, and 1/q stays finite)
             float dvr = (vif[0] - pvj.x) * dxf[0];
             if (NDIM >= 2) dvr += (vif[1] - pvj.y) * dxf[1];
             if (NDIM >= 3) dvr += (vif[2] - pvj.z) * dxf[2];
-            fd.add(mj * dvr * gw * rcp_ftz(rij + 1e-30f));
+            fd.add(mj * dvr * gw * (rq * hi1f));
         }
     };
     auto pair = [&](unsigned pk, const float4& xsj, int typej, const float4& pvj) {
@@ -2114,7 +2118,11 @@ __global__ void __launch_bounds__(128) k_build_nlist(SweepArgs a)
     if (a.S.xsb) a.S.xsb[i] = xsi;
     const int cmax = max(out.cnt, out.cnt2);
     if (cmax > a.nl_stride) { a.red->nl_overflow = 1; if (a.graph) a.red->gfail |= 2; }
-    atomicMax(&a.red->nl_maxcnt, cmax);
+    // the longest row: one atomic per warp (one per particle put 2.1 M
+    // atomics on one word at 128^3)
+    const unsigned am = __activemask();
+    const int wmax = __reduce_max_sync(am, cmax);
+    if ((int)(threadIdx.x & 31u) == __ffs((int)am) - 1) atomicMax(&a.red->nl_maxcnt, wmax);
 }
 
 // largest h (the xs.w the build uses) of each cell's particles (1D pruning)
